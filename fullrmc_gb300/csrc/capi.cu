@@ -1,0 +1,645 @@
+// extern "C" entry points (declared in include/frmc_gpu.h).
+//
+// Host-buffer entry points copy their inputs to the current device on the
+// context's stream, run the kernels, copy the results back and synchronise;
+// they keep no host data between calls (fullrmc mutates its coordinate array
+// between calls, PairDistributionConstraints.py:1092-1122).
+#include <climits>
+#include <cmath>
+#include <cstring>
+
+#include "frmc_gpu.h"
+#include "frmc_runtime.h"
+
+namespace frmc {
+int launch_distances(const float *coords, int n, const float *pts, long long ps, const int *idx, int K,
+                     int fromIndex, int isPBC, const float *basis, float *out, cudaStream_t st);
+int launch_differences(const float *coords, int n, const float *pts, long long ps, const int *idx, int K,
+                       int fromIndex, int isPBC, const float *basis, float *out, cudaStream_t st);
+int launch_from_to(const float *from, const float *to, int n, int isPBC, const float *basis, float *out,
+                   cudaStream_t st);
+int launch_transform(const float *M, const float *coords, int n, float *out, cudaStream_t st);
+int launch_sine(int kind, const float *xs, int nx, const float *ys, const float *f, int ny, double rho, double *out,
+                cudaStream_t st);
+
+static FullTune g_full_tune;
+static std::mutex g_tune_mu;
+
+static FullTune current_tune()
+{
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    return g_full_tune;
+}
+
+static const float kIdentity[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+
+static int check_n(int64_t n, const char *what)
+{
+    if (n < 0 || n > INT_MAX / 4)
+        return set_error(FRMC_E_ARG, "%s: size %lld out of range", what, (long long)n);
+    return FRMC_OK;
+}
+
+static int check_hist(int32_t ne, int32_t hs, int64_t *total)
+{
+    if (ne < 0 || hs < 0)
+        return set_error(FRMC_E_ARG, "negative histogram shape (%d, %d)", ne, hs);
+    int64_t t = (int64_t)ne * ne * hs;
+    if (t > (int64_t)INT_MAX / 8)
+        return set_error(FRMC_E_ARG, "histogram too large (%lld bins)", (long long)t);
+    *total = t;
+    return FRMC_OK;
+}
+
+static int check_indexes(const int32_t *idx, int64_t K, int64_t n)
+{
+    for (int64_t k = 0; k < K; ++k)
+        if (idx[k] < 0 || idx[k] >= n)
+            return set_error(FRMC_E_INDEX, "index %d out of range for %lld atoms", idx[k], (long long)n);
+    return FRMC_OK;
+}
+
+static double accept_fraction(const float *basis, int isPBC, float minD, float maxD)
+{
+    if (!isPBC)
+        return 1.0;
+    const float *B = basis;
+    double det = (double)B[0] * ((double)B[4] * B[8] - (double)B[5] * B[7]) -
+                 (double)B[1] * ((double)B[3] * B[8] - (double)B[5] * B[6]) +
+                 (double)B[2] * ((double)B[3] * B[7] - (double)B[4] * B[6]);
+    double V = std::fabs(det);
+    if (!(V > 0))
+        return 1.0;
+    double lo = minD > 0 ? (double)minD : 0.0;
+    double hi = (double)maxD;
+    if (!(hi > lo))
+        return 0.0;
+    double f = 4.0 / 3.0 * M_PI * (hi * hi * hi - lo * lo * lo) / V;
+    return f > 1.0 ? 1.0 : f;
+}
+
+#define LOCKED_CTX(c)                      \
+    Context *c = nullptr;                  \
+    {                                      \
+        int _rc = get_context(&c);         \
+        if (_rc) return _rc;               \
+    }                                      \
+    std::lock_guard<std::mutex> _lk(c->mu)
+
+#define TRY(x)                   \
+    do {                         \
+        int _rc = (x);           \
+        if (_rc) return _rc;     \
+    } while (0)
+
+static int h2d(void *dst, const void *src, size_t bytes, cudaStream_t st)
+{
+    if (!bytes)
+        return FRMC_OK;
+    FRMC_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+    return FRMC_OK;
+}
+
+static int d2h(void *dst, const void *src, size_t bytes, cudaStream_t st)
+{
+    if (!bytes)
+        return FRMC_OK;
+    FRMC_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st));
+    return FRMC_OK;
+}
+
+static int finish(Context *c)
+{
+    FRMC_CUDA(cudaStreamSynchronize(c->stream));
+    return FRMC_OK;
+}
+
+// Upload coordinates, element and molecule indexes of n atoms.
+static int upload_atoms(Context *c, const float *coords, const int32_t *mol, const int32_t *el, int64_t n)
+{
+    TRY(c->buf[BUF_COORDS].ensure(n * 12 + 16));
+    TRY(h2d(c->buf[BUF_COORDS].p, coords, n * 12, c->stream));
+    if (el) {
+        TRY(c->buf[BUF_EL].ensure(n * 4 + 16));
+        TRY(h2d(c->buf[BUF_EL].p, el, n * 4, c->stream));
+    }
+    if (mol) {
+        TRY(c->buf[BUF_MOL].ensure(n * 4 + 16));
+        TRY(h2d(c->buf[BUF_MOL].p, mol, n * 4, c->stream));
+    }
+    return FRMC_OK;
+}
+
+// Full histogram counts of the atoms already uploaded by upload_atoms.
+static int full_counts(Context *c, int64_t n, const float *basis, int isPBC, int32_t ne, float minD, float maxD,
+                       float bin, int32_t hs, int64_t total, unsigned *counts)
+{
+    const float *B = isPBC ? basis : kIdentity;
+    const int bm = basis_mode(B, isPBC);
+    Basis Bs = make_basis(B);
+    const double pairs = 0.5 * (double)n * (double)(n - 1);
+    FullTune tn = current_tune();
+    if (pairs < tn.min_pairs_tiled) {
+        return launch_rows_hist(c->buf[BUF_COORDS].as<float>(), c->buf[BUF_EL].as<int>(), c->buf[BUF_MOL].as<int>(),
+                                (int)n, nullptr, (int)n, 0, bm, Bs, minD, maxD, bin, ne, hs, counts, counts + total,
+                                c->stream);
+    }
+    TRY(c->buf[BUF_ATOMS4].ensure(n * 16 + 16));
+    float4 *a4 = c->buf[BUF_ATOMS4].as<float4>();
+    TRY(launch_pack_atoms(c->buf[BUF_COORDS].as<float>(), c->buf[BUF_EL].as<int>(), (int)n, a4, c->stream));
+    return launch_full_hist(a4, c->buf[BUF_MOL].as<int>(), (int)n, bm, Bs, minD, maxD, bin, ne, hs, counts,
+                            counts + total, c->buf[BUF_STATUS].as<uint32_t>(), accept_fraction(B, isPBC, minD, maxD),
+                            &tn, c->stream);
+}
+
+static int prepare_counts(Context *c, int64_t total)
+{
+    TRY(c->buf[BUF_COUNTS].ensure(2 * total * 4 + 16));
+    TRY(c->buf[BUF_OUT].ensure(2 * total * 4 + 16));
+    TRY(c->buf[BUF_STATUS].ensure(16));
+    FRMC_CUDA(cudaMemsetAsync(c->buf[BUF_COUNTS].p, 0, 2 * total * 4, c->stream));
+    FRMC_CUDA(cudaMemsetAsync(c->buf[BUF_STATUS].p, 0, 4, c->stream));
+    return FRMC_OK;
+}
+
+// Convert counts to float32 and copy both histograms back; checks the status.
+static int counts_out(Context *c, int64_t total, const float *h0intra, const float *h0inter, float *hintra,
+                      float *hinter)
+{
+    unsigned *cnt = c->buf[BUF_COUNTS].as<unsigned>();
+    float *out = c->buf[BUF_OUT].as<float>();
+    const float *d0i = nullptr, *d0e = nullptr;
+    if (h0intra) {
+        TRY(c->buf[BUF_AUX2].ensure(2 * total * 4 + 16));
+        float *h0 = c->buf[BUF_AUX2].as<float>();
+        TRY(h2d(h0, h0intra, total * 4, c->stream));
+        TRY(h2d(h0 + total, h0inter, total * 4, c->stream));
+        d0i = h0;
+        d0e = h0 + total;
+    }
+    TRY(launch_counts_to_f32(cnt, d0i, out, total, c->stream));
+    TRY(launch_counts_to_f32(cnt + total, d0e, out + total, total, c->stream));
+    TRY(d2h(hintra, out, total * 4, c->stream));
+    TRY(d2h(hinter, out + total, total * 4, c->stream));
+    uint32_t status = 0;
+    TRY(d2h(&status, c->buf[BUF_STATUS].p, 4, c->stream));
+    TRY(finish(c));
+    if (status)
+        return set_error(FRMC_E_TIMEOUT, "device wait gave up (status 0x%x)", status);
+    return FRMC_OK;
+}
+
+}  // namespace frmc
+
+
+using namespace frmc;
+
+extern "C" {
+
+int frmc_version(void) { return 10000; }
+
+const char *frmc_last_error(void) { return last_error(); }
+
+int frmc_set_device(int device)
+{
+    FRMC_CUDA(cudaSetDevice(device));
+    return FRMC_OK;
+}
+
+int frmc_device_info(int *sms, int *max_smem_optin, int *cc_major, int *cc_minor)
+{
+    Context *c;
+    TRY(get_context(&c));
+    if (sms) *sms = c->sms;
+    if (max_smem_optin) *max_smem_optin = c->max_smem_optin;
+    int dev = c->device;
+    if (cc_major) FRMC_CUDA(cudaDeviceGetAttribute(cc_major, cudaDevAttrComputeCapabilityMajor, dev));
+    if (cc_minor) FRMC_CUDA(cudaDeviceGetAttribute(cc_minor, cudaDevAttrComputeCapabilityMinor, dev));
+    return FRMC_OK;
+}
+
+int frmc_set_full_tune(int threads, int rows, int queued, int qcap, int ctas_per_sm, double min_pairs_tiled)
+{
+    if (threads % 32 || threads < 64 || threads > 1024 || (rows != 1 && rows != 2) || qcap < 0 || ctas_per_sm < 1 ||
+        !(min_pairs_tiled >= 0))
+        return set_error(FRMC_E_ARG, "invalid tile configuration");
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_full_tune.threads = threads;
+    g_full_tune.rows = rows;
+    g_full_tune.queued = queued;
+    g_full_tune.qcap = qcap;
+    g_full_tune.ctas_per_sm = ctas_per_sm;
+    g_full_tune.min_pairs_tiled = min_pairs_tiled;
+    return FRMC_OK;
+}
+
+int frmc_sq_limits(float minDistance, float maxDistance, float *s_lo, float *s_hi)
+{
+    sq_limits(minDistance, maxDistance, s_lo, s_hi);
+    return FRMC_OK;
+}
+
+int frmc_basis_mode(const float *basis, int isPBC) { return basis_mode(isPBC ? basis : kIdentity, isPBC); }
+
+int frmc_full_items(int64_t n, int64_t *nitems)
+{
+    TRY(check_n(n, "atoms"));
+    FullTune tn = current_tune();
+    *nitems = n < 2 ? 0 : full_hist_items((int)n, &tn);
+    return FRMC_OK;
+}
+
+// ----------------------------------------------------------- distances (host)
+static int distances_common(int diff, int32_t atomIndex, const int32_t *indexes, int64_t K, const float *points,
+                            int64_t ps, const float *coords, int64_t n, const float *basis, int isPBC, int allAtoms,
+                            float *out)
+{
+    TRY(check_n(n, "coords"));
+    if (K < 0 || K > 65535)
+        return set_error(FRMC_E_ARG, "number of points %lld out of range", (long long)K);
+    int single_index = indexes == nullptr && points == nullptr;
+    if (single_index && (atomIndex < 0 || atomIndex >= n))
+        return set_error(FRMC_E_INDEX, "atomIndex %d out of range for %lld atoms", atomIndex, (long long)n);
+    if (indexes)
+        TRY(check_indexes(indexes, K, n));
+    if (n == 0 || K == 0)
+        return FRMC_OK;
+    const float *B = isPBC ? basis : kIdentity;
+    LOCKED_CTX(c);
+    TRY(upload_atoms(c, coords, nullptr, nullptr, n));
+    const int width = diff ? 3 : 1;
+    const int64_t out_elems = n * width * K;
+    TRY(c->buf[BUF_OUT].ensure(out_elems * 4 + 16));
+    const int *didx = nullptr;
+    const float *dpts = nullptr;
+    if (single_index || indexes) {
+        TRY(c->buf[BUF_ROWS].ensure(K * 4 + 16));
+        TRY(h2d(c->buf[BUF_ROWS].p, single_index ? &atomIndex : indexes, K * 4, c->stream));
+        didx = c->buf[BUF_ROWS].as<int>();
+    } else {
+        TRY(c->buf[BUF_AUX0].ensure(3 * ps * 4 + 16));
+        TRY(h2d(c->buf[BUF_AUX0].p, points, 3 * ps * 4, c->stream));
+        dpts = c->buf[BUF_AUX0].as<float>();
+    }
+    const int fromIndex = (didx && !allAtoms) ? 1 : 0;
+    float *dout = c->buf[BUF_OUT].as<float>();
+    // Multi-index rows below their start keep the caller's values.
+    if (fromIndex && !single_index)
+        TRY(h2d(dout, out, out_elems * 4, c->stream));
+    if (diff)
+        TRY(launch_differences(c->buf[BUF_COORDS].as<float>(), (int)n, dpts, ps, didx, (int)K, fromIndex, isPBC, B,
+                               dout, c->stream));
+    else
+        TRY(launch_distances(c->buf[BUF_COORDS].as<float>(), (int)n, dpts, ps, didx, (int)K, fromIndex, isPBC, B,
+                             dout, c->stream));
+    if (fromIndex && single_index) {
+        const int64_t off = (int64_t)atomIndex * width;
+        TRY(d2h(out + off, dout + off, (out_elems - off) * 4, c->stream));
+    } else {
+        TRY(d2h(out, dout, out_elems * 4, c->stream));
+    }
+    return finish(c);
+}
+
+int frmc_pairs_distances_to_indexcoords(int32_t atomIndex, const float *coords, int64_t n, const float *basis,
+                                        int isPBC, int allAtoms, float *distances)
+{
+    return distances_common(0, atomIndex, nullptr, 1, nullptr, 0, coords, n, basis, isPBC, allAtoms, distances);
+}
+
+int frmc_pairs_distances_to_point(const float *point, const float *coords, int64_t n, const float *basis, int isPBC,
+                                  float *distances)
+{
+    return distances_common(0, 0, nullptr, 1, point, 1, coords, n, basis, isPBC, 1, distances);
+}
+
+int frmc_pairs_distances_to_multi_points(const float *points, int64_t ps, int64_t K, const float *coords, int64_t n,
+                                         const float *basis, int isPBC, float *distances)
+{
+    return distances_common(0, 0, nullptr, K, points, ps, coords, n, basis, isPBC, 1, distances);
+}
+
+int frmc_pairs_distances_to_multi_indexcoords(const int32_t *indexes, int64_t K, const float *coords, int64_t n,
+                                              const float *basis, int isPBC, int allAtoms, float *distances)
+{
+    if (K == 0)
+        return FRMC_OK;
+    return distances_common(0, 0, indexes, K, nullptr, 0, coords, n, basis, isPBC, allAtoms, distances);
+}
+
+int frmc_point_to_point_distance(const float *point1, const float *point2, const float *basis, int isPBC,
+                                 float *distance)
+{
+    return distances_common(0, 0, nullptr, 1, point1, 1, point2, 1, basis, isPBC, 1, distance);
+}
+
+int frmc_pairs_differences_to_point(const float *point, const float *coords, int64_t n, const float *basis,
+                                    int isPBC, float *differences)
+{
+    return distances_common(1, 0, nullptr, 1, point, 1, coords, n, basis, isPBC, 1, differences);
+}
+
+int frmc_pairs_differences_to_indexcoords(int32_t atomIndex, const float *coords, int64_t n, const float *basis,
+                                          int isPBC, int allAtoms, float *differences)
+{
+    return distances_common(1, atomIndex, nullptr, 1, nullptr, 0, coords, n, basis, isPBC, allAtoms, differences);
+}
+
+int frmc_pairs_differences_to_multi_points(const float *points, int64_t ps, int64_t K, const float *coords,
+                                           int64_t n, const float *basis, int isPBC, float *differences)
+{
+    return distances_common(1, 0, nullptr, K, points, ps, coords, n, basis, isPBC, 1, differences);
+}
+
+int frmc_pairs_differences_to_multi_indexcoords(const int32_t *indexes, int64_t K, const float *coords, int64_t n,
+                                                const float *basis, int isPBC, int allAtoms, float *differences)
+{
+    if (K == 0)
+        return FRMC_OK;
+    return distances_common(1, 0, indexes, K, nullptr, 0, coords, n, basis, isPBC, allAtoms, differences);
+}
+
+int frmc_pair_difference_to_point(const float *point1, const float *point2, const float *basis, int isPBC,
+                                  float *difference)
+{
+    // bc(point2 - point1): the "point" is point2, the single coordinate point1.
+    return distances_common(1, 0, nullptr, 1, point2, 1, point1, 1, basis, isPBC, 1, difference);
+}
+
+int frmc_from_to_points_differences(const float *pointsFrom, const float *pointsTo, int64_t n, const float *basis,
+                                    int isPBC, float *differences)
+{
+    TRY(check_n(n, "points"));
+    if (n == 0)
+        return FRMC_OK;
+    const float *B = isPBC ? basis : kIdentity;
+    LOCKED_CTX(c);
+    TRY(c->buf[BUF_COORDS].ensure(n * 12 + 16));
+    TRY(c->buf[BUF_AUX0].ensure(n * 12 + 16));
+    TRY(c->buf[BUF_OUT].ensure(n * 12 + 16));
+    TRY(h2d(c->buf[BUF_COORDS].p, pointsFrom, n * 12, c->stream));
+    TRY(h2d(c->buf[BUF_AUX0].p, pointsTo, n * 12, c->stream));
+    TRY(launch_from_to(c->buf[BUF_COORDS].as<float>(), c->buf[BUF_AUX0].as<float>(), (int)n, isPBC, B,
+                       c->buf[BUF_OUT].as<float>(), c->stream));
+    TRY(d2h(differences, c->buf[BUF_OUT].p, n * 12, c->stream));
+    return finish(c);
+}
+
+int frmc_transform_coordinates(const float *transMatrix, const float *coords, int64_t n, float *out)
+{
+    TRY(check_n(n, "coords"));
+    if (n == 0)
+        return FRMC_OK;
+    LOCKED_CTX(c);
+    TRY(c->buf[BUF_COORDS].ensure(n * 12 + 16));
+    TRY(c->buf[BUF_OUT].ensure(n * 12 + 16));
+    TRY(h2d(c->buf[BUF_COORDS].p, coords, n * 12, c->stream));
+    TRY(launch_transform(transMatrix, c->buf[BUF_COORDS].as<float>(), (int)n, c->buf[BUF_OUT].as<float>(),
+                         c->stream));
+    TRY(d2h(out, c->buf[BUF_OUT].p, n * 12, c->stream));
+    return finish(c);
+}
+
+// ---------------------------------------------------------- histograms (host)
+int frmc_full_pairs_histograms_coords(const float *boxCoords, int64_t n, const float *basis, int isPBC,
+                                      const int32_t *moleculeIndex, const int32_t *elementIndex, int32_t ne,
+                                      float minDistance, float maxDistance, float bin, int32_t hs, float *hintra,
+                                      float *hinter)
+{
+    int64_t total;
+    TRY(check_n(n, "boxCoords"));
+    TRY(check_hist(ne, hs, &total));
+    if (total == 0)
+        return FRMC_OK;
+    if (n < 2) {
+        memset(hintra, 0, total * 4);
+        memset(hinter, 0, total * 4);
+        return FRMC_OK;
+    }
+    LOCKED_CTX(c);
+    TRY(upload_atoms(c, boxCoords, moleculeIndex, elementIndex, n));
+    TRY(prepare_counts(c, total));
+    TRY(full_counts(c, n, basis, isPBC, ne, minDistance, maxDistance, bin, hs, total,
+                    c->buf[BUF_COUNTS].as<unsigned>()));
+    return counts_out(c, total, nullptr, nullptr, hintra, hinter);
+}
+
+int frmc_multiple_pairs_histograms_coords(const int32_t *indexes, int64_t K, const float *boxCoords, int64_t n,
+                                          const float *basis, int isPBC, const int32_t *moleculeIndex,
+                                          const int32_t *elementIndex, int32_t ne, float minDistance,
+                                          float maxDistance, float bin, int32_t hs, int allAtoms, float *hintra,
+                                          float *hinter)
+{
+    int64_t total;
+    TRY(check_n(n, "boxCoords"));
+    TRY(check_hist(ne, hs, &total));
+    if (K < 0 || K > (int64_t)65535 * 64)
+        return set_error(FRMC_E_ARG, "number of indexes %lld out of range", (long long)K);
+    TRY(check_indexes(indexes, K, n));
+    if (total == 0)
+        return FRMC_OK;
+    if (K == 0 || n == 0) {
+        memset(hintra, 0, total * 4);
+        memset(hinter, 0, total * 4);
+        return FRMC_OK;
+    }
+    const float *B = isPBC ? basis : kIdentity;
+    LOCKED_CTX(c);
+    TRY(upload_atoms(c, boxCoords, moleculeIndex, elementIndex, n));
+    TRY(prepare_counts(c, total));
+    TRY(c->buf[BUF_ROWS].ensure(K * 4 + 16));
+    TRY(h2d(c->buf[BUF_ROWS].p, indexes, K * 4, c->stream));
+    unsigned *cnt = c->buf[BUF_COUNTS].as<unsigned>();
+    TRY(launch_rows_hist(c->buf[BUF_COORDS].as<float>(), c->buf[BUF_EL].as<int>(), c->buf[BUF_MOL].as<int>(), (int)n,
+                         c->buf[BUF_ROWS].as<int>(), (int)K, allAtoms, basis_mode(B, isPBC), make_basis(B),
+                         minDistance, maxDistance, bin, ne, hs, cnt, cnt + total, c->stream));
+    return counts_out(c, total, nullptr, nullptr, hintra, hinter);
+}
+
+int frmc_multiple_pairs_histograms_dists(const int32_t *indexes, int64_t K, const float *distances, int64_t n,
+                                         const int32_t *moleculeIndex, const int32_t *elementIndex, int32_t ne,
+                                         float minDistance, float maxDistance, float bin, int32_t hs, int allAtoms,
+                                         float *hintra, float *hinter)
+{
+    int64_t total;
+    TRY(check_n(n, "distances"));
+    TRY(check_hist(ne, hs, &total));
+    if (K < 0 || K > 65535)
+        return set_error(FRMC_E_ARG, "number of indexes %lld out of range", (long long)K);
+    TRY(check_indexes(indexes, K, n));
+    if (total == 0)
+        return FRMC_OK;
+    if (K == 0 || n == 0) {
+        memset(hintra, 0, total * 4);
+        memset(hinter, 0, total * 4);
+        return FRMC_OK;
+    }
+    LOCKED_CTX(c);
+    TRY(c->buf[BUF_AUX0].ensure(n * K * 4 + 16));
+    TRY(h2d(c->buf[BUF_AUX0].p, distances, n * K * 4, c->stream));
+    TRY(c->buf[BUF_EL].ensure(n * 4 + 16));
+    TRY(h2d(c->buf[BUF_EL].p, elementIndex, n * 4, c->stream));
+    TRY(c->buf[BUF_MOL].ensure(n * 4 + 16));
+    TRY(h2d(c->buf[BUF_MOL].p, moleculeIndex, n * 4, c->stream));
+    TRY(c->buf[BUF_ROWS].ensure(K * 4 + 16));
+    TRY(h2d(c->buf[BUF_ROWS].p, indexes, K * 4, c->stream));
+    TRY(prepare_counts(c, total));
+    unsigned *cnt = c->buf[BUF_COUNTS].as<unsigned>();
+    TRY(launch_dists_hist(c->buf[BUF_AUX0].as<float>(), (int)n, (int)K, c->buf[BUF_ROWS].as<int>(),
+                          c->buf[BUF_EL].as<int>(), c->buf[BUF_MOL].as<int>(), allAtoms, minDistance, maxDistance, bin,
+                          ne, hs, cnt, cnt + total, c->stream));
+    return counts_out(c, total, nullptr, nullptr, hintra, hinter);
+}
+
+int frmc_single_pairs_histograms(int32_t atomIndex, const float *distances, int64_t n, const int32_t *moleculeIndex,
+                                 const int32_t *elementIndex, int32_t ne, int32_t hs, float *hintra, float *hinter,
+                                 float minDistance, float maxDistance, float bin, int allAtoms)
+{
+    int64_t total;
+    TRY(check_n(n, "distances"));
+    TRY(check_hist(ne, hs, &total));
+    if (atomIndex < 0 || atomIndex >= n)
+        return set_error(FRMC_E_INDEX, "atomIndex %d out of range for %lld atoms", atomIndex, (long long)n);
+    if (total == 0)
+        return FRMC_OK;
+    LOCKED_CTX(c);
+    TRY(c->buf[BUF_AUX0].ensure(n * 4 + 16));
+    TRY(h2d(c->buf[BUF_AUX0].p, distances, n * 4, c->stream));
+    TRY(c->buf[BUF_EL].ensure(n * 4 + 16));
+    TRY(h2d(c->buf[BUF_EL].p, elementIndex, n * 4, c->stream));
+    TRY(c->buf[BUF_MOL].ensure(n * 4 + 16));
+    TRY(h2d(c->buf[BUF_MOL].p, moleculeIndex, n * 4, c->stream));
+    TRY(c->buf[BUF_ROWS].ensure(16));
+    TRY(h2d(c->buf[BUF_ROWS].p, &atomIndex, 4, c->stream));
+    TRY(prepare_counts(c, total));
+    unsigned *cnt = c->buf[BUF_COUNTS].as<unsigned>();
+    TRY(launch_dists_hist(c->buf[BUF_AUX0].as<float>(), (int)n, 1, c->buf[BUF_ROWS].as<int>(), c->buf[BUF_EL].as<int>(),
+                          c->buf[BUF_MOL].as<int>(), allAtoms, minDistance, maxDistance, bin, ne, hs, cnt, cnt + total,
+                          c->stream));
+    return counts_out(c, total, hintra, hinter, hintra, hinter);
+}
+
+// ------------------------------------------------------------ FP64 transforms
+static int sine_common(int kind, const float *xs, int64_t nx, const float *ys, const float *f, int64_t ny, double rho,
+                       double *out)
+{
+    TRY(check_n(nx, "output grid"));
+    TRY(check_n(ny, "input grid"));
+    if (nx == 0)
+        return FRMC_OK;
+    if (ny < 2)
+        return set_error(FRMC_E_ARG, "the summation grid needs at least two points");
+    LOCKED_CTX(c);
+    TRY(c->buf[BUF_AUX0].ensure(nx * 4 + 16));
+    TRY(c->buf[BUF_AUX1].ensure(ny * 8 + 16));
+    TRY(c->buf[BUF_OUT].ensure(nx * 8 + 16));
+    float *dxs = c->buf[BUF_AUX0].as<float>();
+    float *dys = c->buf[BUF_AUX1].as<float>();
+    float *df = dys + ny;
+    TRY(h2d(dxs, xs, nx * 4, c->stream));
+    TRY(h2d(dys, ys, ny * 4, c->stream));
+    TRY(h2d(df, f, ny * 4, c->stream));
+    TRY(launch_sine(kind, dxs, (int)nx, dys, df, (int)ny, rho, c->buf[BUF_OUT].as<double>(), c->stream));
+    TRY(d2h(out, c->buf[BUF_OUT].p, nx * 8, c->stream));
+    return finish(c);
+}
+
+int frmc_gr_to_sq(const float *distances, const float *gr, int64_t nr, const float *qrange, int64_t nq, double rho,
+                  double *sq)
+{
+    return sine_common(0, qrange, nq, distances, gr, nr, rho, sq);
+}
+
+int frmc_Gr_to_sq(const float *distances, const float *Gr, int64_t nr, const float *qrange, int64_t nq, double *sq)
+{
+    return sine_common(1, qrange, nq, distances, Gr, nr, 0.0, sq);
+}
+
+int frmc_sq_to_Gr(const float *qValues, int64_t nq, const float *rValues, int64_t nr, const float *sq, double *Gr)
+{
+    return sine_common(2, rValues, nr, qValues, sq, nq, 0.0, Gr);
+}
+
+// ------------------------------------------------------------ device entry points
+static int dev_full(const void *atoms4, const int32_t *moleculeIndex, int64_t n, const float *basis_host, int isPBC,
+                    int32_t ne, float minDistance, float maxDistance, float bin, int32_t hs, int64_t item_begin,
+                    int64_t item_end, uint32_t *counts, void *stream)
+{
+    int64_t total;
+    TRY(check_n(n, "atoms"));
+    TRY(check_hist(ne, hs, &total));
+    Context *c;
+    TRY(get_context(&c));
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    FRMC_CUDA(cudaMemsetAsync(counts, 0, 2 * total * 4, st));
+    if (n < 2 || total == 0)
+        return FRMC_OK;
+    if (((uintptr_t)atoms4 & 15u) || ((uintptr_t)moleculeIndex & 15u))
+        return set_error(FRMC_E_ARG, "atoms4 and moleculeIndex must be 16-byte aligned");
+    {
+        std::lock_guard<std::mutex> lk(c->mu);
+        TRY(c->buf[BUF_STATUS].ensure(16));
+    }
+    const float *B = isPBC ? basis_host : kIdentity;
+    FullTune tn = current_tune();
+    return launch_full_hist((const float4 *)atoms4, moleculeIndex, (int)n, basis_mode(B, isPBC), make_basis(B),
+                            minDistance, maxDistance, bin, ne, hs, counts, counts + total,
+                            c->buf[BUF_STATUS].as<uint32_t>(), accept_fraction(B, isPBC, minDistance, maxDistance),
+                            &tn, st, item_begin, item_end);
+}
+
+int frmc_dev_full_hist_counts(const void *atoms4, const int32_t *moleculeIndex, int64_t n, const float *basis_host,
+                              int isPBC, int32_t ne, float minDistance, float maxDistance, float bin, int32_t hs,
+                              uint32_t *counts, void *stream)
+{
+    return dev_full(atoms4, moleculeIndex, n, basis_host, isPBC, ne, minDistance, maxDistance, bin, hs, 0, -1, counts,
+                    stream);
+}
+
+int frmc_dev_full_hist_counts_range(const void *atoms4, const int32_t *moleculeIndex, int64_t n,
+                                    const float *basis_host, int isPBC, int32_t ne, float minDistance,
+                                    float maxDistance, float bin, int32_t hs, int64_t item_begin, int64_t item_end,
+                                    uint32_t *counts, void *stream)
+{
+    if (item_begin < 0 || item_end < item_begin)
+        return set_error(FRMC_E_ARG, "invalid item range [%lld, %lld)", (long long)item_begin, (long long)item_end);
+    return dev_full(atoms4, moleculeIndex, n, basis_host, isPBC, ne, minDistance, maxDistance, bin, hs, item_begin,
+                    item_end, counts, stream);
+}
+
+int frmc_dev_multiple_hist_counts(const int32_t *indexes, int64_t K, const float *boxCoords, int64_t n,
+                                  const float *basis_host, int isPBC, const int32_t *moleculeIndex,
+                                  const int32_t *elementIndex, int32_t ne, float minDistance, float maxDistance,
+                                  float bin, int32_t hs, int allAtoms, uint32_t *counts, void *stream)
+{
+    int64_t total;
+    TRY(check_n(n, "boxCoords"));
+    TRY(check_hist(ne, hs, &total));
+    if (K < 0 || K > (int64_t)65535 * 64)
+        return set_error(FRMC_E_ARG, "number of indexes %lld out of range", (long long)K);
+    Context *c;
+    TRY(get_context(&c));
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    FRMC_CUDA(cudaMemsetAsync(counts, 0, 2 * total * 4, st));
+    const float *B = isPBC ? basis_host : kIdentity;
+    return launch_rows_hist(boxCoords, elementIndex, moleculeIndex, (int)n, indexes, (int)K, allAtoms,
+                            basis_mode(B, isPBC), make_basis(B), minDistance, maxDistance, bin, ne, hs, counts,
+                            counts + total, st);
+}
+
+int frmc_dev_pack_atoms(const float *coords, const int32_t *elementIndex, int64_t n, void *atoms4, void *stream)
+{
+    TRY(check_n(n, "coords"));
+    Context *c;
+    TRY(get_context(&c));
+    return launch_pack_atoms(coords, elementIndex, (int)n, (float4 *)atoms4, stream ? (cudaStream_t)stream : c->stream);
+}
+
+int frmc_dev_counts_to_f32(const uint32_t *counts, int64_t total, float *out, void *stream)
+{
+    Context *c;
+    TRY(get_context(&c));
+    return launch_counts_to_f32(counts, nullptr, out, total, stream ? (cudaStream_t)stream : c->stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,109 @@
+// Host runtime shared by the library's translation units: per-device context
+// (stream, SM count, grow-only device buffers), error reporting and the
+// host-side helpers that prepare kernel parameters.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+
+#include "frmc_gpu.h"
+#include "frmc_math.cuh"
+
+namespace frmc {
+
+// Thread-local last error message; returns `code` for convenience.
+int set_error(int code, const char *fmt, ...);
+const char *last_error();
+int cuda_fail(cudaError_t e, const char *what);
+
+#define FRMC_CUDA(call)                                  \
+    do {                                                 \
+        cudaError_t _e = (call);                         \
+        if (_e != cudaSuccess) return ::frmc::cuda_fail(_e, #call); \
+    } while (0)
+
+// A device allocation that only grows.
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    int ensure(size_t bytes);
+    template <class T>
+    T *as() const { return static_cast<T *>(p); }
+};
+
+// Roles of the drop-in path's device buffers.
+enum BufRole {
+    BUF_COORDS = 0,
+    BUF_EL,
+    BUF_MOL,
+    BUF_ATOMS4,
+    BUF_ROWS,
+    BUF_COUNTS,
+    BUF_OUT,
+    BUF_AUX0,
+    BUF_AUX1,
+    BUF_AUX2,
+    BUF_STATUS,
+    BUF_COUNT_
+};
+
+struct Context {
+    int device = -1;
+    int sms = 0;
+    int max_smem_optin = 0;
+    cudaStream_t stream = nullptr;
+    std::mutex mu;  // serialises host-buffer entry points on this device
+    DevBuf buf[BUF_COUNT_];
+};
+
+// Context of the current device (created on first use).
+int get_context(Context **out);
+
+// Basis shape from the exact zero pattern of B (row-major, rows = vectors).
+int basis_mode(const float *B, int isPBC);
+Basis make_basis(const float *B);
+
+// Squared-distance limits: for d = sqrtf(s) (IEEE),
+//   d >= minD  <=>  s >= s_lo      and      d < maxD  <=>  s < s_hi.
+void sq_limits(float minD, float maxD, float *s_lo, float *s_hi);
+
+// ---------------------------------------------------------------- launchers
+struct FullTune {
+    int threads = 512;  // CTA size
+    int rows = 2;       // row atoms per thread (tile = threads * rows)
+    int queued = -1;    // -1: choose from the expected acceptance
+    int qcap = 16;      // queue slots per thread
+    int ctas_per_sm = 1;
+    double min_pairs_tiled = 8.0e6;
+};
+
+// All-pairs (i < j) histogram of `n` packed atoms (x, y, z, el bits) into
+// uint32 counts intra[total], inter[total] (total = ne*ne*hs), which must be
+// zeroed by the caller.
+int launch_full_hist(const float4 *atoms, const int *mol, int n, int bm, const Basis &B, float minD, float maxD,
+                     float binw, int ne, int hs, unsigned *intra, unsigned *inter, uint32_t *status,
+                     double accept_fraction, const FullTune *tune, cudaStream_t st, long long item_begin = 0,
+                     long long item_end = -1);
+// Number of work items of the all-pairs kernel for n atoms under `tune`.
+long long full_hist_items(int n, const FullTune *tune);
+
+// Rows (explicit atom indexes, or explicit coordinates) against every column
+// atom j in [start, n), j != row atom.  Counts are added with global atomics.
+int launch_rows_hist(const float *coords, const int *el, const int *mol, int n, const int *rows, int K,
+                     int allAtoms, int bm, const Basis &B, float minD, float maxD, float binw, int ne, int hs,
+                     unsigned *intra, unsigned *inter, cudaStream_t st);
+
+// Histogram of given distances: dists is (n, K) row-major, column k holds the
+// distances of atom rows[k].
+int launch_dists_hist(const float *dists, int n, int K, const int *rows, const int *el, const int *mol,
+                      int allAtoms, float minD, float maxD, float binw, int ne, int hs, unsigned *intra,
+                      unsigned *inter, cudaStream_t st);
+
+// out[k] = h0[k] + 1.0f added counts[k] times in float32 (h0 may be null = 0).
+int launch_counts_to_f32(const unsigned *counts, const float *h0, float *out, int64_t total, cudaStream_t st);
+
+// Pack AoS coordinates and element indexes into float4 (x, y, z, el bits).
+int launch_pack_atoms(const float *coords, const int *el, int n, float4 *out, cudaStream_t st);
+
+}  // namespace frmc

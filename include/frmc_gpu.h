@@ -1,0 +1,189 @@
+/*
+ * frmc_gpu.h -- C ABI of the GB300 (sm_103a) pair-distance / histogram library.
+ *
+ * The library replaces fullrmc's Cython modules fullrmc.Core.pairs_distances,
+ * fullrmc.Core.pairs_histograms and fullrmc.Core.reciprocal_space.  Every
+ * entry point below names the reference function it stands in for
+ * (path:line inside the fullrmc source tree).  A thin ctypes layer
+ * (fullrmc_gb300/pairs_*.py) gives them the reference's Python signatures.
+ *
+ * Conventions
+ *   - Plain pointers and sizes; no framework types.  int return: 0 on
+ *     success, a negative FRMC_E_* code otherwise; frmc_last_error() returns
+ *     the thread's last message.
+ *   - "Host" entry points take host memory, copy to the current CUDA device,
+ *     compute and copy back before returning (the drop-in path).  They keep no
+ *     host data between calls.
+ *   - "frmc_dev_*" entry points take device pointers and a cudaStream_t
+ *     (passed as void*, NULL = the library's stream) and return without
+ *     synchronising.
+ *   - Coordinates are float32 (n, 3) row-major; basis is float32 (3, 3)
+ *     row-major with the box vectors as rows (real = box . basis).
+ *   - Histograms are float32 C-contiguous (ne, ne, hs); counts are uint32.
+ *   - Arithmetic is bit-identical to the reference's float32 order; where the
+ *     reference's behaviour is undefined (indexes outside [0, n), arrays
+ *     shorter than n) these functions return FRMC_E_ARG instead.
+ */
+#ifndef FRMC_GPU_H
+#define FRMC_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+#define FRMC_OK 0
+#define FRMC_E_ARG (-1)     /* invalid argument (maps to ValueError)      */
+#define FRMC_E_CUDA (-2)    /* CUDA runtime error                         */
+#define FRMC_E_NOMEM (-3)   /* device allocation failed (MemoryError)     */
+#define FRMC_E_NODEV (-4)   /* no CUDA device                             */
+#define FRMC_E_TIMEOUT (-5) /* a bounded device wait gave up              */
+#define FRMC_E_STATE (-6)   /* object in the wrong state for this call    */
+#define FRMC_E_INDEX (-7)   /* index out of range (maps to IndexError)    */
+
+/* ---------------------------------------------------------------- runtime */
+int frmc_version(void);
+const char *frmc_last_error(void);
+/* Select the CUDA device used by later calls from this thread. */
+int frmc_set_device(int device);
+/* Number of SMs and the opt-in shared-memory limit of the current device. */
+int frmc_device_info(int *sms, int *max_smem_optin, int *cc_major, int *cc_minor);
+
+/* Host-only helpers (no device needed).  Exact squared-distance limits: for
+ * d = sqrtf(s) correctly rounded, d >= minDistance <=> s >= *s_lo and
+ * d < maxDistance <=> s < *s_hi (the kernels test s, and take the IEEE sqrt
+ * and division of pairs_histograms.pyx:63 only for accepted pairs). */
+int frmc_sq_limits(float minDistance, float maxDistance, float *s_lo, float *s_hi);
+/* Basis shape used to drop exactly-zero basis terms: 0 infinite boundary
+ * conditions, 1 diagonal, 2 (a||x, b in xy, c||z), 3 lower triangular,
+ * 4 general. */
+int frmc_basis_mode(const float *basis, int isPBC);
+
+/* --------------------------------------------------- pairs_distances (host)
+ * Extensions/pairs_distances.pyx:874-916 pairs_distances_to_indexcoords:
+ * distances[i] = d(coords[atomIndex], coords[i]) for i in [start, n), start =
+ * allAtoms ? 0 : atomIndex; entries below start are left untouched. */
+int frmc_pairs_distances_to_indexcoords(int32_t atomIndex, const float *coords, int64_t n, const float *basis,
+                                        int isPBC, int allAtoms, float *distances);
+/* pairs_distances.pyx:827-866 pairs_distances_to_point. */
+int frmc_pairs_distances_to_point(const float *point, const float *coords, int64_t n, const float *basis, int isPBC,
+                                  float *distances);
+/* pairs_distances.pyx:924-966 pairs_distances_to_multi_points: point k is
+ * (points[0*ps+k], points[1*ps+k], points[2*ps+k]) -- the reference reads
+ * points[:, k]; distances is (n, K) row-major. */
+int frmc_pairs_distances_to_multi_points(const float *points, int64_t ps, int64_t K, const float *coords, int64_t n,
+                                         const float *basis, int isPBC, float *distances);
+/* pairs_distances.pyx:975-1021 pairs_distances_to_multi_indexcoords:
+ * distances (n, K); rows below indexes[k] untouched when !allAtoms. */
+int frmc_pairs_distances_to_multi_indexcoords(const int32_t *indexes, int64_t K, const float *coords, int64_t n,
+                                              const float *basis, int isPBC, int allAtoms, float *distances);
+/* pairs_distances.pyx:786-819 point_to_point_distance. */
+int frmc_point_to_point_distance(const float *point1, const float *point2, const float *basis, int isPBC,
+                                 float *distance);
+/* pairs_distances.pyx:483-521 from_to_points_differences: out[i] = bc(to[i] - from[i]). */
+int frmc_from_to_points_differences(const float *pointsFrom, const float *pointsTo, int64_t n, const float *basis,
+                                    int isPBC, float *differences);
+/* pairs_distances.pyx:529-561 pair_difference_to_point: out = bc(point2 - point1). */
+int frmc_pair_difference_to_point(const float *point1, const float *point2, const float *basis, int isPBC,
+                                  float *difference);
+/* pairs_distances.pyx:569-607 pairs_differences_to_point: out[i] = bc(point - coords[i]). */
+int frmc_pairs_differences_to_point(const float *point, const float *coords, int64_t n, const float *basis,
+                                    int isPBC, float *differences);
+/* pairs_distances.pyx:615-654 pairs_differences_to_indexcoords. */
+int frmc_pairs_differences_to_indexcoords(int32_t atomIndex, const float *coords, int64_t n, const float *basis,
+                                          int isPBC, int allAtoms, float *differences);
+/* pairs_distances.pyx:662-711 pairs_differences_to_multi_points: out (n, 3, K). */
+int frmc_pairs_differences_to_multi_points(const float *points, int64_t ps, int64_t K, const float *coords,
+                                           int64_t n, const float *basis, int isPBC, float *differences);
+/* pairs_distances.pyx:719-774 pairs_differences_to_multi_indexcoords: out (n, 3, K). */
+int frmc_pairs_differences_to_multi_indexcoords(const int32_t *indexes, int64_t K, const float *coords, int64_t n,
+                                                const float *basis, int isPBC, int allAtoms, float *differences);
+
+/* -------------------------------------------------- pairs_histograms (host)
+ * Extensions/pairs_histograms.pyx:77-141 single_pairs_histograms: adds the
+ * counts of atom atomIndex's distance row to hintra/hinter (ne, ne, hs) in
+ * place, with float32 additions of 1.0 (saturating at 2^24 like the
+ * reference). */
+int frmc_single_pairs_histograms(int32_t atomIndex, const float *distances, int64_t n, const int32_t *moleculeIndex,
+                                 const int32_t *elementIndex, int32_t ne, int32_t hs, float *hintra, float *hinter,
+                                 float minDistance, float maxDistance, float bin, int allAtoms);
+/* pairs_histograms.pyx:150-217 multiple_pairs_histograms_coords: hintra and
+ * hinter (ne, ne, hs) are overwritten. */
+int frmc_multiple_pairs_histograms_coords(const int32_t *indexes, int64_t K, const float *boxCoords, int64_t n,
+                                          const float *basis, int isPBC, const int32_t *moleculeIndex,
+                                          const int32_t *elementIndex, int32_t ne, float minDistance,
+                                          float maxDistance, float bin, int32_t hs, int allAtoms, float *hintra,
+                                          float *hinter);
+/* pairs_histograms.pyx:289-335 full_pairs_histograms_coords (all i < j). */
+int frmc_full_pairs_histograms_coords(const float *boxCoords, int64_t n, const float *basis, int isPBC,
+                                      const int32_t *moleculeIndex, const int32_t *elementIndex, int32_t ne,
+                                      float minDistance, float maxDistance, float bin, int32_t hs, float *hintra,
+                                      float *hinter);
+/* pairs_histograms.pyx:225-281 multiple_pairs_histograms_dists: distances is
+ * (n, K) row-major, column k belongs to atom indexes[k]. */
+int frmc_multiple_pairs_histograms_dists(const int32_t *indexes, int64_t K, const float *distances, int64_t n,
+                                         const int32_t *moleculeIndex, const int32_t *elementIndex, int32_t ne,
+                                         float minDistance, float maxDistance, float bin, int32_t hs, int allAtoms,
+                                         float *hintra, float *hinter);
+
+/* ---------------------------------------------- reciprocal space (host, FP64)
+ * Extensions/reciprocal_space.pyx:42-73 gr_to_sq:
+ *   sq[q] = 1 + 4 pi rho sum_r dr r sin(q r)/q (gr[r] - 1), dr = r[1] - r[0]. */
+int frmc_gr_to_sq(const float *distances, const float *gr, int64_t nr, const float *qrange, int64_t nq, double rho,
+                  double *sq);
+/* reciprocal_space.pyx:82-109 Gr_to_sq: sq[q] = 1 + sum_r dr sin(q r)/q Gr[r]. */
+int frmc_Gr_to_sq(const float *distances, const float *Gr, int64_t nr, const float *qrange, int64_t nq, double *sq);
+/* reciprocal_space.pyx:118-145 sq_to_Gr (the formula the reference intends;
+ * its own body raises TypeError):  Gr[r] = 2/pi sum_q q (sq[q] - 1) sin(q r) dq. */
+int frmc_sq_to_Gr(const float *qValues, int64_t nq, const float *rValues, int64_t nr, const float *sq, double *Gr);
+
+/* ------------------------------------- boundary_conditions_collection (host)
+ * Extensions/boundary_conditions_collection.pyx:88-110 transform_coordinates:
+ * out[i] = coords[i] . M (float32, reference order). */
+int frmc_transform_coordinates(const float *transMatrix, const float *coords, int64_t n, float *out);
+
+/* ------------------------------------------------ device-resident entry points
+ * Same computations on device buffers; counts are uint32 [2][ne][ne][hs]
+ * (index 0 = intra, 1 = inter) and are zeroed by the call.
+ *
+ * All-pairs histogram (full_pairs_histograms_coords, pairs_histograms.pyx:289-335)
+ * of atoms packed as float4 (x, y, z, element index bits). */
+int frmc_dev_full_hist_counts(const void *atoms4, const int32_t *moleculeIndex, int64_t n, const float *basis_host,
+                              int isPBC, int32_t ne, float minDistance, float maxDistance, float bin, int32_t hs,
+                              uint32_t *counts, void *stream);
+/* Tile configuration of the all-pairs kernel: threads per CTA, row atoms
+ * per thread (1 or 2), queued binning (-1 auto, 0 off, 1 on), queue slots per
+ * thread, CTAs per SM, and the pair count from which the host entry point
+ * frmc_full_pairs_histograms_coords uses it (below: the row kernel).  Applies
+ * to later calls from every thread. */
+int frmc_set_full_tune(int threads, int rows, int queued, int qcap, int ctas_per_sm, double min_pairs_tiled);
+/* The same all-pairs histogram restricted to work items [item_begin, item_end)
+ * of the kernel's (row tile, column tile) triangle, for sharding one system
+ * across devices; the per-item partial counts of disjoint ranges sum to the
+ * full counts.  frmc_full_items() gives the item count for n atoms. */
+int frmc_full_items(int64_t n, int64_t *nitems);
+int frmc_dev_full_hist_counts_range(const void *atoms4, const int32_t *moleculeIndex, int64_t n,
+                                    const float *basis_host, int isPBC, int32_t ne, float minDistance,
+                                    float maxDistance, float bin, int32_t hs, int64_t item_begin, int64_t item_end,
+                                    uint32_t *counts, void *stream);
+/* multiple_pairs_histograms_coords on device buffers (boxCoords (n, 3)). */
+int frmc_dev_multiple_hist_counts(const int32_t *indexes, int64_t K, const float *boxCoords, int64_t n,
+                                  const float *basis_host, int isPBC, const int32_t *moleculeIndex,
+                                  const int32_t *elementIndex, int32_t ne, float minDistance, float maxDistance,
+                                  float bin, int32_t hs, int allAtoms, uint32_t *counts, void *stream);
+/* Pack (n, 3) coordinates and element indexes into float4 (x, y, z, el bits). */
+int frmc_dev_pack_atoms(const float *coords, const int32_t *elementIndex, int64_t n, void *atoms4, void *stream);
+/* float32 histogram values of uint32 counts (sequential additions of 1.0f). */
+int frmc_dev_counts_to_f32(const uint32_t *counts, int64_t total, float *out, void *stream);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+#ifdef __cplusplus
+}
+#endif
+#endif /* FRMC_GPU_H */

@@ -1,0 +1,347 @@
+"""CPU oracle for the pair-distance / histogram path (test infrastructure).
+
+Two parts:
+
+* ``frmc_oracle.c`` -- a plain-C restatement of the reference's float32
+  per-pair arithmetic and histogram binning (``Extensions/pairs_distances.pyx``
+  and ``Extensions/pairs_histograms.pyx``), loaded here through ctypes and
+  exposed with the reference's Python signatures.  Compiled on first use into
+  ``oracle/_build/`` with ``gcc -ffp-contract=off``.
+* FP64 restatements (numpy float64) of the host-side reductions that turn the
+  histograms into G(r), g(r), S(Q) and chi-square:
+  ``Constraints/PairDistributionConstraints.py:847-895``,
+  ``Constraints/PairCorrelationConstraints.py:126-167``,
+  ``Constraints/StructureFactorConstraints.py:302-312,772-822``,
+  ``Core/Constraint.py:1363-1395`` and ``Extensions/reciprocal_space.pyx``.
+
+Only tests, the smoke check and the benchmark's CPU-baseline leg use this
+module; the CUDA library never calls it.
+
+Parity pin: the C restatement is checked bit-for-bit against golden vectors
+produced by the compiled reference Cython (``tests/golden/make_golden.py``).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_BUILD = os.path.join(HERE, "_build")
+_SO = os.path.join(_BUILD, "libfrmc_oracle.so")
+_SRC = os.path.join(HERE, "frmc_oracle.c")
+_lock = threading.Lock()
+_lib = None
+
+F32P = ctypes.POINTER(ctypes.c_float)
+I32P = ctypes.POINTER(ctypes.c_int32)
+i64 = ctypes.c_int64
+i32 = ctypes.c_int32
+f32 = ctypes.c_float
+cint = ctypes.c_int
+
+
+def build() -> str:
+    """Compile the C oracle (idempotent)."""
+    os.makedirs(_BUILD, exist_ok=True)
+    if not os.path.exists(_SO) or os.path.getmtime(_SO) < os.path.getmtime(_SRC):
+        tmp = _SO + ".tmp%d" % os.getpid()
+        subprocess.run(["gcc", "-O2", "-fPIC", "-shared", "-ffp-contract=off",
+                        "-fno-fast-math", "-o", tmp, _SRC, "-lm"], check=True)
+        os.replace(tmp, _SO)
+    return _SO
+
+
+def _load():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            lib = ctypes.CDLL(_SO)
+            sig = {
+                "oracle_distances_to_indexcoords": [i32, F32P, i64, F32P, cint, cint, F32P],
+                "oracle_distances_to_point": [F32P, F32P, i64, F32P, cint, F32P],
+                "oracle_distances_to_multi_points": [F32P, i64, i64, F32P, i64, F32P, cint, F32P],
+                "oracle_distances_to_multi_indexcoords": [I32P, i64, F32P, i64, F32P, cint, cint, F32P],
+                "oracle_point_to_point_distance": [F32P, F32P, F32P, cint],
+                "oracle_from_to_points_differences": [F32P, F32P, i64, F32P, cint, F32P],
+                "oracle_pair_difference_to_point": [F32P, F32P, F32P, cint, F32P],
+                "oracle_differences_to_point": [F32P, F32P, i64, F32P, cint, F32P],
+                "oracle_differences_to_indexcoords": [i32, F32P, i64, F32P, cint, cint, F32P],
+                "oracle_differences_to_multi_points": [F32P, i64, i64, F32P, i64, F32P, cint, F32P],
+                "oracle_differences_to_multi_indexcoords": [I32P, i64, F32P, i64, F32P, cint, cint, F32P],
+                "oracle_single_pairs_histograms": [i32, F32P, i64, I32P, I32P, i32, i32, F32P, F32P, f32, f32, f32, cint],
+                "oracle_multiple_pairs_histograms_coords": [I32P, i64, F32P, i64, F32P, cint, I32P, I32P, i32, f32, f32, f32, i32, cint, F32P, F32P],
+                "oracle_full_pairs_histograms_coords": [F32P, i64, F32P, cint, I32P, I32P, i32, f32, f32, f32, i32, F32P, F32P],
+                "oracle_multiple_pairs_histograms_dists": [I32P, i64, F32P, i64, I32P, I32P, i32, f32, f32, f32, i32, cint, F32P, F32P],
+                "oracle_transform_coordinates": [F32P, F32P, i64, F32P],
+            }
+            for name, args in sig.items():
+                fn = getattr(lib, name)
+                fn.argtypes = args
+                fn.restype = f32 if name == "oracle_point_to_point_distance" else None
+            _lib = lib
+    return _lib
+
+
+def _f(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _i(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _p(a, t=F32P):
+    return a.ctypes.data_as(t)
+
+
+# ------------------------------------------------------------------ distances
+def pairs_distances_to_indexcoords(atomIndex, coords, basis, isPBC, allAtoms=True, ncores=1):
+    c, b = _f(coords), _f(basis)
+    out = np.zeros((c.shape[0],), np.float32)
+    _load().oracle_distances_to_indexcoords(int(atomIndex), _p(c), c.shape[0], _p(b), int(bool(isPBC)), int(bool(allAtoms)), _p(out))
+    return out
+
+
+def pairs_distances_to_point(point, coords, basis, isPBC, ncores=1):
+    p, c, b = _f(point), _f(coords), _f(basis)
+    out = np.empty((c.shape[0],), np.float32)
+    _load().oracle_distances_to_point(_p(p), _p(c), c.shape[0], _p(b), int(bool(isPBC)), _p(out))
+    return out
+
+
+def pairs_distances_to_multi_points(points, coords, basis, isPBC, ncores=1):
+    p, c, b = _f(points), _f(coords), _f(basis)
+    K = p.shape[1]
+    out = np.empty((c.shape[0], K), np.float32)
+    _load().oracle_distances_to_multi_points(_p(p), K, K, _p(c), c.shape[0], _p(b), int(bool(isPBC)), _p(out))
+    return out
+
+
+def pairs_distances_to_multi_indexcoords(indexes, coords, basis, isPBC, allAtoms=True, ncores=1):
+    ix, c, b = _i(indexes), _f(coords), _f(basis)
+    out = np.zeros((c.shape[0], ix.shape[0]), np.float32)
+    _load().oracle_distances_to_multi_indexcoords(_p(ix, I32P), ix.shape[0], _p(c), c.shape[0], _p(b), int(bool(isPBC)), int(bool(allAtoms)), _p(out))
+    return out
+
+
+def point_to_point_distance(point1, point2, basis, isPBC, ncores=1):
+    p1, p2, b = _f(point1), _f(point2), _f(basis)
+    return _load().oracle_point_to_point_distance(_p(p1), _p(p2), _p(b), int(bool(isPBC)))
+
+
+# ---------------------------------------------------------------- differences
+def from_to_points_differences(pointsFrom, pointsTo, basis, isPBC, ncores=1):
+    a, t, b = _f(pointsFrom), _f(pointsTo), _f(basis)
+    out = np.empty((a.shape[0], 3), np.float32)
+    _load().oracle_from_to_points_differences(_p(a), _p(t), a.shape[0], _p(b), int(bool(isPBC)), _p(out))
+    return out
+
+
+def pair_difference_to_point(point1, point2, basis, isPBC, ncores=1):
+    p1, p2, b = _f(point1), _f(point2), _f(basis)
+    out = np.empty((3,), np.float32)
+    _load().oracle_pair_difference_to_point(_p(p1), _p(p2), _p(b), int(bool(isPBC)), _p(out))
+    return out
+
+
+def pairs_differences_to_point(point, coords, basis, isPBC, ncores=1):
+    p, c, b = _f(point), _f(coords), _f(basis)
+    out = np.empty((c.shape[0], 3), np.float32)
+    _load().oracle_differences_to_point(_p(p), _p(c), c.shape[0], _p(b), int(bool(isPBC)), _p(out))
+    return out
+
+
+def pairs_differences_to_indexcoords(atomIndex, coords, basis, isPBC, allAtoms=True, ncores=1):
+    c, b = _f(coords), _f(basis)
+    out = np.zeros((c.shape[0], 3), np.float32)
+    _load().oracle_differences_to_indexcoords(int(atomIndex), _p(c), c.shape[0], _p(b), int(bool(isPBC)), int(bool(allAtoms)), _p(out))
+    return out
+
+
+def pairs_differences_to_multi_points(points, coords, basis, isPBC, ncores=1):
+    p, c, b = _f(points), _f(coords), _f(basis)
+    K = p.shape[1]
+    out = np.empty((c.shape[0], 3, K), np.float32)
+    _load().oracle_differences_to_multi_points(_p(p), K, K, _p(c), c.shape[0], _p(b), int(bool(isPBC)), _p(out))
+    return out
+
+
+def pairs_differences_to_multi_indexcoords(indexes, coords, basis, isPBC, allAtoms=True, ncores=1):
+    ix, c, b = _i(indexes), _f(coords), _f(basis)
+    out = np.zeros((c.shape[0], 3, ix.shape[0]), np.float32)
+    _load().oracle_differences_to_multi_indexcoords(_p(ix, I32P), ix.shape[0], _p(c), c.shape[0], _p(b), int(bool(isPBC)), int(bool(allAtoms)), _p(out))
+    return out
+
+
+# ----------------------------------------------------------------- histograms
+def single_pairs_histograms(atomIndex, distances, moleculeIndex, elementIndex, hintra, hinter,
+                            minDistance, maxDistance, bin, allAtoms=True, ncores=1):
+    d, m, e = _f(distances), _i(moleculeIndex), _i(elementIndex)
+    assert hintra.flags.c_contiguous and hintra.dtype == np.float32
+    assert hinter.flags.c_contiguous and hinter.dtype == np.float32
+    ne, hs = hintra.shape[0], hintra.shape[2]
+    _load().oracle_single_pairs_histograms(int(atomIndex), _p(d), d.shape[0], _p(m, I32P), _p(e, I32P), ne, hs,
+                                           _p(hintra), _p(hinter), np.float32(minDistance), np.float32(maxDistance),
+                                           np.float32(bin), int(bool(allAtoms)))
+
+
+def multiple_pairs_histograms_coords(indexes, boxCoords, basis, isPBC, moleculeIndex, elementIndex,
+                                     numberOfElements, minDistance, maxDistance, bin, histSize,
+                                     allAtoms=True, ncores=1):
+    ix, c, b, m, e = _i(indexes), _f(boxCoords), _f(basis), _i(moleculeIndex), _i(elementIndex)
+    ne, hs = int(numberOfElements), int(histSize)
+    hi = np.zeros((ne, ne, hs), np.float32)
+    he = np.zeros((ne, ne, hs), np.float32)
+    _load().oracle_multiple_pairs_histograms_coords(_p(ix, I32P), ix.shape[0], _p(c), c.shape[0], _p(b), int(bool(isPBC)),
+                                                    _p(m, I32P), _p(e, I32P), ne, np.float32(minDistance),
+                                                    np.float32(maxDistance), np.float32(bin), hs, int(bool(allAtoms)),
+                                                    _p(hi), _p(he))
+    return hi, he
+
+
+def full_pairs_histograms_coords(boxCoords, basis, isPBC, moleculeIndex, elementIndex, numberOfElements,
+                                 minDistance, maxDistance, bin, histSize, ncores=1):
+    c, b, m, e = _f(boxCoords), _f(basis), _i(moleculeIndex), _i(elementIndex)
+    ne, hs = int(numberOfElements), int(histSize)
+    hi = np.zeros((ne, ne, hs), np.float32)
+    he = np.zeros((ne, ne, hs), np.float32)
+    _load().oracle_full_pairs_histograms_coords(_p(c), c.shape[0], _p(b), int(bool(isPBC)), _p(m, I32P), _p(e, I32P), ne,
+                                                np.float32(minDistance), np.float32(maxDistance), np.float32(bin), hs,
+                                                _p(hi), _p(he))
+    return hi, he
+
+
+def multiple_pairs_histograms_dists(indexes, distances, moleculeIndex, elementIndex, numberOfElements,
+                                    minDistance, maxDistance, bin, histSize, allAtoms=True, ncores=1):
+    ix, d, m, e = _i(indexes), _f(distances), _i(moleculeIndex), _i(elementIndex)
+    ne, hs = int(numberOfElements), int(histSize)
+    hi = np.zeros((ne, ne, hs), np.float32)
+    he = np.zeros((ne, ne, hs), np.float32)
+    assert d.shape[1] >= ix.shape[0]
+    # the reference reads column i of `distances` for indexes[i]
+    dk = np.ascontiguousarray(d[:, :ix.shape[0]])
+    _load().oracle_multiple_pairs_histograms_dists(_p(ix, I32P), ix.shape[0], _p(dk), dk.shape[0], _p(m, I32P),
+                                                   _p(e, I32P), ne, np.float32(minDistance), np.float32(maxDistance),
+                                                   np.float32(bin), hs, int(bool(allAtoms)), _p(hi), _p(he))
+    return hi, he
+
+
+def full_pairs_histograms_dists(distances, moleculeIndex, elementIndex, numberOfElements, minDistance,
+                                maxDistance, bin, histSize, ncores=1):
+    d = _f(distances)
+    ix = np.arange(d.shape[1], dtype=np.int32)
+    return multiple_pairs_histograms_dists(ix, d, moleculeIndex, elementIndex, numberOfElements, minDistance,
+                                           maxDistance, bin, histSize, allAtoms=False)
+
+
+def transform_coordinates(transMatrix, coords):
+    M, c = _f(transMatrix), _f(coords)
+    out = np.empty((c.shape[0], 3), np.float32)
+    _load().oracle_transform_coordinates(_p(M), _p(c), c.shape[0], _p(out))
+    return out
+
+
+# ----------------------------------------------------------- FP64 reductions
+def pair_density_terms(elementsCount, weights):
+    """Per unordered species pair (i <= j): (i, j, w_ij, N_ij).
+
+    ``N_ij = n_i (n_i - 1) / 2`` for i == j and ``n_i n_j`` otherwise,
+    ``Constraints/PairDistributionConstraints.py:864-878``.  ``weights`` is a
+    symmetric (ne, ne) array of w_ij."""
+    ne = len(elementsCount)
+    out = []
+    for i in range(ne):
+        for j in range(i, ne):
+            ni, nj = float(elementsCount[i]), float(elementsCount[j])
+            Nij = ni * (ni - 1.0) / 2.0 if i == j else ni * nj
+            out.append((i, j, float(weights[i][j]), Nij))
+    return out
+
+
+def pair_counts_fp64(intra, inter, i, j):
+    """n_ij(r): PairDistributionConstraints.py:869,875."""
+    intra = np.asarray(intra, np.float64)
+    inter = np.asarray(inter, np.float64)
+    if i == j:
+        return intra[i, i] + inter[i, i]
+    return intra[i, j] + intra[j, i] + inter[i, j] + inter[j, i]
+
+
+def total_gr_fp64(intra, inter, elementsCount, weights, volume, shellVolumes):
+    """g(r) = sum_ij w_ij n_ij / (N_ij / V) / v(r): PairDistributionConstraints.py:859-881
+    (the same weighted sum is PairCorrelationConstraints.py:130-152)."""
+    hs = np.asarray(intra).shape[2]
+    g = np.zeros(hs, np.float64)
+    for i, j, w, Nij in pair_density_terms(elementsCount, weights):
+        g += w * pair_counts_fp64(intra, inter, i, j) / (Nij / float(volume))
+    return g / np.asarray(shellVolumes, np.float64)
+
+
+def total_Gr_fp64(intra, inter, elementsCount, weights, volume, shellVolumes, shellCenters, rho0):
+    """G(r) = 4 pi r rho0 (g(r) - 1): PairDistributionConstraints.py:881-884."""
+    g = total_gr_fp64(intra, inter, elementsCount, weights, volume, shellVolumes)
+    r = np.asarray(shellCenters, np.float64)
+    return (4.0 * np.pi * r * float(rho0)) * (g - 1.0)
+
+
+def gr2sq_matrix_fp64(shellCenters, qValues):
+    """M[r, q] = dr sin(q r) / q: StructureFactorConstraints.py:302-312."""
+    r = np.asarray(shellCenters, np.float64)
+    q = np.asarray(qValues, np.float64)
+    dr = r[1] - r[0]
+    return dr * np.sin(np.outer(r, q)) / q
+
+
+def sq_from_Gr_fp64(Gr, matrix, reduced=False):
+    """S(q) = sum_r G(r) M[r, q] + 1: StructureFactorConstraints.py:772-773
+    (ReducedStructureFactorConstraint drops the +1, :1255-1256)."""
+    s = np.asarray(Gr, np.float64) @ np.asarray(matrix, np.float64)
+    return s if reduced else s + 1.0
+
+
+def standard_error_fp64(experimental, model, dataWeights=None):
+    """sum w (exp - model)^2: PairDistributionConstraints.py:810-838."""
+    diff = np.asarray(experimental, np.float64) - np.asarray(model, np.float64)
+    if dataWeights is None:
+        return float(np.sum(diff * diff))
+    return float(np.sum(np.asarray(dataWeights, np.float64) * diff * diff))
+
+
+def fit_scale_factor_fp64(experimental, model, dataWeights=None, lo=0.0, hi=np.inf):
+    """sum(w m e) / sum(m^2), clamped: Core/Constraint.py:1363-1395."""
+    e = np.asarray(experimental, np.float64)
+    m = np.asarray(model, np.float64)
+    num = np.sum(m * e) if dataWeights is None else np.sum(np.asarray(dataWeights, np.float64) * m * e)
+    sf = num / np.sum(m * m)
+    return float(min(max(sf, lo), hi))
+
+
+def gr_to_sq_fp64(distances, gr, qrange, rho):
+    """reciprocal_space.pyx:42-73 in float64."""
+    r = np.asarray(distances, np.float64)
+    q = np.asarray(qrange, np.float64)
+    dr = r[1] - r[0]
+    fact = 4.0 * np.pi * float(rho)
+    return 1.0 + fact * ((dr * r * (np.asarray(gr, np.float64) - 1.0)) @ (np.sin(np.outer(r, q)) / q))
+
+
+def Gr_to_sq_fp64(distances, Gr, qrange):
+    """reciprocal_space.pyx:82-109 in float64."""
+    r = np.asarray(distances, np.float64)
+    q = np.asarray(qrange, np.float64)
+    dr = r[1] - r[0]
+    return 1.0 + (dr * np.asarray(Gr, np.float64)) @ (np.sin(np.outer(r, q)) / q)
+
+
+def sq_to_Gr_fp64(qValues, rValues, sq):
+    """reciprocal_space.pyx:118-145 in float64."""
+    q = np.asarray(qValues, np.float64)
+    r = np.asarray(rValues, np.float64)
+    dq = q[1] - q[0]
+    qs = q * (np.asarray(sq, np.float64) - 1.0)
+    return (2.0 / np.pi) * (np.sin(np.outer(r, q)) * dq) @ qs

@@ -1,0 +1,232 @@
+"""Generate the golden vectors from the compiled reference Cython.
+
+Run in a checkout that has the reference sources (``python
+tests/golden/make_golden.py``): it builds ``oracle/_ref`` if needed, imports
+the reference's own ``fullrmc.Core.pairs_distances``,
+``fullrmc.Core.pairs_histograms`` and ``fullrmc.Core.reciprocal_space``
+(always with ``ncores=1``; the reference's OpenMP histogram loop increments
+shared bins without a reduction) and writes ``tests/golden/*.npz``.  Every
+input is seeded, so the files are reproducible.  The reference ships no test
+vectors of its own, so these files pin both the C oracle and the CUDA
+library.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+F = np.float32
+
+
+def triclinic_basis(a, b, c, alpha, beta, gamma):
+    """Row-vector basis: a along x, b in the xy plane (float32)."""
+    al, be, ga = np.radians([alpha, beta, gamma])
+    cx = c * np.cos(be)
+    cy = c * (np.cos(al) - np.cos(be) * np.cos(ga)) / np.sin(ga)
+    cz = np.sqrt(c * c - cx * cx - cy * cy)
+    B = np.array([[a, 0, 0], [b * np.cos(ga), b * np.sin(ga), 0], [cx, cy, cz]], np.float64)
+    B[np.abs(B) < 1e-9] = 0.0
+    return B.astype(F)
+
+
+def grid(rmax, dr=0.01):
+    """fullrmc's limits from an experimental r grid (PairDistributionConstraints.py:726,745-755)."""
+    x = np.arange(0, rmax + dr / 10, dr).astype(F)
+    b = F(x[1] - x[0])
+    return F(x[0] - b / 2.0), F(x[-1] + b / 2.0), b, np.int32(len(x))
+
+
+def species(rng, n, fractions):
+    counts = np.floor(np.asarray(fractions) * n).astype(int)
+    counts[0] += n - counts.sum()
+    el = np.repeat(np.arange(len(fractions)), counts).astype(np.int32)
+    rng.shuffle(el)
+    return el
+
+
+def main():
+    import build_ref
+    build_ref.build()
+    R = build_ref.import_reference()
+    ph, pd, rs = R["pairs_histograms"], R["pairs_distances"], R["reciprocal_space"]
+    bcc = R["boundary_conditions_collection"]
+    out = {}
+
+    def hist_case(name, coords, basis, isPBC, mol, el, ne, lims, groups):
+        mn, mx, b, hs = lims
+        d = dict(coords=coords, basis=basis, isPBC=np.int32(isPBC), mol=mol, el=el, ne=np.int32(ne),
+                 minD=mn, maxD=mx, bin=b, hs=hs)
+        hi, he = ph.full_pairs_histograms_coords(coords, basis, isPBC, mol, el, ne, mn, mx, b, hs, 1)
+        d["full_intra"], d["full_inter"] = hi, he
+        for gi, (idx, allAtoms) in enumerate(groups):
+            hi, he = ph.multiple_pairs_histograms_coords(idx, coords, basis, isPBC, mol, el, ne, mn, mx, b, hs,
+                                                         allAtoms, 1)
+            d["g%d_indexes" % gi] = idx
+            d["g%d_allAtoms" % gi] = np.int32(allAtoms)
+            d["g%d_intra" % gi], d["g%d_inter" % gi] = hi, he
+        out[name] = d
+
+    # A: cubic PBC, binary alloy (config-1 shape, smaller N), atomic molecules.
+    rng = np.random.default_rng(101)
+    n = 2000
+    L = F(38.2 * (n / 5000.0) ** (1 / 3.0))
+    hist_case("cubic_pbc_ne2", rng.random((n, 3)).astype(F), np.diag([L, L, L]).astype(F), True,
+              np.arange(n, dtype=np.int32), species(rng, n, [0.5, 0.5]), 2, grid(15.0),
+              [(np.array([17], np.int32), True), (np.array([5, 900, 1999], np.int32), True),
+               (np.array([0, 3, 1500], np.int32), False)])
+
+    # B: triclinic gamma=120 (config-2 shape, smaller N), 3 species 0.5/0.3/0.2.
+    rng = np.random.default_rng(202)
+    n = 3000
+    a = F((n / 0.1057 / np.sin(np.radians(120))) ** (1 / 3.0))
+    hist_case("triclinic120_ne3", rng.random((n, 3)).astype(F), triclinic_basis(a, a, a, 90, 90, 120), True,
+              np.arange(n, dtype=np.int32), species(rng, n, [0.5, 0.3, 0.2]), 3, grid(10.0),
+              [(np.array([1234], np.int32), True)])
+
+    # C: general triclinic, 4 species, 13-atom molecules (non-empty intra).
+    rng = np.random.default_rng(303)
+    nm, k = 100, 13
+    n = nm * k
+    B = triclinic_basis(26.0, 24.0, 25.0, 78.0, 95.0, 110.0)
+    centres = rng.random((nm, 3))
+    offs = rng.normal(scale=0.04, size=(n, 3))
+    coords = (np.repeat(centres, k, axis=0) + offs).astype(F)
+    mol = np.repeat(np.arange(nm), k).astype(np.int32)
+    el = np.tile(np.array([0, 0, 0, 0, 1, 2, 2, 2, 2, 3, 3, 3, 3]), nm).astype(np.int32)
+    hist_case("general_triclinic_ne4_mol", coords, B, True, mol, el, 4, grid(12.0),
+              [(np.arange(13 * 7, 13 * 8, dtype=np.int32), True), (np.arange(13 * 7, 13 * 8, dtype=np.int32), False),
+               (np.array([], np.int32), True)])
+
+    # D: infinite boundary conditions (real coordinates), 2 species, molecules of 3.
+    rng = np.random.default_rng(404)
+    n = 1000
+    hist_case("ibc_ne2", (rng.random((n, 3)) * 30.0).astype(F), np.eye(3, dtype=F), False,
+              (np.arange(n) // 3).astype(np.int32), species(rng, n, [0.6, 0.4]), 2, grid(15.0),
+              [(np.array([10, 11, 12], np.int32), True)])
+
+    # E: bin overflow.  d = 15.004999f < max = 15.005f but (d - min) / bin
+    # rounds to 1501 == hs, so the count lands in bin 0 of the next row.
+    mn, mx, b, hs = grid(15.0)
+    dov = F(15.004999)
+    assert dov < mx and int((dov - mn) / b) == hs
+    coords = np.array([[0, 0, 0], [dov, 0, 0], [0, dov, 0], [0, 0, 60.0], [3.25, 60.0, 0]], F)
+    el = np.array([0, 0, 1, 1, 0], np.int32)
+    # pairs (0,1): [0][0] -> [0][1][0]; (0,2): [0][1] -> [1][0][0]; (1,2) d=21.2 > max;
+    # atom 3 and 4 are beyond max from everyone except each other (d>max) -> no
+    # out-of-array write can occur.
+    hist_case("bin_overflow_ibc", coords, np.eye(3, dtype=F), False, np.arange(5, dtype=np.int32), el, 2,
+              (mn, mx, b, hs), [(np.array([0], np.int32), True), (np.array([2, 1], np.int32), True)])
+
+    # F: bin edges: atoms at exact float32 bin edges and their neighbours.
+    mn, mx, b, hs = grid(5.0)
+    edges = np.array([F(mn + F(i) * b) for i in range(1, hs, 37)], F)
+    pos = np.concatenate([edges, np.nextafter(edges, F(100)), np.nextafter(edges, F(-100))])
+    coords = np.zeros((pos.size + 1, 3), F)
+    coords[1:, 0] = pos
+    n = coords.shape[0]
+    hist_case("bin_edges_ibc", coords, np.eye(3, dtype=F), False, np.arange(n, dtype=np.int32),
+              (np.arange(n) % 2).astype(np.int32), 2, (mn, mx, b, hs), [(np.array([0], np.int32), True)])
+
+    # G: float32 saturation: 6000 coincident atoms -> 17,997,000 increments of
+    # one bin; a float32 counter stops at 2**24.
+    n = 6000
+    coords = np.zeros((n, 3), F)
+    mn, mx, b, hs = grid(1.0)
+    hi, he = ph.full_pairs_histograms_coords(coords, np.eye(3, dtype=F), False, np.arange(n, dtype=np.int32),
+                                             np.zeros(n, np.int32), 1, mn, mx, b, hs, 1)
+    out["saturation"] = dict(n=np.int32(n), minD=mn, maxD=mx, bin=b, hs=hs, full_intra=hi, full_inter=he)
+
+    # H: edge sizes: one atom, zero atoms.
+    for nn in (0, 1):
+        coords = np.zeros((nn, 3), F)
+        mn, mx, b, hs = grid(3.0)
+        hi, he = ph.full_pairs_histograms_coords(coords, np.eye(3, dtype=F), True, np.zeros(nn, np.int32),
+                                                 np.zeros(nn, np.int32), 2, mn, mx, b, hs, 1)
+        out["tiny_n%d" % nn] = dict(n=np.int32(nn), minD=mn, maxD=mx, bin=b, hs=hs, full_intra=hi, full_inter=he)
+
+    # I: the distance / difference family.
+    for case, isPBC in (("general_triclinic_ne4_mol", True), ("ibc_ne2", False), ("cubic_pbc_ne2", True)):
+        src = out[case]
+        c = np.ascontiguousarray(src["coords"][:300])
+        B = src["basis"]
+        idx = np.array([0, 7, 299, 42], np.int32)
+        pts = np.ascontiguousarray(c[[3, 9, 27, 81]].T)  # (3, 4): the reference reads points[:, k]
+        d = dict(coords=c, basis=B, isPBC=np.int32(isPBC), indexes=idx, points=pts)
+        d["dist_to_point"] = pd.pairs_distances_to_point(c[5], c, B, isPBC, 1)
+        d["dist_to_index_all"] = pd.pairs_distances_to_indexcoords(7, c, B, isPBC, True, 1)
+        d["dist_to_index_from"] = pd.pairs_distances_to_indexcoords(7, c, B, isPBC, False, 1)[7:]
+        d["dist_to_multi_points"] = pd.pairs_distances_to_multi_points(pts, c, B, isPBC, 1)
+        d["dist_to_multi_index"] = pd.pairs_distances_to_multi_indexcoords(idx, c, B, isPBC, True, 1)
+        d["diff_to_point"] = pd.pairs_differences_to_point(c[5], c, B, isPBC, 1)
+        d["diff_to_index_all"] = pd.pairs_differences_to_indexcoords(7, c, B, isPBC, True, 1)
+        d["diff_to_multi_points"] = pd.pairs_differences_to_multi_points(pts, c, B, isPBC, 1)
+        d["diff_to_multi_index"] = pd.pairs_differences_to_multi_indexcoords(idx, c, B, isPBC, True, 1)
+        d["from_to"] = pd.from_to_points_differences(c, np.ascontiguousarray(c[::-1]), B, isPBC, 1)
+        d["p2p"] = np.float32(pd.point_to_point_distance(c[1], c[2], B, isPBC, 1))
+        d["pair_diff"] = pd.pair_difference_to_point(c[1], c[2], B, isPBC, 1)
+        out["dist_" + case] = d
+
+    # J: single_pairs_histograms in place on non-zero histograms, and the
+    # *_dists variants on a distance matrix.
+    src = out["general_triclinic_ne4_mol"]
+    c, B = src["coords"], src["basis"]
+    mol, el = src["mol"], src["el"]
+    mn, mx, b, hs = src["minD"], src["maxD"], src["bin"], src["hs"]
+    rng = np.random.default_rng(505)
+    h0i = rng.integers(0, 50, size=(4, 4, int(hs))).astype(F)
+    h0e = rng.integers(0, 50, size=(4, 4, int(hs))).astype(F)
+    d = dict(h0_intra=h0i.copy(), h0_inter=h0e.copy())
+    for tag, atom, allAtoms in (("a", 100, True), ("b", 650, False)):
+        dist = pd.pairs_distances_to_indexcoords(atom, c, B, True, True, 1)
+        hi, he = h0i.copy(), h0e.copy()
+        ph.single_pairs_histograms(atom, dist, mol, el, hi, he, mn, mx, b, allAtoms, 1)
+        d["dist_" + tag] = dist
+        d["intra_" + tag], d["inter_" + tag] = hi, he
+    idx = np.array([4, 77, 500, 1299], np.int32)
+    dm = pd.pairs_distances_to_multi_indexcoords(idx, c, B, True, True, 1)
+    d["dm_indexes"], d["dm"] = idx, dm
+    d["mdist_intra"], d["mdist_inter"] = ph.multiple_pairs_histograms_dists(idx, dm, mol, el, 4, mn, mx, b, hs, True, 1)
+    dsq = pd.pairs_distances_to_multi_indexcoords(np.arange(40, dtype=np.int32), c[:40], B, True, True, 1)
+    d["dsq"] = dsq
+    d["fdist_intra"], d["fdist_inter"] = ph.full_pairs_histograms_dists(dsq, mol[:40], el[:40], 4, mn, mx, b, hs, 1)
+    out["single_and_dists"] = d
+
+    # K: reciprocal space (reference float32 outputs; FP64 results are
+    # compared at about 1e-5 relative).
+    r = (np.arange(1, 301) * 0.05).astype(F)
+    gr = (1.0 + 0.3 * np.sin(r) * np.exp(-0.2 * r)).astype(F)
+    Gr = (4 * np.pi * 0.08 * r * (gr - 1)).astype(F)
+    q = (0.5 + np.arange(120) * 0.1).astype(F)
+    sq = rs.Gr_to_sq(r, Gr, q)
+    # The reference's sq_to_Gr (reciprocal_space.pyx:143) passes an array to
+    # libc sin and raises TypeError for every input; record that fact.
+    try:
+        rs.sq_to_Gr(q, r, sq.astype(F))
+        sq_to_Gr_raises = 0
+    except TypeError:
+        sq_to_Gr_raises = 1
+    out["reciprocal"] = dict(r=r, gr=gr, Gr=Gr, q=q, rho=F(0.08),
+                             gr_to_sq=rs.gr_to_sq(r, gr, q, F(0.08)), Gr_to_sq=sq,
+                             sq_to_Gr_raises=np.int32(sq_to_Gr_raises))
+
+    # L: transform_coordinates (box -> real through the basis, real -> box
+    # through its inverse).
+    B = triclinic_basis(26.0, 24.0, 25.0, 78.0, 95.0, 110.0)
+    rb = np.linalg.inv(B.astype(np.float64)).astype(F)
+    real = (np.random.default_rng(606).random((500, 3)) * 25.0).astype(F)
+    out["transform"] = dict(basis=B, rbasis=rb, real=real, box=bcc.transform_coordinates(rb, real),
+                            back=bcc.transform_coordinates(B, bcc.transform_coordinates(rb, real)))
+
+    for name, d in out.items():
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
+    print("wrote %d golden files" % len(out))
+
+
+if __name__ == "__main__":
+    main()

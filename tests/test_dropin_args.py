@@ -1,0 +1,92 @@
+"""Argument handling of the drop-in modules mirrors the reference's Cython
+signatures (TypeError for None / wrong types, ValueError for a wrong dtype or
+number of dimensions).  All checks fire before any device work, so no GPU is
+needed."""
+import inspect
+
+import numpy as np
+import pytest
+
+from fullrmc_gb300 import pairs_distances as pd
+from fullrmc_gb300 import pairs_histograms as ph
+from fullrmc_gb300 import reciprocal_space as rs
+
+F, I = np.float32, np.int32
+C = np.zeros((4, 3), F)
+B = np.eye(3, dtype=F)
+M = np.zeros(4, I)
+
+REFERENCE_SIGNATURES = {
+    ph.single_pairs_histograms: "atomIndex, distances, moleculeIndex, elementIndex, hintra, hinter, minDistance, "
+                                "maxDistance, bin, allAtoms=True, ncores=1",
+    ph.multiple_pairs_histograms_coords: "indexes, boxCoords, basis, isPBC, moleculeIndex, elementIndex, "
+                                         "numberOfElements, minDistance, maxDistance, bin, histSize, allAtoms=True, "
+                                         "ncores=1",
+    ph.multiple_pairs_histograms_dists: "indexes, distances, moleculeIndex, elementIndex, numberOfElements, "
+                                        "minDistance, maxDistance, bin, histSize, allAtoms=True, ncores=1",
+    ph.full_pairs_histograms_coords: "boxCoords, basis, isPBC, moleculeIndex, elementIndex, numberOfElements, "
+                                     "minDistance, maxDistance, bin, histSize, ncores=1",
+    ph.full_pairs_histograms_dists: "distances, moleculeIndex, elementIndex, numberOfElements, minDistance, "
+                                    "maxDistance, bin, histSize, ncores=1",
+    pd.pairs_distances_to_indexcoords: "atomIndex, coords, basis, isPBC, allAtoms=True, ncores=1",
+    pd.pairs_distances_to_point: "point, coords, basis, isPBC, ncores=1",
+    pd.pairs_distances_to_multi_points: "points, coords, basis, isPBC, ncores=1",
+    pd.pairs_distances_to_multi_indexcoords: "indexes, coords, basis, isPBC, allAtoms=True, ncores=1",
+    pd.point_to_point_distance: "point1, point2, basis, isPBC, ncores=1",
+    pd.from_to_points_differences: "pointsFrom, pointsTo, basis, isPBC, ncores=1",
+    pd.pair_difference_to_point: "point1, point2, basis, isPBC, ncores=1",
+    pd.pairs_differences_to_point: "point, coords, basis, isPBC, ncores=1",
+    pd.pairs_differences_to_indexcoords: "atomIndex, coords, basis, isPBC, allAtoms=True, ncores=1",
+    pd.pairs_differences_to_multi_points: "points, coords, basis, isPBC, ncores=1",
+    pd.pairs_differences_to_multi_indexcoords: "indexes, coords, basis, isPBC, allAtoms=True, ncores=1",
+    rs.gr_to_sq: "distances, gr, qrange, rho",
+    rs.Gr_to_sq: "distances, Gr, qrange",
+    rs.sq_to_Gr: "qValues, rValues, sq",
+}
+
+
+@pytest.mark.parametrize("fn", list(REFERENCE_SIGNATURES), ids=lambda f: f.__name__)
+def test_signature_matches_reference(fn):
+    assert str(inspect.signature(fn))[1:-1] == REFERENCE_SIGNATURES[fn]
+
+
+def test_none_raises_type_error():
+    with pytest.raises(TypeError):
+        ph.full_pairs_histograms_coords(None, B, True, M, M, 1, 0.0, 1.0, 0.1, 10)
+    with pytest.raises(TypeError):
+        ph.multiple_pairs_histograms_coords(None, C, B, True, M, M, 1, 0.0, 1.0, 0.1, 10)
+
+
+def test_wrong_dtype_raises_value_error():
+    with pytest.raises(ValueError, match="dtype mismatch"):
+        ph.full_pairs_histograms_coords(C.astype(np.float64), B, True, M, M, 1, 0.0, 1.0, 0.1, 10)
+    with pytest.raises(ValueError, match="dtype mismatch"):
+        ph.full_pairs_histograms_coords(C, B, True, M.astype(np.int64), M, 1, 0.0, 1.0, 0.1, 10)
+
+
+def test_wrong_ndim_raises_value_error():
+    with pytest.raises(ValueError, match="dimensions"):
+        ph.full_pairs_histograms_coords(C.ravel(), B, True, M, M, 1, 0.0, 1.0, 0.1, 10)
+
+
+def test_float_for_integer_raises_type_error():
+    with pytest.raises(TypeError):
+        ph.full_pairs_histograms_coords(C, B, True, M, M, 1.5, 0.0, 1.0, 0.1, 10)
+
+
+def test_int32_overflow():
+    with pytest.raises(OverflowError):
+        ph.full_pairs_histograms_coords(C, B, True, M, M, 2 ** 40, 0.0, 1.0, 0.1, 10)
+
+
+def test_short_index_arrays_rejected():
+    with pytest.raises(ValueError):
+        ph.full_pairs_histograms_coords(C, B, True, M[:2], M, 1, 0.0, 1.0, 0.1, 10)
+
+
+def test_empty_inputs_need_no_device():
+    hi, he = ph.multiple_pairs_histograms_coords(np.zeros(0, I), C, B, True, M, M, 2, 0.0, 1.0, 0.1, 10)
+    assert hi.shape == (2, 2, 10) and not hi.any() and not he.any()
+    hi, he = ph.full_pairs_histograms_coords(np.zeros((1, 3), F), B, True, M[:1], M[:1], 2, 0.0, 1.0, 0.1, 10)
+    assert not hi.any() and not he.any()
+    assert ph.full_pairs_histograms_coords(C, B, True, M, M, 0, 0.0, 1.0, 0.1, 10)[0].shape == (0, 0, 10)
