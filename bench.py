@@ -1,0 +1,446 @@
+"""Benchmark: RMC steps/s of 256 mixed-size engines on one GB300.
+
+Workload (seeded synthetic data, shapes of the batching configuration):
+256 independent engines, atom counts log-uniform in [1,000, 20,000], 1-4
+species, cubic or triclinic boxes at 0.08-0.10 atoms/A^3, a seeded synthetic
+G(r) per engine (r 0-12 A, dr 0.01 A), single-atom translation moves of up
+to 0.1 A.  One step = one Metropolis step of every engine, executed as one
+launch of the batched step kernel.
+
+Reported beside the headline:
+* ``plain``: the same engines stepped one at a time on the GPU (the plain
+  path) -- steps/s and the batched/plain ratio;
+* ``e2e``: the batched step driven through the public API with host
+  buffers: each step uploads its moves from pinned host memory and reads
+  every engine's chi2 and decision back;
+* ``allpairs``: the all-pairs histogram of 100,000 atoms (three species,
+  triclinic a = b = c = 103 A, gamma = 120, r 0-20 A): time, pair
+  distances/s and its fraction of the SM issue roofline;
+* ``roofline``: the batched step kernel against the issue roofline
+  (46 algorithmic operations per pair distance, SMs x clock x 128 / 46);
+* ``cpu_baseline``: fullrmc's own Cython path (compiled from its sources)
+  running the same kind of steps on the host cores, on a bounded sample.
+
+Timing: CUDA events on the stepping stream, W untimed warm-up steps, then K
+timed steps each bracketed by its own events, with a write of a buffer larger
+than L2 between steps (outside the events).  ``--impl reference`` times the
+reference CPU path alone.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "RMC steps/s (batched/served vs plain GPU, same accepts)"
+UNIT = "steps/s"
+WORKLOAD = "batched_256_mixed_engines"
+OPS_PER_PAIR = 46
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as fh:
+            d = json.load(fh)
+        return d, "measured"
+    except Exception:
+        return {"sm_max_mhz": 2070.0, "hbm_gbs": 6800.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+# ------------------------------------------------------------- reference arm
+def _ref_worker(args):
+    """Reference Cython host chains for engines `idxs`: one "step" moves every
+    engine of this worker once; returns the duration of each step."""
+    idxs, steps, seed, amp = args
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import build_ref
+    from fullrmc_gb300 import synthetic
+    from fullrmc_gb300.engine import translation_moves
+    from fullrmc_gb300.hostloop import HostPDFChain
+    R = build_ref.import_reference()
+    systems = synthetic.mixed_engines(seed=seed, count=max(idxs) + 1)
+    chains, mv = [], []
+    for e in idxs:
+        s = systems[e]
+        chain = HostPDFChain(s, R["pairs_histograms"], R["boundary_conditions_collection"])
+        chain.compute_data()
+        chains.append(chain)
+        mv.append(translation_moves(np.random.default_rng([seed, 1000 + e]), s.box_coords.shape[0], steps, amp))
+    times = []
+    for k in range(steps):
+        t0 = time.perf_counter()
+        for chain, (a, v, u) in zip(chains, mv):
+            chain.step(a[k], v[k][None, :], u[k])
+        times.append(time.perf_counter() - t0)
+    return len(idxs), times
+
+
+def reference_rate(n_engines_sample, steps, warmup, processes, seed=0, amp=0.1):
+    """Aggregate steps/s of the reference CPU path: `processes` host processes
+    each step their own engines (the engines are independent); a timed step
+    lasts as long as the slowest process."""
+    import multiprocessing as mp
+    engines = list(range(n_engines_sample))
+    chunks = [engines[i::processes] for i in range(processes)]
+    chunks = [c for c in chunks if c]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(len(chunks)) as pool:
+        out = pool.map(_ref_worker, [(c, warmup + steps, seed, amp) for c in chunks])
+    total = sum(max(o[1][k] for o in out) for k in range(warmup, warmup + steps))
+    done = n_engines_sample * steps
+    return done / total, len(chunks)
+
+
+def run_reference(args):
+    ws, rank = _dist()
+    if rank != 0:
+        return 0
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    try:
+        import build_ref
+        build_ref.build()
+        build_ref.import_reference()
+        kind = "reference"
+    except Exception as exc:
+        print(json.dumps({"impl": "reference", "unavailable": "fullrmc Cython could not be built here: %s" % exc}))
+        return 0
+    cores = os.cpu_count() or 1
+    sample = min(2 * cores, 256)
+    value, procs = reference_rate(sample, args.steps, args.warmup, cores)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * 256 / value, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "engines": 256, "atoms": "log-uniform 1000-20000",
+                       "rmax": 12.0, "dr": 0.01, "sample": "%d of the 256 engines, one move each per step" % sample},
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": kind,
+                             "sample": "fullrmc Cython (ncores=1) in %d processes, %d engines, %d timed steps"
+                                       % (procs, sample, args.steps)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+# ------------------------------------------------------------------ our arm
+def _flush_l2(buf):
+    buf.add_(1)
+
+
+def bench_allpairs(torch, native, dev, reps=5):
+    from fullrmc_gb300 import synthetic
+    from fullrmc_gb300._native import F32P
+    s = synthetic.triclinic_100k(seed=0)
+    m = s.model
+    n = s.box_coords.shape[0]
+    ne = len(m.elements_count)
+    total = ne * ne * m.hs
+    st = torch.cuda.Stream()
+    c_t = torch.from_numpy(s.box_coords).to(dev)
+    el_t = torch.from_numpy(s.el).to(dev)
+    mol_t = torch.from_numpy(s.mol).to(dev)
+    a4 = torch.empty((n, 4), dtype=torch.float32, device=dev)
+    cnt = torch.zeros(2 * total, dtype=torch.int32, device=dev)
+    B = np.ascontiguousarray(s.basis)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    with torch.cuda.stream(st):
+        native.call("frmc_dev_pack_atoms", c_t.data_ptr(), el_t.data_ptr(), n, a4.data_ptr(), st.cuda_stream)
+        args = (a4.data_ptr(), mol_t.data_ptr(), n, B.ctypes.data_as(F32P), 1, ne, m.minDistance, m.maxDistance,
+                m.bin, m.hs, cnt.data_ptr(), st.cuda_stream)
+        native.call("frmc_dev_full_hist_counts", *args)
+        times = []
+        for _ in range(reps):
+            _flush_l2(flush)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            native.call("frmc_dev_full_hist_counts", *args)
+            e1.record(st)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    counted = int(cnt.sum().item())
+    ms = statistics.median(times)
+    pairs = n * (n - 1) / 2
+    return {"atoms": n, "ms": ms, "pair_distances_per_s": pairs / (ms * 1e-3), "pairs_in_range": counted,
+            "launches": 1}
+
+
+def run_ours(args):
+    import torch
+    ws, rank = _dist()
+    if ws > 1:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    dev = torch.device("cuda", torch.cuda.current_device())
+    import __graft_entry__
+    __graft_entry__.build()
+    import fullrmc_gb300
+    from fullrmc_gb300 import _native as native
+    from fullrmc_gb300 import synthetic
+    from fullrmc_gb300.engine import EngineSet, translation_moves
+
+    info = native.device_info()
+    peaks, peaks_kind = _peaks()
+    seed = 1000 * rank
+    amp = 0.1
+    systems = synthetic.mixed_engines(seed=seed, count=args.engines)
+    E = len(systems)
+    K, W = args.steps, args.warmup
+    plain_steps = args.plain_steps
+    total_steps = W + 3 * K + plain_steps + 64
+    cap = total_steps
+    moves = [translation_moves(np.random.default_rng([seed, 1000 + e]), s.box_coords.shape[0], total_steps, amp)
+             for e, s in enumerate(systems)]
+    pairs_per_step = float(sum(2 * (s.box_coords.shape[0] - 1) for s in systems))
+
+    # autotune the work list (results are identical under every tuning)
+    tune_cands = [(512, 256, 4), (1024, 256, 4), (2048, 256, 2), (1024, 512, 2), (512, 128, 8), (2048, 512, 1)]
+    best = None
+    es = EngineSet(systems, move_cap=cap)
+    es.init()
+    for e, (a, v, u) in enumerate(moves):
+        es.push_moves(e, a, v, u, 0)
+    done = 0
+    for tn in tune_cands:
+        es.set_tune(*tn)
+        es.step(2, graph=False)
+        t0 = time.perf_counter()
+        es.step(6, graph=False)
+        dt = time.perf_counter() - t0
+        done += 8
+        if best is None or dt < best[0]:
+            best = (dt, tn)
+    es.close()
+    tune = best[1]
+
+    # fresh engines for the measurement
+    es = EngineSet(systems, move_cap=cap, tune=tune)
+    es.init()
+    for e, (a, v, u) in enumerate(moves):
+        es.push_moves(e, a, v, u, 0)
+    st = torch.cuda.Stream()
+    sp = st.cuda_stream
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    with torch.cuda.stream(st):
+        for _ in range(W):
+            es.step(1, graph=False, sync=False, stream=sp)
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+        clocks = ClockSampler(dev.index)
+        clocks.start()
+        ev = []
+        for _ in range(K):
+            _flush_l2(flush)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            es.step(1, graph=False, sync=False, stream=sp)
+            e1.record(st)
+            ev.append((e0, e1))
+        torch.cuda.synchronize()
+        step_ms = [a.elapsed_time(b) for a, b in ev]
+        # steady state: K steps back to back in one CUDA graph (state stays in L2)
+        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        es.step(K, graph=True, sync=False, stream=sp)  # capture + warm
+        torch.cuda.synchronize()
+        steps_done = W + 2 * K
+        g0.record(st)
+        es.step(K, graph=True, sync=False, stream=sp)
+        g1.record(st)
+        torch.cuda.synchronize()
+        steps_done += K
+        graph_ms = g0.elapsed_time(g1) / K
+        clk = clocks.stop()
+    total_ms = sum(step_ms)
+    if ws > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / K
+    value = ws * E * K / (total_ms * 1e-3)
+
+    # plain path: the same engines, one at a time (a sample of engines)
+    sample = list(range(0, E, max(1, E // args.plain_engines)))[:args.plain_engines]
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(st):
+        for e in sample:  # warm
+            es.step(1, engine=e, graph=False, sync=False, stream=sp)
+        torch.cuda.synchronize()
+        p0.record(st)
+        for _ in range(plain_steps - 1):
+            for e in sample:
+                es.step(1, engine=e, graph=False, sync=False, stream=sp)
+        p1.record(st)
+        torch.cuda.synchronize()
+    plain_rate = len(sample) * (plain_steps - 1) / (p0.elapsed_time(p1) * 1e-3)
+    es.close()
+
+    # e2e: public API with host buffers; every step uploads all engines' moves
+    # in one copy and reads all engines' chi2 and decisions back in one copy
+    es2 = EngineSet(systems, move_cap=4, tune=tune)
+    es2.init()
+    hm = [translation_moves(np.random.default_rng([seed, 5000 + e]), s.box_coords.shape[0], W + K, amp)
+          for e, s in enumerate(systems)]
+    A = np.stack([m[0] for m in hm])
+    V = np.stack([m[1] for m in hm])
+    U = np.stack([m[2] for m in hm])
+    for k in range(W + K):
+        if k == W:
+            t0 = time.perf_counter()
+        es2.step_host(A[:, k], V[:, k, :], U[:, k])
+    t_e2e = time.perf_counter() - t0
+    es2.close()
+    e2e_value = E * K / t_e2e
+    h2d = E * 20  # packed (atom, vector, u) per engine
+    d2h = E * 16  # (chi2, accepted, atom) per engine
+
+    allp = bench_allpairs(torch, native, dev)
+    sms = info["sms"]
+    fmax = float(peaks.get("sm_max_mhz", 2070.0)) * 1e6
+    issue_peak = sms * fmax * 128.0 / OPS_PER_PAIR  # pair distances / s
+    step_pairs_rate = pairs_per_step / (ms_per_step * 1e-3)
+    traffic_path = os.path.join(ROOT, "profiles", "traffic.json")
+    traffic = None
+    try:
+        with open(traffic_path) as fh:
+            traffic = json.load(fh).get("k_engine_step_bytes_per_launch")
+    except Exception:
+        pass
+
+    # reference CPU path on a bounded sample of the same workload
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        try:
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import build_ref
+            build_ref.build()
+            build_ref.import_reference()
+            rate, procs = reference_rate(4, 6, 2, 1, seed=seed, amp=amp)
+            cpu = {"value": rate, "unit": UNIT, "cores": 1, "kind": "reference",
+                   "sample": "fullrmc Cython (ncores=1): 4 engines of this workload x 6 timed steps, 1 core"}
+        except Exception as exc:
+            cpu = {"value": None, "unit": UNIT, "cores": 1, "kind": "reference", "sample": "failed: %s" % exc}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
+            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "engines": E, "engines_total": ws * E,
+                       "atoms_total": int(sum(s.box_coords.shape[0] for s in systems)),
+                       "atoms": "log-uniform 1000-20000", "species": "1-4", "rmax": 12.0, "dr": 0.01,
+                       "move": "single-atom translation <= %.1f A" % amp,
+                       "l2": "256 MiB buffer written between timed steps",
+                       "tune": {"tile": tune[0], "threads": tune[1], "ctas_per_sm": tune[2]},
+                       "parallelism": "engines sharded per GPU" if ws > 1 else "single GPU"},
+            "plain": {"steps_per_s": plain_rate, "engines_sampled": len(sample),
+                      "batched_over_plain": value / ws / plain_rate},
+            "steady_graph": {"ms_per_step": graph_ms, "steps_per_s": E / (graph_ms * 1e-3),
+                             "note": "K steps in one CUDA graph, no L2 flush"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "roofline": {"bound": "issue", "achieved": step_pairs_rate / 1e9, "peak": issue_peak / 1e9,
+                         "unit": "Gpair/s", "frac": step_pairs_rate / issue_peak, "traffic": traffic,
+                         "kernel": "k_engine_step", "pairs_per_launch": pairs_per_step,
+                         "peak_basis": "%d SMs x %.0f MHz (%s) x 128 lanes / %d ops per pair"
+                                       % (sms, fmax / 1e6, peaks_kind, OPS_PER_PAIR)},
+            "allpairs": dict(allp, roofline_frac=allp["pair_distances_per_s"] / issue_peak,
+                             issue_peak_pairs_per_s=issue_peak),
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "gpu_launches": K,
+        }
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--engines", type=int, default=256)
+    ap.add_argument("--plain-engines", type=int, default=64)
+    ap.add_argument("--plain-steps", type=int, default=20)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

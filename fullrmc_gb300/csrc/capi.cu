@@ -570,7 +570,7 @@ static int dev_full(const void *atoms4, const int32_t *moleculeIndex, int64_t n,
     TRY(check_hist(ne, hs, &total));
     Context *c;
     TRY(get_context(&c));
-    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    cudaStream_t st = (cudaStream_t)stream;
     FRMC_CUDA(cudaMemsetAsync(counts, 0, 2 * total * 4, st));
     if (n < 2 || total == 0)
         return FRMC_OK;
@@ -619,7 +619,7 @@ int frmc_dev_multiple_hist_counts(const int32_t *indexes, int64_t K, const float
         return set_error(FRMC_E_ARG, "number of indexes %lld out of range", (long long)K);
     Context *c;
     TRY(get_context(&c));
-    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    cudaStream_t st = (cudaStream_t)stream;
     FRMC_CUDA(cudaMemsetAsync(counts, 0, 2 * total * 4, st));
     const float *B = isPBC ? basis_host : kIdentity;
     return launch_rows_hist(boxCoords, elementIndex, moleculeIndex, (int)n, indexes, (int)K, allAtoms,
@@ -632,14 +632,14 @@ int frmc_dev_pack_atoms(const float *coords, const int32_t *elementIndex, int64_
     TRY(check_n(n, "coords"));
     Context *c;
     TRY(get_context(&c));
-    return launch_pack_atoms(coords, elementIndex, (int)n, (float4 *)atoms4, stream ? (cudaStream_t)stream : c->stream);
+    return launch_pack_atoms(coords, elementIndex, (int)n, (float4 *)atoms4, (cudaStream_t)stream);
 }
 
 int frmc_dev_counts_to_f32(const uint32_t *counts, int64_t total, float *out, void *stream)
 {
     Context *c;
     TRY(get_context(&c));
-    return launch_counts_to_f32(counts, nullptr, out, total, stream ? (cudaStream_t)stream : c->stream);
+    return launch_counts_to_f32(counts, nullptr, out, total, (cudaStream_t)stream);
 }
 
 }  // extern "C"

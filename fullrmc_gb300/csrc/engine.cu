@@ -1,0 +1,1155 @@
+// Device-resident RMC engines: many independent fullrmc-style Metropolis
+// chains advanced by one persistent kernel per step.
+//
+// One chain follows fullrmc's step (Engine.py:3278-3344) with a single
+// PairDistributionConstraint (PairDistributionConstraints.py:1044-1166):
+//   1. moved atom a: new real coordinates = real + v, new box coordinates =
+//      transform(reciprocal basis, new real) (boundary_conditions_collection.pyx:88-110);
+//   2. delta histograms of a against every other atom j, before and after the
+//      move, oriented [el(a)][el(j)] as multiple_pairs_histograms_coords does
+//      (the F term of compute_before/after_move is empty for one atom);
+//   3. G(r) of data - before + after (PairDistributionConstraints.py:847-895)
+//      and chi2 = sum w (exp - G)^2 / varianceSquared, in FP64;
+//   4. reject iff chi2_new > chi2_old and u > tolerance (Engine.py:3310-3317);
+//      on accept the counts and coordinates are committed.
+//
+// Layout in HBM: one allocation per engine holding float4 box (x, y, z, el
+// bits) and float4 real coordinates, int mol, int32 oriented counts and deltas
+// [2][ne][ne][hs], the FP64 per-bin tables, the element-pair table, a ring of
+// moves, a ring of step results and the chain state.  A descriptor array
+// holds each engine's pointers and constants.
+//
+// The step kernel walks a work list of (engine, atom tile) items; persistent
+// CTAs claim items from an atomic counter (the last CTA to leave resets it).
+// Each item adds +-1 to its engine's oriented delta, to its element-pair delta
+// and to a touched list with global atomics; the CTA that completes an
+// engine's last item (threadfence + counter, no waiting) then evaluates,
+// decides and commits that engine while the other CTAs keep claiming items.
+// The FP64 evaluation is incremental: G(r) of the current configuration is
+// kept, and only bins whose element-pair counts changed do FP64 work.
+// Nothing spins, so the kernel cannot hang; a chain's arithmetic depends only
+// on its own data and every reduction has a fixed order, so a chain gives
+// bit-identical results alone or batched with any other chains, under any
+// tile or CTA configuration.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <vector>
+
+#include "frmc_gpu_engine.h"
+#include "frmc_math.cuh"
+#include "frmc_runtime.h"
+
+namespace frmc {
+
+struct EState {
+    double chi2;        // SD / varianceSquared of the current configuration
+    double sd;          // sum w (exp - G)^2 of the current configuration
+    long long step;
+    long long accepted;
+    unsigned done;      // items of the current step finished
+    unsigned tcount;    // entries in the touched-bin list of the current step
+};
+
+// Work scheduler of one engine set: CTAs claim items with an atomic counter;
+// the last CTA to leave a launch resets it for the next launch.
+struct Sched {
+    unsigned long long claimed;
+    unsigned finished;
+    unsigned pad;
+};
+
+struct EMove {
+    int atom;
+    float v[3];
+    float u;
+};
+
+struct EResult {
+    double chi2_new;
+    int accepted;
+    int atom;
+};
+
+struct EDesc {
+    int n, ne, hs, bm, npairs, ntiles, move_cap, has_dw;
+    long long total;  // ne*ne*hs
+    float minD, maxD, binw, s_lo, s_hi;
+    Basis B, RB;
+    double var2, tol;
+    float4 *box, *real;
+    int *mol, *counts, *delta, *pi, *pj;
+    int *dP;      // [npairs][hs] per-step change of the element-pair counts
+    int *pidx;    // [ne][ne] element pair -> index into the pair table (-1: none)
+    int *tlist;   // oriented bins touched this step (2 n + 8 entries)
+    double *rfac, *invvol, *expd, *dw, *pc;
+    double *K;    // [npairs][hs] rfac * invvol * pair_coef: G = sum_p K_p n_p - rfac
+    double *Gcur; // [hs] G(r) of the current configuration
+    double *dG;   // [hs] change of G(r) proposed this step
+    EMove *moves;
+    EResult *results;
+    EState *st;
+};
+
+struct StepParams {
+    const EDesc *desc;
+    const int2 *items;
+    int nitems;
+    int tile;
+    int eval_only;  // 1: compute G(r) and chi2 of the current counts, no move
+    Sched *sched;
+};
+
+constexpr int kRedLanes = 256;
+
+// transform_coordinates row-vector product (boundary_conditions_collection.pyx:104-106)
+__device__ __forceinline__ float3 to_box(const Basis &RB, float x, float y, float z)
+{
+    float3 r;
+    r.x = __fadd_rn(__fadd_rn(__fmul_rn(x, RB.b[0]), __fmul_rn(y, RB.b[3])), __fmul_rn(z, RB.b[6]));
+    r.y = __fadd_rn(__fadd_rn(__fmul_rn(x, RB.b[1]), __fmul_rn(y, RB.b[4])), __fmul_rn(z, RB.b[7]));
+    r.z = __fadd_rn(__fadd_rn(__fmul_rn(x, RB.b[2]), __fmul_rn(y, RB.b[5])), __fmul_rn(z, RB.b[8]));
+    return r;
+}
+
+// Record a +-1 change of oriented bin `flat` (offset `half` selects intra or
+// inter): the oriented delta, the element-pair delta used by the FP64
+// evaluation, and the touched list used by the commit.
+__device__ __forceinline__ void bump(const EDesc &D, long long half, long long flat, int ra, int rb, int bin, int v)
+{
+    atomicAdd(D.delta + half + flat, v);
+    const unsigned k = atomicAdd(&D.st->tcount, 1u);
+    D.tlist[k] = (int)(half + flat);
+    if (bin >= D.hs) {
+        // A count past the last bin lands in bin 0.. of the next oriented row
+        // of the C-contiguous array, as with the reference's unchecked index.
+        const long long row = flat / D.hs;
+        bin = (int)(flat - row * D.hs);
+        ra = (int)(row / D.ne);
+        rb = (int)(row - (long long)ra * D.ne);
+    }
+    const int p = D.pidx[ra * D.ne + rb];
+    if (p >= 0)
+        atomicAdd(D.dP + (long long)p * D.hs + bin, v);
+}
+
+template <int BM>
+__device__ void item_delta(const EDesc &D, int tile, int atom, float3 o, float3 nw, int ela, int mola, int t)
+{
+    const int j0 = t * tile;
+    const int j1 = min(D.n, j0 + tile);
+    const long long arow = (long long)ela * D.ne;
+    for (int j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
+        if (j == atom)
+            continue;
+        const float4 c = D.box[j];
+        const float s0 = pair_s<BM>(o.x, o.y, o.z, c.x, c.y, c.z, D.B);
+        const float s1 = pair_s<BM>(nw.x, nw.y, nw.z, c.x, c.y, c.z, D.B);
+        const bool a0 = (s0 >= D.s_lo) & (s0 < D.s_hi);
+        const bool a1 = (s1 >= D.s_lo) & (s1 < D.s_hi);
+        if (!(a0 | a1))
+            continue;
+        const int elj = __float_as_int(c.w);
+        const long long half = D.mol[j] == mola ? 0 : D.total;
+        long long f0 = -1, f1 = -1;
+        int b0 = 0, b1 = 0;
+        if (a0) {
+            b0 = pair_bin(s0, D.minD, D.binw);
+            long long f = (arow + elj) * D.hs + b0;
+            if ((unsigned long long)f < (unsigned long long)D.total) f0 = f;
+        }
+        if (a1) {
+            b1 = pair_bin(s1, D.minD, D.binw);
+            long long f = (arow + elj) * D.hs + b1;
+            if ((unsigned long long)f < (unsigned long long)D.total) f1 = f;
+        }
+        if (f0 == f1)
+            continue;
+        if (f0 >= 0)
+            bump(D, half, f0, ela, elj, b0, -1);
+        if (f1 >= 0)
+            bump(D, half, f1, ela, elj, b1, +1);
+    }
+}
+
+// FP64 reductions with a fixed order that does not depend on the CTA size:
+// bin b's contribution c(b) is computed by any thread into shared memory,
+// then lane L (0..255) sums the contributions of bins b = L (mod 256) in
+// increasing order and a fixed binary tree combines the 256 lanes.
+constexpr int kChunk = 2048;    // bins per shared-memory chunk
+constexpr int kMaxPairsU = 10;  // element pairs handled with unrolled loads (ne <= 4)
+
+__device__ void lanes_zero(double *red)
+{
+    for (int L = threadIdx.x; L < kRedLanes; L += blockDim.x) red[L] = 0.0;
+}
+
+__device__ void lanes_add_chunk(double *red, const double *cb, int c0, int cn)
+{
+    __syncthreads();
+    for (int L = threadIdx.x; L < kRedLanes; L += blockDim.x) {
+        int b = c0 + ((L - c0 % kRedLanes) + kRedLanes) % kRedLanes;
+        double acc = red[L];
+        for (; b < c0 + cn; b += kRedLanes) acc += cb[b - c0];
+        red[L] = acc;
+    }
+    __syncthreads();
+}
+
+__device__ double lanes_total(double *red)
+{
+    for (int s = kRedLanes / 2; s > 0; s >>= 1) {
+        for (int L = threadIdx.x; L < s; L += blockDim.x) red[L] += red[L + s];
+        __syncthreads();
+    }
+    const double v = red[0];
+    __syncthreads();
+    return v;
+}
+
+// Element-pair count n_p(b) from the oriented counts (intra + inter, both
+// orientations for unlike elements; PairDistributionConstraints.py:864-878).
+__device__ __forceinline__ long long pair_count(const EDesc &D, int q, int b)
+{
+    const int i = D.pi[q], j = D.pj[q];
+    const long long kij = (long long)(i * D.ne + j) * D.hs + b;
+    long long c = (long long)D.counts[kij] + D.counts[D.total + kij];
+    if (i != j) {
+        const long long kji = (long long)(j * D.ne + i) * D.hs + b;
+        c += (long long)D.counts[kji] + D.counts[D.total + kji];
+    }
+    return c;
+}
+
+// G(r) of the current counts and its sum of squared deviations (set-up):
+// G(b) = sum_p K_p(b) n_p(b) - rfac(b)  (PairDistributionConstraints.py:864-884).
+__device__ double eval_full(const EDesc &D, double *red, double *cb)
+{
+    lanes_zero(red);
+    for (int c0 = 0; c0 < D.hs; c0 += kChunk) {
+        const int cn = min(kChunk, D.hs - c0);
+        for (int b = c0 + threadIdx.x; b < c0 + cn; b += blockDim.x) {
+            double G = -D.rfac[b];
+            for (int q = 0; q < D.npairs; ++q) G = fma(D.K[(long long)q * D.hs + b], (double)pair_count(D, q, b), G);
+            D.Gcur[b] = G;
+            const double d = D.expd[b] - G;
+            cb[b - c0] = (D.has_dw ? D.dw[b] * d : d) * d;
+        }
+        lanes_add_chunk(red, cb, c0, cn);
+    }
+    return lanes_total(red);
+}
+
+// Change of the sum of squared deviations for this step's delta: only bins
+// whose element-pair counts changed do FP64 work,
+//   dG = sum_p K_p dP_p,  d(sd) = w dG (dG - 2 (exp - G)).
+// The element-pair deltas are cleared as they are read; dG is kept for the
+// commit.  All loads of a bin are issued before any is used.
+__device__ double eval_delta(const EDesc &D, double *red, double *cb)
+{
+    lanes_zero(red);
+    const int np = D.npairs;
+    for (int c0 = 0; c0 < D.hs; c0 += kChunk) {
+        const int cn = min(kChunk, D.hs - c0);
+        for (int b = c0 + threadIdx.x; b < c0 + cn; b += blockDim.x) {
+            double dg = 0.0;
+            bool touched = false;
+            if (np <= kMaxPairsU) {
+                int d[kMaxPairsU];
+#pragma unroll
+                for (int q = 0; q < kMaxPairsU; ++q) d[q] = q < np ? __ldcg(D.dP + (long long)q * D.hs + b) : 0;
+#pragma unroll
+                for (int q = 0; q < kMaxPairsU; ++q)
+                    if (d[q]) {
+                        dg = fma(D.K[(long long)q * D.hs + b], (double)d[q], dg);
+                        D.dP[(long long)q * D.hs + b] = 0;
+                        touched = true;
+                    }
+            } else {
+                for (int q = 0; q < np; ++q) {
+                    const int d = __ldcg(D.dP + (long long)q * D.hs + b);
+                    if (d) {
+                        dg = fma(D.K[(long long)q * D.hs + b], (double)d, dg);
+                        D.dP[(long long)q * D.hs + b] = 0;
+                        touched = true;
+                    }
+                }
+            }
+            D.dG[b] = dg;
+            double c = 0.0;
+            if (touched) {
+                const double e = D.expd[b] - D.Gcur[b];
+                c = (D.has_dw ? D.dw[b] * dg : dg) * (dg - 2.0 * e);
+            }
+            cb[b - c0] = c;
+        }
+        lanes_add_chunk(red, cb, c0, cn);
+    }
+    return lanes_total(red);
+}
+
+__device__ void finish_engine(const EDesc &D, int atom, float3 nw, float4 nreal, double *red, double *cb,
+                              int *s_flag)
+{
+    const double dsd = eval_delta(D, red, cb);
+    const EState &S0 = *D.st;
+    const double sd_new = S0.sd + dsd;
+    const double chi2_new = sd_new / D.var2;
+    if (threadIdx.x == 0) {
+        const EMove &m = D.moves[S0.step % D.move_cap];
+        const bool reject = (chi2_new > S0.chi2) && (m.u > D.tol);
+        *s_flag = reject ? 0 : 1;
+    }
+    __syncthreads();
+    const bool accept = *s_flag != 0;
+    const unsigned nt = __ldcg(&D.st->tcount);
+    for (unsigned k = threadIdx.x; k < nt; k += blockDim.x) {
+        const int f = __ldcg(D.tlist + k);
+        const int d = atomicExch(D.delta + f, 0);
+        if (accept && d)
+            D.counts[f] += d;
+    }
+    if (accept)
+        for (int b = threadIdx.x; b < D.hs; b += blockDim.x) {
+            const double g = D.dG[b];
+            if (g != 0.0)
+                D.Gcur[b] += g;
+        }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        EState &S = *D.st;
+        EResult &r = D.results[S.step % D.move_cap];
+        r.chi2_new = chi2_new;
+        r.accepted = accept ? 1 : 0;
+        r.atom = atom;
+        if (accept) {
+            const float4 ob = D.box[atom];
+            D.box[atom] = make_float4(nw.x, nw.y, nw.z, ob.w);
+            D.real[atom] = nreal;
+            S.chi2 = chi2_new;
+            S.sd = sd_new;
+            S.accepted += 1;
+        }
+        S.step += 1;
+        S.done = 0u;
+        S.tcount = 0u;
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_engine_step(StepParams p)
+{
+    __shared__ double red[kRedLanes];
+    __shared__ double cb[kChunk];
+    __shared__ int s_last, s_flag, s_item;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const unsigned long long k = atomicAdd(&p.sched->claimed, 1ull);
+            s_item = k < (unsigned long long)p.nitems ? (int)k : -1;
+        }
+        __syncthreads();
+        const int it = s_item;
+        __syncthreads();
+        if (it < 0)
+            break;
+        const int2 item = p.items[it];
+        const EDesc &D = p.desc[item.x];
+        if (p.eval_only) {
+            const double sd = eval_full(D, red, cb);
+            if (threadIdx.x == 0) {
+                D.st->sd = sd;
+                D.st->chi2 = sd / D.var2;
+                D.st->done = 0u;
+                D.st->tcount = 0u;
+            }
+            __syncthreads();
+            continue;
+        }
+        const long long step = D.st->step;
+        const EMove m = D.moves[step % D.move_cap];
+        const int atom = m.atom;
+        const float4 ob = D.box[atom];
+        const float4 orl = D.real[atom];
+        const float4 nreal =
+            make_float4(__fadd_rn(orl.x, m.v[0]), __fadd_rn(orl.y, m.v[1]), __fadd_rn(orl.z, m.v[2]), 0.0f);
+        const float3 nw =
+            D.bm == BM_IBC ? make_float3(nreal.x, nreal.y, nreal.z) : to_box(D.RB, nreal.x, nreal.y, nreal.z);
+        const float3 o = make_float3(ob.x, ob.y, ob.z);
+        const int ela = __float_as_int(ob.w);
+        const int mola = D.mol[atom];
+        switch (D.bm) {
+        case BM_IBC: item_delta<BM_IBC>(D, p.tile, atom, o, nw, ela, mola, item.y); break;
+        case BM_DIAG: item_delta<BM_DIAG>(D, p.tile, atom, o, nw, ela, mola, item.y); break;
+        case BM_XYTRI: item_delta<BM_XYTRI>(D, p.tile, atom, o, nw, ela, mola, item.y); break;
+        case BM_LOWER: item_delta<BM_LOWER>(D, p.tile, atom, o, nw, ela, mola, item.y); break;
+        default: item_delta<BM_GENERAL>(D, p.tile, atom, o, nw, ela, mola, item.y); break;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            const unsigned prev = atomicAdd(&D.st->done, 1u);
+            s_last = (prev == (unsigned)D.ntiles - 1u) ? 1 : 0;
+        }
+        __syncthreads();
+        if (s_last) {
+            __threadfence();
+            finish_engine(D, atom, nw, nreal, red, cb, &s_flag);
+        }
+        __syncthreads();
+    }
+    // The last CTA to leave resets the scheduler for the next launch.
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned f = atomicAdd(&p.sched->finished, 1u);
+        if (f == gridDim.x - 1) {
+            p.sched->claimed = 0ull;
+            p.sched->finished = 0u;
+            __threadfence();
+        }
+    }
+}
+
+// Host-buffer stepping: scatter this step's moves into each engine's ring
+// and gather the step's results (one copy each way for all engines).
+__global__ void k_scatter_moves(const EDesc *desc, const int *ids, const EMove *staged, int count)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < count) {
+        const EDesc &D = desc[ids[k]];
+        D.moves[D.st->step % D.move_cap] = staged[k];
+    }
+}
+
+__global__ void k_gather_results(const EDesc *desc, const int *ids, EResult *out, int count)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < count) {
+        const EDesc &D = desc[ids[k]];
+        out[k] = D.results[(D.st->step + D.move_cap - 1) % D.move_cap];
+    }
+}
+
+// --------------------------------------------------------------- host side
+struct Slot {
+    bool live = false;
+    bool initialized = false;
+    EDesc d;
+    void *blob = nullptr;
+    size_t bytes = 0;
+};
+
+struct EngineSet {
+    std::vector<Slot> slots;
+    std::vector<int> live;        // live engine ids in work-list order
+    std::vector<int> item_first;  // per engine id: first item (or -1)
+    std::vector<int> item_count;
+    int tile = 1024, threads = 256, ctas_per_sm = 4;
+    EDesc *ddesc = nullptr;
+    int ddesc_cap = 0;
+    int2 *items = nullptr;
+    int items_cap = 0;
+    int nitems = 0;
+    int *dlive = nullptr;
+    int dlive_cap = 0;
+    EMove *hstage_m = nullptr;     // pinned
+    EResult *hstage_r = nullptr;   // pinned
+    EMove *dstage_m = nullptr;
+    EResult *dstage_r = nullptr;
+    int stage_cap = 0;
+    Sched *sched = nullptr;
+    cudaStream_t stream = nullptr;
+    std::map<std::pair<int, int>, cudaGraphExec_t> graphs;
+    bool dirty = true;
+};
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+struct BlobLayout {
+    size_t box, real, mol, counts, delta, rfac, invvol, expd, dw, pc, pi, pj, dP, pidx, tlist, K, Gcur, dG, moves,
+        results, st, total;
+};
+
+static BlobLayout blob_layout(const frmc_engine_spec &sp)
+{
+    BlobLayout L;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t o = off;
+        off += align256(bytes);
+        return o;
+    };
+    const size_t n = sp.n, hs = sp.hs, tot = (size_t)sp.ne * sp.ne * sp.hs;
+    L.box = take(16 * n);
+    L.real = take(16 * n);
+    L.mol = take(4 * n);
+    L.counts = take(8 * tot);
+    L.delta = take(8 * tot);
+    L.rfac = take(8 * hs);
+    L.invvol = take(8 * hs);
+    L.expd = take(8 * hs);
+    L.dw = take(sp.data_weights ? 8 * hs : 0);
+    L.pc = take(8 * (size_t)sp.npairs);
+    L.pi = take(4 * (size_t)sp.npairs);
+    L.pj = take(4 * (size_t)sp.npairs);
+    L.dP = take(4 * (size_t)sp.npairs * hs);
+    L.pidx = take(4 * (size_t)sp.ne * sp.ne);
+    L.tlist = take(4 * (2 * n + 8));
+    L.K = take(8 * (size_t)sp.npairs * hs);
+    L.Gcur = take(8 * hs);
+    L.dG = take(8 * hs);
+    L.moves = take(sizeof(EMove) * (size_t)sp.move_cap);
+    L.results = take(sizeof(EResult) * (size_t)sp.move_cap);
+    L.st = take(sizeof(EState));
+    L.total = off;
+    return L;
+}
+
+static int check_spec(const frmc_engine_spec &sp)
+{
+    if (sp.n < 1 || sp.ne < 1 || sp.hs < 1 || sp.npairs < 1 || sp.move_cap < 1 || !sp.box_coords ||
+        !sp.real_coords || !sp.el || !sp.mol || !sp.basis || !sp.rbasis || !sp.pair_i || !sp.pair_j ||
+        !sp.pair_coef || !sp.rfac || !sp.inv_shell_volume || !sp.experimental || !(sp.variance_squared > 0))
+        return set_error(FRMC_E_ARG, "engine spec: missing or invalid field");
+    if ((double)sp.ne * sp.ne * sp.hs > 2.0e8)
+        return set_error(FRMC_E_ARG, "engine spec: histogram too large");
+    for (int q = 0; q < sp.npairs; ++q)
+        if (sp.pair_i[q] < 0 || sp.pair_i[q] >= sp.ne || sp.pair_j[q] < 0 || sp.pair_j[q] >= sp.ne)
+            return set_error(FRMC_E_ARG, "engine spec: element pair %d out of range", q);
+    for (int i = 0; i < sp.n; ++i)
+        if (sp.el[i] < 0 || sp.el[i] >= sp.ne)
+            return set_error(FRMC_E_ARG, "engine spec: atom %d element out of range", i);
+    return FRMC_OK;
+}
+
+static void drop_graphs(EngineSet *s)
+{
+    for (auto &kv : s->graphs) cudaGraphExecDestroy(kv.second);
+    s->graphs.clear();
+}
+
+// Rebuild the work list over live engines and upload descriptors.
+static int refresh(EngineSet *s)
+{
+    if (!s->dirty)
+        return FRMC_OK;
+    const int nslots = (int)s->slots.size();
+    std::vector<int2> items;
+    s->item_first.assign(nslots, -1);
+    s->item_count.assign(nslots, 0);
+    for (int id : s->live) {
+        EDesc &D = s->slots[id].d;
+        D.ntiles = std::max(1, (D.n + s->tile - 1) / s->tile);
+        s->item_first[id] = (int)items.size();
+        s->item_count[id] = D.ntiles;
+        for (int t = 0; t < D.ntiles; ++t) items.push_back(make_int2(id, t));
+    }
+    if (nslots > s->ddesc_cap) {
+        if (s->ddesc) cudaFree(s->ddesc);
+        s->ddesc = nullptr;
+        int cap = std::max(nslots, 2 * s->ddesc_cap);
+        FRMC_CUDA(cudaMalloc(&s->ddesc, sizeof(EDesc) * cap));
+        s->ddesc_cap = cap;
+    }
+    if ((int)items.size() > s->items_cap) {
+        if (s->items) cudaFree(s->items);
+        s->items = nullptr;
+        int cap = std::max((int)items.size(), 2 * s->items_cap);
+        FRMC_CUDA(cudaMalloc(&s->items, sizeof(int2) * cap));
+        s->items_cap = cap;
+    }
+    if ((int)s->live.size() > s->dlive_cap) {
+        if (s->dlive) cudaFree(s->dlive);
+        s->dlive = nullptr;
+        int cap = std::max((int)s->live.size(), 2 * s->dlive_cap);
+        FRMC_CUDA(cudaMalloc(&s->dlive, sizeof(int) * cap));
+        s->dlive_cap = cap;
+    }
+    std::vector<EDesc> hd(nslots);
+    for (int k = 0; k < nslots; ++k) hd[k] = s->slots[k].d;
+    FRMC_CUDA(cudaStreamSynchronize(s->stream));
+    if (nslots)
+        FRMC_CUDA(cudaMemcpy(s->ddesc, hd.data(), sizeof(EDesc) * nslots, cudaMemcpyHostToDevice));
+    if (!items.empty())
+        FRMC_CUDA(cudaMemcpy(s->items, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice));
+    if (!s->live.empty())
+        FRMC_CUDA(cudaMemcpy(s->dlive, s->live.data(), sizeof(int) * s->live.size(), cudaMemcpyHostToDevice));
+    s->nitems = (int)items.size();
+    drop_graphs(s);
+    s->dirty = false;
+    return FRMC_OK;
+}
+
+static int launch_items(EngineSet *s, const int2 *items, int count, int eval_only, cudaStream_t st)
+{
+    Context *c;
+    FRMC_TRY(get_context(&c));
+    int grid = c->sms * s->ctas_per_sm;
+    if (grid > count)
+        grid = count;
+    if (grid < 1)
+        return FRMC_OK;
+    StepParams p{s->ddesc, items, count, s->tile, eval_only, s->sched};
+    k_engine_step<<<grid, s->threads, 0, st>>>(p);
+    FRMC_CUDA(cudaGetLastError());
+    return FRMC_OK;
+}
+
+// All-pairs counts and initial chi2 of engine `id` (synchronous).
+static int init_engine(EngineSet *s, int id)
+{
+    Context *c;
+    FRMC_TRY(get_context(&c));
+    EDesc &D = s->slots[id].d;
+    {
+        std::lock_guard<std::mutex> lk(c->mu);
+        FRMC_TRY(c->buf[BUF_STATUS].ensure(16));
+        FRMC_TRY(c->buf[BUF_AUX0].ensure(12 * (size_t)D.n + 16));
+        FRMC_TRY(c->buf[BUF_AUX1].ensure(4 * (size_t)D.n + 16));
+    }
+    FRMC_CUDA(cudaMemsetAsync(c->buf[BUF_STATUS].p, 0, 4, s->stream));
+    FRMC_CUDA(cudaMemsetAsync(D.counts, 0, sizeof(int) * 2 * D.total, s->stream));
+    FRMC_CUDA(cudaMemsetAsync(D.delta, 0, sizeof(int) * 2 * D.total, s->stream));
+    FRMC_CUDA(cudaMemsetAsync(D.st, 0, sizeof(EState), s->stream));
+    unsigned *cnt = (unsigned *)D.counts;
+    FullTune tn;
+    if (D.n >= 2) {
+        const double pairs = 0.5 * (double)D.n * (D.n - 1);
+        if (pairs < tn.min_pairs_tiled) {
+            // the row kernel reads AoS float coordinates: unpack once
+            std::lock_guard<std::mutex> lk(c->mu);
+            FRMC_TRY(launch_unpack_atoms(D.box, D.n, c->buf[BUF_AUX0].as<float>(), c->buf[BUF_AUX1].as<int>(),
+                                         s->stream));
+            FRMC_TRY(launch_rows_hist(c->buf[BUF_AUX0].as<float>(), c->buf[BUF_AUX1].as<int>(), D.mol, D.n, nullptr,
+                                      D.n, 0, D.bm, D.B, D.minD, D.maxD, D.binw, D.ne, D.hs, cnt, cnt + D.total,
+                                      s->stream));
+            FRMC_CUDA(cudaStreamSynchronize(s->stream));
+        } else {
+            FRMC_TRY(launch_full_hist(D.box, D.mol, D.n, D.bm, D.B, D.minD, D.maxD, D.binw, D.ne, D.hs, cnt,
+                                      cnt + D.total, c->buf[BUF_STATUS].as<uint32_t>(), 0.05, &tn, s->stream));
+        }
+    }
+    FRMC_TRY(refresh(s));
+    int2 item = make_int2(id, 0);
+    int2 *ditem = nullptr;
+    FRMC_CUDA(cudaMalloc(&ditem, sizeof(int2)));
+    FRMC_CUDA(cudaMemcpyAsync(ditem, &item, sizeof(int2), cudaMemcpyHostToDevice, s->stream));
+    int rc = launch_items(s, ditem, 1, 1, s->stream);
+    cudaError_t ce = cudaStreamSynchronize(s->stream);
+    cudaFree(ditem);
+    if (rc)
+        return rc;
+    if (ce != cudaSuccess)
+        return cuda_fail(ce, "engine init");
+    uint32_t status = 0;
+    FRMC_CUDA(cudaMemcpy(&status, c->buf[BUF_STATUS].p, 4, cudaMemcpyDeviceToHost));
+    if (status)
+        return set_error(FRMC_E_TIMEOUT, "engine init: device wait gave up (0x%x)", status);
+    s->slots[id].initialized = true;
+    return FRMC_OK;
+}
+
+static int add_engine(EngineSet *s, const frmc_engine_spec &sp, int *out_id)
+{
+    FRMC_TRY(check_spec(sp));
+    BlobLayout L = blob_layout(sp);
+    Slot sl;
+    FRMC_CUDA(cudaMalloc(&sl.blob, L.total));
+    sl.bytes = L.total;
+    char *b = (char *)sl.blob;
+    EDesc &D = sl.d;
+    memset(&D, 0, sizeof(D));
+    D.n = sp.n;
+    D.ne = sp.ne;
+    D.hs = sp.hs;
+    D.npairs = sp.npairs;
+    D.move_cap = sp.move_cap;
+    D.bm = sp.isPBC ? basis_mode(sp.basis, 1) : BM_IBC;
+    D.B = make_basis(sp.isPBC ? sp.basis : nullptr);
+    D.RB = make_basis(sp.isPBC ? sp.rbasis : nullptr);
+    D.minD = sp.minDistance;
+    D.maxD = sp.maxDistance;
+    D.binw = sp.bin;
+    sq_limits(sp.minDistance, sp.maxDistance, &D.s_lo, &D.s_hi);
+    D.total = (long long)sp.ne * sp.ne * sp.hs;
+    D.var2 = sp.variance_squared;
+    D.tol = sp.tolerance;
+    D.has_dw = sp.data_weights ? 1 : 0;
+    D.box = (float4 *)(b + L.box);
+    D.real = (float4 *)(b + L.real);
+    D.mol = (int *)(b + L.mol);
+    D.counts = (int *)(b + L.counts);
+    D.delta = (int *)(b + L.delta);
+    D.rfac = (double *)(b + L.rfac);
+    D.invvol = (double *)(b + L.invvol);
+    D.expd = (double *)(b + L.expd);
+    D.dw = (double *)(b + L.dw);
+    D.pc = (double *)(b + L.pc);
+    D.pi = (int *)(b + L.pi);
+    D.pj = (int *)(b + L.pj);
+    D.dP = (int *)(b + L.dP);
+    D.pidx = (int *)(b + L.pidx);
+    D.tlist = (int *)(b + L.tlist);
+    D.K = (double *)(b + L.K);
+    D.Gcur = (double *)(b + L.Gcur);
+    D.dG = (double *)(b + L.dG);
+    D.moves = (EMove *)(b + L.moves);
+    D.results = (EResult *)(b + L.results);
+    D.st = (EState *)(b + L.st);
+    std::vector<int> pidx((size_t)sp.ne * sp.ne, -1);
+    for (int q = 0; q < sp.npairs; ++q) {
+        pidx[(size_t)sp.pair_i[q] * sp.ne + sp.pair_j[q]] = q;
+        pidx[(size_t)sp.pair_j[q] * sp.ne + sp.pair_i[q]] = q;
+    }
+    std::vector<double> K((size_t)sp.npairs * sp.hs);
+    for (int q = 0; q < sp.npairs; ++q)
+        for (int bb = 0; bb < sp.hs; ++bb)
+            K[(size_t)q * sp.hs + bb] = sp.rfac[bb] * sp.inv_shell_volume[bb] * sp.pair_coef[q];
+    std::vector<float4> b4(sp.n), r4(sp.n);
+    for (int i = 0; i < sp.n; ++i) {
+        b4[i] = make_float4(sp.box_coords[3 * i], sp.box_coords[3 * i + 1], sp.box_coords[3 * i + 2],
+                            int_bits_as_float(sp.el[i]));
+        r4[i] = make_float4(sp.real_coords[3 * i], sp.real_coords[3 * i + 1], sp.real_coords[3 * i + 2], 0.f);
+    }
+    int rc = FRMC_OK;
+    auto up = [&](void *dst, const void *src, size_t bytes) {
+        if (rc || !bytes)
+            return;
+        cudaError_t ce = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s->stream);
+        if (ce != cudaSuccess)
+            rc = cuda_fail(ce, "cudaMemcpyAsync");
+    };
+    up(D.box, b4.data(), 16 * (size_t)sp.n);
+    up(D.real, r4.data(), 16 * (size_t)sp.n);
+    up(D.mol, sp.mol, 4 * (size_t)sp.n);
+    up(D.rfac, sp.rfac, 8 * (size_t)sp.hs);
+    up(D.invvol, sp.inv_shell_volume, 8 * (size_t)sp.hs);
+    up(D.expd, sp.experimental, 8 * (size_t)sp.hs);
+    if (sp.data_weights)
+        up(D.dw, sp.data_weights, 8 * (size_t)sp.hs);
+    up(D.pc, sp.pair_coef, 8 * (size_t)sp.npairs);
+    up(D.pi, sp.pair_i, 4 * (size_t)sp.npairs);
+    up(D.pj, sp.pair_j, 4 * (size_t)sp.npairs);
+    up(D.pidx, pidx.data(), 4 * pidx.size());
+    up(D.K, K.data(), 8 * K.size());
+    if (!rc) {
+        cudaError_t ce = cudaMemsetAsync(D.moves, 0, sizeof(EMove) * sp.move_cap, s->stream);
+        if (ce == cudaSuccess)
+            ce = cudaMemsetAsync(D.dP, 0, 4 * (size_t)sp.npairs * sp.hs, s->stream);
+        if (ce == cudaSuccess)
+            ce = cudaMemsetAsync(D.results, 0, sizeof(EResult) * sp.move_cap, s->stream);
+        if (ce == cudaSuccess)
+            ce = cudaStreamSynchronize(s->stream);
+        if (ce != cudaSuccess)
+            rc = cuda_fail(ce, "engine upload");
+    }
+    if (rc) {
+        cudaFree(sl.blob);
+        return rc;
+    }
+    // reuse a free slot id if any
+    int id = -1;
+    for (int k = 0; k < (int)s->slots.size(); ++k)
+        if (!s->slots[k].live && !s->slots[k].blob) {
+            id = k;
+            break;
+        }
+    if (id < 0) {
+        id = (int)s->slots.size();
+        s->slots.push_back(Slot());
+    }
+    sl.live = true;
+    s->slots[id] = sl;
+    s->live.push_back(id);
+    std::sort(s->live.begin(), s->live.end());
+    s->dirty = true;
+    *out_id = id;
+    return FRMC_OK;
+}
+
+static void free_set(EngineSet *s)
+{
+    if (s->stream)
+        cudaStreamSynchronize(s->stream);
+    drop_graphs(s);
+    for (auto &sl : s->slots)
+        if (sl.blob) cudaFree(sl.blob);
+    void *ptrs[] = {s->ddesc, s->items, s->dlive, s->dstage_m, s->dstage_r, s->sched};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (s->hstage_m) cudaFreeHost(s->hstage_m);
+    if (s->hstage_r) cudaFreeHost(s->hstage_r);
+    if (s->stream)
+        cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+static EngineSet *as_set(void *h) { return (EngineSet *)h; }
+
+static bool valid_id(EngineSet *s, int e) { return e >= 0 && e < (int)s->slots.size() && s->slots[e].live; }
+
+}  // namespace frmc
+
+using namespace frmc;
+
+extern "C" {
+
+int frmc_engine_footprint(const frmc_engine_spec *spec, int64_t *bytes)
+{
+    if (!spec || !bytes)
+        return set_error(FRMC_E_ARG, "engine_footprint: null argument");
+    *bytes = (int64_t)blob_layout(*spec).total;
+    return FRMC_OK;
+}
+
+int frmc_engines_new(void **handle)
+{
+    if (!handle)
+        return set_error(FRMC_E_ARG, "engines_new: null handle");
+    Context *c;
+    FRMC_TRY(get_context(&c));
+    EngineSet *s = new EngineSet();
+    cudaError_t ce = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (ce == cudaSuccess)
+        ce = cudaMalloc(&s->sched, sizeof(Sched));
+    if (ce == cudaSuccess)
+        ce = cudaMemset(s->sched, 0, sizeof(Sched));
+    if (ce != cudaSuccess) {
+        free_set(s);
+        return cuda_fail(ce, "engine set");
+    }
+    *handle = s;
+    return FRMC_OK;
+}
+
+int frmc_engines_create(const frmc_engine_spec *specs, int32_t E, void **handle)
+{
+    if (!specs || E <= 0 || !handle)
+        return set_error(FRMC_E_ARG, "engines_create: need at least one spec");
+    for (int e = 0; e < E; ++e) FRMC_TRY(check_spec(specs[e]));
+    void *h = nullptr;
+    FRMC_TRY(frmc_engines_new(&h));
+    EngineSet *s = as_set(h);
+    for (int e = 0; e < E; ++e) {
+        int id;
+        int rc = add_engine(s, specs[e], &id);
+        if (rc) {
+            free_set(s);
+            return rc;
+        }
+    }
+    *handle = s;
+    return FRMC_OK;
+}
+
+int frmc_engines_add(void *handle, const frmc_engine_spec *spec, int32_t *id)
+{
+    EngineSet *s = as_set(handle);
+    if (!s || !spec || !id)
+        return set_error(FRMC_E_ARG, "engines_add: null argument");
+    int k;
+    FRMC_TRY(add_engine(s, *spec, &k));
+    int rc = init_engine(s, k);
+    if (rc) {
+        frmc_engines_remove(handle, k);
+        return rc;
+    }
+    *id = k;
+    return FRMC_OK;
+}
+
+int frmc_engines_remove(void *handle, int32_t id)
+{
+    EngineSet *s = as_set(handle);
+    if (!s || !valid_id(s, id))
+        return set_error(FRMC_E_ARG, "engines_remove: invalid engine %d", id);
+    FRMC_CUDA(cudaStreamSynchronize(s->stream));
+    FRMC_CUDA(cudaDeviceSynchronize());
+    cudaFree(s->slots[id].blob);
+    s->slots[id] = Slot();
+    s->live.erase(std::remove(s->live.begin(), s->live.end(), id), s->live.end());
+    s->dirty = true;
+    return FRMC_OK;
+}
+
+int frmc_engines_live(void *handle, int32_t *ids, int32_t cap, int32_t *count)
+{
+    EngineSet *s = as_set(handle);
+    if (!s || !count)
+        return set_error(FRMC_E_ARG, "engines_live: null argument");
+    *count = (int32_t)s->live.size();
+    for (int k = 0; k < (int)s->live.size() && k < cap; ++k) ids[k] = s->live[k];
+    return FRMC_OK;
+}
+
+int frmc_engines_destroy(void *handle)
+{
+    if (handle)
+        free_set(as_set(handle));
+    return FRMC_OK;
+}
+
+int frmc_engines_set_tune(void *handle, int tile, int threads, int ctas_per_sm)
+{
+    EngineSet *s = as_set(handle);
+    if (!s || tile < 32 || threads < 32 || threads > 1024 || threads % 32 || ctas_per_sm < 1 || ctas_per_sm > 32)
+        return set_error(FRMC_E_ARG, "engines_set_tune: invalid configuration");
+    FRMC_CUDA(cudaStreamSynchronize(s->stream));
+    s->tile = tile;
+    s->threads = threads;
+    s->ctas_per_sm = ctas_per_sm;
+    s->dirty = true;
+    return refresh(s);
+}
+
+int frmc_engines_get_tune(void *handle, int *tile, int *threads, int *ctas_per_sm, int *nitems)
+{
+    EngineSet *s = as_set(handle);
+    if (!s)
+        return set_error(FRMC_E_ARG, "null handle");
+    FRMC_TRY(refresh(s));
+    if (tile) *tile = s->tile;
+    if (threads) *threads = s->threads;
+    if (ctas_per_sm) *ctas_per_sm = s->ctas_per_sm;
+    if (nitems) *nitems = s->nitems;
+    return FRMC_OK;
+}
+
+int frmc_engines_init(void *handle)
+{
+    EngineSet *s = as_set(handle);
+    if (!s)
+        return set_error(FRMC_E_ARG, "null handle");
+    for (int id : std::vector<int>(s->live))
+        if (!s->slots[id].initialized)
+            FRMC_TRY(init_engine(s, id));
+    return FRMC_OK;
+}
+
+int frmc_engines_push_moves(void *handle, int32_t e, const int32_t *atoms, const float *vecs, const float *u,
+                            int32_t count, int64_t first_step, int from_device)
+{
+    EngineSet *s = as_set(handle);
+    if (!s || !valid_id(s, e) || count < 0 || first_step < 0 || from_device)
+        return set_error(FRMC_E_ARG, "push_moves: invalid arguments");
+    const EDesc &D = s->slots[e].d;
+    if (count > D.move_cap)
+        return set_error(FRMC_E_ARG, "push_moves: %d moves exceed the ring of %d", count, D.move_cap);
+    for (int k = 0; k < count; ++k)
+        if (atoms[k] < 0 || atoms[k] >= D.n)
+            return set_error(FRMC_E_INDEX, "push_moves: atom %d out of range", atoms[k]);
+    std::vector<EMove> mv(count);
+    for (int k = 0; k < count; ++k) {
+        mv[k].atom = atoms[k];
+        mv[k].v[0] = vecs[3 * k];
+        mv[k].v[1] = vecs[3 * k + 1];
+        mv[k].v[2] = vecs[3 * k + 2];
+        mv[k].u = u ? u[k] : 1.0f;
+    }
+    long long pos = first_step % D.move_cap;
+    int done = 0;
+    while (done < count) {
+        int chunk = (int)std::min<long long>(count - done, D.move_cap - pos);
+        FRMC_CUDA(cudaMemcpyAsync(D.moves + pos, mv.data() + done, sizeof(EMove) * chunk, cudaMemcpyHostToDevice,
+                                  s->stream));
+        done += chunk;
+        pos = 0;
+    }
+    FRMC_CUDA(cudaStreamSynchronize(s->stream));
+    return FRMC_OK;
+}
+
+int frmc_engines_step(void *handle, int32_t engine, int32_t steps, int use_graph, void *stream)
+{
+    EngineSet *s = as_set(handle);
+    if (!s || steps < 0 || (engine != -1 && !valid_id(s, engine)))
+        return set_error(FRMC_E_ARG, "engines_step: invalid arguments");
+    FRMC_TRY(refresh(s));
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
+    const int first = engine < 0 ? 0 : s->item_first[engine];
+    const int count = engine < 0 ? s->nitems : s->item_count[engine];
+    if (count == 0 || steps == 0)
+        return FRMC_OK;
+    if (!use_graph) {
+        for (int k = 0; k < steps; ++k) FRMC_TRY(launch_items(s, s->items + first, count, 0, st));
+        return FRMC_OK;
+    }
+    auto key = std::make_pair(engine, steps);
+    auto it = s->graphs.find(key);
+    if (it == s->graphs.end()) {
+        cudaStream_t cap;
+        FRMC_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        cudaGraph_t g;
+        cudaError_t ce = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+        int rc = FRMC_OK;
+        if (ce == cudaSuccess) {
+            for (int k = 0; k < steps && !rc; ++k) rc = launch_items(s, s->items + first, count, 0, cap);
+            ce = cudaStreamEndCapture(cap, &g);
+        }
+        cudaStreamDestroy(cap);
+        if (rc)
+            return rc;
+        if (ce != cudaSuccess)
+            return cuda_fail(ce, "graph capture");
+        cudaGraphExec_t ex;
+        ce = cudaGraphInstantiate(&ex, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess)
+            return cuda_fail(ce, "cudaGraphInstantiate");
+        it = s->graphs.emplace(key, ex).first;
+    }
+    FRMC_CUDA(cudaGraphLaunch(it->second, st));
+    return FRMC_OK;
+}
+
+int frmc_engines_step_host(void *handle, const int32_t *atoms, const float *vecs, const float *u, double *chi2_new,
+                           int32_t *accepted)
+{
+    EngineSet *s = as_set(handle);
+    if (!s)
+        return set_error(FRMC_E_ARG, "null handle");
+    FRMC_TRY(refresh(s));
+    const int E = (int)s->live.size();
+    if (E == 0)
+        return FRMC_OK;
+    for (int k = 0; k < E; ++k)
+        if (atoms[k] < 0 || atoms[k] >= s->slots[s->live[k]].d.n)
+            return set_error(FRMC_E_INDEX, "step_host: atom %d out of range for engine %d", atoms[k], s->live[k]);
+    if (E > s->stage_cap) {
+        if (s->hstage_m) cudaFreeHost(s->hstage_m);
+        if (s->hstage_r) cudaFreeHost(s->hstage_r);
+        if (s->dstage_m) cudaFree(s->dstage_m);
+        if (s->dstage_r) cudaFree(s->dstage_r);
+        s->hstage_m = nullptr;
+        s->hstage_r = nullptr;
+        s->dstage_m = nullptr;
+        s->dstage_r = nullptr;
+        int cap = std::max(E, 2 * s->stage_cap);
+        FRMC_CUDA(cudaMallocHost(&s->hstage_m, sizeof(EMove) * cap));
+        FRMC_CUDA(cudaMallocHost(&s->hstage_r, sizeof(EResult) * cap));
+        FRMC_CUDA(cudaMalloc(&s->dstage_m, sizeof(EMove) * cap));
+        FRMC_CUDA(cudaMalloc(&s->dstage_r, sizeof(EResult) * cap));
+        s->stage_cap = cap;
+    }
+    for (int k = 0; k < E; ++k) {
+        EMove &m = s->hstage_m[k];
+        m.atom = atoms[k];
+        m.v[0] = vecs[3 * k];
+        m.v[1] = vecs[3 * k + 1];
+        m.v[2] = vecs[3 * k + 2];
+        m.u = u ? u[k] : 1.0f;
+    }
+    cudaStream_t st = s->stream;
+    FRMC_CUDA(cudaMemcpyAsync(s->dstage_m, s->hstage_m, sizeof(EMove) * E, cudaMemcpyHostToDevice, st));
+    k_scatter_moves<<<(E + 127) / 128, 128, 0, st>>>(s->ddesc, s->dlive, s->dstage_m, E);
+    FRMC_CUDA(cudaGetLastError());
+    FRMC_TRY(launch_items(s, s->items, s->nitems, 0, st));
+    k_gather_results<<<(E + 127) / 128, 128, 0, st>>>(s->ddesc, s->dlive, s->dstage_r, E);
+    FRMC_CUDA(cudaGetLastError());
+    FRMC_CUDA(cudaMemcpyAsync(s->hstage_r, s->dstage_r, sizeof(EResult) * E, cudaMemcpyDeviceToHost, st));
+    FRMC_CUDA(cudaStreamSynchronize(st));
+    for (int k = 0; k < E; ++k) {
+        if (chi2_new) chi2_new[k] = s->hstage_r[k].chi2_new;
+        if (accepted) accepted[k] = s->hstage_r[k].accepted;
+    }
+    return FRMC_OK;
+}
+
+int frmc_engines_sync(void *handle)
+{
+    EngineSet *s = as_set(handle);
+    if (!s)
+        return set_error(FRMC_E_ARG, "null handle");
+    FRMC_CUDA(cudaStreamSynchronize(s->stream));
+    return FRMC_OK;
+}
+
+int frmc_engines_state(void *handle, int32_t e, double *chi2, int64_t *step, int64_t *accepted)
+{
+    EngineSet *s = as_set(handle);
+    if (!s || !valid_id(s, e))
+        return set_error(FRMC_E_ARG, "engines_state: invalid engine");
+    EState S;
+    FRMC_CUDA(cudaMemcpy(&S, s->slots[e].d.st, sizeof(EState), cudaMemcpyDeviceToHost));
+    if (chi2) *chi2 = S.chi2;
+    if (step) *step = S.step;
+    if (accepted) *accepted = S.accepted;
+    return FRMC_OK;
+}
+
+int frmc_engines_results(void *handle, int32_t e, int64_t first_step, int32_t count, double *chi2_new,
+                         int32_t *accepted, int32_t *atoms)
+{
+    EngineSet *s = as_set(handle);
+    if (!s || !valid_id(s, e) || count < 0 || first_step < 0)
+        return set_error(FRMC_E_ARG, "engines_results: invalid arguments");
+    const EDesc &D = s->slots[e].d;
+    if (count > D.move_cap)
+        return set_error(FRMC_E_ARG, "engines_results: more results than the ring holds");
+    std::vector<EResult> r(count);
+    long long pos = first_step % D.move_cap;
+    int done = 0;
+    while (done < count) {
+        int chunk = (int)std::min<long long>(count - done, D.move_cap - pos);
+        FRMC_CUDA(cudaMemcpy(r.data() + done, D.results + pos, sizeof(EResult) * chunk, cudaMemcpyDeviceToHost));
+        done += chunk;
+        pos = 0;
+    }
+    for (int k = 0; k < count; ++k) {
+        if (chi2_new) chi2_new[k] = r[k].chi2_new;
+        if (accepted) accepted[k] = r[k].accepted;
+        if (atoms) atoms[k] = r[k].atom;
+    }
+    return FRMC_OK;
+}
+
+int frmc_engines_counts(void *handle, int32_t e, int32_t *counts)
+{
+    EngineSet *s = as_set(handle);
+    if (!s || !valid_id(s, e))
+        return set_error(FRMC_E_ARG, "engines_counts: invalid engine");
+    const EDesc &D = s->slots[e].d;
+    FRMC_CUDA(cudaMemcpy(counts, D.counts, sizeof(int) * 2 * D.total, cudaMemcpyDeviceToHost));
+    return FRMC_OK;
+}
+
+int frmc_engines_coords(void *handle, int32_t e, float *box_coords, float *real_coords)
+{
+    EngineSet *s = as_set(handle);
+    if (!s || !valid_id(s, e))
+        return set_error(FRMC_E_ARG, "engines_coords: invalid engine");
+    const EDesc &D = s->slots[e].d;
+    std::vector<float4> b(D.n), r(D.n);
+    FRMC_CUDA(cudaMemcpy(b.data(), D.box, sizeof(float4) * D.n, cudaMemcpyDeviceToHost));
+    FRMC_CUDA(cudaMemcpy(r.data(), D.real, sizeof(float4) * D.n, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < D.n; ++i) {
+        if (box_coords) {
+            box_coords[3 * i] = b[i].x;
+            box_coords[3 * i + 1] = b[i].y;
+            box_coords[3 * i + 2] = b[i].z;
+        }
+        if (real_coords) {
+            real_coords[3 * i] = r[i].x;
+            real_coords[3 * i + 1] = r[i].y;
+            real_coords[3 * i + 2] = r[i].z;
+        }
+    }
+    return FRMC_OK;
+}
+
+int frmc_engines_info(void *handle, int32_t *E, int64_t *total_atoms, int64_t *device_bytes)
+{
+    EngineSet *s = as_set(handle);
+    if (!s)
+        return set_error(FRMC_E_ARG, "null handle");
+    long long atoms = 0, bytes = 0;
+    for (int id : s->live) {
+        atoms += s->slots[id].d.n;
+        bytes += (long long)s->slots[id].bytes;
+    }
+    if (E) *E = (int32_t)s->live.size();
+    if (total_atoms) *total_atoms = atoms;
+    if (device_bytes) *device_bytes = bytes;
+    return FRMC_OK;
+}
+
+}  // extern "C"

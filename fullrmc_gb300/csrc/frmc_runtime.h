@@ -23,6 +23,21 @@ int cuda_fail(cudaError_t e, const char *what);
         if (_e != cudaSuccess) return ::frmc::cuda_fail(_e, #call); \
     } while (0)
 
+#define FRMC_TRY(x)              \
+    do {                         \
+        int _rc = (x);           \
+        if (_rc) return _rc;     \
+    } while (0)
+#define TRY_RC FRMC_TRY
+
+inline float int_bits_as_float(int v)
+{
+    float f;
+    static_assert(sizeof(f) == sizeof(v), "int/float size");
+    __builtin_memcpy(&f, &v, sizeof(f));
+    return f;
+}
+
 // A device allocation that only grows.
 struct DevBuf {
     void *p = nullptr;
@@ -105,5 +120,7 @@ int launch_counts_to_f32(const unsigned *counts, const float *h0, float *out, in
 
 // Pack AoS coordinates and element indexes into float4 (x, y, z, el bits).
 int launch_pack_atoms(const float *coords, const int *el, int n, float4 *out, cudaStream_t st);
+// The inverse: float4 (x, y, z, el bits) -> AoS coordinates and elements.
+int launch_unpack_atoms(const float4 *atoms, int n, float *coords, int *el, cudaStream_t st);
 
 }  // namespace frmc

@@ -417,6 +417,19 @@ __global__ void k_pack_atoms(const float *__restrict__ coords, const int *__rest
                              __int_as_float(el[i]));
 }
 
+__global__ void k_unpack_atoms(const float4 *__restrict__ atoms, int n, float *__restrict__ coords,
+                               int *__restrict__ el)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        float4 a = atoms[i];
+        coords[3 * (long long)i] = a.x;
+        coords[3 * (long long)i + 1] = a.y;
+        coords[3 * (long long)i + 2] = a.z;
+        el[i] = __float_as_int(a.w);
+    }
+}
+
 // ================================================================ launchers
 template <int BM, int R, bool Q>
 static int launch_full_typed(const FullParams &p, int threads, int grid, size_t smem, cudaStream_t st)
@@ -566,6 +579,15 @@ int launch_counts_to_f32(const unsigned *counts, const float *h0, float *out, in
     if (blocks > 4096)
         blocks = 4096;
     k_counts_to_f32<<<(int)blocks, 256, 0, st>>>(counts, h0, out, total);
+    FRMC_CUDA(cudaGetLastError());
+    return FRMC_OK;
+}
+
+int launch_unpack_atoms(const float4 *atoms, int n, float *coords, int *el, cudaStream_t st)
+{
+    if (n <= 0)
+        return FRMC_OK;
+    k_unpack_atoms<<<(n + 255) / 256, 256, 0, st>>>(atoms, n, coords, el);
     FRMC_CUDA(cudaGetLastError());
     return FRMC_OK;
 }

@@ -1,0 +1,343 @@
+"""Device-resident RMC engines (the batched path) over ``frmc_engines_*``.
+
+An engine is one fullrmc Metropolis chain with a single
+PairDistributionConstraint whose whole state -- coordinates, oriented
+histogram counts, experimental curve, chi2 -- lives in HBM.  A batched step
+advances every engine of a set by one move in one kernel launch (captured in
+a CUDA graph for runs of steps); ``step(engine=e)`` advances one engine alone
+(the plain one-engine-at-a-time GPU path).  Moves are generated on the host
+by seeded per-engine streams and pushed into device rings ahead of the steps,
+so each chain is strictly sequential and gives the same accept sequence,
+chi2 values and counts alone or in any batch.
+
+Host-side set-up follows fullrmc's constraint definitions:
+``PairDistributionConstraints.py:726-774`` (limits, edges, shell volumes),
+``:847-895`` (G(r) from the histograms) and ``Core/Constraint.py`` (chi2 =
+standard error / varianceSquared); these constants are FP64.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from ._native import F32P, F64P, I32P, check, load, register
+
+F32 = np.float32
+
+
+class _Spec(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int32), ("ne", ctypes.c_int32), ("hs", ctypes.c_int32), ("isPBC", ctypes.c_int32),
+                ("box_coords", F32P), ("real_coords", F32P), ("el", I32P), ("mol", I32P), ("basis", F32P),
+                ("rbasis", F32P), ("minDistance", ctypes.c_float), ("maxDistance", ctypes.c_float),
+                ("bin", ctypes.c_float), ("npairs", ctypes.c_int32), ("pair_i", I32P), ("pair_j", I32P),
+                ("pair_coef", F64P), ("rfac", F64P), ("inv_shell_volume", F64P), ("experimental", F64P),
+                ("data_weights", F64P), ("variance_squared", ctypes.c_double), ("tolerance", ctypes.c_double),
+                ("move_cap", ctypes.c_int32)]
+
+
+_vp = ctypes.c_void_p
+_i32, _i64 = ctypes.c_int32, ctypes.c_int64
+register("frmc_engine_footprint", [ctypes.POINTER(_Spec), ctypes.POINTER(_i64)])
+register("frmc_engines_new", [ctypes.POINTER(_vp)])
+register("frmc_engines_create", [ctypes.POINTER(_Spec), _i32, ctypes.POINTER(_vp)])
+register("frmc_engines_add", [_vp, ctypes.POINTER(_Spec), ctypes.POINTER(_i32)])
+register("frmc_engines_remove", [_vp, _i32])
+register("frmc_engines_live", [_vp, I32P, _i32, ctypes.POINTER(_i32)])
+register("frmc_engines_step_host", [_vp, I32P, F32P, F32P, F64P, I32P])
+register("frmc_engines_destroy", [_vp])
+register("frmc_engines_set_tune", [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int])
+register("frmc_engines_get_tune", [_vp] + [ctypes.POINTER(ctypes.c_int)] * 4)
+register("frmc_engines_init", [_vp])
+register("frmc_engines_push_moves", [_vp, _i32, I32P, F32P, F32P, _i32, _i64, ctypes.c_int])
+register("frmc_engines_step", [_vp, _i32, _i32, ctypes.c_int, _vp])
+register("frmc_engines_sync", [_vp])
+register("frmc_engines_state", [_vp, _i32, F64P, ctypes.POINTER(_i64), ctypes.POINTER(_i64)])
+register("frmc_engines_results", [_vp, _i32, _i64, _i32, F64P, I32P, I32P])
+register("frmc_engines_counts", [_vp, _i32, I32P])
+register("frmc_engines_coords", [_vp, _i32, F32P, F32P])
+register("frmc_engines_info", [_vp, ctypes.POINTER(_i32), ctypes.POINTER(_i64), ctypes.POINTER(_i64)])
+
+
+def normalized_weighting(counts, scattering):
+    """w_ij = (2 - delta_ij) c_i c_j b_i b_j / (sum_k c_k b_k)^2, c_i = n_i / N.
+
+    The definition of the element-pair weights in fullrmc's documentation
+    (PairDistributionConstraints.py:66-86); sum_{i<=j} w_ij = 1."""
+    n = np.asarray(counts, np.float64)
+    b = np.asarray(scattering, np.float64)
+    c = n / n.sum()
+    s = (c * b).sum()
+    w = np.outer(c * b, c * b) / (s * s)
+    w = w * (2.0 - np.eye(len(n)))
+    return w
+
+
+@dataclass
+class PDFModel:
+    """FP64 constants of one PairDistributionConstraint on an r grid."""
+    r: np.ndarray                # experimental r grid (float32, uniform)
+    G_exp: np.ndarray            # experimental G(r)
+    elements_count: np.ndarray   # atoms per element index
+    weights: np.ndarray          # (ne, ne) symmetric w_ij
+    volume: float
+    data_weights: np.ndarray | None = None
+    variance_squared: float = 1.0
+
+    def __post_init__(self):
+        x = np.asarray(self.r, F32)
+        self.r = x
+        b = F32(x[1] - x[0])
+        self.bin = b
+        self.minDistance = F32(x[0] - b / F32(2.0))
+        self.maxDistance = F32(x[-1] + b / F32(2.0))
+        edges = np.concatenate([x - b / F32(2.0), [x[-1] + b / F32(2.0)]]).astype(F32)
+        self.edges = edges
+        self.hs = len(x)
+        e64 = edges.astype(np.float64)
+        self.shell_volumes = 4.0 / 3.0 * np.pi * (e64[1:] ** 3 - e64[:-1] ** 3)
+        n = np.asarray(self.elements_count, np.float64)
+        self.n_atoms = int(n.sum())
+        self.rho0 = self.n_atoms / float(self.volume)
+        self.rfac = 4.0 * np.pi * x.astype(np.float64) * self.rho0
+        ne = len(n)
+        pi, pj, pc = [], [], []
+        for i in range(ne):
+            for j in range(i, ne):
+                Nij = n[i] * (n[i] - 1.0) / 2.0 if i == j else n[i] * n[j]
+                if Nij <= 0:
+                    continue
+                pi.append(i)
+                pj.append(j)
+                pc.append(float(self.weights[i][j]) * float(self.volume) / Nij)
+        self.pair_i = np.asarray(pi, np.int32)
+        self.pair_j = np.asarray(pj, np.int32)
+        self.pair_coef = np.asarray(pc, np.float64)
+
+    def G_fp64(self, intra, inter):
+        """G(r) of oriented (ne, ne, hs) counts (the engine's formula, FP64)."""
+        intra = np.asarray(intra, np.float64)
+        inter = np.asarray(inter, np.float64)
+        g = np.zeros(self.hs)
+        for i, j, c in zip(self.pair_i, self.pair_j, self.pair_coef):
+            if i == j:
+                nij = intra[i, i] + inter[i, i]
+            else:
+                nij = intra[i, j] + intra[j, i] + inter[i, j] + inter[j, i]
+            g += c * nij
+        g /= self.shell_volumes
+        return self.rfac * (g - 1.0)
+
+    def chi2_fp64(self, intra, inter):
+        d = np.asarray(self.G_exp, np.float64) - self.G_fp64(intra, inter)
+        w = 1.0 if self.data_weights is None else np.asarray(self.data_weights, np.float64)
+        return float(np.sum(w * d * d) / self.variance_squared)
+
+
+@dataclass
+class EngineSystem:
+    box_coords: np.ndarray
+    real_coords: np.ndarray
+    el: np.ndarray
+    mol: np.ndarray
+    basis: np.ndarray
+    rbasis: np.ndarray
+    isPBC: bool
+    model: PDFModel
+    tolerance: float = 0.0
+    keep: list = field(default_factory=list, repr=False)
+
+
+def translation_moves(rng: np.random.Generator, n_atoms: int, count: int, amplitude: float):
+    """Single-atom random translations: atom uniform in [0, n), direction
+    uniform, length uniform in [0, amplitude) (the distribution of
+    TranslationGenerator, Generators/Translations.py:171-190 with
+    Core/Collection.py:674-700), plus one uniform per step for the tolerance
+    test.  float32, like fullrmc's move vectors."""
+    atoms = rng.integers(0, n_atoms, size=count).astype(np.int32)
+    v = (1.0 - 2.0 * rng.random((count, 3))).astype(F32)
+    norm = np.sqrt((v.astype(np.float64) ** 2).sum(axis=1)).astype(F32)
+    norm[norm == 0] = F32(1.0)
+    v = v / norm[:, None]
+    v = (v * (rng.random(count) * amplitude).astype(F32)[:, None]).astype(F32)
+    u = rng.random(count).astype(F32)
+    return atoms, np.ascontiguousarray(v), u
+
+
+def make_spec(system, move_cap):
+    """ctypes spec of one system; returns (spec, arrays that must stay alive)."""
+    s = system
+    m = s.model
+    arrs = dict(box=np.ascontiguousarray(s.box_coords, F32), real=np.ascontiguousarray(s.real_coords, F32),
+                el=np.ascontiguousarray(s.el, np.int32), mol=np.ascontiguousarray(s.mol, np.int32),
+                B=np.ascontiguousarray(s.basis, F32), RB=np.ascontiguousarray(s.rbasis, F32),
+                pi=np.ascontiguousarray(m.pair_i), pj=np.ascontiguousarray(m.pair_j),
+                pc=np.ascontiguousarray(m.pair_coef), rfac=np.ascontiguousarray(m.rfac),
+                iv=np.ascontiguousarray(1.0 / m.shell_volumes),
+                ex=np.ascontiguousarray(np.asarray(m.G_exp, np.float64)),
+                dw=None if m.data_weights is None else np.ascontiguousarray(m.data_weights, np.float64))
+    sp = _Spec()
+    sp.n = arrs["box"].shape[0]
+    sp.ne = len(m.elements_count)
+    sp.hs = m.hs
+    sp.isPBC = int(bool(s.isPBC))
+    sp.box_coords = arrs["box"].ctypes.data_as(F32P)
+    sp.real_coords = arrs["real"].ctypes.data_as(F32P)
+    sp.el = arrs["el"].ctypes.data_as(I32P)
+    sp.mol = arrs["mol"].ctypes.data_as(I32P)
+    sp.basis = arrs["B"].ctypes.data_as(F32P)
+    sp.rbasis = arrs["RB"].ctypes.data_as(F32P)
+    sp.minDistance, sp.maxDistance, sp.bin = m.minDistance, m.maxDistance, m.bin
+    sp.npairs = len(m.pair_i)
+    sp.pair_i = arrs["pi"].ctypes.data_as(I32P)
+    sp.pair_j = arrs["pj"].ctypes.data_as(I32P)
+    sp.pair_coef = arrs["pc"].ctypes.data_as(F64P)
+    sp.rfac = arrs["rfac"].ctypes.data_as(F64P)
+    sp.inv_shell_volume = arrs["iv"].ctypes.data_as(F64P)
+    sp.experimental = arrs["ex"].ctypes.data_as(F64P)
+    sp.data_weights = arrs["dw"].ctypes.data_as(F64P) if arrs["dw"] is not None else None
+    sp.variance_squared = float(m.variance_squared)
+    sp.tolerance = float(s.tolerance)
+    sp.move_cap = int(move_cap)
+    return sp, arrs
+
+
+def footprint(system, move_cap):
+    """Device bytes an engine of this system occupies."""
+    sp, _keep = make_spec(system, move_cap)
+    b = ctypes.c_int64()
+    check(load().frmc_engine_footprint(ctypes.byref(sp), ctypes.byref(b)))
+    return b.value
+
+
+class EngineSet:
+    """A set of device-resident engines stepped together or one at a time."""
+
+    def __init__(self, systems=(), move_cap: int = 4096, tune=None):
+        load()
+        self.move_cap = int(move_cap)
+        self.systems = {}
+        h = ctypes.c_void_p()
+        systems = list(systems)
+        if systems:
+            specs = (_Spec * len(systems))()
+            keep = []
+            for k, s in enumerate(systems):
+                sp, arrs = make_spec(s, self.move_cap)
+                specs[k] = sp
+                keep.append(arrs)
+            check(load().frmc_engines_create(specs, len(systems), ctypes.byref(h)))
+            self.systems = {k: s for k, s in enumerate(systems)}
+        else:
+            check(load().frmc_engines_new(ctypes.byref(h)))
+        self.handle = h
+        if tune is not None:
+            self.set_tune(*tune)
+
+    @property
+    def E(self):
+        return len(self.systems)
+
+    def add(self, system, move_cap=None):
+        """Add (and initialise) one engine; returns its id."""
+        sp, _keep = make_spec(system, move_cap or self.move_cap)
+        i = ctypes.c_int32()
+        check(load().frmc_engines_add(self.handle, ctypes.byref(sp), ctypes.byref(i)))
+        self.systems[i.value] = system
+        return i.value
+
+    def remove(self, e):
+        check(load().frmc_engines_remove(self.handle, int(e)))
+        self.systems.pop(int(e), None)
+
+    def live(self):
+        ids = np.empty(max(1, len(self.systems)), np.int32)
+        c = ctypes.c_int32()
+        check(load().frmc_engines_live(self.handle, ids.ctypes.data_as(I32P), len(ids), ctypes.byref(c)))
+        return ids[:c.value].copy()
+
+    def step_host(self, atoms, vecs, u):
+        """One batched step of all live engines from host arrays (live-id order);
+        returns (chi2_new, accepted)."""
+        atoms = np.ascontiguousarray(atoms, np.int32)
+        vecs = np.ascontiguousarray(vecs, F32)
+        u = np.ascontiguousarray(u, F32)
+        c2 = np.empty(len(atoms), np.float64)
+        acc = np.empty(len(atoms), np.int32)
+        check(load().frmc_engines_step_host(self.handle, atoms.ctypes.data_as(I32P), vecs.ctypes.data_as(F32P),
+                                            u.ctypes.data_as(F32P), c2.ctypes.data_as(F64P),
+                                            acc.ctypes.data_as(I32P)))
+        return c2, acc
+
+    # ------------------------------------------------------------ control
+    def set_tune(self, tile, threads, ctas_per_sm):
+        check(load().frmc_engines_set_tune(self.handle, int(tile), int(threads), int(ctas_per_sm)))
+
+    def get_tune(self):
+        v = [ctypes.c_int() for _ in range(4)]
+        check(load().frmc_engines_get_tune(self.handle, *[ctypes.byref(x) for x in v]))
+        return tuple(x.value for x in v)
+
+    def init(self):
+        check(load().frmc_engines_init(self.handle))
+
+    def push_moves(self, e, atoms, vecs, u, first_step):
+        atoms = np.ascontiguousarray(atoms, np.int32)
+        vecs = np.ascontiguousarray(vecs, F32)
+        u = np.ascontiguousarray(u, F32)
+        check(load().frmc_engines_push_moves(self.handle, int(e), atoms.ctypes.data_as(I32P),
+                                             vecs.ctypes.data_as(F32P), u.ctypes.data_as(F32P), len(atoms),
+                                             int(first_step), 0))
+
+    def step(self, steps=1, engine=-1, graph=True, sync=True, stream=None):
+        check(load().frmc_engines_step(self.handle, int(engine), int(steps), int(bool(graph)), stream))
+        if sync:
+            self.sync()
+
+    def sync(self):
+        check(load().frmc_engines_sync(self.handle))
+
+    # ------------------------------------------------------------ queries
+    def state(self, e):
+        c2, st, acc = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
+        check(load().frmc_engines_state(self.handle, int(e), ctypes.byref(c2), ctypes.byref(st), ctypes.byref(acc)))
+        return c2.value, st.value, acc.value
+
+    def results(self, e, first_step, count):
+        c = np.empty(count, np.float64)
+        a = np.empty(count, np.int32)
+        at = np.empty(count, np.int32)
+        check(load().frmc_engines_results(self.handle, int(e), int(first_step), int(count), c.ctypes.data_as(F64P),
+                                          a.ctypes.data_as(I32P), at.ctypes.data_as(I32P)))
+        return c, a, at
+
+    def counts(self, e):
+        s = self.systems[e]
+        ne, hs = len(s.model.elements_count), s.model.hs
+        out = np.empty((2, ne, ne, hs), np.int32)
+        check(load().frmc_engines_counts(self.handle, int(e), out.ctypes.data_as(I32P)))
+        return out[0], out[1]
+
+    def coords(self, e):
+        n = self.systems[e].box_coords.shape[0]
+        b = np.empty((n, 3), F32)
+        r = np.empty((n, 3), F32)
+        check(load().frmc_engines_coords(self.handle, int(e), b.ctypes.data_as(F32P), r.ctypes.data_as(F32P)))
+        return b, r
+
+    def info(self):
+        E, a, b = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int64()
+        check(load().frmc_engines_info(self.handle, ctypes.byref(E), ctypes.byref(a), ctypes.byref(b)))
+        return {"engines": E.value, "atoms": a.value, "device_bytes": b.value}
+
+    def close(self):
+        if getattr(self, "handle", None):
+            check(load().frmc_engines_destroy(self.handle))
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

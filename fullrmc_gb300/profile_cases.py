@@ -1,0 +1,92 @@
+"""Small, self-contained runs of the hot kernels, sized for profiling.
+
+    python -m fullrmc_gb300.profile_cases allpairs --n 30000 --reps 3
+    python -m fullrmc_gb300.profile_cases engines --count 64 --steps 5
+
+``allpairs`` runs the all-pairs histogram (three species, triclinic box with
+gamma = 120 degrees at 0.1057 atoms/A^3, r 0-20 A) on device buffers;
+``engines`` runs batched Metropolis steps of ``count`` mixed-size engines.
+Both print one JSON line with the CUDA-event time per launch.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+
+import numpy as np
+
+
+def allpairs(n, reps):
+    import torch
+    from fullrmc_gb300 import _native as native
+    from fullrmc_gb300 import synthetic
+    from fullrmc_gb300._native import F32P
+    s = synthetic.triclinic_100k(seed=0, n=n)
+    m = s.model
+    ne = len(m.elements_count)
+    total = ne * ne * m.hs
+    dev = torch.device("cuda", 0)
+    st = torch.cuda.Stream()
+    c = torch.from_numpy(s.box_coords).to(dev)
+    el = torch.from_numpy(s.el).to(dev)
+    mol = torch.from_numpy(s.mol).to(dev)
+    a4 = torch.empty((n, 4), dtype=torch.float32, device=dev)
+    cnt = torch.zeros(2 * total, dtype=torch.int32, device=dev)
+    B = np.ascontiguousarray(s.basis)
+    with torch.cuda.stream(st):
+        native.call("frmc_dev_pack_atoms", c.data_ptr(), el.data_ptr(), n, a4.data_ptr(), st.cuda_stream)
+        args = (a4.data_ptr(), mol.data_ptr(), n, B.ctypes.data_as(F32P), 1, ne, m.minDistance, m.maxDistance,
+                m.bin, m.hs, cnt.data_ptr(), st.cuda_stream)
+        ev = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            native.call("frmc_dev_full_hist_counts", *args)
+            e1.record(st)
+            ev.append((e0, e1))
+    torch.cuda.synchronize()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    return {"case": "allpairs", "atoms": n, "ms": ms, "pairs": n * (n - 1) / 2, "in_range": int(cnt.sum().item())}
+
+
+def engines(count, steps):
+    import torch
+    from fullrmc_gb300 import synthetic
+    from fullrmc_gb300.engine import EngineSet, translation_moves
+    systems = synthetic.mixed_engines(seed=0, count=count)
+    es = EngineSet(systems, move_cap=steps + 4)
+    es.init()
+    for e, s in enumerate(systems):
+        a, v, u = translation_moves(np.random.default_rng([0, e]), s.box_coords.shape[0], steps, 0.1)
+        es.push_moves(e, a, v, u, 0)
+    st = torch.cuda.Stream()
+    ev = []
+    with torch.cuda.stream(st):
+        for _ in range(steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            es.step(1, graph=False, sync=False, stream=st.cuda_stream)
+            e1.record(st)
+            ev.append((e0, e1))
+    torch.cuda.synchronize()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    pairs = sum(2 * (s.box_coords.shape[0] - 1) for s in systems)
+    acc = sum(es.state(e)[2] for e in range(count))
+    es.close()
+    return {"case": "engines", "engines": count, "steps": steps, "ms": ms, "pairs_per_step": pairs, "accepted": acc}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("case", choices=["allpairs", "engines"])
+    ap.add_argument("--n", type=int, default=30000)
+    ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--count", type=int, default=64)
+    ap.add_argument("--steps", type=int, default=5)
+    a = ap.parse_args()
+    out = allpairs(a.n, a.reps) if a.case == "allpairs" else engines(a.count, a.steps)
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

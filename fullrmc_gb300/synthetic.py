@@ -1,0 +1,122 @@
+"""Seeded synthetic systems with the shapes of the benchmark configurations.
+
+No dataset is involved: coordinates are uniform random from a seed, and
+each engine's target G(r) is a seeded synthetic curve.  All sizes follow the
+workload definitions:
+
+* ``alloy_5000``: 5,000 atoms, two species 50/50, cubic box of side 38.2 A,
+  r 0-15 A, dr 0.01 A.
+* ``triclinic_100k``: 100,000 atoms, three species 0.5/0.3/0.2, triclinic box
+  a = b = c = 103 A, alpha = beta = 90, gamma = 120 degrees, r 0-20 A.
+* ``mixed_engines``: 256 engines, atom counts log-uniform in [1,000, 20,000],
+  1-4 species, cubic or triclinic boxes at 0.08-0.10 atoms/A^3, r 0-12 A.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .engine import EngineSystem, PDFModel, normalized_weighting
+
+F32 = np.float32
+
+
+def r_grid(rmax, dr=0.01):
+    return np.arange(0.0, rmax + dr / 10.0, dr).astype(F32)
+
+
+def triclinic(a, b, c, alpha, beta, gamma):
+    """Row-vector basis with a along x and b in the xy plane (exact zeros kept)."""
+    al, be, ga = np.radians([alpha, beta, gamma])
+    cx = c * np.cos(be)
+    cy = c * (np.cos(al) - np.cos(be) * np.cos(ga)) / np.sin(ga)
+    cz = np.sqrt(max(c * c - cx * cx - cy * cy, 0.0))
+    B = np.array([[a, 0, 0], [b * np.cos(ga), b * np.sin(ga), 0], [cx, cy, cz]], np.float64)
+    B[np.abs(B) < 1e-9 * max(a, b, c)] = 0.0
+    return B.astype(F32)
+
+
+def transform_f32(M, coords):
+    """coords . M in float32 with the reference's operation order."""
+    M = np.asarray(M, F32)
+    c = np.asarray(coords, F32)
+    out = np.empty_like(c)
+    for k in range(3):
+        out[:, k] = (c[:, 0] * M[0, k] + c[:, 1] * M[1, k]) + c[:, 2] * M[2, k]
+    return out
+
+
+def species(rng, n, fractions):
+    counts = np.floor(np.asarray(fractions, np.float64) * n).astype(int)
+    counts[0] += n - counts.sum()
+    el = np.repeat(np.arange(len(fractions)), counts).astype(np.int32)
+    rng.shuffle(el)
+    return el
+
+
+def synthetic_G(rng, r, rho):
+    """A damped liquid-like G(r) with seeded shape: 4 pi r rho (g - 1),
+    g(r) = 1 + A exp(-r / lam) sin(2 pi (r - r0) / d) / r beyond a core."""
+    r64 = r.astype(np.float64)
+    A = rng.uniform(0.8, 1.6)
+    lam = rng.uniform(2.0, 4.0)
+    d = rng.uniform(2.5, 3.5)
+    r0 = rng.uniform(2.0, 2.6)
+    g = np.where(r64 < r0 * 0.85, 0.0, 1.0 + A * np.exp(-(r64 - r0) / lam) * np.cos(2 * np.pi * (r64 - r0) / d))
+    G = 4 * np.pi * r64 * rho * (g - 1.0)
+    return (G + rng.normal(0.0, 0.01, size=r.shape)).astype(F32)
+
+
+def make_system(rng, n, fractions, basis, rmax, molsize=1, isPBC=True, target=None):
+    """One engine system: seeded coordinates, elements, molecules and an FP64 PDF model."""
+    basis = np.asarray(basis, F32)
+    rbasis = np.linalg.inv(basis.astype(np.float64)).astype(F32)
+    frac = rng.random((n, 3))
+    real = (frac @ basis.astype(np.float64)).astype(F32)
+    # box coordinates as fullrmc derives them from the real ones
+    # (Engine.py:2265 -> boundary_conditions_collection.pyx:104-106, float32)
+    box = transform_f32(rbasis, real)
+    el = species(rng, n, fractions)
+    mol = (np.arange(n) // molsize).astype(np.int32)
+    volume = abs(float(np.linalg.det(basis.astype(np.float64))))
+    r = r_grid(rmax)
+    counts = np.bincount(el, minlength=len(fractions))
+    weights = normalized_weighting(counts, np.ones(len(fractions)) + 0.25 * np.arange(len(fractions)))
+    G = synthetic_G(rng, r, n / volume) if target is None else target
+    model = PDFModel(r=r, G_exp=G, elements_count=counts, weights=weights, volume=volume)
+    return EngineSystem(box_coords=box, real_coords=real, el=el, mol=mol, basis=basis, rbasis=rbasis,
+                        isPBC=isPBC, model=model)
+
+
+def alloy_5000(seed=0, n=5000):
+    rng = np.random.default_rng(seed)
+    L = 38.2 * (n / 5000.0) ** (1.0 / 3.0)
+    return make_system(rng, n, [0.5, 0.5], np.diag([L, L, L]), 15.0)
+
+
+def triclinic_100k(seed=0, n=100000):
+    rng = np.random.default_rng(seed)
+    a = 103.0 * (n / 100000.0) ** (1.0 / 3.0)
+    return make_system(rng, n, [0.5, 0.3, 0.2], triclinic(a, a, a, 90, 90, 120), 20.0)
+
+
+def mixed_engines(seed=0, count=256, nmin=1000, nmax=20000, rmax=12.0):
+    """``count`` engines with log-uniform sizes, 1-4 species, cubic or
+    triclinic boxes at 0.08-0.10 atoms/A^3."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        n = int(round(np.exp(rng.uniform(np.log(nmin), np.log(nmax)))))
+        ns = int(rng.integers(1, 5))
+        fr = rng.dirichlet(np.ones(ns) * 3.0)
+        rho = rng.uniform(0.08, 0.10)
+        if rng.random() < 0.5:
+            L = (n / rho) ** (1.0 / 3.0)
+            B = np.diag([L, L, L])
+        else:
+            al, be, ga = rng.uniform(80, 100), rng.uniform(80, 100), rng.uniform(95, 120)
+            unit = triclinic(1.0, 1.0, 1.0, al, be, ga).astype(np.float64)
+            vol1 = abs(np.linalg.det(unit))
+            a = (n / rho / vol1) ** (1.0 / 3.0)
+            B = triclinic(a, a, a, al, be, ga)
+        out.append(make_system(np.random.default_rng([seed, k]), n, fr, B, rmax))
+    return out

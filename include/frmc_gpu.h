@@ -15,8 +15,8 @@
  *     compute and copy back before returning (the drop-in path).  They keep no
  *     host data between calls.
  *   - "frmc_dev_*" entry points take device pointers and a cudaStream_t
- *     (passed as void*, NULL = the library's stream) and return without
- *     synchronising.
+ *     (passed as void*; NULL is the CUDA legacy default stream) and return
+ *     without synchronising.
  *   - Coordinates are float32 (n, 3) row-major; basis is float32 (3, 3)
  *     row-major with the box vectors as rows (real = box . basis).
  *   - Histograms are float32 C-contiguous (ne, ne, hs); counts are uint32.

@@ -1,0 +1,108 @@
+/*
+ * frmc_gpu_engine.h -- device-resident RMC engines (batched and served).
+ *
+ * Each engine is one fullrmc Metropolis chain with a single
+ * PairDistributionConstraint, stepped entirely on the GPU:
+ *   - the step is fullrmc's Engine.run step (Engine.py:3278-3344) with
+ *     single-atom translation moves (Generators/Translations.py:171-190),
+ *   - the histogram update is the M term of compute_before_move /
+ *     compute_after_move (Constraints/PairDistributionConstraints.py:1044-1129),
+ *     kept as oriented int32 counts equal to the constraint's running data,
+ *   - G(r) (PairDistributionConstraints.py:847-895) and chi2 are FP64.
+ * Moves (atom, displacement vector, uniform number for the tolerance test)
+ * are generated by the caller and pushed into a per-engine ring, so the
+ * chains stay strictly sequential and reproducible: an engine gives the same
+ * accept sequence and bit-identical counts alone or in any batch.
+ *
+ * There is no counterpart of these entry points in fullrmc itself; they are
+ * the batched engines and the serving loop built around the histogram path.
+ * Conventions as in frmc_gpu.h (int status, frmc_last_error()).
+ */
+#ifndef FRMC_GPU_ENGINE_H
+#define FRMC_GPU_ENGINE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+typedef struct {
+    int32_t n;            /* atoms                                              */
+    int32_t ne;           /* elements                                           */
+    int32_t hs;           /* histogram bins                                     */
+    int32_t isPBC;
+    const float *box_coords;   /* (n, 3) box (fractional) coordinates           */
+    const float *real_coords;  /* (n, 3) real coordinates                       */
+    const int32_t *el;         /* (n,) element index in [0, ne)                 */
+    const int32_t *mol;        /* (n,) molecule index                           */
+    const float *basis;        /* (3, 3) rows = box vectors                     */
+    const float *rbasis;       /* (3, 3) inverse of basis (real -> box)         */
+    float minDistance, maxDistance, bin;
+    int32_t npairs;            /* unordered element pairs (i <= j)              */
+    const int32_t *pair_i;
+    const int32_t *pair_j;
+    const double *pair_coef;   /* w_ij / (N_ij / V)                             */
+    const double *rfac;        /* (hs,) 4 pi r rho0                             */
+    const double *inv_shell_volume; /* (hs,) 1 / shell volume                   */
+    const double *experimental;     /* (hs,) experimental G(r)                  */
+    const double *data_weights;     /* (hs,) or NULL                            */
+    double variance_squared;
+    double tolerance;          /* Engine tolerance (reject iff chi2 rises and u > tolerance) */
+    int32_t move_cap;          /* ring size for moves and step results          */
+} frmc_engine_spec;
+
+/* Device bytes one engine of this spec occupies (its state, tables and rings). */
+int frmc_engine_footprint(const frmc_engine_spec *spec, int64_t *bytes);
+/* An empty engine set on the current device. */
+int frmc_engines_new(void **handle);
+/* Create E engines on the current device (all state resident in HBM); engine
+ * ids are 0..E-1.  frmc_engines_init computes their initial histograms. */
+int frmc_engines_create(const frmc_engine_spec *specs, int32_t E, void **handle);
+/* Add one engine (allocated, uploaded and initialised; *id receives its id)
+ * or remove one; ids of removed engines are reused.  Used by the serving loop. */
+int frmc_engines_add(void *handle, const frmc_engine_spec *spec, int32_t *id);
+int frmc_engines_remove(void *handle, int32_t id);
+/* Live engine ids in stepping order (ascending); *count receives the number. */
+int frmc_engines_live(void *handle, int32_t *ids, int32_t cap, int32_t *count);
+int frmc_engines_destroy(void *handle);
+/* Work-list configuration: atoms per item, threads per CTA, CTAs per SM. */
+int frmc_engines_set_tune(void *handle, int tile, int threads, int ctas_per_sm);
+int frmc_engines_get_tune(void *handle, int *tile, int *threads, int *ctas_per_sm, int *nitems);
+/* All-pairs histograms of the initial coordinates and the initial chi2. */
+int frmc_engines_init(void *handle);
+/* Moves for steps [first_step, first_step + count) of engine e: atoms (count,),
+ * vecs (count, 3) real-space displacements, u (count,) uniforms (NULL = 1). */
+int frmc_engines_push_moves(void *handle, int32_t e, const int32_t *atoms, const float *vecs, const float *u,
+                            int32_t count, int64_t first_step, int from_device);
+/* Advance `steps` steps: engine == -1 steps every engine in one launch per
+ * step (the batched path); engine >= 0 steps that engine alone.  use_graph
+ * captures the launches in a CUDA graph (cached per engine/steps).  Returns
+ * without synchronising; stream NULL = the set's own stream. */
+int frmc_engines_step(void *handle, int32_t engine, int32_t steps, int use_graph, void *stream);
+/* One batched step of every live engine from host buffers: atoms (E,), vecs
+ * (E, 3), u (E,) in live-id order are uploaded in one copy, the step runs,
+ * and each engine's new chi2 and decision come back in one copy (chi2_new,
+ * accepted may be NULL).  Synchronous. */
+int frmc_engines_step_host(void *handle, const int32_t *atoms, const float *vecs, const float *u, double *chi2_new,
+                           int32_t *accepted);
+int frmc_engines_sync(void *handle);
+int frmc_engines_state(void *handle, int32_t e, double *chi2, int64_t *step, int64_t *accepted);
+/* Per-step results of steps [first_step, first_step + count). */
+int frmc_engines_results(void *handle, int32_t e, int64_t first_step, int32_t count, double *chi2_new,
+                         int32_t *accepted, int32_t *atoms);
+/* Oriented int32 counts [2][ne][ne][hs] (0 = intra, 1 = inter). */
+int frmc_engines_counts(void *handle, int32_t e, int32_t *counts);
+int frmc_engines_coords(void *handle, int32_t e, float *box_coords, float *real_coords);
+int frmc_engines_info(void *handle, int32_t *E, int64_t *total_atoms, int64_t *device_bytes);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+#ifdef __cplusplus
+}
+#endif
+#endif /* FRMC_GPU_ENGINE_H */

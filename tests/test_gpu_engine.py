@@ -1,0 +1,168 @@
+"""Device-resident engines: exactness against the oracle, and identical
+chains alone or batched, under any tile configuration or graph capture."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _systems(count=6, seed=3, nmin=600, nmax=3000):
+    from fullrmc_gb300 import synthetic
+    return synthetic.mixed_engines(seed=seed, count=count, nmin=nmin, nmax=nmax, rmax=10.0)
+
+
+def _moves(systems, steps, seed=11, amp=0.3):
+    from fullrmc_gb300.engine import translation_moves
+    return [translation_moves(np.random.default_rng([seed, k]), s.box_coords.shape[0], steps, amp)
+            for k, s in enumerate(systems)]
+
+
+def _run(systems, moves, steps, mode, tune=None, graph=True, chunk=None):
+    from fullrmc_gb300.engine import EngineSet
+    es = EngineSet(systems, move_cap=max(64, steps), tune=tune)
+    es.init()
+    chi2_0 = [es.state(e)[0] for e in range(len(systems))]
+    for e, (a, v, u) in enumerate(moves):
+        es.push_moves(e, a[:steps], v[:steps], u[:steps], 0)
+    chunk = chunk or steps
+    if mode == "batched":
+        for s0 in range(0, steps, chunk):
+            es.step(min(chunk, steps - s0), engine=-1, graph=graph)
+    else:
+        for e in range(len(systems)):
+            for s0 in range(0, steps, chunk):
+                es.step(min(chunk, steps - s0), engine=e, graph=graph)
+    out = []
+    for e in range(len(systems)):
+        c2, a, at = es.results(e, 0, steps)
+        out.append(dict(chi2=c2, acc=a, atoms=at, state=es.state(e), counts=es.counts(e), coords=es.coords(e),
+                        chi2_0=chi2_0[e]))
+    es.close()
+    return out
+
+
+def _same(r1, r2):
+    for a, b in zip(r1, r2):
+        assert np.array_equal(a["acc"], b["acc"])
+        assert np.array_equal(a["chi2"].view(np.int64), b["chi2"].view(np.int64))  # bit-identical FP64
+        assert a["state"] == b["state"]
+        assert np.array_equal(a["counts"][0], b["counts"][0]) and np.array_equal(a["counts"][1], b["counts"][1])
+        assert np.array_equal(a["coords"][0], b["coords"][0]) and np.array_equal(a["coords"][1], b["coords"][1])
+
+
+def test_init_counts_match_oracle(oracle_mod):
+    from fullrmc_gb300.engine import EngineSet
+    systems = _systems(count=3)
+    es = EngineSet(systems, move_cap=8)
+    es.init()
+    for e, s in enumerate(systems):
+        m = s.model
+        want = oracle_mod.full_pairs_histograms_coords(s.box_coords, s.basis, True, s.mol, s.el,
+                                                       len(m.elements_count), m.minDistance, m.maxDistance, m.bin,
+                                                       m.hs)
+        got = es.counts(e)
+        assert np.array_equal(got[0].astype(np.float32), want[0])
+        assert np.array_equal(got[1].astype(np.float32), want[1])
+        c2 = es.state(e)[0]
+        ref = m.chi2_fp64(want[0], want[1])
+        assert abs(c2 - ref) <= 1e-10 * abs(ref)
+    es.close()
+
+
+def test_batched_equals_solo():
+    systems = _systems()
+    steps = 120
+    mv = _moves(systems, steps)
+    batched = _run(systems, mv, steps, "batched")
+    solo = _run(systems, mv, steps, "solo")
+    _same(batched, solo)
+    assert sum(int(r["acc"].sum()) for r in batched) > 0
+
+
+def test_tune_and_graph_do_not_change_results():
+    systems = _systems(count=4, seed=5)
+    steps = 80
+    mv = _moves(systems, steps, seed=2)
+    base = _run(systems, mv, steps, "batched", tune=(1024, 256, 4))
+    _same(base, _run(systems, mv, steps, "batched", tune=(128, 128, 8), graph=False))
+    _same(base, _run(systems, mv, steps, "batched", tune=(4096, 512, 1), chunk=7))
+
+
+def test_engine_replays_on_oracle(oracle_mod):
+    """Replay the device chain on the host with the oracle's histograms and
+    the device's decisions: every step's chi2 agrees to 1e-10 relative, the
+    decisions follow the FP64 rule, and the final counts and coordinates are
+    bit-identical."""
+    from fullrmc_gb300.hostloop import HostPDFChain
+    systems = _systems(count=2, seed=9, nmin=800, nmax=1500)
+    steps = 150
+    mv = _moves(systems, steps, seed=4, amp=0.4)
+    res = _run(systems, mv, steps, "batched")
+    for e, s in enumerate(systems):
+        chain = HostPDFChain(s, oracle_mod, oracle_mod)
+        chain.compute_data()
+        m = s.model
+        chi2 = res[e]["chi2_0"]
+        assert abs(chi2 - m.chi2_fp64(*chain.data)) <= 1e-10 * abs(chi2)
+        a, v, u = mv[e]
+        for k in range(steps):
+            acc = bool(res[e]["acc"][k])
+            chain.step(a[k], v[k][None, :], u[k], force=acc)
+            c_new = m.chi2_fp64(chain.last[0], chain.last[1])
+            assert abs(c_new - res[e]["chi2"][k]) <= 1e-10 * abs(c_new), k
+            expect = not (res[e]["chi2"][k] > chi2 and u[k] > 0.0)
+            assert acc == expect, k
+            if acc:
+                chi2 = res[e]["chi2"][k]
+        got = res[e]["counts"]
+        assert np.array_equal(got[0].astype(np.float32), chain.data[0])
+        assert np.array_equal(got[1].astype(np.float32), chain.data[1])
+        assert np.array_equal(res[e]["coords"][0], chain.box)
+        assert np.array_equal(res[e]["coords"][1], chain.real)
+
+
+def test_step_host_matches_ring_steps():
+    """The host-buffer batched step gives the same chains as pushed moves."""
+    from fullrmc_gb300.engine import EngineSet
+    systems = _systems(count=5, seed=13)
+    steps = 40
+    mv = _moves(systems, steps, seed=8)
+    ring = _run(systems, mv, steps, "batched")
+    es = EngineSet(systems, move_cap=4)
+    es.init()
+    A = np.stack([m[0] for m in mv])
+    V = np.stack([m[1] for m in mv])
+    U = np.stack([m[2] for m in mv])
+    for k in range(steps):
+        c2, acc = es.step_host(A[:, k], V[:, k, :], U[:, k])
+        for e in range(len(systems)):
+            assert c2[e] == ring[e]["chi2"][k] and acc[e] == ring[e]["acc"][k]
+    for e in range(len(systems)):
+        assert es.state(e) == ring[e]["state"]
+    es.close()
+
+
+def test_add_remove_keeps_other_chains_exact():
+    """Engines added and removed between steps (the serving pattern) do not
+    change the results of the others."""
+    from fullrmc_gb300.engine import EngineSet
+    systems = _systems(count=4, seed=17)
+    steps = 30
+    mv = _moves(systems, steps, seed=3)
+    base = _run(systems[:2], mv[:2], steps, "batched")
+    es = EngineSet([], move_cap=64)
+    ids = [es.add(systems[0]), es.add(systems[1])]
+    for e, i in enumerate(ids):
+        a, v, u = mv[e]
+        es.push_moves(i, a, v, u, 0)
+    es.step(10, graph=False)
+    extra = es.add(systems[2])
+    es.push_moves(extra, *mv[2], 0)
+    es.step(10, graph=True)
+    es.remove(extra)
+    es.step(10, graph=False)
+    for e, i in enumerate(ids):
+        c2, acc, _ = es.results(i, 0, steps)
+        assert np.array_equal(acc, base[e]["acc"])
+        assert np.array_equal(c2.view(np.int64), base[e]["chi2"].view(np.int64))
+    es.close()
