@@ -70,6 +70,7 @@ SIGNATURES = {
     "frmc_dev_full_hist_counts_range": [vp, vp, i64, F32P, cint, i32, f32, f32, f32, i32, i64, i64, vp, vp],
     "frmc_dev_multiple_hist_counts": [vp, i64, vp, i64, F32P, cint, vp, vp, i32, f32, f32, f32, i32, cint, vp, vp],
     "frmc_dev_pack_atoms": [vp, vp, i64, vp, vp],
+    "frmc_dev_full_pairs_histograms_noalloc": [vp, vp, i64, F32P, cint, i32, f32, f32, f32, i32, vp, vp, vp],
     "frmc_dev_counts_to_f32": [vp, i64, vp, vp],
 }
 _RESTYPE = {"frmc_last_error": ctypes.c_char_p}

@@ -25,7 +25,7 @@ int launch_sine(int kind, const float *xs, int nx, const float *ys, const float 
 static FullTune g_full_tune;
 static std::mutex g_tune_mu;
 
-static FullTune current_tune()
+FullTune current_tune()
 {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     return g_full_tune;
@@ -59,7 +59,7 @@ static int check_indexes(const int32_t *idx, int64_t K, int64_t n)
     return FRMC_OK;
 }
 
-static double accept_fraction(const float *basis, int isPBC, float minD, float maxD)
+double accept_fraction(const float *basis, int isPBC, float minD, float maxD)
 {
     if (!isPBC)
         return 1.0;

@@ -100,6 +100,17 @@ int launch_full_hist(const float4 *atoms, const int *mol, int n, int bm, const B
                      float binw, int ne, int hs, unsigned *intra, unsigned *inter, uint32_t *status,
                      double accept_fraction, const FullTune *tune, cudaStream_t st, long long item_begin = 0,
                      long long item_end = -1);
+// The same with the device's SM count and opt-in shared-memory limit given
+// (touches no library context).
+int launch_full_hist_on(int sms, int max_smem_optin, const float4 *atoms, const int *mol, int n, int bm,
+                        const Basis &B, float minD, float maxD, float binw, int ne, int hs, unsigned *intra,
+                        unsigned *inter, uint32_t *status, double accept_fraction, const FullTune *tune,
+                        cudaStream_t st, long long item_begin = 0, long long item_end = -1);
+// Tile configuration currently set by frmc_set_full_tune.
+FullTune current_tune();
+// Expected fraction of pairs inside [minD, maxD) for uniform density
+// (chooses queued or direct binning).
+double accept_fraction(const float *basis, int isPBC, float minD, float maxD);
 // Number of work items of the all-pairs kernel for n atoms under `tune`.
 long long full_hist_items(int n, const FullTune *tune);
 

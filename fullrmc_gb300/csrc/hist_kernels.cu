@@ -471,6 +471,17 @@ int launch_full_hist(const float4 *atoms, const int *mol, int n, int bm, const B
     int rc = get_context(&ctx);
     if (rc)
         return rc;
+    return launch_full_hist_on(ctx->sms, ctx->max_smem_optin, atoms, mol, n, bm, B, minD, maxD, binw, ne, hs, intra,
+                               inter, status, accept_fraction, tune, st, item_begin, item_end);
+}
+
+int launch_full_hist_on(int sms, int max_smem_optin, const float4 *atoms, const int *mol, int n, int bm,
+                        const Basis &B, float minD, float maxD, float binw, int ne, int hs, unsigned *intra,
+                        unsigned *inter, uint32_t *status, double accept_fraction, const FullTune *tune,
+                        cudaStream_t st, long long item_begin, long long item_end)
+{
+    if (n < 2)
+        return FRMC_OK;
     FullTune tn = tune ? *tune : FullTune();
     const int R = tn.rows == 1 ? 1 : 2;
     const int threads = tn.threads;
@@ -503,11 +514,11 @@ int launch_full_hist(const float4 *atoms, const int *mol, int n, int bm, const B
     const size_t base = 16 + (size_t)p.T * 40;
     const size_t hist_bytes = ((size_t)p.total * 4 + 15) & ~(size_t)15;
     const size_t queue_bytes = queued ? (size_t)p.qcap * threads * 8 : 0;
-    p.smem_hist = (base + hist_bytes + queue_bytes) <= (size_t)ctx->max_smem_optin ? 1 : 0;
+    p.smem_hist = (base + hist_bytes + queue_bytes) <= (size_t)max_smem_optin ? 1 : 0;
     size_t smem = base + (p.smem_hist ? hist_bytes : 0) + queue_bytes;
-    if (smem > (size_t)ctx->max_smem_optin)
+    if (smem > (size_t)max_smem_optin)
         return set_error(FRMC_E_ARG, "full histogram: tile configuration needs %zu bytes of shared memory", smem);
-    long long grid = (long long)ctx->sms * (tn.ctas_per_sm > 0 ? tn.ctas_per_sm : 1);
+    long long grid = (long long)sms * (tn.ctas_per_sm > 0 ? tn.ctas_per_sm : 1);
     if (grid > p.nitems - p.item_begin)
         grid = p.nitems - p.item_begin;
     switch (bm) {

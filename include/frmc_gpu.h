@@ -175,6 +175,22 @@ int frmc_dev_multiple_hist_counts(const int32_t *indexes, int64_t K, const float
                                   const float *basis_host, int isPBC, const int32_t *moleculeIndex,
                                   const int32_t *elementIndex, int32_t ne, float minDistance, float maxDistance,
                                   float bin, int32_t hs, int allAtoms, uint32_t *counts, void *stream);
+/* All-pairs histograms into caller-owned float32 device buffers hintra and
+ * hinter (ne, ne, hs) without allocating device memory -- for callers that
+ * cannot let a library call cudaMalloc (a framework that owns all device
+ * memory through its own pool, or a loop that must not stall on an
+ * allocation).  There is no counterpart of this entry point in fullrmc; the
+ * histograms equal those of full_pairs_histograms_coords.  The uint32
+ * counts live in one fixed device array of 2^20 counts (4 MiB) that every GPU
+ * loading the library holds until exit: 2*ne*ne*hs above 1048576 returns
+ * FRMC_E_ARG.  The first call on a device resolves that array's address and
+ * should come before any stream capture.  All calls share the array, so calls
+ * that overlap on the GPU (other streams, other threads) race.  Synchronises
+ * `stream` before returning. */
+int frmc_dev_full_pairs_histograms_noalloc(const void *atoms4, const int32_t *moleculeIndex, int64_t n,
+                                           const float *basis_host, int isPBC, int32_t ne, float minDistance,
+                                           float maxDistance, float bin, int32_t hs, float *hintra, float *hinter,
+                                           void *stream);
 /* Pack (n, 3) coordinates and element indexes into float4 (x, y, z, el bits). */
 int frmc_dev_pack_atoms(const float *coords, const int32_t *elementIndex, int64_t n, void *atoms4, void *stream);
 /* float32 histogram values of uint32 counts (sequential additions of 1.0f). */
