@@ -263,7 +263,7 @@ def run_ours(args):
     pairs_per_step = float(sum(2 * (s.box_coords.shape[0] - 1) for s in systems))
 
     # autotune the work list (results are identical under every tuning)
-    tune_cands = [(512, 256, 4), (1024, 256, 4), (2048, 256, 2), (1024, 512, 2), (512, 128, 8), (2048, 512, 1)]
+    tune_cands = [(1024, 256, 2), (1024, 512, 1), (2048, 512, 1), (512, 128, 4), (1024, 256, 4), (2048, 256, 2)]
     best = None
     es = EngineSet(systems, move_cap=cap)
     es.init()

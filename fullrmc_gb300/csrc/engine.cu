@@ -84,13 +84,47 @@ struct EDesc {
     int *pidx;    // [ne][ne] element pair -> index into the pair table (-1: none)
     int *tlist;   // oriented bins touched this step (2 n + 8 entries)
     double *rfac, *invvol, *expd, *dw, *pc;
-    double *K;    // [npairs][hs] rfac * invvol * pair_coef: G = sum_p K_p n_p - rfac
-    double *Gcur; // [hs] G(r) of the current configuration
-    double *dG;   // [hs] change of G(r) proposed this step
+    double *R;    // [hs] rfac * invvol: G(b) = R(b) sum_p pair_coef_p n_p(b) - rfac(b)
+    double *A;    // [hs] w R^2
+    double *Bq;   // [hs] 2 w R (exp - G) of the current configuration
+    double *Sb;   // [hs] S(b) = sum_p pair_coef_p dP_p(b) proposed this step (large hs only)
     EMove *moves;
     EResult *results;
     EState *st;
 };
+
+// The fields the per-column loops read, copied into registers once per item
+// (through a const reference every access would be a global load that the
+// compiler must repeat after each store, since the stores might alias it).
+struct ColView {
+    Basis B;
+    float s_lo, s_hi, minD, binw;
+    int n, ne, hs;
+    long long total;
+    const float4 *__restrict__ box;
+    const int *__restrict__ mol;
+    const int *__restrict__ pidx;
+    int *__restrict__ tlist;
+};
+
+__device__ __forceinline__ ColView col_view(const EDesc &D)
+{
+    ColView v;
+    v.B = D.B;
+    v.s_lo = D.s_lo;
+    v.s_hi = D.s_hi;
+    v.minD = D.minD;
+    v.binw = D.binw;
+    v.n = D.n;
+    v.ne = D.ne;
+    v.hs = D.hs;
+    v.total = D.total;
+    v.box = D.box;
+    v.mol = D.mol;
+    v.pidx = D.pidx;
+    v.tlist = D.tlist;
+    return v;
+}
 
 struct StepParams {
     const EDesc *desc;
@@ -113,63 +147,120 @@ __device__ __forceinline__ float3 to_box(const Basis &RB, float x, float y, floa
     return r;
 }
 
-// Record a +-1 change of oriented bin `flat` (offset `half` selects intra or
-// inter): the oriented delta, the element-pair delta used by the FP64
-// evaluation, and the touched list used by the commit.
-__device__ __forceinline__ void bump(const EDesc &D, long long half, long long flat, int ra, int rb, int bin, int v)
+// Element-pair index and bin of an oriented flat index.  A count past the
+// last bin lands in bin 0.. of the next oriented row of the C-contiguous
+// array, as with the reference's unchecked index.
+template <class V>
+__device__ __forceinline__ void pair_of_flat(const V &D, int flat, int ra, int rb, int bin, int &p, int &b)
 {
-    atomicAdd(D.delta + half + flat, v);
-    const unsigned k = atomicAdd(&D.st->tcount, 1u);
-    D.tlist[k] = (int)(half + flat);
     if (bin >= D.hs) {
-        // A count past the last bin lands in bin 0.. of the next oriented row
-        // of the C-contiguous array, as with the reference's unchecked index.
-        const long long row = flat / D.hs;
-        bin = (int)(flat - row * D.hs);
-        ra = (int)(row / D.ne);
-        rb = (int)(row - (long long)ra * D.ne);
+        const int row = flat / D.hs;
+        bin = flat - row * D.hs;
+        ra = row / D.ne;
+        rb = row - ra * D.ne;
     }
-    const int p = D.pidx[ra * D.ne + rb];
-    if (p >= 0)
-        atomicAdd(D.dP + (long long)p * D.hs + bin, v);
+    p = D.pidx[ra * D.ne + rb];
+    b = bin;
 }
 
-template <int BM>
-__device__ void item_delta(const EDesc &D, int tile, int atom, float3 o, float3 nw, int ela, int mola, int t)
+// Bins of column j before and after the move: flat oriented indexes f0, f1
+// (-1 when out of range or unchanged), `half` (0 intra, total inter), bins and
+// the column's element.  32-bit indexes: 2 * ne * ne * hs < 2^31 is checked
+// when an engine is created.
+template <int BM, class V>
+__device__ __forceinline__ void column_bins(const V &D, float3 o, float3 nw, float4 c, int mj, int arow, int mola,
+                                            int &f0, int &f1, int &half, int &b0, int &b1, int &elj)
 {
-    const int j0 = t * tile;
-    const int j1 = min(D.n, j0 + tile);
-    const long long arow = (long long)ela * D.ne;
-    for (int j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
-        if (j == atom)
-            continue;
-        const float4 c = D.box[j];
-        const float s0 = pair_s<BM>(o.x, o.y, o.z, c.x, c.y, c.z, D.B);
-        const float s1 = pair_s<BM>(nw.x, nw.y, nw.z, c.x, c.y, c.z, D.B);
-        const bool a0 = (s0 >= D.s_lo) & (s0 < D.s_hi);
-        const bool a1 = (s1 >= D.s_lo) & (s1 < D.s_hi);
-        if (!(a0 | a1))
-            continue;
-        const int elj = __float_as_int(c.w);
-        const long long half = D.mol[j] == mola ? 0 : D.total;
-        long long f0 = -1, f1 = -1;
-        int b0 = 0, b1 = 0;
+    f0 = f1 = -1;
+    const float s0 = pair_s<BM>(o.x, o.y, o.z, c.x, c.y, c.z, D.B);
+    const float s1 = pair_s<BM>(nw.x, nw.y, nw.z, c.x, c.y, c.z, D.B);
+    const bool a0 = (s0 >= D.s_lo) & (s0 < D.s_hi);
+    const bool a1 = (s1 >= D.s_lo) & (s1 < D.s_hi);
+    if (a0 | a1) {
+        elj = __float_as_int(c.w);
+        half = mj == mola ? 0 : (int)D.total;
+        const long long rowb = (long long)(arow + elj) * D.hs;
         if (a0) {
             b0 = pair_bin(s0, D.minD, D.binw);
-            long long f = (arow + elj) * D.hs + b0;
-            if ((unsigned long long)f < (unsigned long long)D.total) f0 = f;
+            const long long f = rowb + b0;
+            if ((unsigned long long)f < (unsigned long long)D.total) f0 = (int)f;
         }
         if (a1) {
             b1 = pair_bin(s1, D.minD, D.binw);
-            long long f = (arow + elj) * D.hs + b1;
-            if ((unsigned long long)f < (unsigned long long)D.total) f1 = f;
+            const long long f = rowb + b1;
+            if ((unsigned long long)f < (unsigned long long)D.total) f1 = (int)f;
         }
         if (f0 == f1)
-            continue;
-        if (f0 >= 0)
-            bump(D, half, f0, ela, elj, b0, -1);
-        if (f1 >= 0)
-            bump(D, half, f1, ela, elj, b1, +1);
+            f0 = f1 = -1;
+    }
+}
+
+constexpr int kItemUnroll = 4;
+
+// One item: the moved atom against atoms [t*tile, (t+1)*tile).  For every
+// column j the pair before and after the move is binned; a changed bin adds
+// -1 / +1 to the oriented delta and to the element-pair delta, and its
+// oriented index is appended to the touched list (one list reservation per
+// warp and round).  Coordinates of kItemUnroll columns are loaded before any
+// is used.
+// One item of the split path: the moved atom against atoms
+// [t*tile, (t+1)*tile), adding to the engine's global deltas.  Per column
+// the warp reserves its touched-list entries with one atomic.
+template <int BM>
+__device__ void item_delta(const EDesc &Dg, int tile, int atom, float3 o, float3 nw, int ela, int mola, int t)
+{
+    const ColView D = col_view(Dg);
+    int *__restrict__ delta = Dg.delta;
+    int *__restrict__ dP = Dg.dP;
+    unsigned *tcount = &Dg.st->tcount;
+    const int j0 = t * tile;
+    const int j1 = min(D.n, j0 + tile);
+    const int arow = ela * D.ne;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned lt = (1u << lane) - 1u;
+    for (int jb = j0; jb < j1; jb += kItemUnroll * blockDim.x) {
+        float4 c[kItemUnroll];
+        int mj[kItemUnroll];
+#pragma unroll
+        for (int u = 0; u < kItemUnroll; ++u) {
+            const int j = jb + u * blockDim.x + threadIdx.x;
+            if (j < j1) {
+                c[u] = D.box[j];
+                mj[u] = D.mol[j];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kItemUnroll; ++u) {
+            const int j = jb + u * blockDim.x + threadIdx.x;
+            int f0 = -1, f1 = -1, half = 0, b0 = 0, b1 = 0, elj = 0;
+            if (j < j1 && j != atom)
+                column_bins<BM>(D, o, nw, c[u], mj[u], arow, mola, f0, f1, half, b0, b1, elj);
+            const unsigned m0 = __ballot_sync(0xffffffffu, f0 >= 0);
+            const unsigned m1 = __ballot_sync(0xffffffffu, f1 >= 0);
+            if ((m0 | m1) == 0u)
+                continue;
+            unsigned base = 0;
+            if (lane == 0)
+                base = atomicAdd(tcount, __popc(m0) + __popc(m1));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            unsigned pos = base + __popc(m0 & lt) + __popc(m1 & lt);
+            if (f0 >= 0) {
+                atomicSub(delta + half + f0, 1);
+                D.tlist[pos++] = half + f0;
+                int p, b;
+                pair_of_flat(D, f0, ela, elj, b0, p, b);
+                if (p >= 0)
+                    atomicSub(dP + p * D.hs + b, 1);
+            }
+            if (f1 >= 0) {
+                atomicAdd(delta + half + f1, 1);
+                D.tlist[pos] = half + f1;
+                int p, b;
+                pair_of_flat(D, f1, ela, elj, b1, p, b);
+                if (p >= 0)
+                    atomicAdd(dP + p * D.hs + b, 1);
+            }
+        }
     }
 }
 
@@ -178,7 +269,6 @@ __device__ void item_delta(const EDesc &D, int tile, int atom, float3 o, float3 
 // then lane L (0..255) sums the contributions of bins b = L (mod 256) in
 // increasing order and a fixed binary tree combines the 256 lanes.
 constexpr int kChunk = 2048;    // bins per shared-memory chunk
-constexpr int kMaxPairsU = 10;  // element pairs handled with unrolled loads (ne <= 4)
 
 __device__ void lanes_zero(double *red)
 {
@@ -199,6 +289,7 @@ __device__ void lanes_add_chunk(double *red, const double *cb, int c0, int cn)
 
 __device__ double lanes_total(double *red)
 {
+    __syncthreads();  // every lane's partial sum is written
     for (int s = kRedLanes / 2; s > 0; s >>= 1) {
         for (int L = threadIdx.x; L < s; L += blockDim.x) red[L] += red[L + s];
         __syncthreads();
@@ -223,76 +314,115 @@ __device__ __forceinline__ long long pair_count(const EDesc &D, int q, int b)
 }
 
 // G(r) of the current counts and its sum of squared deviations (set-up):
-// G(b) = sum_p K_p(b) n_p(b) - rfac(b)  (PairDistributionConstraints.py:864-884).
+// G(b) = R(b) sum_p pair_coef_p n_p(b) - rfac(b)  (PairDistributionConstraints.py:864-884);
+// also the per-bin state Bq(b) = 2 w R (exp - G).
 __device__ double eval_full(const EDesc &D, double *red, double *cb)
 {
     lanes_zero(red);
     for (int c0 = 0; c0 < D.hs; c0 += kChunk) {
         const int cn = min(kChunk, D.hs - c0);
         for (int b = c0 + threadIdx.x; b < c0 + cn; b += blockDim.x) {
-            double G = -D.rfac[b];
-            for (int q = 0; q < D.npairs; ++q) G = fma(D.K[(long long)q * D.hs + b], (double)pair_count(D, q, b), G);
-            D.Gcur[b] = G;
-            const double d = D.expd[b] - G;
-            cb[b - c0] = (D.has_dw ? D.dw[b] * d : d) * d;
+            double S = 0.0;
+            for (int q = 0; q < D.npairs; ++q) S = fma(D.pc[q], (double)pair_count(D, q, b), S);
+            const double G = fma(D.R[b], S, -D.rfac[b]);
+            const double e = D.expd[b] - G;
+            const double w = D.has_dw ? D.dw[b] : 1.0;
+            D.Bq[b] = 2.0 * (w * D.R[b]) * e;
+            cb[b - c0] = (w * e) * e;
         }
         lanes_add_chunk(red, cb, c0, cn);
     }
     return lanes_total(red);
 }
 
-// Change of the sum of squared deviations for this step's delta: only bins
-// whose element-pair counts changed do FP64 work,
-//   dG = sum_p K_p dP_p,  d(sd) = w dG (dG - 2 (exp - G)).
-// The element-pair deltas are cleared as they are read; dG is kept for the
-// commit.  All loads of a bin are issued before any is used.
-__device__ double eval_delta(const EDesc &D, double *red, double *cb)
+// Change of the sum of squared deviations for this step.  With
+// dG(b) = R(b) S(b), S(b) = sum_p pair_coef_p dP_p(b):
+//   d(sd) = sum_b w [(exp - G - dG)^2 - (exp - G)^2] = sum_b S (A S - Bq).
+// Each thread takes bins b = tid, tid + blockDim, ...; all loads of a bin are
+// issued before any is used and FP64 work is done only where some dP is
+// non-zero.  The element-pair deltas are cleared as they are read; S is kept
+// in shared memory (chunk) or global memory (Sb) for the commit.  Sums use the
+// fixed lane order, so the result does not depend on the CTA size.
+constexpr int kMaxP = 10;  // element pairs loaded with unrolled loads (ne <= 4)
+
+// SMEM: the element-pair deltas are this CTA's shared-memory copy (one CTA per
+// engine); otherwise they are the engine's global array, filled by several
+// CTAs, read through L2 and cleared as they are read.
+template <bool SMEM>
+__device__ double eval_delta(const EDesc &Dg, int *dP, double *red, double *cb, double *sbs, double *coef)
 {
+    struct {
+        int hs;
+        const double *__restrict__ A;
+        const double *__restrict__ Bq;
+        double *__restrict__ Sb;
+        const double *__restrict__ pc;
+    } D = {Dg.hs, Dg.A, Dg.Bq, Dg.Sb, Dg.pc};
+    const int np = Dg.npairs;
+    if (!SMEM)
+        for (int q = threadIdx.x; q < np; q += blockDim.x) coef[q] = D.pc[q];
     lanes_zero(red);
-    const int np = D.npairs;
+    __syncthreads();
+    const bool big = D.hs > kChunk;
     for (int c0 = 0; c0 < D.hs; c0 += kChunk) {
         const int cn = min(kChunk, D.hs - c0);
         for (int b = c0 + threadIdx.x; b < c0 + cn; b += blockDim.x) {
-            double dg = 0.0;
-            bool touched = false;
-            if (np <= kMaxPairsU) {
-                int d[kMaxPairsU];
+            int d[kMaxP];
 #pragma unroll
-                for (int q = 0; q < kMaxPairsU; ++q) d[q] = q < np ? __ldcg(D.dP + (long long)q * D.hs + b) : 0;
+            for (int q = 0; q < kMaxP; ++q) {
+                int v = 0;
+                if (q < np)
+                    v = SMEM ? dP[q * D.hs + b] : __ldcg(dP + (long long)q * D.hs + b);
+                d[q] = v;
+            }
+            const double a = D.A[b];
+            const double bq = D.Bq[b];
+            bool any = false;
 #pragma unroll
-                for (int q = 0; q < kMaxPairsU; ++q)
-                    if (d[q]) {
-                        dg = fma(D.K[(long long)q * D.hs + b], (double)d[q], dg);
-                        D.dP[(long long)q * D.hs + b] = 0;
-                        touched = true;
-                    }
-            } else {
-                for (int q = 0; q < np; ++q) {
-                    const int d = __ldcg(D.dP + (long long)q * D.hs + b);
-                    if (d) {
-                        dg = fma(D.K[(long long)q * D.hs + b], (double)d, dg);
-                        D.dP[(long long)q * D.hs + b] = 0;
-                        touched = true;
+            for (int q = 0; q < kMaxP; ++q) any |= d[q] != 0;
+            for (int q = kMaxP; q < np; ++q)
+                any |= (SMEM ? dP[q * D.hs + b] : __ldcg(dP + (long long)q * D.hs + b)) != 0;
+            double S = 0.0, c = 0.0;
+            if (any) {
+#pragma unroll
+                for (int q = 0; q < kMaxP; ++q) {
+                    const int v = d[q];
+                    if (v) {
+                        if (!SMEM)
+                            dP[(long long)q * D.hs + b] = 0;
+                        const double cf = coef[q];
+                        S += v == 1 ? cf : (v == -1 ? -cf : cf * (double)v);
                     }
                 }
-            }
-            D.dG[b] = dg;
-            double c = 0.0;
-            if (touched) {
-                const double e = D.expd[b] - D.Gcur[b];
-                c = (D.has_dw ? D.dw[b] * dg : dg) * (dg - 2.0 * e);
+                for (int q = kMaxP; q < np; ++q) {
+                    int *dp = dP + (long long)q * D.hs + b;
+                    const int v = SMEM ? *dp : __ldcg(dp);
+                    if (v) {
+                        if (!SMEM)
+                            *dp = 0;
+                        const double cf = coef[q];
+                        S += v == 1 ? cf : (v == -1 ? -cf : cf * (double)v);
+                    }
+                }
+                c = S * fma(a, S, -bq);
             }
             cb[b - c0] = c;
+            if (big)
+                D.Sb[b] = S;
+            else
+                sbs[b] = S;
         }
         lanes_add_chunk(red, cb, c0, cn);
     }
     return lanes_total(red);
 }
 
+constexpr int kCommitUnroll = 4;
+
 __device__ void finish_engine(const EDesc &D, int atom, float3 nw, float4 nreal, double *red, double *cb,
-                              int *s_flag)
+                              double *sbs, double *coef, int *s_flag)
 {
-    const double dsd = eval_delta(D, red, cb);
+    const double dsd = eval_delta<false>(D, D.dP, red, cb, sbs, coef);
     const EState &S0 = *D.st;
     const double sd_new = S0.sd + dsd;
     const double chi2_new = sd_new / D.var2;
@@ -303,19 +433,33 @@ __device__ void finish_engine(const EDesc &D, int atom, float3 nw, float4 nreal,
     }
     __syncthreads();
     const bool accept = *s_flag != 0;
+    // commit (or drop) the oriented delta through the touched list; duplicates
+    // are harmless: atomicExch hands each bin's delta to exactly one entry
     const unsigned nt = __ldcg(&D.st->tcount);
-    for (unsigned k = threadIdx.x; k < nt; k += blockDim.x) {
-        const int f = __ldcg(D.tlist + k);
-        const int d = atomicExch(D.delta + f, 0);
-        if (accept && d)
-            D.counts[f] += d;
-    }
-    if (accept)
-        for (int b = threadIdx.x; b < D.hs; b += blockDim.x) {
-            const double g = D.dG[b];
-            if (g != 0.0)
-                D.Gcur[b] += g;
+    for (unsigned k0 = threadIdx.x; k0 < nt; k0 += kCommitUnroll * blockDim.x) {
+        int f[kCommitUnroll], d[kCommitUnroll];
+#pragma unroll
+        for (int u = 0; u < kCommitUnroll; ++u) {
+            const unsigned k = k0 + u * blockDim.x;
+            f[u] = k < nt ? __ldcg(D.tlist + k) : -1;
         }
+#pragma unroll
+        for (int u = 0; u < kCommitUnroll; ++u) d[u] = f[u] >= 0 ? atomicExch(D.delta + f[u], 0) : 0;
+        if (accept) {
+#pragma unroll
+            for (int u = 0; u < kCommitUnroll; ++u)
+                if (d[u]) D.counts[f[u]] += d[u];
+        }
+    }
+    // on accept G += R S, hence Bq -= 2 A S on the bins that changed
+    if (accept) {
+        const bool big = D.hs > kChunk;
+        for (int b = threadIdx.x; b < D.hs; b += blockDim.x) {
+            const double S = big ? D.Sb[b] : sbs[b];
+            if (S != 0.0)
+                D.Bq[b] = fma(-2.0 * D.A[b], S, D.Bq[b]);
+        }
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
         EState &S = *D.st;
@@ -337,11 +481,189 @@ __device__ void finish_engine(const EDesc &D, int atom, float3 nw, float4 nreal,
     }
 }
 
-__global__ void __launch_bounds__(1024) k_engine_step(StepParams p)
+// Fused path: one CTA advances one engine by one step.  The element-pair
+// deltas live in this CTA's shared memory (sdP, npairs * hs ints), changes are
+// listed as (oriented bin, sign) in the engine's touched list, and an accepted
+// move is committed with fire-and-forget atomics on the counts.  No other CTA
+// touches the engine during the step, so there is no cross-CTA hand-off.
+// Columns of the fused path.  Batches of kItemUnroll * blockDim columns are
+// software-pipelined: the next batch's coordinates are loaded before the
+// current batch is binned, and each warp reserves the batch's touched-list
+// entries with one shared-memory atomic.
+template <int BM>
+__device__ void fused_columns(const EDesc &Dg, int *sdP, unsigned *s_tcount, int atom, float3 o, float3 nw, int ela,
+                              int mola)
+{
+    const ColView D = col_view(Dg);
+    const int arow = ela * D.ne;
+    const unsigned lane = threadIdx.x & 31u;
+    const int step = kItemUnroll * blockDim.x;
+    float4 c[kItemUnroll];
+    int mj[kItemUnroll];
+#pragma unroll
+    for (int u = 0; u < kItemUnroll; ++u) {
+        const int j = u * blockDim.x + threadIdx.x;
+        c[u] = j < D.n ? D.box[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        mj[u] = j < D.n ? D.mol[j] : 0;
+    }
+    for (int jb = 0; jb < D.n; jb += step) {
+        float4 cn[kItemUnroll];
+        int mn[kItemUnroll];
+#pragma unroll
+        for (int u = 0; u < kItemUnroll; ++u) {
+            const int j = jb + step + u * blockDim.x + threadIdx.x;
+            cn[u] = j < D.n ? D.box[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+            mn[u] = j < D.n ? D.mol[j] : 0;
+        }
+        int f0[kItemUnroll], f1[kItemUnroll], half[kItemUnroll], b0[kItemUnroll], b1[kItemUnroll],
+            elj[kItemUnroll];
+        unsigned mine = 0;
+#pragma unroll
+        for (int u = 0; u < kItemUnroll; ++u) {
+            const int j = jb + u * blockDim.x + threadIdx.x;
+            f0[u] = f1[u] = -1;
+            half[u] = b0[u] = b1[u] = elj[u] = 0;
+            if (j < D.n && j != atom)
+                column_bins<BM>(D, o, nw, c[u], mj[u], arow, mola, f0[u], f1[u], half[u], b0[u], b1[u], elj[u]);
+            mine += (f0[u] >= 0) + (f1[u] >= 0);
+        }
+        unsigned incl = mine;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const unsigned v = __shfl_up_sync(0xffffffffu, incl, off);
+            if (lane >= (unsigned)off) incl += v;
+        }
+        const unsigned tot = __shfl_sync(0xffffffffu, incl, 31);
+        if (tot) {
+            unsigned base = 0;
+            if (lane == 31)
+                base = atomicAdd(s_tcount, tot);
+            base = __shfl_sync(0xffffffffu, base, 31);
+            unsigned pos = base + incl - mine;
+#pragma unroll
+            for (int u = 0; u < kItemUnroll; ++u) {
+                if (f0[u] >= 0) {
+                    D.tlist[pos++] = (half[u] + f0[u]) << 1;
+                    int p, b;
+                    pair_of_flat(D, f0[u], ela, elj[u], b0[u], p, b);
+                    if (p >= 0)
+                        atomicSub(sdP + p * D.hs + b, 1);
+                }
+                if (f1[u] >= 0) {
+                    D.tlist[pos++] = ((half[u] + f1[u]) << 1) | 1;
+                    int p, b;
+                    pair_of_flat(D, f1[u], ela, elj[u], b1[u], p, b);
+                    if (p >= 0)
+                        atomicAdd(sdP + p * D.hs + b, 1);
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kItemUnroll; ++u) {
+            c[u] = cn[u];
+            mj[u] = mn[u];
+        }
+    }
+}
+
+__device__ void engine_fused(const EDesc &D, int *sdP, double *red, double *cb, double *sbs, double *coef,
+                             int *s_flag, unsigned *s_tcount, float *s_mv, int *s_mi)
+{
+    if (threadIdx.x == 0) {
+        const long long step = D.st->step;
+        const EMove m = D.moves[step % D.move_cap];
+        const float4 ob = D.box[m.atom];
+        const float4 orl = D.real[m.atom];
+        const float rx = __fadd_rn(orl.x, m.v[0]), ry = __fadd_rn(orl.y, m.v[1]), rz = __fadd_rn(orl.z, m.v[2]);
+        const float3 nw = D.bm == BM_IBC ? make_float3(rx, ry, rz) : to_box(D.RB, rx, ry, rz);
+        s_mv[0] = ob.x; s_mv[1] = ob.y; s_mv[2] = ob.z;
+        s_mv[3] = nw.x; s_mv[4] = nw.y; s_mv[5] = nw.z;
+        s_mv[6] = rx; s_mv[7] = ry; s_mv[8] = rz;
+        s_mi[0] = m.atom;
+        s_mi[1] = __float_as_int(ob.w);
+        s_mi[2] = D.mol[m.atom];
+        *s_tcount = 0u;
+    }
+    const int np = D.npairs;
+    const int nph = np * D.hs;
+    for (int k = threadIdx.x; k < nph; k += blockDim.x) sdP[k] = 0;
+    for (int q = threadIdx.x; q < np; q += blockDim.x) coef[q] = D.pc[q];
+    __syncthreads();
+    const int atom = s_mi[0], ela = s_mi[1], mola = s_mi[2];
+    const float3 o = make_float3(s_mv[0], s_mv[1], s_mv[2]);
+    const float3 nw = make_float3(s_mv[3], s_mv[4], s_mv[5]);
+    switch (D.bm) {
+    case BM_IBC: fused_columns<BM_IBC>(D, sdP, s_tcount, atom, o, nw, ela, mola); break;
+    case BM_DIAG: fused_columns<BM_DIAG>(D, sdP, s_tcount, atom, o, nw, ela, mola); break;
+    case BM_XYTRI: fused_columns<BM_XYTRI>(D, sdP, s_tcount, atom, o, nw, ela, mola); break;
+    case BM_LOWER: fused_columns<BM_LOWER>(D, sdP, s_tcount, atom, o, nw, ela, mola); break;
+    default: fused_columns<BM_GENERAL>(D, sdP, s_tcount, atom, o, nw, ela, mola); break;
+    }
+    __syncthreads();
+    const double dsd = eval_delta<true>(D, sdP, red, cb, sbs, coef);
+    const EState &S0 = *D.st;
+    const double sd_new = S0.sd + dsd;
+    const double chi2_new = sd_new / D.var2;
+    if (threadIdx.x == 0) {
+        const EMove &m = D.moves[S0.step % D.move_cap];
+        const bool reject = (chi2_new > S0.chi2) && (m.u > D.tol);
+        *s_flag = reject ? 0 : 1;
+    }
+    __syncthreads();
+    const bool accept = *s_flag != 0;
+    if (accept) {
+        const unsigned nt = *s_tcount;
+        const int *__restrict__ tl = D.tlist;
+        int *__restrict__ cnt = D.counts;
+        for (unsigned k = threadIdx.x; k < nt; k += blockDim.x) {
+            const int e = tl[k];
+            atomicAdd(cnt + (e >> 1), (e & 1) ? 1 : -1);
+        }
+        const int hs = D.hs;
+        const bool big = hs > kChunk;
+        const double *__restrict__ Sb = D.Sb;
+        const double *__restrict__ A = D.A;
+        double *__restrict__ Bq = D.Bq;
+        for (int b = threadIdx.x; b < hs; b += blockDim.x) {
+            const double Sv = big ? Sb[b] : sbs[b];
+            if (Sv != 0.0)
+                Bq[b] = fma(-2.0 * A[b], Sv, Bq[b]);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        EState &S = *D.st;
+        EResult &r = D.results[S.step % D.move_cap];
+        r.chi2_new = chi2_new;
+        r.accepted = accept ? 1 : 0;
+        r.atom = atom;
+        if (accept) {
+            const float4 ob = D.box[atom];
+            D.box[atom] = make_float4(nw.x, nw.y, nw.z, ob.w);
+            D.real[atom] = make_float4(s_mv[6], s_mv[7], s_mv[8], 0.0f);
+            S.chi2 = chi2_new;
+            S.sd = sd_new;
+            S.accepted += 1;
+        }
+        S.step += 1;
+    }
+}
+
+constexpr int kMaxEngineThreads = 512;  // CTA size limit of the step kernels (128 registers per thread)
+
+template <bool FUSED>
+__global__ void __launch_bounds__(kMaxEngineThreads, 1) k_engine_step(StepParams p)
 {
     __shared__ double red[kRedLanes];
     __shared__ double cb[kChunk];
+    __shared__ double sbs[kChunk];
+    __shared__ double coef[64];
+    __shared__ float s_mv[9];
+    __shared__ int s_mi[3];
+    __shared__ unsigned s_tcount;
     __shared__ int s_last, s_flag, s_item;
+    extern __shared__ int sdP[];
+    (void)sdP;
     for (;;) {
         if (threadIdx.x == 0) {
             const unsigned long long k = atomicAdd(&p.sched->claimed, 1ull);
@@ -354,7 +676,12 @@ __global__ void __launch_bounds__(1024) k_engine_step(StepParams p)
             break;
         const int2 item = p.items[it];
         const EDesc &D = p.desc[item.x];
-        if (p.eval_only) {
+        if (FUSED) {
+            engine_fused(D, sdP, red, cb, sbs, coef, &s_flag, &s_tcount, s_mv, s_mi);
+            __syncthreads();
+            continue;
+        }
+        if (!FUSED && p.eval_only) {
             const double sd = eval_full(D, red, cb);
             if (threadIdx.x == 0) {
                 D.st->sd = sd;
@@ -384,6 +711,9 @@ __global__ void __launch_bounds__(1024) k_engine_step(StepParams p)
         case BM_LOWER: item_delta<BM_LOWER>(D, p.tile, atom, o, nw, ela, mola, item.y); break;
         default: item_delta<BM_GENERAL>(D, p.tile, atom, o, nw, ela, mola, item.y); break;
         }
+        // Release: the barrier orders every thread's delta atomics and
+        // touched-list stores before thread 0's gpu-scope fence, which is
+        // cumulative, so they are visible to the CTA that sees the count.
         __syncthreads();
         if (threadIdx.x == 0) {
             __threadfence();
@@ -393,7 +723,7 @@ __global__ void __launch_bounds__(1024) k_engine_step(StepParams p)
         __syncthreads();
         if (s_last) {
             __threadfence();
-            finish_engine(D, atom, nw, nreal, red, cb, &s_flag);
+            finish_engine(D, atom, nw, nreal, red, cb, sbs, coef, &s_flag);
         }
         __syncthreads();
     }
@@ -438,8 +768,16 @@ struct Slot {
     size_t bytes = 0;
 };
 
+constexpr int kFusedSmemMax = 96 * 1024;  // shared-memory element-pair deltas of one engine
+constexpr int kFusedMaxAtoms = 49152;     // larger engines are split over several CTAs
+
 struct EngineSet {
     std::vector<Slot> slots;
+    int fused = 1;         // batched steps use one CTA per engine where it fits
+    int fused_smem = 0;    // dynamic shared memory of batched launches
+    int nsolo = 0;         // items [0, nsolo): tiles of every engine (one-engine steps)
+    int nbatch = 0;        // items [nsolo, nsolo + nbatch): the batched work list
+    int nfused = 0;        // of which the first nfused are one-CTA-per-engine items
     std::vector<int> live;        // live engine ids in work-list order
     std::vector<int> item_first;  // per engine id: first item (or -1)
     std::vector<int> item_count;
@@ -465,7 +803,7 @@ struct EngineSet {
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct BlobLayout {
-    size_t box, real, mol, counts, delta, rfac, invvol, expd, dw, pc, pi, pj, dP, pidx, tlist, K, Gcur, dG, moves,
+    size_t box, real, mol, counts, delta, rfac, invvol, expd, dw, pc, pi, pj, dP, pidx, tlist, R, A, Bq, Sb, moves,
         results, st, total;
 };
 
@@ -494,9 +832,10 @@ static BlobLayout blob_layout(const frmc_engine_spec &sp)
     L.dP = take(4 * (size_t)sp.npairs * hs);
     L.pidx = take(4 * (size_t)sp.ne * sp.ne);
     L.tlist = take(4 * (2 * n + 8));
-    L.K = take(8 * (size_t)sp.npairs * hs);
-    L.Gcur = take(8 * hs);
-    L.dG = take(8 * hs);
+    L.R = take(8 * hs);
+    L.A = take(8 * hs);
+    L.Bq = take(8 * hs);
+    L.Sb = take(8 * hs);
     L.moves = take(sizeof(EMove) * (size_t)sp.move_cap);
     L.results = take(sizeof(EResult) * (size_t)sp.move_cap);
     L.st = take(sizeof(EState));
@@ -511,7 +850,9 @@ static int check_spec(const frmc_engine_spec &sp)
         !sp.pair_coef || !sp.rfac || !sp.inv_shell_volume || !sp.experimental || !(sp.variance_squared > 0))
         return set_error(FRMC_E_ARG, "engine spec: missing or invalid field");
     if ((double)sp.ne * sp.ne * sp.hs > 2.0e8)
-        return set_error(FRMC_E_ARG, "engine spec: histogram too large");
+        return set_error(FRMC_E_ARG, "engine spec: histogram too large (ne*ne*hs must stay below 2e8)");
+    if (sp.npairs > 64)
+        return set_error(FRMC_E_ARG, "engine spec: at most 64 element pairs (10 elements)");
     for (int q = 0; q < sp.npairs; ++q)
         if (sp.pair_i[q] < 0 || sp.pair_i[q] >= sp.ne || sp.pair_j[q] < 0 || sp.pair_j[q] >= sp.ne)
             return set_error(FRMC_E_ARG, "engine spec: element pair %d out of range", q);
@@ -543,6 +884,29 @@ static int refresh(EngineSet *s)
         s->item_count[id] = D.ntiles;
         for (int t = 0; t < D.ntiles; ++t) items.push_back(make_int2(id, t));
     }
+    s->nsolo = (int)items.size();
+    // batched list: fused engines largest first, then the tiles of the others
+    std::vector<int> fused_ids;
+    s->fused_smem = 0;
+    for (int id : s->live) {
+        const EDesc &D = s->slots[id].d;
+        const long long smem = 4ll * D.npairs * D.hs;
+        if (s->fused && smem <= kFusedSmemMax && D.n <= kFusedMaxAtoms) {
+            fused_ids.push_back(id);
+            s->fused_smem = std::max(s->fused_smem, (int)smem);
+        }
+    }
+    std::stable_sort(fused_ids.begin(), fused_ids.end(),
+                     [s](int a, int b) { return s->slots[a].d.n > s->slots[b].d.n; });
+    for (int id : fused_ids) items.push_back(make_int2(id, -1));
+    s->nfused = (int)fused_ids.size();
+    for (int id : s->live) {
+        if (std::find(fused_ids.begin(), fused_ids.end(), id) != fused_ids.end())
+            continue;
+        const EDesc &D = s->slots[id].d;
+        for (int t = 0; t < D.ntiles; ++t) items.push_back(make_int2(id, t));
+    }
+    s->nbatch = (int)items.size() - s->nsolo;
     if (nslots > s->ddesc_cap) {
         if (s->ddesc) cudaFree(s->ddesc);
         s->ddesc = nullptr;
@@ -579,7 +943,8 @@ static int refresh(EngineSet *s)
     return FRMC_OK;
 }
 
-static int launch_items(EngineSet *s, const int2 *items, int count, int eval_only, cudaStream_t st)
+static int launch_items(EngineSet *s, const int2 *items, int count, int eval_only, cudaStream_t st,
+                        int dyn_smem = 0, bool fused = false)
 {
     Context *c;
     FRMC_TRY(get_context(&c));
@@ -589,8 +954,24 @@ static int launch_items(EngineSet *s, const int2 *items, int count, int eval_onl
     if (grid < 1)
         return FRMC_OK;
     StepParams p{s->ddesc, items, count, s->tile, eval_only, s->sched};
-    k_engine_step<<<grid, s->threads, 0, st>>>(p);
+    if (fused) {
+        FRMC_CUDA(cudaFuncSetAttribute(k_engine_step<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem));
+        k_engine_step<true><<<grid, s->threads, dyn_smem, st>>>(p);
+    } else {
+        k_engine_step<false><<<grid, s->threads, 0, st>>>(p);
+    }
     FRMC_CUDA(cudaGetLastError());
+    return FRMC_OK;
+}
+
+// The batched work list (every live engine advances one step): the fused
+// engines in one launch, then the tiles of the split ones.
+static int launch_batched(EngineSet *s, cudaStream_t st)
+{
+    if (s->nfused > 0)
+        FRMC_TRY(launch_items(s, s->items + s->nsolo, s->nfused, 0, st, s->fused_smem, true));
+    if (s->nbatch > s->nfused)
+        FRMC_TRY(launch_items(s, s->items + s->nsolo + s->nfused, s->nbatch - s->nfused, 0, st));
     return FRMC_OK;
 }
 
@@ -689,9 +1070,10 @@ static int add_engine(EngineSet *s, const frmc_engine_spec &sp, int *out_id)
     D.dP = (int *)(b + L.dP);
     D.pidx = (int *)(b + L.pidx);
     D.tlist = (int *)(b + L.tlist);
-    D.K = (double *)(b + L.K);
-    D.Gcur = (double *)(b + L.Gcur);
-    D.dG = (double *)(b + L.dG);
+    D.R = (double *)(b + L.R);
+    D.A = (double *)(b + L.A);
+    D.Bq = (double *)(b + L.Bq);
+    D.Sb = (double *)(b + L.Sb);
     D.moves = (EMove *)(b + L.moves);
     D.results = (EResult *)(b + L.results);
     D.st = (EState *)(b + L.st);
@@ -700,10 +1082,12 @@ static int add_engine(EngineSet *s, const frmc_engine_spec &sp, int *out_id)
         pidx[(size_t)sp.pair_i[q] * sp.ne + sp.pair_j[q]] = q;
         pidx[(size_t)sp.pair_j[q] * sp.ne + sp.pair_i[q]] = q;
     }
-    std::vector<double> K((size_t)sp.npairs * sp.hs);
-    for (int q = 0; q < sp.npairs; ++q)
-        for (int bb = 0; bb < sp.hs; ++bb)
-            K[(size_t)q * sp.hs + bb] = sp.rfac[bb] * sp.inv_shell_volume[bb] * sp.pair_coef[q];
+    std::vector<double> Rt(sp.hs), At(sp.hs);
+    for (int bb = 0; bb < sp.hs; ++bb) {
+        Rt[bb] = sp.rfac[bb] * sp.inv_shell_volume[bb];
+        const double w = sp.data_weights ? sp.data_weights[bb] : 1.0;
+        At[bb] = w * Rt[bb] * Rt[bb];
+    }
     std::vector<float4> b4(sp.n), r4(sp.n);
     for (int i = 0; i < sp.n; ++i) {
         b4[i] = make_float4(sp.box_coords[3 * i], sp.box_coords[3 * i + 1], sp.box_coords[3 * i + 2],
@@ -730,7 +1114,8 @@ static int add_engine(EngineSet *s, const frmc_engine_spec &sp, int *out_id)
     up(D.pi, sp.pair_i, 4 * (size_t)sp.npairs);
     up(D.pj, sp.pair_j, 4 * (size_t)sp.npairs);
     up(D.pidx, pidx.data(), 4 * pidx.size());
-    up(D.K, K.data(), 8 * K.size());
+    up(D.R, Rt.data(), 8 * Rt.size());
+    up(D.A, At.data(), 8 * At.size());
     if (!rc) {
         cudaError_t ce = cudaMemsetAsync(D.moves, 0, sizeof(EMove) * sp.move_cap, s->stream);
         if (ce == cudaSuccess)
@@ -891,12 +1276,25 @@ int frmc_engines_destroy(void *handle)
 int frmc_engines_set_tune(void *handle, int tile, int threads, int ctas_per_sm)
 {
     EngineSet *s = as_set(handle);
-    if (!s || tile < 32 || threads < 32 || threads > 1024 || threads % 32 || ctas_per_sm < 1 || ctas_per_sm > 32)
-        return set_error(FRMC_E_ARG, "engines_set_tune: invalid configuration");
+    if (!s || tile < 32 || threads < 32 || threads > kMaxEngineThreads || threads % 32 || ctas_per_sm < 1 ||
+        ctas_per_sm > 32)
+        return set_error(FRMC_E_ARG, "engines_set_tune: threads must be a multiple of 32 in [32, %d]",
+                         kMaxEngineThreads);
     FRMC_CUDA(cudaStreamSynchronize(s->stream));
     s->tile = tile;
     s->threads = threads;
     s->ctas_per_sm = ctas_per_sm;
+    s->dirty = true;
+    return refresh(s);
+}
+
+int frmc_engines_set_mode(void *handle, int fused)
+{
+    EngineSet *s = as_set(handle);
+    if (!s)
+        return set_error(FRMC_E_ARG, "null handle");
+    FRMC_CUDA(cudaStreamSynchronize(s->stream));
+    s->fused = fused ? 1 : 0;
     s->dirty = true;
     return refresh(s);
 }
@@ -910,7 +1308,7 @@ int frmc_engines_get_tune(void *handle, int *tile, int *threads, int *ctas_per_s
     if (tile) *tile = s->tile;
     if (threads) *threads = s->threads;
     if (ctas_per_sm) *ctas_per_sm = s->ctas_per_sm;
-    if (nitems) *nitems = s->nitems;
+    if (nitems) *nitems = s->nbatch;
     return FRMC_OK;
 }
 
@@ -965,12 +1363,14 @@ int frmc_engines_step(void *handle, int32_t engine, int32_t steps, int use_graph
         return set_error(FRMC_E_ARG, "engines_step: invalid arguments");
     FRMC_TRY(refresh(s));
     cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
-    const int first = engine < 0 ? 0 : s->item_first[engine];
-    const int count = engine < 0 ? s->nitems : s->item_count[engine];
+    const int count = engine < 0 ? s->nbatch : s->item_count[engine];
     if (count == 0 || steps == 0)
         return FRMC_OK;
+    auto one = [&](cudaStream_t sx) {
+        return engine < 0 ? launch_batched(s, sx) : launch_items(s, s->items + s->item_first[engine], count, 0, sx);
+    };
     if (!use_graph) {
-        for (int k = 0; k < steps; ++k) FRMC_TRY(launch_items(s, s->items + first, count, 0, st));
+        for (int k = 0; k < steps; ++k) FRMC_TRY(one(st));
         return FRMC_OK;
     }
     auto key = std::make_pair(engine, steps);
@@ -982,7 +1382,7 @@ int frmc_engines_step(void *handle, int32_t engine, int32_t steps, int use_graph
         cudaError_t ce = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
         int rc = FRMC_OK;
         if (ce == cudaSuccess) {
-            for (int k = 0; k < steps && !rc; ++k) rc = launch_items(s, s->items + first, count, 0, cap);
+            for (int k = 0; k < steps && !rc; ++k) rc = one(cap);
             ce = cudaStreamEndCapture(cap, &g);
         }
         cudaStreamDestroy(cap);
@@ -1042,7 +1442,7 @@ int frmc_engines_step_host(void *handle, const int32_t *atoms, const float *vecs
     FRMC_CUDA(cudaMemcpyAsync(s->dstage_m, s->hstage_m, sizeof(EMove) * E, cudaMemcpyHostToDevice, st));
     k_scatter_moves<<<(E + 127) / 128, 128, 0, st>>>(s->ddesc, s->dlive, s->dstage_m, E);
     FRMC_CUDA(cudaGetLastError());
-    FRMC_TRY(launch_items(s, s->items, s->nitems, 0, st));
+    FRMC_TRY(launch_batched(s, st));
     k_gather_results<<<(E + 127) / 128, 128, 0, st>>>(s->ddesc, s->dlive, s->dstage_r, E);
     FRMC_CUDA(cudaGetLastError());
     FRMC_CUDA(cudaMemcpyAsync(s->hstage_r, s->dstage_r, sizeof(EResult) * E, cudaMemcpyDeviceToHost, st));

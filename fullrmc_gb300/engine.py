@@ -49,6 +49,7 @@ register("frmc_engines_step_host", [_vp, I32P, F32P, F32P, F64P, I32P])
 register("frmc_engines_destroy", [_vp])
 register("frmc_engines_set_tune", [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int])
 register("frmc_engines_get_tune", [_vp] + [ctypes.POINTER(ctypes.c_int)] * 4)
+register("frmc_engines_set_mode", [_vp, ctypes.c_int])
 register("frmc_engines_init", [_vp])
 register("frmc_engines_push_moves", [_vp, _i32, I32P, F32P, F32P, _i32, _i64, ctypes.c_int])
 register("frmc_engines_step", [_vp, _i32, _i32, ctypes.c_int, _vp])
@@ -273,6 +274,9 @@ class EngineSet:
     # ------------------------------------------------------------ control
     def set_tune(self, tile, threads, ctas_per_sm):
         check(load().frmc_engines_set_tune(self.handle, int(tile), int(threads), int(ctas_per_sm)))
+
+    def set_mode(self, fused):
+        check(load().frmc_engines_set_mode(self.handle, int(bool(fused))))
 
     def get_tune(self):
         v = [ctypes.c_int() for _ in range(4)]

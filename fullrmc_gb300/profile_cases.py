@@ -1,7 +1,7 @@
 """Small, self-contained runs of the hot kernels, sized for profiling.
 
     python -m fullrmc_gb300.profile_cases allpairs --n 30000 --reps 3
-    python -m fullrmc_gb300.profile_cases engines --count 64 --steps 5
+    python -m fullrmc_gb300.profile_cases engines --count 64 --steps 5 [--tune 1024,1024,1]
 
 ``allpairs`` runs the all-pairs histogram (three species, triclinic box with
 gamma = 120 degrees at 0.1057 atoms/A^3, r 0-20 A) on device buffers;
@@ -49,12 +49,12 @@ def allpairs(n, reps):
     return {"case": "allpairs", "atoms": n, "ms": ms, "pairs": n * (n - 1) / 2, "in_range": int(cnt.sum().item())}
 
 
-def engines(count, steps):
+def engines(count, steps, tune=None):
     import torch
     from fullrmc_gb300 import synthetic
     from fullrmc_gb300.engine import EngineSet, translation_moves
     systems = synthetic.mixed_engines(seed=0, count=count)
-    es = EngineSet(systems, move_cap=steps + 4)
+    es = EngineSet(systems, move_cap=steps + 4, tune=tune)
     es.init()
     for e, s in enumerate(systems):
         a, v, u = translation_moves(np.random.default_rng([0, e]), s.box_coords.shape[0], steps, 0.1)
@@ -83,8 +83,10 @@ def main():
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--count", type=int, default=64)
     ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--tune", default=None, help="tile,threads,ctas_per_sm of the engine work list")
     a = ap.parse_args()
-    out = allpairs(a.n, a.reps) if a.case == "allpairs" else engines(a.count, a.steps)
+    tune = tuple(int(x) for x in a.tune.split(",")) if a.tune else None
+    out = allpairs(a.n, a.reps) if a.case == "allpairs" else engines(a.count, a.steps, tune)
     print(json.dumps(out))
 
 

@@ -69,9 +69,14 @@ int frmc_engines_remove(void *handle, int32_t id);
 /* Live engine ids in stepping order (ascending); *count receives the number. */
 int frmc_engines_live(void *handle, int32_t *ids, int32_t cap, int32_t *count);
 int frmc_engines_destroy(void *handle);
-/* Work-list configuration: atoms per item, threads per CTA, CTAs per SM. */
+/* Work-list configuration: atoms per item, threads per CTA (multiple of 32,
+ * at most 512), CTAs per SM. */
 int frmc_engines_set_tune(void *handle, int tile, int threads, int ctas_per_sm);
 int frmc_engines_get_tune(void *handle, int *tile, int *threads, int *ctas_per_sm, int *nitems);
+/* Batched steps run one CTA per engine where the engine's element-pair deltas
+ * fit in shared memory (fused = 1, the default), else every engine is split
+ * over atom tiles (fused = 0).  Results are identical either way. */
+int frmc_engines_set_mode(void *handle, int fused);
 /* All-pairs histograms of the initial coordinates and the initial chi2. */
 int frmc_engines_init(void *handle);
 /* Moves for steps [first_step, first_step + count) of engine e: atoms (count,),

@@ -86,6 +86,7 @@ def test_tune_and_graph_do_not_change_results():
     base = _run(systems, mv, steps, "batched", tune=(1024, 256, 4))
     _same(base, _run(systems, mv, steps, "batched", tune=(128, 128, 8), graph=False))
     _same(base, _run(systems, mv, steps, "batched", tune=(4096, 512, 1), chunk=7))
+    _same(base, _run(systems, mv, steps, "solo", tune=(256, 64, 2), chunk=9))
 
 
 def test_engine_replays_on_oracle(oracle_mod):
@@ -166,3 +167,24 @@ def test_add_remove_keeps_other_chains_exact():
         assert np.array_equal(acc, base[e]["acc"])
         assert np.array_equal(c2.view(np.int64), base[e]["chi2"].view(np.int64))
     es.close()
+
+
+def test_fused_and_split_batched_paths_agree():
+    """One-CTA-per-engine steps (shared-memory deltas) and tile-split steps
+    (global deltas) give bit-identical chains."""
+    from fullrmc_gb300.engine import EngineSet
+    systems = _systems(count=5, seed=23, nmin=700, nmax=4000)
+    steps = 60
+    mv = _moves(systems, steps, seed=6)
+    out = []
+    for fused in (1, 0):
+        es = EngineSet(systems, move_cap=64)
+        es.set_mode(fused)
+        es.init()
+        for e, (a, v, u) in enumerate(mv):
+            es.push_moves(e, a, v, u, 0)
+        es.step(steps, graph=bool(fused))
+        out.append([dict(zip(("chi2", "acc", "atoms"), es.results(e, 0, steps)), state=es.state(e),
+                         counts=es.counts(e), coords=es.coords(e)) for e in range(len(systems))])
+        es.close()
+    _same(out[0], out[1])
