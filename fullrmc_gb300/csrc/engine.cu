@@ -44,12 +44,16 @@
 namespace frmc {
 
 struct EState {
-    double chi2;        // SD / varianceSquared of the current configuration
+    double chi2;        // sd / varianceSquared (+ sd_sq / sq varianceSquared)
     double sd;          // sum w (exp - G)^2 of the current configuration
+    double sd_sq;       // sum w (S_exp - S)^2 of the current configuration
+    double dsd;         // change of sd proposed this step (engines with S(Q))
     long long step;
     long long accepted;
     unsigned done;      // items of the current step finished
     unsigned tcount;    // entries in the touched-bin list of the current step
+    unsigned sq_done;   // S(Q) row blocks of the current step finished
+    int fmt;            // touched-list format of the step: 1 = (flat << 1) | sign, 0 = flat
 };
 
 // Work scheduler of one engine set: CTAs claim items with an atomic counter;
@@ -87,7 +91,21 @@ struct EDesc {
     double *R;    // [hs] rfac * invvol: G(b) = R(b) sum_p pair_coef_p n_p(b) - rfac(b)
     double *A;    // [hs] w R^2
     double *Bq;   // [hs] 2 w R (exp - G) of the current configuration
-    double *Sb;   // [hs] S(b) = sum_p pair_coef_p dP_p(b) proposed this step (large hs only)
+    double *Sb;   // [hs] S(b) = sum_p pair_coef_p dP_p(b) proposed this step (large hs or S(Q))
+    // S(Q) term (sq = 1): with x(b) = Rq(b) S(b) the change of the S(Q)
+    // shells' G, d(sd_sq) = x^T K x - x^T h, h = 2 M W (S_exp - S).
+    int sq, nq, sqblk;
+    double var2q;
+    const double *M;    // [hs][nq] G -> S(Q) table (shared)
+    const double *K;    // [hs][hs] M W M^T (shared, symmetric)
+    const double *wq;   // [nq] data weights or null (shared)
+    double *Rq;         // [hs] 4 pi r rho0 / shell volume of the S(Q) shells
+    double *rfacq;      // [hs] 4 pi r rho0 of the S(Q) shells
+    double *sqexp;      // [nq] experimental S(Q)
+    double *h;          // [hs] 2 M W (S_exp - S) of the current configuration
+    double *y;          // [hs] K x of this step
+    double *sqpart;     // [sqblk] this step's partial sums of x (y - h)
+    double *sqv;        // [nq] S(Q) written by the evaluation kernel
     EMove *moves;
     EResult *results;
     EState *st;
@@ -359,6 +377,7 @@ __device__ double eval_delta(const EDesc &Dg, int *dP, double *red, double *cb, 
         const double *__restrict__ pc;
     } D = {Dg.hs, Dg.A, Dg.Bq, Dg.Sb, Dg.pc};
     const int np = Dg.npairs;
+    const bool sq = Dg.sq != 0;
     if (!SMEM)
         for (int q = threadIdx.x; q < np; q += blockDim.x) coef[q] = D.pc[q];
     lanes_zero(red);
@@ -407,9 +426,9 @@ __device__ double eval_delta(const EDesc &Dg, int *dP, double *red, double *cb, 
                 c = S * fma(a, S, -bq);
             }
             cb[b - c0] = c;
-            if (big)
+            if (big || sq)
                 D.Sb[b] = S;
-            else
+            if (!big)
                 sbs[b] = S;
         }
         lanes_add_chunk(red, cb, c0, cn);
@@ -423,6 +442,16 @@ __device__ void finish_engine(const EDesc &D, int atom, float3 nw, float4 nreal,
                               double *sbs, double *coef, int *s_flag)
 {
     const double dsd = eval_delta<false>(D, D.dP, red, cb, sbs, coef);
+    if (D.sq) {
+        // the S(Q) kernel evaluates its term, decides and commits
+        if (threadIdx.x == 0) {
+            EState &S = *D.st;
+            S.dsd = dsd;
+            S.fmt = 0;
+            S.done = 0u;
+        }
+        return;
+    }
     const EState &S0 = *D.st;
     const double sd_new = S0.sd + dsd;
     const double chi2_new = sd_new / D.var2;
@@ -601,6 +630,16 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *red, double *cb, 
     }
     __syncthreads();
     const double dsd = eval_delta<true>(D, sdP, red, cb, sbs, coef);
+    if (D.sq) {
+        // the S(Q) kernel evaluates its term, decides and commits
+        if (threadIdx.x == 0) {
+            EState &S = *D.st;
+            S.dsd = dsd;
+            S.tcount = *s_tcount;
+            S.fmt = 1;
+        }
+        return;
+    }
     const EState &S0 = *D.st;
     const double sd_new = S0.sd + dsd;
     const double chi2_new = sd_new / D.var2;
@@ -759,12 +798,316 @@ __global__ void k_gather_results(const EDesc *desc, const int *ids, EResult *out
     }
 }
 
+// ------------------------------------------------------------------ S(Q) term
+// Engines with a StructureFactorConstraint finish every step here.  The
+// histogram kernels have left S(b) in Sb, the G(r) change in st->dsd and the
+// touched list; with x(b) = Rq(b) S(b), the change of the S(Q) term is
+//   d(sd_sq) = sum_Q w [(e - dS)^2 - e^2] = x^T K x - x^T h,
+// e = S_exp - S, dS = M^T x, K = M W M^T, h = 2 M W e.
+// Items are (engine, block of kSqRows rows of K).  A CTA lists the non-zero
+// x(c) in increasing c, computes y(b) = sum_c K[c][b] x(c) for its rows (K is
+// symmetric, so row c is read contiguously) and its rows' share of x (y - h);
+// the CTA that finishes an engine's last block adds the shares in block
+// order, decides and commits: counts, Bq -= 2 A S, h -= 2 y, coordinates.
+constexpr int kSqRows = 256;      // rows of K per item = threads per CTA
+constexpr int kSqMaxBins = 4096;  // histogram bins of an engine with an S(Q) term
+
+struct SqParams {
+    const EDesc *desc;
+    const int2 *items;
+    int nitems;
+    Sched *sched;
+};
+
+__device__ void sq_finish(const EDesc &D, int *s_flag, double *s_val)
+{
+    if (threadIdx.x == 0) {
+        double dsq = 0.0;
+        for (int k = 0; k < D.sqblk; ++k) dsq += __ldcg(D.sqpart + k);
+        const EState &S0 = *D.st;
+        const double sd_new = S0.sd + S0.dsd;
+        const double sq_new = S0.sd_sq + dsq;
+        const double chi2_new = sd_new / D.var2 + sq_new / D.var2q;
+        const EMove &m = D.moves[S0.step % D.move_cap];
+        const bool reject = (chi2_new > S0.chi2) && (m.u > D.tol);
+        *s_flag = reject ? 0 : 1;
+        s_val[0] = chi2_new;
+        s_val[1] = sd_new;
+        s_val[2] = sq_new;
+    }
+    __syncthreads();
+    const bool accept = *s_flag != 0;
+    const unsigned nt = D.st->tcount;
+    if (D.st->fmt) {
+        // one CTA's shared-memory deltas: entries (flat << 1) | sign
+        if (accept)
+            for (unsigned k = threadIdx.x; k < nt; k += blockDim.x) {
+                const int e = D.tlist[k];
+                atomicAdd(D.counts + (e >> 1), (e & 1) ? 1 : -1);
+            }
+    } else {
+        // global oriented deltas: atomicExch hands each bin's delta to one entry
+        for (unsigned k = threadIdx.x; k < nt; k += blockDim.x) {
+            const int f = D.tlist[k];
+            const int d = atomicExch(D.delta + f, 0);
+            if (accept && d)
+                D.counts[f] += d;
+        }
+    }
+    if (accept) {
+        for (int b = threadIdx.x; b < D.hs; b += blockDim.x) {
+            const double sv = D.Sb[b];
+            if (sv != 0.0)
+                D.Bq[b] = fma(-2.0 * D.A[b], sv, D.Bq[b]);
+            D.h[b] = fma(-2.0, __ldcg(D.y + b), D.h[b]);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        EState &S = *D.st;
+        const EMove m = D.moves[S.step % D.move_cap];
+        EResult &r = D.results[S.step % D.move_cap];
+        r.chi2_new = s_val[0];
+        r.accepted = accept ? 1 : 0;
+        r.atom = m.atom;
+        if (accept) {
+            const float4 ob = D.box[m.atom];
+            const float4 orl = D.real[m.atom];
+            const float rx = __fadd_rn(orl.x, m.v[0]), ry = __fadd_rn(orl.y, m.v[1]), rz = __fadd_rn(orl.z, m.v[2]);
+            const float3 nw = D.bm == BM_IBC ? make_float3(rx, ry, rz) : to_box(D.RB, rx, ry, rz);
+            D.box[m.atom] = make_float4(nw.x, nw.y, nw.z, ob.w);
+            D.real[m.atom] = make_float4(rx, ry, rz, 0.0f);
+            S.chi2 = s_val[0];
+            S.sd = s_val[1];
+            S.sd_sq = s_val[2];
+            S.accepted += 1;
+        }
+        S.step += 1;
+        S.tcount = 0u;
+        S.sq_done = 0u;
+        S.dsd = 0.0;
+    }
+}
+
+__global__ void __launch_bounds__(kSqRows) k_sq_step(SqParams p)
+{
+    extern __shared__ double sq_smem[];  // x values [hs], then their bins (int) [hs]
+    __shared__ double red[kSqRows];
+    __shared__ double s_val[3];
+    __shared__ int s_wsum[kSqRows / 32];
+    __shared__ int s_item, s_last, s_flag, s_base;
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const unsigned long long k = atomicAdd(&p.sched->claimed, 1ull);
+            s_item = k < (unsigned long long)p.nitems ? (int)k : -1;
+            s_base = 0;
+        }
+        __syncthreads();
+        const int it = s_item;
+        if (it < 0)
+            break;
+        const int2 item = p.items[it];
+        const EDesc &D = p.desc[item.x];
+        const int hs = D.hs;
+        double *xv = sq_smem;
+        int *xi = (int *)(sq_smem + hs);
+        for (int c0 = 0; c0 < hs; c0 += kSqRows) {
+            const int c = c0 + threadIdx.x;
+            double x = 0.0;
+            if (c < hs) {
+                const double sv = __ldcg(D.Sb + c);
+                if (sv != 0.0)
+                    x = D.Rq[c] * sv;
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, x != 0.0);
+            if (lane == 0)
+                s_wsum[warp] = __popc(bal);
+            __syncthreads();
+            int off = s_base;
+            for (unsigned w = 0; w < warp; ++w) off += s_wsum[w];
+            if (x != 0.0) {
+                const int pos = off + __popc(bal & ((1u << lane) - 1u));
+                xv[pos] = x;
+                xi[pos] = c;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                int t = 0;
+                for (int w = 0; w < kSqRows / 32; ++w) t += s_wsum[w];
+                s_base += t;
+            }
+            __syncthreads();
+        }
+        const int nx = s_base;
+        const int b = item.y * kSqRows + threadIdx.x;
+        double part = 0.0;
+        if (b < hs) {
+            const double *__restrict__ K = D.K + b;
+            double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+            int k = 0;
+            for (; k + 4 <= nx; k += 4) {
+                const double k0 = __ldg(K + (size_t)xi[k] * hs), k1 = __ldg(K + (size_t)xi[k + 1] * hs);
+                const double k2 = __ldg(K + (size_t)xi[k + 2] * hs), k3 = __ldg(K + (size_t)xi[k + 3] * hs);
+                a0 = fma(k0, xv[k], a0);
+                a1 = fma(k1, xv[k + 1], a1);
+                a2 = fma(k2, xv[k + 2], a2);
+                a3 = fma(k3, xv[k + 3], a3);
+            }
+            for (; k < nx; ++k) a0 = fma(__ldg(K + (size_t)xi[k] * hs), xv[k], a0);
+            const double yb = (a0 + a1) + (a2 + a3);
+            D.y[b] = yb;
+            const double sv = __ldcg(D.Sb + b);
+            if (sv != 0.0)
+                part = (D.Rq[b] * sv) * (yb - D.h[b]);
+        }
+        red[threadIdx.x] = part;
+        __syncthreads();
+        for (int st = kSqRows / 2; st > 0; st >>= 1) {
+            if ((int)threadIdx.x < st)
+                red[threadIdx.x] += red[threadIdx.x + st];
+            __syncthreads();
+        }
+        // release: y and the share are visible before the block is counted
+        if (threadIdx.x == 0) {
+            D.sqpart[item.y] = red[0];
+            __threadfence();
+            const unsigned prev = atomicAdd(&D.st->sq_done, 1u);
+            s_last = (prev == (unsigned)D.sqblk - 1u) ? 1 : 0;
+        }
+        __syncthreads();
+        if (s_last) {
+            __threadfence();
+            sq_finish(D, &s_flag, s_val);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned f = atomicAdd(&p.sched->finished, 1u);
+        if (f == gridDim.x - 1) {
+            p.sched->claimed = 0ull;
+            p.sched->finished = 0u;
+            __threadfence();
+        }
+    }
+}
+
+// S(Q) of engine `id`'s current counts (StructureFactorConstraints.py:780-822
+// with scale factor 1 and no window): G_S(b) = Rq(b) sum_p pair_coef_p n_p(b)
+// - rfacq(b) in shared memory, S(q) = sum_b G_S(b) M[b][q] + 1 into sqv.
+// With commit, also sd_sq = sum_q w (S_exp - S)^2, h(b) = 2 sum_q M[b][q] w
+// (S_exp - S) and the chain's chi2 (set-up).  One CTA, fixed summation orders.
+__global__ void __launch_bounds__(512) k_sq_eval(const EDesc *desc, int id, int commit)
+{
+    extern __shared__ double gs[];  // [hs]
+    __shared__ double red[kRedLanes];
+    __shared__ double cb[kChunk];
+    const EDesc &D = desc[id];
+    const int hs = D.hs, nq = D.nq;
+    for (int b = threadIdx.x; b < hs; b += blockDim.x) {
+        double S = 0.0;
+        for (int q = 0; q < D.npairs; ++q) S = fma(D.pc[q], (double)pair_count(D, q, b), S);
+        gs[b] = fma(D.Rq[b], S, -D.rfacq[b]);
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+        double a = 0.0;
+        for (int b = 0; b < hs; ++b) a = fma(gs[b], D.M[(size_t)b * nq + q], a);
+        D.sqv[q] = a + 1.0;
+    }
+    if (!commit)
+        return;
+    lanes_zero(red);
+    for (int c0 = 0; c0 < nq; c0 += kChunk) {
+        const int cn = min(kChunk, nq - c0);
+        for (int q = c0 + threadIdx.x; q < c0 + cn; q += blockDim.x) {
+            const double e = D.sqexp[q] - D.sqv[q];
+            const double w = D.wq ? D.wq[q] : 1.0;
+            cb[q - c0] = (w * e) * e;
+        }
+        lanes_add_chunk(red, cb, c0, cn);
+    }
+    const double sdq = lanes_total(red);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int b = warp; b < hs; b += nwarps) {
+        const double *row = D.M + (size_t)b * nq;
+        double a = 0.0;
+        for (int q = lane; q < nq; q += 32) {
+            const double w = D.wq ? D.wq[q] : 1.0;
+            a = fma(row[q], w * (D.sqexp[q] - D.sqv[q]), a);
+        }
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if (lane == 0)
+            D.h[b] = 2.0 * a;
+    }
+    if (threadIdx.x == 0) {
+        EState &S = *D.st;
+        S.sd_sq = sdq;
+        S.chi2 = S.sd / D.var2 + sdq / D.var2q;
+    }
+}
+
+// K[b][c] = sum_q (M[b][q] M[c][q]) w_q in increasing q: 64 x 64 tiles of K
+// per CTA, 4 x 4 per thread, M staged through shared memory 16 Q points at a
+// time.  The product M[b][q] M[c][q] is formed before the weight, so K is
+// exactly symmetric.
+__global__ void __launch_bounds__(256) k_sq_gram(const double *M, const double *w, int hs, int nq, double *K)
+{
+    __shared__ double A[16][65];
+    __shared__ double Bt[16][65];
+    const int b0 = blockIdx.y * 64, c0 = blockIdx.x * 64;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    double acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+    for (int q0 = 0; q0 < nq; q0 += 16) {
+        for (int k = threadIdx.x; k < 64 * 16; k += 256) {
+            const int r = k >> 4, qq = k & 15, q = q0 + qq;
+            A[qq][r] = (b0 + r < hs && q < nq) ? M[(size_t)(b0 + r) * nq + q] : 0.0;
+            Bt[qq][r] = (c0 + r < hs && q < nq) ? M[(size_t)(c0 + r) * nq + q] : 0.0;
+        }
+        __syncthreads();
+        const int qn = min(16, nq - q0);
+        for (int qq = 0; qq < qn; ++qq) {
+            const double wq = w ? w[q0 + qq] : 1.0;
+            double a[4], bb[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) a[i] = A[qq][ty + 16 * i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) bb[j] = Bt[qq][tx + 16 * j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i] * bb[j], wq, acc[i][j]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int b = b0 + ty + 16 * i, c = c0 + tx + 16 * j;
+            if (b < hs && c < hs)
+                K[(size_t)b * hs + c] = acc[i][j];
+        }
+}
+
 // --------------------------------------------------------------- host side
 struct Slot {
     bool live = false;
     bool initialized = false;
     EDesc d;
     void *blob = nullptr;
+    size_t bytes = 0;
+};
+
+struct SqTable {
+    int hs = 0, nq = 0;
+    void *blob = nullptr;
+    double *M = nullptr, *K = nullptr, *w = nullptr;
     size_t bytes = 0;
 };
 
@@ -794,7 +1137,13 @@ struct EngineSet {
     EMove *dstage_m = nullptr;
     EResult *dstage_r = nullptr;
     int stage_cap = 0;
-    Sched *sched = nullptr;
+    Sched *sched = nullptr;        // [0]: histogram step kernels, [1]: S(Q) kernel
+    std::vector<SqTable> tables;
+    std::vector<int2> sq_host;     // (engine, row block) of every live engine with an S(Q) term
+    std::vector<int> sq_first, sq_count;
+    int2 *sq_items = nullptr;
+    int sq_cap = 0;
+    int sq_smem = 0;               // dynamic shared memory of the S(Q) kernel
     cudaStream_t stream = nullptr;
     std::map<std::pair<int, int>, cudaGraphExec_t> graphs;
     bool dirty = true;
@@ -804,7 +1153,7 @@ static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct BlobLayout {
     size_t box, real, mol, counts, delta, rfac, invvol, expd, dw, pc, pi, pj, dP, pidx, tlist, R, A, Bq, Sb, moves,
-        results, st, total;
+        results, st, Rq, rfacq, sqexp, h, y, sqpart, sqv, total;
 };
 
 static BlobLayout blob_layout(const frmc_engine_spec &sp)
@@ -839,6 +1188,15 @@ static BlobLayout blob_layout(const frmc_engine_spec &sp)
     L.moves = take(sizeof(EMove) * (size_t)sp.move_cap);
     L.results = take(sizeof(EResult) * (size_t)sp.move_cap);
     L.st = take(sizeof(EState));
+    const bool sq = sp.sq_table >= 0;
+    const size_t nq = sq ? (size_t)sp.nq : 0, hq = sq ? hs : 0;
+    L.Rq = take(8 * hq);
+    L.rfacq = take(8 * hq);
+    L.sqexp = take(8 * nq);
+    L.h = take(8 * hq);
+    L.y = take(8 * hq);
+    L.sqpart = take(sq ? 8 * (size_t)((sp.hs + kSqRows - 1) / kSqRows) : 0);
+    L.sqv = take(8 * nq);
     L.total = off;
     return L;
 }
@@ -859,6 +1217,13 @@ static int check_spec(const frmc_engine_spec &sp)
     for (int i = 0; i < sp.n; ++i)
         if (sp.el[i] < 0 || sp.el[i] >= sp.ne)
             return set_error(FRMC_E_ARG, "engine spec: atom %d element out of range", i);
+    if (sp.sq_table >= 0) {
+        if (sp.nq < 1 || !sp.sq_rfac || !sp.sq_inv_shell_volume || !sp.sq_experimental ||
+            !(sp.sq_variance_squared > 0))
+            return set_error(FRMC_E_ARG, "engine spec: missing or invalid S(Q) field");
+        if (sp.hs > kSqMaxBins)
+            return set_error(FRMC_E_ARG, "engine spec: an S(Q) term needs hs <= %d", kSqMaxBins);
+    }
     return FRMC_OK;
 }
 
@@ -907,6 +1272,26 @@ static int refresh(EngineSet *s)
         for (int t = 0; t < D.ntiles; ++t) items.push_back(make_int2(id, t));
     }
     s->nbatch = (int)items.size() - s->nsolo;
+    s->sq_host.clear();
+    s->sq_first.assign(nslots, -1);
+    s->sq_count.assign(nslots, 0);
+    s->sq_smem = 0;
+    for (int id : s->live) {
+        const EDesc &D = s->slots[id].d;
+        if (!D.sq)
+            continue;
+        s->sq_first[id] = (int)s->sq_host.size();
+        s->sq_count[id] = D.sqblk;
+        for (int k = 0; k < D.sqblk; ++k) s->sq_host.push_back(make_int2(id, k));
+        s->sq_smem = std::max(s->sq_smem, 12 * D.hs);
+    }
+    if ((int)s->sq_host.size() > s->sq_cap) {
+        if (s->sq_items) cudaFree(s->sq_items);
+        s->sq_items = nullptr;
+        int cap = std::max((int)s->sq_host.size(), 2 * s->sq_cap);
+        FRMC_CUDA(cudaMalloc(&s->sq_items, sizeof(int2) * cap));
+        s->sq_cap = cap;
+    }
     if (nslots > s->ddesc_cap) {
         if (s->ddesc) cudaFree(s->ddesc);
         s->ddesc = nullptr;
@@ -937,6 +1322,9 @@ static int refresh(EngineSet *s)
         FRMC_CUDA(cudaMemcpy(s->items, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice));
     if (!s->live.empty())
         FRMC_CUDA(cudaMemcpy(s->dlive, s->live.data(), sizeof(int) * s->live.size(), cudaMemcpyHostToDevice));
+    if (!s->sq_host.empty())
+        FRMC_CUDA(cudaMemcpy(s->sq_items, s->sq_host.data(), sizeof(int2) * s->sq_host.size(),
+                             cudaMemcpyHostToDevice));
     s->nitems = (int)items.size();
     drop_graphs(s);
     s->dirty = false;
@@ -964,14 +1352,40 @@ static int launch_items(EngineSet *s, const int2 *items, int count, int eval_onl
     return FRMC_OK;
 }
 
+// S(Q) row blocks [first, first + count) of the set's S(Q) item list.
+static int launch_sq(EngineSet *s, int first, int count, cudaStream_t st)
+{
+    if (count <= 0)
+        return FRMC_OK;
+    Context *c;
+    FRMC_TRY(get_context(&c));
+    int grid = std::min(count, c->sms * 4);
+    SqParams p{s->ddesc, s->sq_items + first, count, s->sched + 1};
+    FRMC_CUDA(cudaFuncSetAttribute(k_sq_step, cudaFuncAttributeMaxDynamicSharedMemorySize, s->sq_smem));
+    k_sq_step<<<grid, kSqRows, s->sq_smem, st>>>(p);
+    FRMC_CUDA(cudaGetLastError());
+    return FRMC_OK;
+}
+
 // The batched work list (every live engine advances one step): the fused
-// engines in one launch, then the tiles of the split ones.
+// engines in one launch, then the tiles of the split ones, then the S(Q)
+// blocks of the engines that have an S(Q) term.
 static int launch_batched(EngineSet *s, cudaStream_t st)
 {
     if (s->nfused > 0)
         FRMC_TRY(launch_items(s, s->items + s->nsolo, s->nfused, 0, st, s->fused_smem, true));
     if (s->nbatch > s->nfused)
         FRMC_TRY(launch_items(s, s->items + s->nsolo + s->nfused, s->nbatch - s->nfused, 0, st));
+    FRMC_TRY(launch_sq(s, 0, (int)s->sq_host.size(), st));
+    return FRMC_OK;
+}
+
+static int launch_sq_eval(EngineSet *s, int id, int commit, cudaStream_t st)
+{
+    const int bytes = 8 * s->slots[id].d.hs;
+    FRMC_CUDA(cudaFuncSetAttribute(k_sq_eval, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    k_sq_eval<<<1, 512, bytes, st>>>(s->ddesc, id, commit);
+    FRMC_CUDA(cudaGetLastError());
     return FRMC_OK;
 }
 
@@ -1015,6 +1429,8 @@ static int init_engine(EngineSet *s, int id)
     FRMC_CUDA(cudaMalloc(&ditem, sizeof(int2)));
     FRMC_CUDA(cudaMemcpyAsync(ditem, &item, sizeof(int2), cudaMemcpyHostToDevice, s->stream));
     int rc = launch_items(s, ditem, 1, 1, s->stream);
+    if (!rc && D.sq)
+        rc = launch_sq_eval(s, id, 1, s->stream);
     cudaError_t ce = cudaStreamSynchronize(s->stream);
     cudaFree(ditem);
     if (rc)
@@ -1032,6 +1448,15 @@ static int init_engine(EngineSet *s, int id)
 static int add_engine(EngineSet *s, const frmc_engine_spec &sp, int *out_id)
 {
     FRMC_TRY(check_spec(sp));
+    const SqTable *tab = nullptr;
+    if (sp.sq_table >= 0) {
+        if (sp.sq_table >= (int)s->tables.size())
+            return set_error(FRMC_E_ARG, "engine spec: unknown S(Q) table %d", sp.sq_table);
+        tab = &s->tables[sp.sq_table];
+        if (tab->hs != sp.hs || tab->nq != sp.nq)
+            return set_error(FRMC_E_ARG, "engine spec: S(Q) table %d is %d x %d, the engine needs %d x %d",
+                             sp.sq_table, tab->hs, tab->nq, sp.hs, sp.nq);
+    }
     BlobLayout L = blob_layout(sp);
     Slot sl;
     FRMC_CUDA(cudaMalloc(&sl.blob, L.total));
@@ -1077,6 +1502,25 @@ static int add_engine(EngineSet *s, const frmc_engine_spec &sp, int *out_id)
     D.moves = (EMove *)(b + L.moves);
     D.results = (EResult *)(b + L.results);
     D.st = (EState *)(b + L.st);
+    std::vector<double> Rqt;
+    if (tab) {
+        D.sq = 1;
+        D.nq = sp.nq;
+        D.sqblk = (sp.hs + kSqRows - 1) / kSqRows;
+        D.var2q = sp.sq_variance_squared;
+        D.M = tab->M;
+        D.K = tab->K;
+        D.wq = tab->w;
+        D.Rq = (double *)(b + L.Rq);
+        D.rfacq = (double *)(b + L.rfacq);
+        D.sqexp = (double *)(b + L.sqexp);
+        D.h = (double *)(b + L.h);
+        D.y = (double *)(b + L.y);
+        D.sqpart = (double *)(b + L.sqpart);
+        D.sqv = (double *)(b + L.sqv);
+        Rqt.resize(sp.hs);
+        for (int bb = 0; bb < sp.hs; ++bb) Rqt[bb] = sp.sq_rfac[bb] * sp.sq_inv_shell_volume[bb];
+    }
     std::vector<int> pidx((size_t)sp.ne * sp.ne, -1);
     for (int q = 0; q < sp.npairs; ++q) {
         pidx[(size_t)sp.pair_i[q] * sp.ne + sp.pair_j[q]] = q;
@@ -1116,6 +1560,11 @@ static int add_engine(EngineSet *s, const frmc_engine_spec &sp, int *out_id)
     up(D.pidx, pidx.data(), 4 * pidx.size());
     up(D.R, Rt.data(), 8 * Rt.size());
     up(D.A, At.data(), 8 * At.size());
+    if (tab) {
+        up(D.Rq, Rqt.data(), 8 * Rqt.size());
+        up(D.rfacq, sp.sq_rfac, 8 * (size_t)sp.hs);
+        up(D.sqexp, sp.sq_experimental, 8 * (size_t)sp.nq);
+    }
     if (!rc) {
         cudaError_t ce = cudaMemsetAsync(D.moves, 0, sizeof(EMove) * sp.move_cap, s->stream);
         if (ce == cudaSuccess)
@@ -1158,7 +1607,9 @@ static void free_set(EngineSet *s)
     drop_graphs(s);
     for (auto &sl : s->slots)
         if (sl.blob) cudaFree(sl.blob);
-    void *ptrs[] = {s->ddesc, s->items, s->dlive, s->dstage_m, s->dstage_r, s->sched};
+    for (auto &t : s->tables)
+        if (t.blob) cudaFree(t.blob);
+    void *ptrs[] = {s->ddesc, s->items, s->dlive, s->dstage_m, s->dstage_r, s->sched, s->sq_items};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (s->hstage_m) cudaFreeHost(s->hstage_m);
@@ -1195,9 +1646,9 @@ int frmc_engines_new(void **handle)
     EngineSet *s = new EngineSet();
     cudaError_t ce = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
     if (ce == cudaSuccess)
-        ce = cudaMalloc(&s->sched, sizeof(Sched));
+        ce = cudaMalloc(&s->sched, 2 * sizeof(Sched));
     if (ce == cudaSuccess)
-        ce = cudaMemset(s->sched, 0, sizeof(Sched));
+        ce = cudaMemset(s->sched, 0, 2 * sizeof(Sched));
     if (ce != cudaSuccess) {
         free_set(s);
         return cuda_fail(ce, "engine set");
@@ -1367,7 +1818,10 @@ int frmc_engines_step(void *handle, int32_t engine, int32_t steps, int use_graph
     if (count == 0 || steps == 0)
         return FRMC_OK;
     auto one = [&](cudaStream_t sx) {
-        return engine < 0 ? launch_batched(s, sx) : launch_items(s, s->items + s->item_first[engine], count, 0, sx);
+        if (engine < 0)
+            return launch_batched(s, sx);
+        FRMC_TRY(launch_items(s, s->items + s->item_first[engine], count, 0, sx));
+        return launch_sq(s, s->sq_first[engine], s->sq_count[engine], sx);
     };
     if (!use_graph) {
         for (int k = 0; k < steps; ++k) FRMC_TRY(one(st));
@@ -1536,6 +1990,65 @@ int frmc_engines_coords(void *handle, int32_t e, float *box_coords, float *real_
     return FRMC_OK;
 }
 
+int frmc_engines_sq_table(void *handle, int32_t hs, int32_t nq, const double *M, const double *weights,
+                          int32_t *table)
+{
+    EngineSet *s = as_set(handle);
+    if (!s || !M || !table || hs < 1 || hs > kSqMaxBins || nq < 1)
+        return set_error(FRMC_E_ARG, "engines_sq_table: need 1 <= hs <= %d, nq >= 1 and a table", kSqMaxBins);
+    SqTable t;
+    t.hs = hs;
+    t.nq = nq;
+    const size_t nm = (size_t)hs * nq, nk = (size_t)hs * hs;
+    t.bytes = 8 * (nm + nk + (weights ? (size_t)nq : 0));
+    FRMC_CUDA(cudaMalloc(&t.blob, t.bytes));
+    t.M = (double *)t.blob;
+    t.K = t.M + nm;
+    t.w = weights ? t.K + nk : nullptr;
+    cudaError_t ce = cudaMemcpyAsync(t.M, M, 8 * nm, cudaMemcpyHostToDevice, s->stream);
+    if (ce == cudaSuccess && weights)
+        ce = cudaMemcpyAsync(t.w, weights, 8 * (size_t)nq, cudaMemcpyHostToDevice, s->stream);
+    if (ce == cudaSuccess) {
+        dim3 grid((hs + 63) / 64, (hs + 63) / 64);
+        k_sq_gram<<<grid, 256, 0, s->stream>>>(t.M, t.w, hs, nq, t.K);
+        ce = cudaGetLastError();
+    }
+    if (ce == cudaSuccess)
+        ce = cudaStreamSynchronize(s->stream);
+    if (ce != cudaSuccess) {
+        cudaFree(t.blob);
+        return cuda_fail(ce, "S(Q) table");
+    }
+    s->tables.push_back(t);
+    *table = (int32_t)s->tables.size() - 1;
+    return FRMC_OK;
+}
+
+int frmc_engines_sq(void *handle, int32_t e, double *sq)
+{
+    EngineSet *s = as_set(handle);
+    if (!s || !valid_id(s, e) || !sq || !s->slots[e].d.sq)
+        return set_error(FRMC_E_ARG, "engines_sq: engine %d has no S(Q) term", e);
+    FRMC_TRY(refresh(s));
+    const EDesc &D = s->slots[e].d;
+    FRMC_TRY(launch_sq_eval(s, e, 0, s->stream));
+    FRMC_CUDA(cudaMemcpyAsync(sq, D.sqv, 8 * (size_t)D.nq, cudaMemcpyDeviceToHost, s->stream));
+    FRMC_CUDA(cudaStreamSynchronize(s->stream));
+    return FRMC_OK;
+}
+
+int frmc_engines_terms(void *handle, int32_t e, double *sd, double *sd_sq)
+{
+    EngineSet *s = as_set(handle);
+    if (!s || !valid_id(s, e))
+        return set_error(FRMC_E_ARG, "engines_terms: invalid engine");
+    EState S;
+    FRMC_CUDA(cudaMemcpy(&S, s->slots[e].d.st, sizeof(EState), cudaMemcpyDeviceToHost));
+    if (sd) *sd = S.sd;
+    if (sd_sq) *sd_sq = S.sd_sq;
+    return FRMC_OK;
+}
+
 int frmc_engines_info(void *handle, int32_t *E, int64_t *total_atoms, int64_t *device_bytes)
 {
     EngineSet *s = as_set(handle);
@@ -1546,6 +2059,7 @@ int frmc_engines_info(void *handle, int32_t *E, int64_t *total_atoms, int64_t *d
         atoms += s->slots[id].d.n;
         bytes += (long long)s->slots[id].bytes;
     }
+    for (const auto &t : s->tables) bytes += (long long)t.bytes;
     if (E) *E = (int32_t)s->live.size();
     if (total_atoms) *total_atoms = atoms;
     if (device_bytes) *device_bytes = bytes;

@@ -1,8 +1,9 @@
 """Device-resident RMC engines (the batched path) over ``frmc_engines_*``.
 
-An engine is one fullrmc Metropolis chain with a single
-PairDistributionConstraint whose whole state -- coordinates, oriented
-histogram counts, experimental curve, chi2 -- lives in HBM.  A batched step
+An engine is one fullrmc Metropolis chain with a PairDistributionConstraint
+and optionally a StructureFactorConstraint on the same histograms, whose
+whole state -- coordinates, oriented histogram counts, experimental curves,
+chi2 -- lives in HBM.  A batched step
 advances every engine of a set by one move in one kernel launch (captured in
 a CUDA graph for runs of steps); ``step(engine=e)`` advances one engine alone
 (the plain one-engine-at-a-time GPU path).  Moves are generated on the host
@@ -12,8 +13,10 @@ chi2 values and counts alone or in any batch.
 
 Host-side set-up follows fullrmc's constraint definitions:
 ``PairDistributionConstraints.py:726-774`` (limits, edges, shell volumes),
-``:847-895`` (G(r) from the histograms) and ``Core/Constraint.py`` (chi2 =
-standard error / varianceSquared); these constants are FP64.
+``:847-895`` (G(r) from the histograms), ``StructureFactorConstraints.py``
+``:302-312`` and ``:780-822`` (S(Q) from G(r)) and ``Engine.py:3000-3029`` /
+``Core/Constraint.py`` (chi2 = sum of standard error / varianceSquared); these
+constants are FP64.
 """
 from __future__ import annotations
 
@@ -34,7 +37,9 @@ class _Spec(ctypes.Structure):
                 ("bin", ctypes.c_float), ("npairs", ctypes.c_int32), ("pair_i", I32P), ("pair_j", I32P),
                 ("pair_coef", F64P), ("rfac", F64P), ("inv_shell_volume", F64P), ("experimental", F64P),
                 ("data_weights", F64P), ("variance_squared", ctypes.c_double), ("tolerance", ctypes.c_double),
-                ("move_cap", ctypes.c_int32)]
+                ("move_cap", ctypes.c_int32), ("sq_table", ctypes.c_int32), ("nq", ctypes.c_int32),
+                ("sq_rfac", F64P), ("sq_inv_shell_volume", F64P), ("sq_experimental", F64P),
+                ("sq_variance_squared", ctypes.c_double)]
 
 
 _vp = ctypes.c_void_p
@@ -59,6 +64,9 @@ register("frmc_engines_results", [_vp, _i32, _i64, _i32, F64P, I32P, I32P])
 register("frmc_engines_counts", [_vp, _i32, I32P])
 register("frmc_engines_coords", [_vp, _i32, F32P, F32P])
 register("frmc_engines_info", [_vp, ctypes.POINTER(_i32), ctypes.POINTER(_i64), ctypes.POINTER(_i64)])
+register("frmc_engines_sq_table", [_vp, _i32, _i32, F64P, F64P, ctypes.POINTER(_i32)])
+register("frmc_engines_sq", [_vp, _i32, F64P])
+register("frmc_engines_terms", [_vp, _i32, F64P, F64P])
 
 
 def normalized_weighting(counts, scattering):
@@ -136,6 +144,87 @@ class PDFModel:
         return float(np.sum(w * d * d) / self.variance_squared)
 
 
+_M_CACHE = {}
+
+
+def sq_matrix(centers, q):
+    """M[r, Q] = dr sin(Q r) / Q in FP64 of the float32 shell centers and Q
+    values, dr = r[1] - r[0] (StructureFactorConstraints.py:302-312).  Cached
+    per grid, since every fit on the same grids shares it."""
+    centers = np.asarray(centers, F32)
+    q = np.asarray(q, F32)
+    key = (centers.tobytes(), q.tobytes())
+    M = _M_CACHE.get(key)
+    if M is None:
+        r = centers.astype(np.float64)
+        q64 = q.astype(np.float64)
+        M = (r[1] - r[0]) * np.sin(np.outer(r, q64)) / q64
+        M.setflags(write=False)
+        if len(_M_CACHE) >= 4:
+            _M_CACHE.pop(next(iter(_M_CACHE)))
+        _M_CACHE[key] = M
+    return M
+
+
+@dataclass
+class SQModel:
+    """FP64 constants of one StructureFactorConstraint that shares the
+    engine's histograms: its rmin, dr and rmax are the G(r) constraint's
+    minDistance, bin and maxDistance, so the pair counts are the same.  Its own
+    shells follow StructureFactorConstraints.py:330-360 (edges = arange(rmin,
+    rmax + dr, dr) in float32, centers = midpoints, volumes 4/3 pi (e1^3 -
+    e0^3)); S(Q) = sum_r G_S(r) M[r, Q] + 1 (:772-822, scale factor 1, no
+    window) with G_S = 4 pi r rho0 (g(r) - 1) on those shells and the same
+    element-pair weights."""
+    pdf: PDFModel
+    q: np.ndarray                # experimental Q values (float32)
+    S_exp: np.ndarray            # experimental S(Q)
+    data_weights: np.ndarray | None = None
+    variance_squared: float = 1.0
+
+    def __post_init__(self):
+        m = self.pdf
+        self.q = np.asarray(self.q, F32)
+        self.nq = len(self.q)
+        self.hs = m.hs
+        e = (float(m.minDistance) + float(m.bin) * np.arange(m.hs + 1)).astype(F32)
+        self.edges = e
+        self.centers = ((e[:-1] + e[1:]) / F32(2.0)).astype(F32)
+        e64 = e.astype(np.float64)
+        self.shell_volumes = 4.0 / 3.0 * np.pi * (e64[1:] ** 3 - e64[:-1] ** 3)
+        self.rfac = 4.0 * np.pi * self.centers.astype(np.float64) * m.rho0
+        self.M = sq_matrix(self.centers, self.q)
+
+    def key(self):
+        w = None if self.data_weights is None else np.asarray(self.data_weights, np.float64).tobytes()
+        return (self.centers.tobytes(), self.q.tobytes(), w)
+
+    def table_bytes(self):
+        return 8 * (self.hs * self.nq + self.hs * self.hs + (self.nq if self.data_weights is not None else 0))
+
+    def G_fp64(self, intra, inter):
+        m = self.pdf
+        intra = np.asarray(intra, np.float64)
+        inter = np.asarray(inter, np.float64)
+        g = np.zeros(self.hs)
+        for i, j, c in zip(m.pair_i, m.pair_j, m.pair_coef):
+            if i == j:
+                nij = intra[i, i] + inter[i, i]
+            else:
+                nij = intra[i, j] + intra[j, i] + inter[i, j] + inter[j, i]
+            g += c * nij
+        g /= self.shell_volumes
+        return self.rfac * (g - 1.0)
+
+    def S_fp64(self, intra, inter):
+        return self.G_fp64(intra, inter) @ self.M + 1.0
+
+    def sd_fp64(self, intra, inter):
+        d = np.asarray(self.S_exp, np.float64) - self.S_fp64(intra, inter)
+        w = 1.0 if self.data_weights is None else np.asarray(self.data_weights, np.float64)
+        return float(np.sum(w * d * d))
+
+
 @dataclass
 class EngineSystem:
     box_coords: np.ndarray
@@ -148,6 +237,14 @@ class EngineSystem:
     model: PDFModel
     tolerance: float = 0.0
     keep: list = field(default_factory=list, repr=False)
+    sq: SQModel | None = None
+
+    def chi2_fp64(self, intra, inter):
+        """chi2 of the engine's constraints from oriented counts (FP64)."""
+        c = self.model.chi2_fp64(intra, inter)
+        if self.sq is not None:
+            c += self.sq.sd_fp64(intra, inter) / self.sq.variance_squared
+        return c
 
 
 def translation_moves(rng: np.random.Generator, n_atoms: int, count: int, amplitude: float):
@@ -166,8 +263,9 @@ def translation_moves(rng: np.random.Generator, n_atoms: int, count: int, amplit
     return atoms, np.ascontiguousarray(v), u
 
 
-def make_spec(system, move_cap):
-    """ctypes spec of one system; returns (spec, arrays that must stay alive)."""
+def make_spec(system, move_cap, sq_table=-1):
+    """ctypes spec of one system; returns (spec, arrays that must stay alive).
+    `sq_table` is the set's table id for the system's S(Q) term."""
     s = system
     m = s.model
     arrs = dict(box=np.ascontiguousarray(s.box_coords, F32), real=np.ascontiguousarray(s.real_coords, F32),
@@ -201,12 +299,24 @@ def make_spec(system, move_cap):
     sp.variance_squared = float(m.variance_squared)
     sp.tolerance = float(s.tolerance)
     sp.move_cap = int(move_cap)
+    sp.sq_table = -1
+    if s.sq is not None:
+        q = s.sq
+        arrs.update(sq_rfac=np.ascontiguousarray(q.rfac), sq_iv=np.ascontiguousarray(1.0 / q.shell_volumes),
+                    sq_exp=np.ascontiguousarray(np.asarray(q.S_exp, np.float64)))
+        sp.sq_table = int(sq_table)
+        sp.nq = q.nq
+        sp.sq_rfac = arrs["sq_rfac"].ctypes.data_as(F64P)
+        sp.sq_inv_shell_volume = arrs["sq_iv"].ctypes.data_as(F64P)
+        sp.sq_experimental = arrs["sq_exp"].ctypes.data_as(F64P)
+        sp.sq_variance_squared = float(q.variance_squared)
     return sp, arrs
 
 
 def footprint(system, move_cap):
-    """Device bytes an engine of this system occupies."""
-    sp, _keep = make_spec(system, move_cap)
+    """Device bytes an engine of this system occupies (without the S(Q) table
+    it shares with other engines on the same grids)."""
+    sp, _keep = make_spec(system, move_cap, sq_table=0)
     b = ctypes.c_int64()
     check(load().frmc_engine_footprint(ctypes.byref(sp), ctypes.byref(b)))
     return b.value
@@ -219,9 +329,16 @@ class EngineSet:
         load()
         self.move_cap = int(move_cap)
         self.systems = {}
+        self.tables = {}
         h = ctypes.c_void_p()
         systems = list(systems)
-        if systems:
+        if any(s.sq is not None for s in systems):
+            # S(Q) tables must exist before their engines: add one by one
+            check(load().frmc_engines_new(ctypes.byref(h)))
+            self.handle = h
+            for s in systems:
+                self.add(s)
+        elif systems:
             specs = (_Spec * len(systems))()
             keep = []
             for k, s in enumerate(systems):
@@ -236,13 +353,27 @@ class EngineSet:
         if tune is not None:
             self.set_tune(*tune)
 
+    def sq_table(self, sq):
+        """Id of the device table of an SQModel's grids (created once per set)."""
+        key = sq.key()
+        t = self.tables.get(key)
+        if t is None:
+            w = None if sq.data_weights is None else np.ascontiguousarray(sq.data_weights, np.float64)
+            M = np.ascontiguousarray(sq.M, np.float64)
+            i = ctypes.c_int32()
+            check(load().frmc_engines_sq_table(self.handle, sq.hs, sq.nq, M.ctypes.data_as(F64P),
+                                               None if w is None else w.ctypes.data_as(F64P), ctypes.byref(i)))
+            t = self.tables[key] = i.value
+        return t
+
     @property
     def E(self):
         return len(self.systems)
 
     def add(self, system, move_cap=None):
         """Add (and initialise) one engine; returns its id."""
-        sp, _keep = make_spec(system, move_cap or self.move_cap)
+        tid = self.sq_table(system.sq) if system.sq is not None else -1
+        sp, _keep = make_spec(system, move_cap or self.move_cap, tid)
         i = ctypes.c_int32()
         check(load().frmc_engines_add(self.handle, ctypes.byref(sp), ctypes.byref(i)))
         self.systems[i.value] = system
@@ -307,6 +438,18 @@ class EngineSet:
         c2, st, acc = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
         check(load().frmc_engines_state(self.handle, int(e), ctypes.byref(c2), ctypes.byref(st), ctypes.byref(acc)))
         return c2.value, st.value, acc.value
+
+    def terms(self, e):
+        """(sd of the G(r) term, sd of the S(Q) term) of engine e."""
+        a, b = ctypes.c_double(), ctypes.c_double()
+        check(load().frmc_engines_terms(self.handle, int(e), ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def sq(self, e):
+        """S(Q) of engine e's current counts (FP64)."""
+        out = np.empty(self.systems[e].sq.nq, np.float64)
+        check(load().frmc_engines_sq(self.handle, int(e), out.ctypes.data_as(F64P)))
+        return out
 
     def results(self, e, first_step, count):
         c = np.empty(count, np.float64)

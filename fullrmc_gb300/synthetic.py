@@ -10,12 +10,15 @@ workload definitions:
   a = b = c = 103 A, alpha = beta = 90, gamma = 120 degrees, r 0-20 A.
 * ``mixed_engines``: 256 engines, atom counts log-uniform in [1,000, 20,000],
   1-4 species, cubic or triclinic boxes at 0.08-0.10 atoms/A^3, r 0-12 A.
+* ``serving_fit``: one fit of the serving stream: atoms log-uniform in
+  [2,000, 200,000], 1-3 species, G(r) on r 0-12 A and S(Q) on Q 0.5-25 A^-1
+  (dQ 0.01, 2451 points), 2,000-50,000 steps.
 """
 from __future__ import annotations
 
 import numpy as np
 
-from .engine import EngineSystem, PDFModel, normalized_weighting
+from .engine import EngineSystem, PDFModel, SQModel, normalized_weighting
 
 F32 = np.float32
 
@@ -66,8 +69,20 @@ def synthetic_G(rng, r, rho):
     return (G + rng.normal(0.0, 0.01, size=r.shape)).astype(F32)
 
 
-def make_system(rng, n, fractions, basis, rmax, molsize=1, isPBC=True, target=None):
-    """One engine system: seeded coordinates, elements, molecules and an FP64 PDF model."""
+def q_grid(qmin=0.5, qmax=25.0, dq=0.01):
+    return (qmin + dq * np.arange(int(round((qmax - qmin) / dq)) + 1)).astype(F32)
+
+
+def synthetic_S(rng, sq, G_target):
+    """Experimental S(Q) of a target G(r): its transform on the S(Q) shells
+    plus N(0, 0.01) noise, float32 like read data."""
+    S = np.asarray(G_target, np.float64) @ sq.M + 1.0
+    return (S + rng.normal(0.0, 0.01, size=S.shape)).astype(F32)
+
+
+def make_system(rng, n, fractions, basis, rmax, molsize=1, isPBC=True, target=None, q=None):
+    """One engine system: seeded coordinates, elements, molecules and an FP64
+    PDF model; with `q` (Q values) also an S(Q) term on the same histograms."""
     basis = np.asarray(basis, F32)
     rbasis = np.linalg.inv(basis.astype(np.float64)).astype(F32)
     frac = rng.random((n, 3))
@@ -83,8 +98,12 @@ def make_system(rng, n, fractions, basis, rmax, molsize=1, isPBC=True, target=No
     weights = normalized_weighting(counts, np.ones(len(fractions)) + 0.25 * np.arange(len(fractions)))
     G = synthetic_G(rng, r, n / volume) if target is None else target
     model = PDFModel(r=r, G_exp=G, elements_count=counts, weights=weights, volume=volume)
+    sq = None
+    if q is not None:
+        sq = SQModel(pdf=model, q=q, S_exp=np.zeros(len(q)))
+        sq.S_exp = synthetic_S(rng, sq, G)
     return EngineSystem(box_coords=box, real_coords=real, el=el, mol=mol, basis=basis, rbasis=rbasis,
-                        isPBC=isPBC, model=model)
+                        isPBC=isPBC, model=model, sq=sq)
 
 
 def alloy_5000(seed=0, n=5000):
@@ -120,3 +139,25 @@ def mixed_engines(seed=0, count=256, nmin=1000, nmax=20000, rmax=12.0):
             B = triclinic(a, a, a, al, be, ga)
         out.append(make_system(np.random.default_rng([seed, k]), n, fr, B, rmax))
     return out
+
+
+def random_box(rng, n, rho):
+    """Cubic (half the time) or triclinic box holding n atoms at density rho."""
+    if rng.random() < 0.5:
+        L = (n / rho) ** (1.0 / 3.0)
+        return np.diag([L, L, L])
+    al, be, ga = rng.uniform(80, 100), rng.uniform(80, 100), rng.uniform(95, 120)
+    unit = triclinic(1.0, 1.0, 1.0, al, be, ga).astype(np.float64)
+    a = (n / rho / abs(np.linalg.det(unit))) ** (1.0 / 3.0)
+    return triclinic(a, a, a, al, be, ga)
+
+
+def serving_fit(seed, nmin=2000, nmax=200000, smin=2000, smax=50000, rmax=12.0, sq=True):
+    """One request of the serving stream: (system, steps)."""
+    rng = np.random.default_rng([seed, 7])
+    n = int(round(np.exp(rng.uniform(np.log(nmin), np.log(nmax)))))
+    ns = int(rng.integers(1, 4))
+    fr = rng.dirichlet(np.ones(ns) * 3.0)
+    B = random_box(rng, n, rng.uniform(0.08, 0.10))
+    steps = int(rng.integers(smin, smax + 1))
+    return make_system(rng, n, fr, B, rmax, q=q_grid() if sq else None), steps

@@ -1,14 +1,16 @@
 /*
  * frmc_gpu_engine.h -- device-resident RMC engines (batched and served).
  *
- * Each engine is one fullrmc Metropolis chain with a single
- * PairDistributionConstraint, stepped entirely on the GPU:
+ * Each engine is one fullrmc Metropolis chain with a PairDistributionConstraint
+ * and optionally a StructureFactorConstraint on the same histograms, stepped
+ * entirely on the GPU:
  *   - the step is fullrmc's Engine.run step (Engine.py:3278-3344) with
  *     single-atom translation moves (Generators/Translations.py:171-190),
  *   - the histogram update is the M term of compute_before_move /
  *     compute_after_move (Constraints/PairDistributionConstraints.py:1044-1129),
  *     kept as oriented int32 counts equal to the constraint's running data,
- *   - G(r) (PairDistributionConstraints.py:847-895) and chi2 are FP64.
+ *   - G(r) (PairDistributionConstraints.py:847-895), S(Q)
+ *     (StructureFactorConstraints.py:780-822) and chi2 are FP64.
  * Moves (atom, displacement vector, uniform number for the tolerance test)
  * are generated by the caller and pushed into a per-engine ring, so the
  * chains stay strictly sequential and reproducible: an engine gives the same
@@ -53,9 +55,36 @@ typedef struct {
     double variance_squared;
     double tolerance;          /* Engine tolerance (reject iff chi2 rises and u > tolerance) */
     int32_t move_cap;          /* ring size for moves and step results          */
+    /* Optional StructureFactorConstraint on the same histograms (its rmin, dr
+     * and rmax equal to minDistance, bin and maxDistance above):
+     * S(Q) = 1 + sum_r G_S(r) M[r][Q], G_S = 4 pi r rho0 (g(r) - 1) with the
+     * S(Q) shells' own r and volumes, chi2 term sum_Q w (S_exp - S)^2 /
+     * sq_variance_squared (StructureFactorConstraints.py:742-822).  sq_table
+     * is an id from frmc_engines_sq_table (-1: no S(Q) term); nq its Q points. */
+    int32_t sq_table;
+    int32_t nq;
+    const double *sq_rfac;             /* (hs,) 4 pi r rho0 on the S(Q) shells  */
+    const double *sq_inv_shell_volume; /* (hs,) 1 / S(Q) shell volume           */
+    const double *sq_experimental;     /* (nq,) experimental S(Q)               */
+    double sq_variance_squared;
 } frmc_engine_spec;
 
-/* Device bytes one engine of this spec occupies (its state, tables and rings). */
+/* A G(r) -> S(Q) table shared by the set's engines that use the same r shells
+ * (hs) and Q points (nq): M (hs, nq) row-major, M[r][Q] = dr sin(Q r) / Q
+ * (StructureFactorConstraints.py:302-312), and optional per-Q data weights w
+ * (NULL = 1).  The set keeps M, w and K = M diag(w) M^T (hs x hs, computed on
+ * the device) until it is destroyed; *table receives the id to put in a
+ * spec's sq_table.  Device bytes: 8 (hs nq + hs hs + nq).  hs <= 4096. */
+int frmc_engines_sq_table(void *handle, int32_t hs, int32_t nq, const double *M, const double *weights,
+                          int32_t *table);
+/* Current S(Q) of engine e recomputed from its counts (FP64, nq values). */
+int frmc_engines_sq(void *handle, int32_t e, double *sq);
+/* The two chi2 terms of engine e: sd = sum w (G_exp - G)^2 of the G(r) term and
+ * sd_sq of the S(Q) term (0 without one); chi2 = sd / variance_squared +
+ * sd_sq / sq_variance_squared. */
+int frmc_engines_terms(void *handle, int32_t e, double *sd, double *sd_sq);
+/* Device bytes one engine of this spec occupies (its state, tables and rings;
+ * a shared S(Q) table is not included). */
 int frmc_engine_footprint(const frmc_engine_spec *spec, int64_t *bytes);
 /* An empty engine set on the current device. */
 int frmc_engines_new(void **handle);

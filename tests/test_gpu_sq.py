@@ -1,0 +1,173 @@
+"""Engines with a StructureFactorConstraint term on the device.
+
+S(Q), the S(Q) standard error and chi2 are checked against the oracle's FP64
+restatement of StructureFactorConstraints.py (total G(r) on the S(Q) shells,
+the dr sin(Qr)/Q matrix, sum w (S_exp - S)^2) from the same integer counts;
+every step of a device chain is replayed on the host with the oracle's
+histograms; and a chain gives bit-identical results solo, batched, fused,
+tile-split and next to engines without an S(Q) term.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10  # relative, FP64 S(Q) / chi2 against the oracle
+
+
+def _systems(count, seed, nmin=600, nmax=2500, dq=0.02):
+    from fullrmc_gb300 import synthetic
+    rng = np.random.default_rng(seed)
+    q = synthetic.q_grid(0.5, 25.0, dq)
+    out = []
+    for k in range(count):
+        n = int(rng.integers(nmin, nmax))
+        ns = int(rng.integers(1, 4))
+        fr = rng.dirichlet(np.ones(ns) * 3.0)
+        B = synthetic.random_box(rng, n, rng.uniform(0.08, 0.10))
+        out.append(synthetic.make_system(np.random.default_rng([seed, k]), n, fr, B, 10.0, q=q))
+    return out
+
+
+def _moves(systems, steps, seed=11, amp=0.3):
+    from fullrmc_gb300.engine import translation_moves
+    return [translation_moves(np.random.default_rng([seed, k]), s.box_coords.shape[0], steps, amp)
+            for k, s in enumerate(systems)]
+
+
+def _oracle_S(oracle_mod, s, intra, inter):
+    """S(Q) and its standard error by the oracle's functions."""
+    sq, m = s.sq, s.model
+    e = sq.edges
+    centers = ((e[:-1] + e[1:]) / np.float32(2.0)).astype(np.float32)
+    e64 = e.astype(np.float64)
+    vols = 4.0 / 3.0 * np.pi * (e64[1:] ** 3 - e64[:-1] ** 3)
+    Gr = oracle_mod.total_Gr_fp64(intra, inter, m.elements_count, m.weights, m.volume, vols, centers, m.rho0)
+    S = oracle_mod.sq_from_Gr_fp64(Gr, oracle_mod.gr2sq_matrix_fp64(centers, sq.q))
+    return S, oracle_mod.standard_error_fp64(sq.S_exp, S, sq.data_weights)
+
+
+def _oracle_chi2(oracle_mod, s, intra, inter):
+    _S, sd_sq = _oracle_S(oracle_mod, s, intra, inter)
+    return s.model.chi2_fp64(intra, inter) + sd_sq / s.sq.variance_squared
+
+
+def _run(systems, moves, steps, mode="batched", fused=1, graph=True, chunk=None, tune=None):
+    from fullrmc_gb300.engine import EngineSet
+    es = EngineSet(systems, move_cap=max(64, steps), tune=tune)
+    es.set_mode(fused)
+    es.init()
+    for e, (a, v, u) in enumerate(moves):
+        es.push_moves(e, a[:steps], v[:steps], u[:steps], 0)
+    chunk = chunk or steps
+    engines = [-1] if mode == "batched" else list(range(len(systems)))
+    for eng in engines:
+        for s0 in range(0, steps, chunk):
+            es.step(min(chunk, steps - s0), engine=eng, graph=graph)
+    out = []
+    for e in range(len(systems)):
+        c2, a, at = es.results(e, 0, steps)
+        out.append(dict(chi2=c2, acc=a, state=es.state(e), terms=es.terms(e), counts=es.counts(e),
+                        coords=es.coords(e)))
+    es.close()
+    return out
+
+
+def _same(r1, r2):
+    for a, b in zip(r1, r2):
+        assert np.array_equal(a["acc"], b["acc"])
+        assert np.array_equal(a["chi2"].view(np.int64), b["chi2"].view(np.int64))
+        assert a["state"] == b["state"] and a["terms"] == b["terms"]
+        assert np.array_equal(a["counts"][0], b["counts"][0]) and np.array_equal(a["counts"][1], b["counts"][1])
+        assert np.array_equal(a["coords"][0], b["coords"][0]) and np.array_equal(a["coords"][1], b["coords"][1])
+
+
+def test_initial_sq_and_chi2_match_oracle(oracle_mod):
+    from fullrmc_gb300.engine import EngineSet
+    systems = _systems(3, seed=1)
+    es = EngineSet(systems, move_cap=8)
+    es.init()
+    for e, s in enumerate(systems):
+        intra, inter = es.counts(e)
+        S_ref, sd_ref = _oracle_S(oracle_mod, s, intra, inter)
+        S = es.sq(e)
+        assert np.max(np.abs(S - S_ref)) <= TOL * np.max(np.abs(S_ref))
+        sd, sd_sq = es.terms(e)
+        assert abs(sd_sq - sd_ref) <= TOL * sd_ref
+        chi2 = es.state(e)[0]
+        ref = _oracle_chi2(oracle_mod, s, intra, inter)
+        assert abs(chi2 - ref) <= TOL * ref
+    assert len(es.tables) == 1  # one table for the shared grids
+    es.close()
+
+
+def test_sq_chain_replays_on_oracle(oracle_mod):
+    """Every step's chi2 (G(r) + S(Q) terms) agrees with the oracle's FP64
+    value to 1e-10 relative, decisions follow the rule, and the final counts,
+    coordinates and S(Q) agree."""
+    from fullrmc_gb300.hostloop import HostPDFChain
+    systems = _systems(2, seed=5, nmin=700, nmax=1200)
+    steps = 120
+    mv = _moves(systems, steps, seed=4, amp=0.4)
+    res = _run(systems, mv, steps)
+    for e, s in enumerate(systems):
+        chain = HostPDFChain(s, oracle_mod, oracle_mod)
+        chain.compute_data()
+        chi2 = _oracle_chi2(oracle_mod, s, *chain.data)
+        a, v, u = mv[e]
+        for k in range(steps):
+            acc = bool(res[e]["acc"][k])
+            chain.step(a[k], v[k][None, :], u[k], force=acc)
+            c_new = _oracle_chi2(oracle_mod, s, chain.last[0], chain.last[1])
+            assert abs(c_new - res[e]["chi2"][k]) <= TOL * abs(c_new), k
+            assert acc == (not (res[e]["chi2"][k] > chi2 and u[k] > 0.0)), k
+            if acc:
+                chi2 = res[e]["chi2"][k]
+        got = res[e]["counts"]
+        assert np.array_equal(got[0].astype(np.float32), chain.data[0])
+        assert np.array_equal(got[1].astype(np.float32), chain.data[1])
+        assert np.array_equal(res[e]["coords"][0], chain.box)
+        _S, sd_ref = _oracle_S(oracle_mod, s, *chain.data)
+        assert abs(res[e]["terms"][1] - sd_ref) <= TOL * sd_ref
+        assert int(res[e]["acc"].sum()) > 0
+
+
+def test_sq_chains_identical_solo_batched_fused_split():
+    systems = _systems(4, seed=9, nmin=500, nmax=3000)
+    steps = 60
+    mv = _moves(systems, steps, seed=2)
+    base = _run(systems, mv, steps)
+    _same(base, _run(systems, mv, steps, mode="solo", chunk=7))
+    _same(base, _run(systems, mv, steps, fused=0, graph=False))
+    _same(base, _run(systems, mv, steps, tune=(128, 128, 8), chunk=13))
+
+
+def test_sq_and_plain_engines_mixed():
+    """Engines with and without an S(Q) term in one set keep their solo chains."""
+    from fullrmc_gb300 import synthetic
+    sq_sys = _systems(2, seed=21)
+    plain = synthetic.mixed_engines(seed=4, count=2, nmin=600, nmax=2000, rmax=10.0)
+    steps = 50
+    mixed = [sq_sys[0], plain[0], sq_sys[1], plain[1]]
+    mv = _moves(mixed, steps, seed=8)
+    both = _run(mixed, mv, steps)
+    for k in range(4):
+        _same([both[k]], _run([mixed[k]], [mv[k]], steps))
+
+
+def test_table_shape_mismatch_is_refused():
+    from fullrmc_gb300 import synthetic
+    from fullrmc_gb300._native import NativeError
+    from fullrmc_gb300.engine import EngineSet, SQModel
+    a = _systems(1, seed=3)[0]
+    es = EngineSet([], move_cap=8)
+    other = SQModel(pdf=a.model, q=synthetic.q_grid(0.5, 10.0, 0.05), S_exp=np.zeros(191))
+    tid = es.sq_table(other)
+    from fullrmc_gb300.engine import make_spec
+    from fullrmc_gb300._native import load, check
+    import ctypes
+    sp, _keep = make_spec(a, 8, sq_table=tid)
+    i = ctypes.c_int32()
+    with pytest.raises((ValueError, NativeError)):
+        check(load().frmc_engines_add(es.handle, ctypes.byref(sp), ctypes.byref(i)))
+    es.close()
