@@ -19,7 +19,13 @@ Reported beside the headline:
 * ``roofline``: the batched step kernel against the issue roofline
   (46 algorithmic operations per pair distance, SMs x clock x 128 / 46);
 * ``cpu_baseline``: fullrmc's own Cython path (compiled from its sources)
-  running the same kind of steps on the host cores, on a bounded sample.
+  running the same kind of steps on the host cores, on a bounded sample;
+* ``serving``: the serving loop on a Poisson stream of fit requests (20 per
+  second; 2,000-200,000 atoms log-uniform, 1-3 species, G(r) on r 0-12 A
+  plus S(Q) on Q 0.5-25 A^-1 with dQ 0.01, 2,000-50,000 steps each), admitted
+  by device footprint and batched across the live fits: total fit-steps/s,
+  p50/p99 per-step latency, fit latency, and the same fits stepped one at a
+  time (plain) for comparison.
 
 Timing: CUDA events on the stepping stream, W untimed warm-up steps, then K
 timed steps each bracketed by its own events, with a write of a buffer larger
@@ -364,6 +370,10 @@ def run_ours(args):
     d2h = E * 16  # (chi2, accepted, atom) per engine
 
     allp = bench_allpairs(torch, native, dev)
+    serving = None
+    if args.serve_seconds > 0 and rank == 0:
+        from fullrmc_gb300 import serve
+        serving = serve.benchmark_stream(args.serve_seconds, args.serve_limit, seed=seed)
     sms = info["sms"]
     fmax = float(peaks.get("sm_max_mhz", 2070.0)) * 1e6
     issue_peak = sms * fmax * 128.0 / OPS_PER_PAIR  # pair distances / s
@@ -414,6 +424,7 @@ def run_ours(args):
                                        % (sms, fmax / 1e6, peaks_kind, OPS_PER_PAIR)},
             "allpairs": dict(allp, roofline_frac=allp["pair_distances_per_s"] / issue_peak,
                              issue_peak_pairs_per_s=issue_peak),
+            "serving": serving,
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": K,
@@ -434,6 +445,8 @@ def main():
     ap.add_argument("--plain-engines", type=int, default=64)
     ap.add_argument("--plain-steps", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--serve-seconds", type=float, default=10.0, help="arrival window of the serving stream (0: skip)")
+    ap.add_argument("--serve-limit", type=float, default=60.0, help="wall-clock limit of the serving run")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

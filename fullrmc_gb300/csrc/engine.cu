@@ -93,11 +93,15 @@ struct EDesc {
     double *Bq;   // [hs] 2 w R (exp - G) of the current configuration
     double *Sb;   // [hs] S(b) = sum_p pair_coef_p dP_p(b) proposed this step (large hs or S(Q))
     // S(Q) term (sq = 1): with x(b) = Rq(b) S(b) the change of the S(Q)
-    // shells' G, d(sd_sq) = x^T K x - x^T h, h = 2 M W (S_exp - S).
+    // shells' G, d(sd_sq) = x^T y - x^T h, y = K x, K = M W M^T,
+    // h = 2 M W (S_exp - S).  y is computed exactly in integers from the
+    // element-pair deltas: y(b) = yscale sum_p pair_coef_p z_p(b),
+    // z_p(b) = sum_c T[c][b] dP_p(c), T[c][b] = round(K[c][b] R0(c) 2^s).
     int sq, nq, sqblk;
     double var2q;
+    double yscale;      // rho0 2^-s
     const double *M;    // [hs][nq] G -> S(Q) table (shared)
-    const double *K;    // [hs][hs] M W M^T (shared, symmetric)
+    const long long *T; // [hs][hs] fixed-point K R0 (shared)
     const double *wq;   // [nq] data weights or null (shared)
     double *Rq;         // [hs] 4 pi r rho0 / shell volume of the S(Q) shells
     double *rfacq;      // [hs] 4 pi r rho0 of the S(Q) shells
@@ -106,6 +110,8 @@ struct EDesc {
     double *y;          // [hs] K x of this step
     double *sqpart;     // [sqblk] this step's partial sums of x (y - h)
     double *sqv;        // [nq] S(Q) written by the evaluation kernel
+    int *evl;           // [npairs][hs] this step's non-zero element-pair deltas, per pair
+    int *evn;           // [kMaxP] their counts (-1: a delta beyond 16 bits, read dP instead)
     EMove *moves;
     EResult *results;
     EState *st;
@@ -377,7 +383,19 @@ __device__ double eval_delta(const EDesc &Dg, int *dP, double *red, double *cb, 
         const double *__restrict__ pc;
     } D = {Dg.hs, Dg.A, Dg.Bq, Dg.Sb, Dg.pc};
     const int np = Dg.npairs;
+    // engines with an S(Q) term leave the element-pair deltas in the global
+    // array for the S(Q) kernel, which clears them
+    // and list them per element pair as (bin << 16) | (delta & 0xffff)
     const bool sq = Dg.sq != 0;
+    int *__restrict__ gdP = Dg.dP;
+    int *__restrict__ evl = Dg.evl;
+    __shared__ int s_evn[kMaxP];
+    __shared__ int s_wide;
+    if (sq) {
+        for (int q = threadIdx.x; q < kMaxP; q += blockDim.x) s_evn[q] = 0;
+        if (threadIdx.x == 0)
+            s_wide = 0;
+    }
     if (!SMEM)
         for (int q = threadIdx.x; q < np; q += blockDim.x) coef[q] = D.pc[q];
     lanes_zero(red);
@@ -407,8 +425,15 @@ __device__ double eval_delta(const EDesc &Dg, int *dP, double *red, double *cb, 
                 for (int q = 0; q < kMaxP; ++q) {
                     const int v = d[q];
                     if (v) {
-                        if (!SMEM)
+                        if (!SMEM && !sq)
                             dP[(long long)q * D.hs + b] = 0;
+                        if (sq) {
+                            if (SMEM)
+                                gdP[q * D.hs + b] = v;
+                            evl[q * D.hs + atomicAdd(&s_evn[q], 1)] = (b << 16) | (v & 0xffff);
+                            if (v > 32767 || v < -32768)
+                                s_wide = 1;
+                        }
                         const double cf = coef[q];
                         S += v == 1 ? cf : (v == -1 ? -cf : cf * (double)v);
                     }
@@ -433,7 +458,10 @@ __device__ double eval_delta(const EDesc &Dg, int *dP, double *red, double *cb, 
         }
         lanes_add_chunk(red, cb, c0, cn);
     }
-    return lanes_total(red);
+    const double total = lanes_total(red);
+    if (sq && (int)threadIdx.x < np)
+        Dg.evn[threadIdx.x] = s_wide ? -1 : s_evn[threadIdx.x];
+    return total;
 }
 
 constexpr int kCommitUnroll = 4;
@@ -800,17 +828,26 @@ __global__ void k_gather_results(const EDesc *desc, const int *ids, EResult *out
 
 // ------------------------------------------------------------------ S(Q) term
 // Engines with a StructureFactorConstraint finish every step here.  The
-// histogram kernels have left S(b) in Sb, the G(r) change in st->dsd and the
-// touched list; with x(b) = Rq(b) S(b), the change of the S(Q) term is
-//   d(sd_sq) = sum_Q w [(e - dS)^2 - e^2] = x^T K x - x^T h,
-// e = S_exp - S, dS = M^T x, K = M W M^T, h = 2 M W e.
-// Items are (engine, block of kSqRows rows of K).  A CTA lists the non-zero
-// x(c) in increasing c, computes y(b) = sum_c K[c][b] x(c) for its rows (K is
-// symmetric, so row c is read contiguously) and its rows' share of x (y - h);
-// the CTA that finishes an engine's last block adds the shares in block
-// order, decides and commits: counts, Bq -= 2 A S, h -= 2 y, coordinates.
-constexpr int kSqRows = 256;      // rows of K per item = threads per CTA
+// histogram kernels have left S(b) in Sb, the element-pair deltas dP_p(b) in
+// the global dP array, the G(r) change in st->dsd and the touched list.  With
+// x(b) = Rq(b) S(b) the change of the S(Q) shells' G(r), the change of the
+// S(Q) term is
+//   d(sd_sq) = sum_Q w [(e - dS)^2 - e^2] = x^T y - x^T h,
+// e = S_exp - S, dS = M^T x, y = K x, K = M W M^T, h = 2 M W e.
+// y is formed from the integer deltas and the fixed-point table T (K scaled
+// by the shells' 4 pi r / volume and 2^s): z_p(b) = sum_c T[c][b] dP_p(c) is
+// an exact int64 sum, so its value does not depend on the order of the
+// terms, and y(b) = rho0 2^-s sum_p pair_coef_p z_p(b).  This keeps the
+// O(changed bins x bins) part on the integer pipes, which run many times
+// faster than FP64 on this GPU.
+// Items are (engine, block of kSqRows rows).  A CTA lists each element
+// pair's non-zero deltas, accumulates z_p for its rows (thread = row, T read
+// along rows), forms y and its rows' share of x (y - h); the CTA that
+// finishes an engine's last block adds the shares in block order, decides and
+// commits: counts, Bq -= 2 A S, h -= 2 y, coordinates, and clears dP.
+constexpr int kSqRows = 256;      // rows per item = threads per CTA
 constexpr int kSqMaxBins = 4096;  // histogram bins of an engine with an S(Q) term
+constexpr int kSqBits = 48;       // largest |T| is below 2^48: 2^15 unit deltas fit in an int64 sum
 
 struct SqParams {
     const EDesc *desc;
@@ -854,6 +891,8 @@ __device__ void sq_finish(const EDesc &D, int *s_flag, double *s_val)
                 D.counts[f] += d;
         }
     }
+    const int nph = D.npairs * D.hs;
+    for (int k = threadIdx.x; k < nph; k += blockDim.x) D.dP[k] = 0;
     if (accept) {
         for (int b = threadIdx.x; b < D.hs; b += blockDim.x) {
             const double sv = D.Sb[b];
@@ -889,19 +928,17 @@ __device__ void sq_finish(const EDesc &D, int *s_flag, double *s_val)
     }
 }
 
+constexpr int kSqUnroll = 16;  // table loads in flight per thread
+
 __global__ void __launch_bounds__(kSqRows) k_sq_step(SqParams p)
 {
-    extern __shared__ double sq_smem[];  // x values [hs], then their bins (int) [hs]
     __shared__ double red[kSqRows];
     __shared__ double s_val[3];
-    __shared__ int s_wsum[kSqRows / 32];
-    __shared__ int s_item, s_last, s_flag, s_base;
-    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    __shared__ int s_item, s_last, s_flag;
     for (;;) {
         if (threadIdx.x == 0) {
             const unsigned long long k = atomicAdd(&p.sched->claimed, 1ull);
             s_item = k < (unsigned long long)p.nitems ? (int)k : -1;
-            s_base = 0;
         }
         __syncthreads();
         const int it = s_item;
@@ -909,57 +946,50 @@ __global__ void __launch_bounds__(kSqRows) k_sq_step(SqParams p)
             break;
         const int2 item = p.items[it];
         const EDesc &D = p.desc[item.x];
-        const int hs = D.hs;
-        double *xv = sq_smem;
-        int *xi = (int *)(sq_smem + hs);
-        for (int c0 = 0; c0 < hs; c0 += kSqRows) {
-            const int c = c0 + threadIdx.x;
-            double x = 0.0;
-            if (c < hs) {
-                const double sv = __ldcg(D.Sb + c);
-                if (sv != 0.0)
-                    x = D.Rq[c] * sv;
-            }
-            const unsigned bal = __ballot_sync(0xffffffffu, x != 0.0);
-            if (lane == 0)
-                s_wsum[warp] = __popc(bal);
-            __syncthreads();
-            int off = s_base;
-            for (unsigned w = 0; w < warp; ++w) off += s_wsum[w];
-            if (x != 0.0) {
-                const int pos = off + __popc(bal & ((1u << lane) - 1u));
-                xv[pos] = x;
-                xi[pos] = c;
-            }
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                int t = 0;
-                for (int w = 0; w < kSqRows / 32; ++w) t += s_wsum[w];
-                s_base += t;
-            }
-            __syncthreads();
-        }
-        const int nx = s_base;
+        const int hs = D.hs, np = D.npairs;
         const int b = item.y * kSqRows + threadIdx.x;
-        double part = 0.0;
-        if (b < hs) {
-            const double *__restrict__ K = D.K + b;
-            double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-            int k = 0;
-            for (; k + 4 <= nx; k += 4) {
-                const double k0 = __ldg(K + (size_t)xi[k] * hs), k1 = __ldg(K + (size_t)xi[k + 1] * hs);
-                const double k2 = __ldg(K + (size_t)xi[k + 2] * hs), k3 = __ldg(K + (size_t)xi[k + 3] * hs);
-                a0 = fma(k0, xv[k], a0);
-                a1 = fma(k1, xv[k + 1], a1);
-                a2 = fma(k2, xv[k + 2], a2);
-                a3 = fma(k3, xv[k + 3], a3);
+        const bool row = b < hs;
+        const long long *__restrict__ T = D.T + (row ? b : 0);
+        double y = 0.0;
+        for (int q = 0; q < np; ++q) {
+            const int n = __ldcg(D.evn + q);
+            const int *__restrict__ ev = D.evl + q * hs;
+            long long z = 0;
+            if (n >= 0) {
+                int k = 0;
+                for (; k + kSqUnroll <= n; k += kSqUnroll) {
+                    long long t[kSqUnroll];
+                    int v[kSqUnroll];
+#pragma unroll
+                    for (int u = 0; u < kSqUnroll; ++u) {
+                        const int e = __ldcg(ev + k + u);
+                        v[u] = (int)(short)(e & 0xffff);
+                        t[u] = __ldg(T + (size_t)(e >> 16) * hs);
+                    }
+#pragma unroll
+                    for (int u = 0; u < kSqUnroll; ++u) z += (long long)v[u] * t[u];
+                }
+                for (; k < n; ++k) {
+                    const int e = __ldcg(ev + k);
+                    z += (long long)(short)(e & 0xffff) * __ldg(T + (size_t)(e >> 16) * hs);
+                }
+            } else {
+                // a delta beyond 16 bits: read the pair's deltas directly
+                const int *__restrict__ dq = D.dP + q * hs;
+                for (int c = 0; c < hs; ++c) {
+                    const int v = __ldcg(dq + c);
+                    if (v)
+                        z += (long long)v * __ldg(T + (size_t)c * hs);
+                }
             }
-            for (; k < nx; ++k) a0 = fma(__ldg(K + (size_t)xi[k] * hs), xv[k], a0);
-            const double yb = (a0 + a1) + (a2 + a3);
-            D.y[b] = yb;
+            y = fma(D.pc[q] * D.yscale, (double)z, y);
+        }
+        double part = 0.0;
+        if (row) {
+            D.y[b] = y;
             const double sv = __ldcg(D.Sb + b);
             if (sv != 0.0)
-                part = (D.Rq[b] * sv) * (yb - D.h[b]);
+                part = (D.Rq[b] * sv) * (y - D.h[b]);
         }
         red[threadIdx.x] = part;
         __syncthreads();
@@ -1048,6 +1078,28 @@ __global__ void __launch_bounds__(512) k_sq_eval(const EDesc *desc, int id, int 
     }
 }
 
+// Largest |K[c][b] R0(c)| (non-negative doubles order like their bit patterns).
+__global__ void k_sq_absmax(const double *K, const double *R0, int hs, unsigned long long *out)
+{
+    const long long n = (long long)hs * hs;
+    double m = 0.0;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+        m = fmax(m, fabs(K[k] * R0[k / hs]));
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0)
+        atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
+// T[c][b] = round(K[c][b] R0(c) 2^s), in place over K.
+__global__ void k_sq_quantize(double *K, const double *R0, int hs, int s)
+{
+    const long long n = (long long)hs * hs;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        const double v = ldexp(K[k] * R0[k / hs], s);
+        ((long long *)K)[k] = llrint(v);
+    }
+}
+
 // K[b][c] = sum_q (M[b][q] M[c][q]) w_q in increasing q: 64 x 64 tiles of K
 // per CTA, 4 x 4 per thread, M staged through shared memory 16 Q points at a
 // time.  The product M[b][q] M[c][q] is formed before the weight, so K is
@@ -1106,8 +1158,10 @@ struct Slot {
 
 struct SqTable {
     int hs = 0, nq = 0;
+    int s = 0;  // T = round(K R0 2^s)
     void *blob = nullptr;
-    double *M = nullptr, *K = nullptr, *w = nullptr;
+    double *M = nullptr, *w = nullptr, *R0 = nullptr;
+    long long *T = nullptr;
     size_t bytes = 0;
 };
 
@@ -1153,7 +1207,7 @@ static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct BlobLayout {
     size_t box, real, mol, counts, delta, rfac, invvol, expd, dw, pc, pi, pj, dP, pidx, tlist, R, A, Bq, Sb, moves,
-        results, st, Rq, rfacq, sqexp, h, y, sqpart, sqv, total;
+        results, st, Rq, rfacq, sqexp, h, y, sqpart, sqv, evl, evn, total;
 };
 
 static BlobLayout blob_layout(const frmc_engine_spec &sp)
@@ -1197,6 +1251,8 @@ static BlobLayout blob_layout(const frmc_engine_spec &sp)
     L.y = take(8 * hq);
     L.sqpart = take(sq ? 8 * (size_t)((sp.hs + kSqRows - 1) / kSqRows) : 0);
     L.sqv = take(8 * nq);
+    L.evl = take(sq ? 4 * (size_t)sp.npairs * hs : 0);
+    L.evn = take(sq ? 4 * 16 : 0);
     L.total = off;
     return L;
 }
@@ -1219,10 +1275,12 @@ static int check_spec(const frmc_engine_spec &sp)
             return set_error(FRMC_E_ARG, "engine spec: atom %d element out of range", i);
     if (sp.sq_table >= 0) {
         if (sp.nq < 1 || !sp.sq_rfac || !sp.sq_inv_shell_volume || !sp.sq_experimental ||
-            !(sp.sq_variance_squared > 0))
+            !(sp.sq_variance_squared > 0) || !(sp.sq_rho0 > 0))
             return set_error(FRMC_E_ARG, "engine spec: missing or invalid S(Q) field");
         if (sp.hs > kSqMaxBins)
             return set_error(FRMC_E_ARG, "engine spec: an S(Q) term needs hs <= %d", kSqMaxBins);
+        if (sp.npairs > kMaxP)
+            return set_error(FRMC_E_ARG, "engine spec: an S(Q) term needs at most %d element pairs", kMaxP);
     }
     return FRMC_OK;
 }
@@ -1283,7 +1341,7 @@ static int refresh(EngineSet *s)
         s->sq_first[id] = (int)s->sq_host.size();
         s->sq_count[id] = D.sqblk;
         for (int k = 0; k < D.sqblk; ++k) s->sq_host.push_back(make_int2(id, k));
-        s->sq_smem = std::max(s->sq_smem, 12 * D.hs);
+        s->sq_smem = 0;
     }
     if ((int)s->sq_host.size() > s->sq_cap) {
         if (s->sq_items) cudaFree(s->sq_items);
@@ -1509,8 +1567,9 @@ static int add_engine(EngineSet *s, const frmc_engine_spec &sp, int *out_id)
         D.sqblk = (sp.hs + kSqRows - 1) / kSqRows;
         D.var2q = sp.sq_variance_squared;
         D.M = tab->M;
-        D.K = tab->K;
+        D.T = tab->T;
         D.wq = tab->w;
+        D.yscale = std::ldexp(sp.sq_rho0, -tab->s);
         D.Rq = (double *)(b + L.Rq);
         D.rfacq = (double *)(b + L.rfacq);
         D.sqexp = (double *)(b + L.sqexp);
@@ -1518,6 +1577,8 @@ static int add_engine(EngineSet *s, const frmc_engine_spec &sp, int *out_id)
         D.y = (double *)(b + L.y);
         D.sqpart = (double *)(b + L.sqpart);
         D.sqv = (double *)(b + L.sqv);
+        D.evl = (int *)(b + L.evl);
+        D.evn = (int *)(b + L.evn);
         Rqt.resize(sp.hs);
         for (int bb = 0; bb < sp.hs; ++bb) Rqt[bb] = sp.sq_rfac[bb] * sp.sq_inv_shell_volume[bb];
     }
@@ -1991,26 +2052,55 @@ int frmc_engines_coords(void *handle, int32_t e, float *box_coords, float *real_
 }
 
 int frmc_engines_sq_table(void *handle, int32_t hs, int32_t nq, const double *M, const double *weights,
-                          int32_t *table)
+                          const double *r0fac, int32_t *table)
 {
     EngineSet *s = as_set(handle);
-    if (!s || !M || !table || hs < 1 || hs > kSqMaxBins || nq < 1)
-        return set_error(FRMC_E_ARG, "engines_sq_table: need 1 <= hs <= %d, nq >= 1 and a table", kSqMaxBins);
+    if (!s || !M || !r0fac || !table || hs < 1 || hs > kSqMaxBins || nq < 1)
+        return set_error(FRMC_E_ARG, "engines_sq_table: need 1 <= hs <= %d, nq >= 1, M, r0fac and a table",
+                         kSqMaxBins);
+    Context *c;
+    FRMC_TRY(get_context(&c));
     SqTable t;
     t.hs = hs;
     t.nq = nq;
     const size_t nm = (size_t)hs * nq, nk = (size_t)hs * hs;
-    t.bytes = 8 * (nm + nk + (weights ? (size_t)nq : 0));
+    t.bytes = 8 * (nm + nk + hs + (weights ? (size_t)nq : 0) + 1);
     FRMC_CUDA(cudaMalloc(&t.blob, t.bytes));
     t.M = (double *)t.blob;
-    t.K = t.M + nm;
-    t.w = weights ? t.K + nk : nullptr;
+    double *K = t.M + nm;
+    t.R0 = K + nk;
+    unsigned long long *dmax = (unsigned long long *)(t.R0 + hs);
+    t.w = weights ? (double *)(dmax + 1) : nullptr;
+    t.T = (long long *)K;
+    unsigned long long mx = 0;
     cudaError_t ce = cudaMemcpyAsync(t.M, M, 8 * nm, cudaMemcpyHostToDevice, s->stream);
+    if (ce == cudaSuccess)
+        ce = cudaMemcpyAsync(t.R0, r0fac, 8 * (size_t)hs, cudaMemcpyHostToDevice, s->stream);
     if (ce == cudaSuccess && weights)
         ce = cudaMemcpyAsync(t.w, weights, 8 * (size_t)nq, cudaMemcpyHostToDevice, s->stream);
+    if (ce == cudaSuccess)
+        ce = cudaMemsetAsync(dmax, 0, 8, s->stream);
     if (ce == cudaSuccess) {
         dim3 grid((hs + 63) / 64, (hs + 63) / 64);
-        k_sq_gram<<<grid, 256, 0, s->stream>>>(t.M, t.w, hs, nq, t.K);
+        k_sq_gram<<<grid, 256, 0, s->stream>>>(t.M, t.w, hs, nq, K);
+        k_sq_absmax<<<c->sms * 2, 256, 0, s->stream>>>(K, t.R0, hs, dmax);
+        ce = cudaGetLastError();
+    }
+    if (ce == cudaSuccess)
+        ce = cudaMemcpyAsync(&mx, dmax, 8, cudaMemcpyDeviceToHost, s->stream);
+    if (ce == cudaSuccess)
+        ce = cudaStreamSynchronize(s->stream);
+    if (ce == cudaSuccess) {
+        const double m = reinterpret_cast<const double &>(mx);
+        int ex = 0;
+        if (m > 0.0 && std::isfinite(m))
+            std::frexp(m, &ex);
+        t.s = m > 0.0 ? kSqBits - ex : 0;  // max |K R0| 2^s < 2^kSqBits
+        if (!std::isfinite(m)) {
+            cudaFree(t.blob);
+            return set_error(FRMC_E_ARG, "engines_sq_table: the table has non-finite entries");
+        }
+        k_sq_quantize<<<c->sms * 2, 256, 0, s->stream>>>(K, t.R0, hs, t.s);
         ce = cudaGetLastError();
     }
     if (ce == cudaSuccess)

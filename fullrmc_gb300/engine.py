@@ -39,7 +39,7 @@ class _Spec(ctypes.Structure):
                 ("data_weights", F64P), ("variance_squared", ctypes.c_double), ("tolerance", ctypes.c_double),
                 ("move_cap", ctypes.c_int32), ("sq_table", ctypes.c_int32), ("nq", ctypes.c_int32),
                 ("sq_rfac", F64P), ("sq_inv_shell_volume", F64P), ("sq_experimental", F64P),
-                ("sq_variance_squared", ctypes.c_double)]
+                ("sq_variance_squared", ctypes.c_double), ("sq_rho0", ctypes.c_double)]
 
 
 _vp = ctypes.c_void_p
@@ -64,7 +64,7 @@ register("frmc_engines_results", [_vp, _i32, _i64, _i32, F64P, I32P, I32P])
 register("frmc_engines_counts", [_vp, _i32, I32P])
 register("frmc_engines_coords", [_vp, _i32, F32P, F32P])
 register("frmc_engines_info", [_vp, ctypes.POINTER(_i32), ctypes.POINTER(_i64), ctypes.POINTER(_i64)])
-register("frmc_engines_sq_table", [_vp, _i32, _i32, F64P, F64P, ctypes.POINTER(_i32)])
+register("frmc_engines_sq_table", [_vp, _i32, _i32, F64P, F64P, F64P, ctypes.POINTER(_i32)])
 register("frmc_engines_sq", [_vp, _i32, F64P])
 register("frmc_engines_terms", [_vp, _i32, F64P, F64P])
 
@@ -192,6 +192,7 @@ class SQModel:
         self.centers = ((e[:-1] + e[1:]) / F32(2.0)).astype(F32)
         e64 = e.astype(np.float64)
         self.shell_volumes = 4.0 / 3.0 * np.pi * (e64[1:] ** 3 - e64[:-1] ** 3)
+        self.r0fac = 4.0 * np.pi * self.centers.astype(np.float64) / self.shell_volumes
         self.rfac = 4.0 * np.pi * self.centers.astype(np.float64) * m.rho0
         self.M = sq_matrix(self.centers, self.q)
 
@@ -200,7 +201,8 @@ class SQModel:
         return (self.centers.tobytes(), self.q.tobytes(), w)
 
     def table_bytes(self):
-        return 8 * (self.hs * self.nq + self.hs * self.hs + (self.nq if self.data_weights is not None else 0))
+        return 8 * (self.hs * self.nq + self.hs * self.hs + self.hs + 1 +
+                    (self.nq if self.data_weights is not None else 0))
 
     def G_fp64(self, intra, inter):
         m = self.pdf
@@ -310,6 +312,7 @@ def make_spec(system, move_cap, sq_table=-1):
         sp.sq_inv_shell_volume = arrs["sq_iv"].ctypes.data_as(F64P)
         sp.sq_experimental = arrs["sq_exp"].ctypes.data_as(F64P)
         sp.sq_variance_squared = float(q.variance_squared)
+        sp.sq_rho0 = float(s.model.rho0)
     return sp, arrs
 
 
@@ -360,9 +363,11 @@ class EngineSet:
         if t is None:
             w = None if sq.data_weights is None else np.ascontiguousarray(sq.data_weights, np.float64)
             M = np.ascontiguousarray(sq.M, np.float64)
+            r0 = np.ascontiguousarray(sq.r0fac, np.float64)
             i = ctypes.c_int32()
             check(load().frmc_engines_sq_table(self.handle, sq.hs, sq.nq, M.ctypes.data_as(F64P),
-                                               None if w is None else w.ctypes.data_as(F64P), ctypes.byref(i)))
+                                               None if w is None else w.ctypes.data_as(F64P),
+                                               r0.ctypes.data_as(F64P), ctypes.byref(i)))
             t = self.tables[key] = i.value
         return t
 

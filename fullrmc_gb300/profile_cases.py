@@ -1,12 +1,15 @@
 """Small, self-contained runs of the hot kernels, sized for profiling.
 
     python -m fullrmc_gb300.profile_cases allpairs --n 30000 --reps 3
-    python -m fullrmc_gb300.profile_cases engines --count 64 --steps 5 [--tune 1024,1024,1]
+    python -m fullrmc_gb300.profile_cases engines --count 64 --steps 5 [--tune 1024,1024,1] [--sq]
+    python -m fullrmc_gb300.profile_cases serve --seconds 3 --limit 30
 
 ``allpairs`` runs the all-pairs histogram (three species, triclinic box with
 gamma = 120 degrees at 0.1057 atoms/A^3, r 0-20 A) on device buffers;
-``engines`` runs batched Metropolis steps of ``count`` mixed-size engines.
-Both print one JSON line with the CUDA-event time per launch.
+``engines`` runs batched Metropolis steps of ``count`` mixed-size engines
+(with ``--sq`` each also has an S(Q) term on Q 0.5-25 A^-1, dQ 0.01);
+``serve`` runs the serving loop on a Poisson stream of fits.  Each prints one
+JSON line (CUDA-event times per launch for the first two).
 """
 from __future__ import annotations
 
@@ -49,11 +52,17 @@ def allpairs(n, reps):
     return {"case": "allpairs", "atoms": n, "ms": ms, "pairs": n * (n - 1) / 2, "in_range": int(cnt.sum().item())}
 
 
-def engines(count, steps, tune=None):
+def engines(count, steps, tune=None, sq=False):
     import torch
     from fullrmc_gb300 import synthetic
     from fullrmc_gb300.engine import EngineSet, translation_moves
     systems = synthetic.mixed_engines(seed=0, count=count)
+    if sq:
+        from fullrmc_gb300.engine import SQModel
+        q = synthetic.q_grid()
+        for k, s in enumerate(systems):
+            s.sq = SQModel(pdf=s.model, q=q, S_exp=np.zeros(len(q)))
+            s.sq.S_exp = synthetic.synthetic_S(np.random.default_rng([k, 3]), s.sq, s.model.G_exp)
     es = EngineSet(systems, move_cap=steps + 4, tune=tune)
     es.init()
     for e, s in enumerate(systems):
@@ -73,20 +82,30 @@ def engines(count, steps, tune=None):
     pairs = sum(2 * (s.box_coords.shape[0] - 1) for s in systems)
     acc = sum(es.state(e)[2] for e in range(count))
     es.close()
-    return {"case": "engines", "engines": count, "steps": steps, "ms": ms, "pairs_per_step": pairs, "accepted": acc}
+    return {"case": "engines", "engines": count, "steps": steps, "sq": sq, "ms": ms, "pairs_per_step": pairs,
+            "accepted": acc}
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["allpairs", "engines"])
+    ap.add_argument("case", choices=["allpairs", "engines", "serve"])
     ap.add_argument("--n", type=int, default=30000)
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--count", type=int, default=64)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--tune", default=None, help="tile,threads,ctas_per_sm of the engine work list")
+    ap.add_argument("--sq", action="store_true")
+    ap.add_argument("--seconds", type=float, default=3.0)
+    ap.add_argument("--limit", type=float, default=30.0)
     a = ap.parse_args()
     tune = tuple(int(x) for x in a.tune.split(",")) if a.tune else None
-    out = allpairs(a.n, a.reps) if a.case == "allpairs" else engines(a.count, a.steps, tune)
+    if a.case == "allpairs":
+        out = allpairs(a.n, a.reps)
+    elif a.case == "engines":
+        out = engines(a.count, a.steps, tune, a.sq)
+    else:
+        from fullrmc_gb300 import serve
+        out = serve.benchmark_stream(a.seconds, a.limit)
     print(json.dumps(out))
 
 

@@ -245,6 +245,15 @@ class Server:
                 break  # the head of the queue can never be admitted
             it += 1
 
+    def close(self):
+        """Cancel every queued and live fit (live ones keep their partial results)."""
+        now = self.clock()
+        while self.queue:
+            req = self.queue.popleft()
+            self.results[req.rid] = FitResult(req.rid, "cancelled", arrival=req.arrival)
+        for rid in list(self.live):
+            self._retire(rid, "cancelled", now)
+
     # ------------------------------------------------------------ reporting
     def step_latency(self, pct):
         return weighted_percentile(self.lat_values, self.lat_weights, pct)
@@ -288,3 +297,72 @@ def run_stream(server: Server, requests, wall_limit: float, clock=time.perf_coun
         else:
             sleep(min(0.001, max(0.0, pending[0].arrival - now)))
     return clock() - start
+
+
+def benchmark_stream(seconds, wall_limit, seed=0, rate=20.0, budget_gib=16, plain_fits=6, plain_steps=100):
+    """The serving loop on a Poisson stream of fit requests: `rate` requests
+    per second for `seconds` (sizes log-uniform in 2,000-200,000 atoms, 1-3
+    species, G(r) on r 0-12 A plus S(Q) on Q 0.5-25 A^-1 with dQ 0.01, 2,000-
+    50,000 steps each), run in real time until every fit is done or
+    `wall_limit` seconds pass.  Reports total fit-steps/s, p50/p99 per-step
+    latency, fit latency, and the same kind of fits stepped one at a time (the
+    plain path) for comparison.  Needs the GPU library."""
+    from . import synthetic
+    from .engine import EngineSet, footprint
+    cap = 4096
+    arr = poisson_arrivals(np.random.default_rng([seed, 99]), rate, seconds)
+    reqs = []
+    for i, t in enumerate(arr):
+        system, steps = synthetic.serving_fit(seed * 100000 + i)
+        reqs.append(FitRequest(i, system, steps, seed=seed * 100000 + i, arrival=t))
+    es = EngineSet([], move_cap=cap)
+    srv = Server(es, lambda s: footprint(s, cap), budget_gib << 30, max_k=32)
+    # warm the kernels and the shared S(Q) table outside the timed stream
+    warm = Server(es, lambda s: footprint(s, cap), budget_gib << 30, max_k=32)
+    w_sys, _ = synthetic.serving_fit(seed * 100000 + 99999, nmax=3000)
+    warm.submit(FitRequest(-1, w_sys, 64, seed=1))
+    warm.drain()
+    elapsed = run_stream(srv, reqs, wall_limit)
+    done = [r for r in srv.results.values() if r.status == "done"]
+    failed = [r for r in srv.results.values() if r.status == "failed"]
+    atoms = [r.system.box_coords.shape[0] for r in reqs]
+    out = {
+        "steps_per_s": srv.steps_done / elapsed,
+        "fit_steps": srv.steps_done,
+        "elapsed_s": elapsed,
+        "busy_s": srv.busy_time,
+        "p50_step_latency_ms": 1e3 * srv.step_latency(50) if srv.lat_values else None,
+        "p99_step_latency_ms": 1e3 * srv.step_latency(99) if srv.lat_values else None,
+        "p50_fit_latency_s": srv.fit_latency(50),
+        "p99_fit_latency_s": srv.fit_latency(99),
+        "requests": len(reqs), "fits_done": len(done), "fits_failed": len(failed),
+        "fits_unfinished": sum(1 for r in reqs if r.rid not in srv.results),
+        "peak_live": srv.peak_live, "peak_device_bytes": srv.peak_used, "hbm_budget_bytes": budget_gib << 30,
+        "iterations": srv.iterations,
+        "stream": {"rate_per_s": rate, "arrivals_s": seconds, "wall_limit_s": wall_limit,
+                   "atoms": "log-uniform 2000-200000 (mean of this stream %.0f)" % (np.mean(atoms) if atoms else 0),
+                   "species": "1-3", "G(r)": "r 0-12 A, dr 0.01", "S(Q)": "Q 0.5-25, dQ 0.01 (2451 points)",
+                   "steps_per_fit": "uniform 2000-50000"},
+    }
+    srv.close()
+    # plain: a sample of the stream's fits stepped one at a time
+    sample = reqs[:plain_fits]
+    ids = []
+    for r in sample:
+        e = es.add(r.system)
+        a, v, u = translation_moves(np.random.default_rng(r.seed), r.system.box_coords.shape[0], plain_steps + 1,
+                                    r.amplitude)
+        es.push_moves(e, a, v, u, 0)
+        ids.append(e)
+    for e in ids:
+        es.step(1, engine=e, graph=False)
+    t0 = time.perf_counter()
+    for e in ids:
+        es.step(plain_steps, engine=e, graph=False, sync=False)
+    es.sync()
+    t_plain = time.perf_counter() - t0
+    out["plain"] = {"steps_per_s": len(ids) * plain_steps / t_plain, "fits_sampled": len(ids),
+                    "atoms": [r.system.box_coords.shape[0] for r in sample]}
+    out["served_over_plain"] = out["steps_per_s"] / out["plain"]["steps_per_s"]
+    es.close()
+    return out

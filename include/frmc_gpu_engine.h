@@ -67,16 +67,19 @@ typedef struct {
     const double *sq_inv_shell_volume; /* (hs,) 1 / S(Q) shell volume           */
     const double *sq_experimental;     /* (nq,) experimental S(Q)               */
     double sq_variance_squared;
+    double sq_rho0;                    /* number density: sq_rfac = sq_rho0 r0fac of the table */
 } frmc_engine_spec;
 
 /* A G(r) -> S(Q) table shared by the set's engines that use the same r shells
  * (hs) and Q points (nq): M (hs, nq) row-major, M[r][Q] = dr sin(Q r) / Q
- * (StructureFactorConstraints.py:302-312), and optional per-Q data weights w
- * (NULL = 1).  The set keeps M, w and K = M diag(w) M^T (hs x hs, computed on
- * the device) until it is destroyed; *table receives the id to put in a
- * spec's sq_table.  Device bytes: 8 (hs nq + hs hs + nq).  hs <= 4096. */
+ * (StructureFactorConstraints.py:302-312), optional per-Q data weights w
+ * (NULL = 1) and r0fac (hs,) = 4 pi r / shell volume of those shells.  The
+ * set keeps M, w and the fixed-point table round(K r0fac 2^s), K = M diag(w)
+ * M^T (hs x hs, built on the device), until it is destroyed; *table receives
+ * the id to put in a spec's sq_table.  Device bytes: 8 (hs nq + hs hs + hs +
+ * nq + 1).  hs <= 4096. */
 int frmc_engines_sq_table(void *handle, int32_t hs, int32_t nq, const double *M, const double *weights,
-                          int32_t *table);
+                          const double *r0fac, int32_t *table);
 /* Current S(Q) of engine e recomputed from its counts (FP64, nq values). */
 int frmc_engines_sq(void *handle, int32_t e, double *sq);
 /* The two chi2 terms of engine e: sd = sum w (G_exp - G)^2 of the G(r) term and

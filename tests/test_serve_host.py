@@ -230,3 +230,14 @@ def test_run_stream_with_a_fake_clock():
     p50, p99 = s.step_latency(50), s.step_latency(99)
     assert p50 == pytest.approx(0.002 / 8) and p99 >= p50
     assert s.fit_latency(50) > 0
+
+
+def test_close_cancels_queued_and_live_fits():
+    s = make_server(budget=1300 + 1)
+    reqs = [serve.FitRequest(i, system(300), 100, seed=i) for i in range(3)]
+    for r in reqs:
+        s.submit(r)
+    s.iterate()
+    s.close()
+    assert [s.results[i].status for i in range(3)] == ["cancelled"] * 3
+    assert 0 < s.results[0].steps < 100 and s.used == 0 and not s.es.eng
