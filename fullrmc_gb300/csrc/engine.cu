@@ -39,6 +39,7 @@
 
 #include "frmc_gpu_engine.h"
 #include "frmc_math.cuh"
+#include "frmc_ptx.cuh"
 #include "frmc_runtime.h"
 
 namespace frmc {
@@ -61,7 +62,7 @@ struct EState {
 struct Sched {
     unsigned long long claimed;
     unsigned finished;
-    unsigned pad;
+    unsigned status;  // DeviceStatus bits raised by the kernels (a bounded wait gave up)
 };
 
 struct EMove {
@@ -155,11 +156,13 @@ struct StepParams {
     const int2 *items;
     int nitems;
     int tile;
-    int eval_only;  // 1: compute G(r) and chi2 of the current counts, no move
+    int eval_only;      // 1: compute G(r) and chi2 of the current counts, no move
+    int fused_dp_ints;  // fused launches: ints of the element-pair deltas (a multiple of 4)
+    int fused_bins;     // fused launches: doubles of each of A and Bq (even)
     Sched *sched;
 };
 
-constexpr int kRedLanes = 256;
+constexpr int kRedLanes = 64;
 
 // transform_coordinates row-vector product (boundary_conditions_collection.pyx:104-106)
 __device__ __forceinline__ float3 to_box(const Basis &RB, float x, float y, float z)
@@ -191,15 +194,17 @@ __device__ __forceinline__ void pair_of_flat(const V &D, int flat, int ra, int r
 // (-1 when out of range or unchanged), `half` (0 intra, total inter), bins and
 // the column's element.  32-bit indexes: 2 * ne * ne * hs < 2^31 is checked
 // when an engine is created.
-template <int BM, class V>
-__device__ __forceinline__ void column_bins(const V &D, float3 o, float3 nw, float4 c, int mj, int arow, int mola,
-                                            int &f0, int &f1, int &half, int &b0, int &b1, int &elj)
+// Bins of one column from its squared distances to the moved atom before
+// (s0) and after (s1) the move; `valid` is false for a column past the end or
+// the moved atom itself.  The squared distances of all columns of a batch are
+// computed first, without branches, so their independent chains interleave.
+template <class V>
+__device__ __forceinline__ void column_bins(const V &D, float s0, float s1, bool valid, float4 c, int mj, int arow,
+                                            int mola, int &f0, int &f1, int &half, int &b0, int &b1, int &elj)
 {
     f0 = f1 = -1;
-    const float s0 = pair_s<BM>(o.x, o.y, o.z, c.x, c.y, c.z, D.B);
-    const float s1 = pair_s<BM>(nw.x, nw.y, nw.z, c.x, c.y, c.z, D.B);
-    const bool a0 = (s0 >= D.s_lo) & (s0 < D.s_hi);
-    const bool a1 = (s1 >= D.s_lo) & (s1 < D.s_hi);
+    const bool a0 = valid & (s0 >= D.s_lo) & (s0 < D.s_hi);
+    const bool a1 = valid & (s1 >= D.s_lo) & (s1 < D.s_hi);
     if (a0 | a1) {
         elj = __float_as_int(c.w);
         half = mj == mola ? 0 : (int)D.total;
@@ -221,15 +226,12 @@ __device__ __forceinline__ void column_bins(const V &D, float3 o, float3 nw, flo
 
 constexpr int kItemUnroll = 4;
 
-// One item: the moved atom against atoms [t*tile, (t+1)*tile).  For every
-// column j the pair before and after the move is binned; a changed bin adds
-// -1 / +1 to the oriented delta and to the element-pair delta, and its
-// oriented index is appended to the touched list (one list reservation per
-// warp and round).  Coordinates of kItemUnroll columns are loaded before any
-// is used.
 // One item of the split path: the moved atom against atoms
-// [t*tile, (t+1)*tile), adding to the engine's global deltas.  Per column
-// the warp reserves its touched-list entries with one atomic.
+// [t*tile, (t+1)*tile).  For every column j the pair before and after the
+// move is binned; a changed bin adds -1 / +1 to the engine's global oriented
+// delta and element-pair delta, and its oriented index is appended to the
+// touched list (one list reservation per warp and column).  Coordinates of
+// kItemUnroll columns are loaded before any is used.
 template <int BM>
 __device__ void item_delta(const EDesc &Dg, int tile, int atom, float3 o, float3 nw, int ela, int mola, int t)
 {
@@ -248,17 +250,20 @@ __device__ void item_delta(const EDesc &Dg, int tile, int atom, float3 o, float3
 #pragma unroll
         for (int u = 0; u < kItemUnroll; ++u) {
             const int j = jb + u * blockDim.x + threadIdx.x;
-            if (j < j1) {
-                c[u] = D.box[j];
-                mj[u] = D.mol[j];
-            }
+            c[u] = j < j1 ? D.box[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+            mj[u] = j < j1 ? D.mol[j] : 0;
+        }
+        float s0[kItemUnroll], s1[kItemUnroll];
+#pragma unroll
+        for (int u = 0; u < kItemUnroll; ++u) {
+            s0[u] = pair_s<BM>(o.x, o.y, o.z, c[u].x, c[u].y, c[u].z, D.B);
+            s1[u] = pair_s<BM>(nw.x, nw.y, nw.z, c[u].x, c[u].y, c[u].z, D.B);
         }
 #pragma unroll
         for (int u = 0; u < kItemUnroll; ++u) {
             const int j = jb + u * blockDim.x + threadIdx.x;
             int f0 = -1, f1 = -1, half = 0, b0 = 0, b1 = 0, elj = 0;
-            if (j < j1 && j != atom)
-                column_bins<BM>(D, o, nw, c[u], mj[u], arow, mola, f0, f1, half, b0, b1, elj);
+            column_bins(D, s0[u], s1[u], j < j1 && j != atom, c[u], mj[u], arow, mola, f0, f1, half, b0, b1, elj);
             const unsigned m0 = __ballot_sync(0xffffffffu, f0 >= 0);
             const unsigned m1 = __ballot_sync(0xffffffffu, f1 >= 0);
             if ((m0 | m1) == 0u)
@@ -311,16 +316,41 @@ __device__ void lanes_add_chunk(double *red, const double *cb, int c0, int cn)
     __syncthreads();
 }
 
+// The lanes are combined by warp 0: each group of 32 lanes by a fixed
+// shuffle tree, then the group sums by a fixed pairwise tree.
 __device__ double lanes_total(double *red)
 {
+    constexpr int G = kRedLanes / 32;
+    static_assert((G & (G - 1)) == 0, "lane groups must be a power of two");
+    __shared__ double s_total;
     __syncthreads();  // every lane's partial sum is written
-    for (int s = kRedLanes / 2; s > 0; s >>= 1) {
-        for (int L = threadIdx.x; L < s; L += blockDim.x) red[L] += red[L + s];
-        __syncthreads();
+    if (threadIdx.x < 32) {
+        double g[G];
+#pragma unroll
+        for (int k = 0; k < G; ++k) {
+            double v = red[32 * k + threadIdx.x];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            g[k] = v;
+        }
+#pragma unroll
+        for (int w = G / 2; w > 0; w >>= 1)
+#pragma unroll
+            for (int i = 0; i < w; ++i) g[i] += g[i + w];
+        if (threadIdx.x == 0)
+            s_total = g[0];
     }
-    const double v = red[0];
     __syncthreads();
-    return v;
+    return s_total;
+}
+
+// -2 x by exponent and sign arithmetic (exact; x is a sum of a few pair
+// coefficients times small integers, so it is zero or a normal number).
+__device__ __forceinline__ double neg_twice(double x)
+{
+    const long long b = __double_as_longlong(x);
+    const long long e = (b & 0x7ff0000000000000ll) ? (1ll << 52) : 0ll;
+    return __longlong_as_double((b ^ (long long)0x8000000000000000ull) + e);
 }
 
 // Element-pair count n_p(b) from the oriented counts (intra + inter, both
@@ -371,92 +401,153 @@ constexpr int kMaxP = 10;  // element pairs loaded with unrolled loads (ne <= 4)
 
 // SMEM: the element-pair deltas are this CTA's shared-memory copy (one CTA per
 // engine); otherwise they are the engine's global array, filled by several
-// CTAs, read through L2 and cleared as they are read.
+// CTAs, read through L2 and cleared as they are read (engines with an S(Q)
+// term leave them for the S(Q) kernel, which clears them, and list them per
+// element pair as (bin << 16) | (delta & 0xffff)).
+//
+// The bins whose element-pair counts changed are first listed, chunk by
+// chunk, in increasing bin order (sbin[k]); the FP64 work then runs on the
+// list only, so each warp-level FP64 instruction -- the FP64 pipe is narrow
+// on this GPU -- serves up to 32 changed bins.  Lane L of the fixed-order
+// reduction sums the list entries k = L (mod 256) in increasing k.  For
+// hs <= kChunk the list, its -2 S values (sbs[k]) and its length (*s_nchg)
+// stay in shared memory for the commit; larger histograms, and engines with
+// an S(Q) term, also keep S in the global Sb (zero for unchanged bins).
+// pair_coef_p * v for |v| <= 4 comes from a small table, so a changed bin
+// costs one FP64 add per non-zero element-pair delta.
 template <bool SMEM>
-__device__ double eval_delta(const EDesc &Dg, int *dP, double *red, double *cb, double *sbs, double *coef)
+__device__ double eval_delta(const EDesc &Dg, int *dP, const double *Ab, const double *Bqb, double *red, double *cb,
+                             double *sbs, int *sbin, int *s_nchg, double *coef)
 {
-    struct {
-        int hs;
-        const double *__restrict__ A;
-        const double *__restrict__ Bq;
-        double *__restrict__ Sb;
-        const double *__restrict__ pc;
-    } D = {Dg.hs, Dg.A, Dg.Bq, Dg.Sb, Dg.pc};
+    const int hs = Dg.hs;
+    const double *__restrict__ A = Ab;
+    const double *__restrict__ Bq = Bqb;
+    double *__restrict__ Sb = Dg.Sb;
     const int np = Dg.npairs;
-    // engines with an S(Q) term leave the element-pair deltas in the global
-    // array for the S(Q) kernel, which clears them
-    // and list them per element pair as (bin << 16) | (delta & 0xffff)
     const bool sq = Dg.sq != 0;
     int *__restrict__ gdP = Dg.dP;
     int *__restrict__ evl = Dg.evl;
     __shared__ int s_evn[kMaxP];
     __shared__ int s_wide;
+    __shared__ int s_cnt[kChunk / 32];  // changed bins per 32-bin group, then their list offsets
+    __shared__ double tabv[kMaxP * 9];  // pair_coef_q * v, v = -4..4
     if (sq) {
         for (int q = threadIdx.x; q < kMaxP; q += blockDim.x) s_evn[q] = 0;
         if (threadIdx.x == 0)
             s_wide = 0;
     }
-    if (!SMEM)
-        for (int q = threadIdx.x; q < np; q += blockDim.x) coef[q] = D.pc[q];
+    if (!SMEM) {
+        for (int q = threadIdx.x; q < np; q += blockDim.x) coef[q] = Dg.pc[q];
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < min(np, kMaxP) * 9; i += blockDim.x) {
+        const int v = i % 9 - 4;
+        const double cf = coef[i / 9];
+        tabv[i] = v == 1 ? cf : (v == -1 ? -cf : cf * (double)v);
+    }
     lanes_zero(red);
     __syncthreads();
-    const bool big = D.hs > kChunk;
-    for (int c0 = 0; c0 < D.hs; c0 += kChunk) {
-        const int cn = min(kChunk, D.hs - c0);
-        for (int b = c0 + threadIdx.x; b < c0 + cn; b += blockDim.x) {
-            int d[kMaxP];
+    const bool big = hs > kChunk;
+    const unsigned lane = threadIdx.x & 31u;
+    auto delta_at = [&](int q, int b) -> int {
+        return SMEM ? dP[q * hs + b] : __ldcg(dP + (long long)q * hs + b);
+    };
+    for (int c0 = 0; c0 < hs; c0 += kChunk) {
+        const int cn = min(kChunk, hs - c0);
+        const int span = (cn + 31) & ~31;  // whole 32-bin groups, so every ballot has full warps
+        // 1. which bins changed
+        unsigned long long mine = 0;  // bit r: this thread's bin of round r changed
+        int r = 0;
+        for (int i = threadIdx.x; i < span; i += blockDim.x, ++r) {
+            bool any = false;
+            if (i < cn) {
+                const int b = c0 + i;
+#pragma unroll
+                for (int q = 0; q < kMaxP; ++q)
+                    if (q < np)
+                        any |= delta_at(q, b) != 0;
+                for (int q = kMaxP; q < np; ++q) any |= delta_at(q, b) != 0;
+                if ((sq || big) && !any)
+                    Sb[b] = 0.0;
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, any);
+            if (lane == 0)
+                s_cnt[i >> 5] = __popc(bal);
+            if (any)
+                mine |= 1ull << r;
+        }
+        __syncthreads();
+        // 2. exclusive scan of the group counts (warp 0)
+        if (threadIdx.x < 32) {
+            const int ngroups = span >> 5;
+            int run = 0;
+            for (int g0 = 0; g0 < ngroups; g0 += 32) {
+                const int gi = g0 + (int)lane;
+                const int v = gi < ngroups ? s_cnt[gi] : 0;
+                int incl = v;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                    if ((int)lane >= o)
+                        incl += t;
+                }
+                if (gi < ngroups)
+                    s_cnt[gi] = run + incl - v;
+                run += __shfl_sync(0xffffffffu, incl, 31);
+            }
+            if (lane == 0)
+                *s_nchg = run;
+        }
+        __syncthreads();
+        // 3. the list, in increasing bin order
+        r = 0;
+        for (int i = threadIdx.x; i < span; i += blockDim.x, ++r) {
+            const bool any = (mine >> r) & 1ull;
+            const unsigned bal = __ballot_sync(0xffffffffu, any);
+            if (any)
+                sbin[s_cnt[i >> 5] + __popc(bal & ((1u << lane) - 1u))] = c0 + i;
+        }
+        __syncthreads();
+        const int n = *s_nchg;
+        // 4. FP64 on the listed bins
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {
+            const int b = sbin[k];
+            const double a = A[b];
+            const double bq = Bq[b];
+            double S = 0.0;
 #pragma unroll
             for (int q = 0; q < kMaxP; ++q) {
-                int v = 0;
-                if (q < np)
-                    v = SMEM ? dP[q * D.hs + b] : __ldcg(dP + (long long)q * D.hs + b);
-                d[q] = v;
-            }
-            const double a = D.A[b];
-            const double bq = D.Bq[b];
-            bool any = false;
-#pragma unroll
-            for (int q = 0; q < kMaxP; ++q) any |= d[q] != 0;
-            for (int q = kMaxP; q < np; ++q)
-                any |= (SMEM ? dP[q * D.hs + b] : __ldcg(dP + (long long)q * D.hs + b)) != 0;
-            double S = 0.0, c = 0.0;
-            if (any) {
-#pragma unroll
-                for (int q = 0; q < kMaxP; ++q) {
-                    const int v = d[q];
-                    if (v) {
-                        if (!SMEM && !sq)
-                            dP[(long long)q * D.hs + b] = 0;
-                        if (sq) {
-                            if (SMEM)
-                                gdP[q * D.hs + b] = v;
-                            evl[q * D.hs + atomicAdd(&s_evn[q], 1)] = (b << 16) | (v & 0xffff);
-                            if (v > 32767 || v < -32768)
-                                s_wide = 1;
-                        }
-                        const double cf = coef[q];
-                        S += v == 1 ? cf : (v == -1 ? -cf : cf * (double)v);
+                if (q >= np)
+                    break;
+                const int v = delta_at(q, b);
+                if (v) {
+                    if (!SMEM && !sq)
+                        dP[(long long)q * hs + b] = 0;
+                    if (sq) {
+                        if (SMEM)
+                            gdP[q * hs + b] = v;
+                        evl[q * hs + atomicAdd(&s_evn[q], 1)] = (b << 16) | (v & 0xffff);
+                        if (v > 32767 || v < -32768)
+                            s_wide = 1;
                     }
+                    S += (unsigned)(v + 4) <= 8u ? tabv[q * 9 + v + 4] : coef[q] * (double)v;
                 }
-                for (int q = kMaxP; q < np; ++q) {
-                    int *dp = dP + (long long)q * D.hs + b;
-                    const int v = SMEM ? *dp : __ldcg(dp);
-                    if (v) {
-                        if (!SMEM)
-                            *dp = 0;
-                        const double cf = coef[q];
-                        S += v == 1 ? cf : (v == -1 ? -cf : cf * (double)v);
-                    }
-                }
-                c = S * fma(a, S, -bq);
             }
-            cb[b - c0] = c;
+            for (int q = kMaxP; q < np; ++q) {
+                const int v = delta_at(q, b);
+                if (v) {
+                    if (!SMEM)
+                        dP[(long long)q * hs + b] = 0;
+                    const double cf = coef[q];
+                    S += v == 1 ? cf : (v == -1 ? -cf : cf * (double)v);
+                }
+            }
+            cb[k] = S * fma(a, S, -bq);
+            sbs[k] = neg_twice(S);
             if (big || sq)
-                D.Sb[b] = S;
-            if (!big)
-                sbs[b] = S;
+                Sb[b] = S;
         }
-        lanes_add_chunk(red, cb, c0, cn);
+        lanes_add_chunk(red, cb, 0, n);
     }
     const double total = lanes_total(red);
     if (sq && (int)threadIdx.x < np)
@@ -467,9 +558,9 @@ __device__ double eval_delta(const EDesc &Dg, int *dP, double *red, double *cb, 
 constexpr int kCommitUnroll = 4;
 
 __device__ void finish_engine(const EDesc &D, int atom, float3 nw, float4 nreal, double *red, double *cb,
-                              double *sbs, double *coef, int *s_flag)
+                              double *sbs, int *sbin, int *s_nchg, double *coef, int *s_flag)
 {
-    const double dsd = eval_delta<false>(D, D.dP, red, cb, sbs, coef);
+    const double dsd = eval_delta<false>(D, D.dP, D.A, D.Bq, red, cb, sbs, sbin, s_nchg, coef);
     if (D.sq) {
         // the S(Q) kernel evaluates its term, decides and commits
         if (threadIdx.x == 0) {
@@ -510,11 +601,18 @@ __device__ void finish_engine(const EDesc &D, int atom, float3 nw, float4 nreal,
     }
     // on accept G += R S, hence Bq -= 2 A S on the bins that changed
     if (accept) {
-        const bool big = D.hs > kChunk;
-        for (int b = threadIdx.x; b < D.hs; b += blockDim.x) {
-            const double S = big ? D.Sb[b] : sbs[b];
-            if (S != 0.0)
-                D.Bq[b] = fma(-2.0 * D.A[b], S, D.Bq[b]);
+        if (D.hs > kChunk) {
+            for (int b = threadIdx.x; b < D.hs; b += blockDim.x) {
+                const double S = D.Sb[b];
+                if (S != 0.0)
+                    D.Bq[b] = fma(-2.0 * D.A[b], S, D.Bq[b]);
+            }
+        } else {
+            const int n = *s_nchg;
+            for (int k = threadIdx.x; k < n; k += blockDim.x) {
+                const int b = sbin[k];
+                D.Bq[b] = fma(D.A[b], sbs[k], D.Bq[b]);
+            }
         }
     }
     __syncthreads();
@@ -574,14 +672,19 @@ __device__ void fused_columns(const EDesc &Dg, int *sdP, unsigned *s_tcount, int
         }
         int f0[kItemUnroll], f1[kItemUnroll], half[kItemUnroll], b0[kItemUnroll], b1[kItemUnroll],
             elj[kItemUnroll];
+        float s0[kItemUnroll], s1[kItemUnroll];
+#pragma unroll
+        for (int u = 0; u < kItemUnroll; ++u) {
+            s0[u] = pair_s<BM>(o.x, o.y, o.z, c[u].x, c[u].y, c[u].z, D.B);
+            s1[u] = pair_s<BM>(nw.x, nw.y, nw.z, c[u].x, c[u].y, c[u].z, D.B);
+        }
         unsigned mine = 0;
 #pragma unroll
         for (int u = 0; u < kItemUnroll; ++u) {
             const int j = jb + u * blockDim.x + threadIdx.x;
-            f0[u] = f1[u] = -1;
             half[u] = b0[u] = b1[u] = elj[u] = 0;
-            if (j < D.n && j != atom)
-                column_bins<BM>(D, o, nw, c[u], mj[u], arow, mola, f0[u], f1[u], half[u], b0[u], b1[u], elj[u]);
+            column_bins(D, s0[u], s1[u], j < D.n && j != atom, c[u], mj[u], arow, mola, f0[u], f1[u], half[u], b0[u],
+                        b1[u], elj[u]);
             mine += (f0[u] >= 0) + (f1[u] >= 0);
         }
         unsigned incl = mine;
@@ -623,10 +726,20 @@ __device__ void fused_columns(const EDesc &Dg, int *sdP, unsigned *s_tcount, int
     }
 }
 
-__device__ void engine_fused(const EDesc &D, int *sdP, double *red, double *cb, double *sbs, double *coef,
-                             int *s_flag, unsigned *s_tcount, float *s_mv, int *s_mi)
+// sA, sBq: shared-memory copies of A and Bq, brought in by bulk copies on
+// `bar` while the columns run; parity = this CTA's count of fused items mod 2.
+__device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, uint64_t *bar, uint32_t parity,
+                             uint32_t *status, double *red, double *cb, double *sbs, int *sbin, int *s_nchg,
+                             double *coef, int *s_flag, unsigned *s_tcount, float *s_mv, int *s_mi)
 {
     if (threadIdx.x == 0) {
+        // the previous item's reads of sA / sBq are ordered before this
+        // item's bulk copies by the barrier at the item boundary
+        const uint32_t bytes = (uint32_t)((8 * D.hs + 15) & ~15);
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(bar, 2 * bytes);
+        bulk_g2s(sA, D.A, bytes, bar);
+        bulk_g2s(sBq, D.Bq, bytes, bar);
         const long long step = D.st->step;
         const EMove m = D.moves[step % D.move_cap];
         const float4 ob = D.box[m.atom];
@@ -657,7 +770,8 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *red, double *cb, 
     default: fused_columns<BM_GENERAL>(D, sdP, s_tcount, atom, o, nw, ela, mola); break;
     }
     __syncthreads();
-    const double dsd = eval_delta<true>(D, sdP, red, cb, sbs, coef);
+    mbar_wait(bar, parity, status);
+    const double dsd = eval_delta<true>(D, sdP, sA, sBq, red, cb, sbs, sbin, s_nchg, coef);
     if (D.sq) {
         // the S(Q) kernel evaluates its term, decides and commits
         if (threadIdx.x == 0) {
@@ -686,15 +800,20 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *red, double *cb, 
             const int e = tl[k];
             atomicAdd(cnt + (e >> 1), (e & 1) ? 1 : -1);
         }
-        const int hs = D.hs;
-        const bool big = hs > kChunk;
-        const double *__restrict__ Sb = D.Sb;
-        const double *__restrict__ A = D.A;
         double *__restrict__ Bq = D.Bq;
-        for (int b = threadIdx.x; b < hs; b += blockDim.x) {
-            const double Sv = big ? Sb[b] : sbs[b];
-            if (Sv != 0.0)
-                Bq[b] = fma(-2.0 * A[b], Sv, Bq[b]);
+        if (D.hs > kChunk) {
+            const double *__restrict__ Sb = D.Sb;
+            for (int b = threadIdx.x; b < D.hs; b += blockDim.x) {
+                const double Sv = Sb[b];
+                if (Sv != 0.0)
+                    Bq[b] = fma(-2.0 * sA[b], Sv, sBq[b]);
+            }
+        } else {
+            const int n = *s_nchg;
+            for (int k = threadIdx.x; k < n; k += blockDim.x) {
+                const int b = sbin[k];
+                Bq[b] = fma(sA[b], sbs[k], sBq[b]);
+            }
         }
     }
     __syncthreads();
@@ -705,8 +824,7 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *red, double *cb, 
         r.accepted = accept ? 1 : 0;
         r.atom = atom;
         if (accept) {
-            const float4 ob = D.box[atom];
-            D.box[atom] = make_float4(nw.x, nw.y, nw.z, ob.w);
+            D.box[atom] = make_float4(nw.x, nw.y, nw.z, __int_as_float(s_mi[1]));
             D.real[atom] = make_float4(s_mv[6], s_mv[7], s_mv[8], 0.0f);
             S.chi2 = chi2_new;
             S.sd = sd_new;
@@ -724,13 +842,28 @@ __global__ void __launch_bounds__(kMaxEngineThreads, 1) k_engine_step(StepParams
     __shared__ double red[kRedLanes];
     __shared__ double cb[kChunk];
     __shared__ double sbs[kChunk];
+    __shared__ int sbin[kChunk];
+    __shared__ int s_nchg;
     __shared__ double coef[64];
     __shared__ float s_mv[9];
     __shared__ int s_mi[3];
     __shared__ unsigned s_tcount;
     __shared__ int s_last, s_flag, s_item;
-    extern __shared__ int sdP[];
+    __shared__ __align__(8) uint64_t s_bar;
+    extern __shared__ __align__(16) int sdP[];
     (void)sdP;
+    uint32_t fused_items = 0;
+    double *sA = nullptr, *sBq = nullptr;
+    if (FUSED) {
+        // dynamic layout: element-pair deltas, then A and Bq (16-byte aligned)
+        sA = reinterpret_cast<double *>(sdP + p.fused_dp_ints);
+        sBq = sA + p.fused_bins;
+        if (threadIdx.x == 0) {
+            mbar_init(&s_bar, 1);
+            mbar_fence_init();
+        }
+        __syncthreads();
+    }
     for (;;) {
         if (threadIdx.x == 0) {
             const unsigned long long k = atomicAdd(&p.sched->claimed, 1ull);
@@ -744,7 +877,9 @@ __global__ void __launch_bounds__(kMaxEngineThreads, 1) k_engine_step(StepParams
         const int2 item = p.items[it];
         const EDesc &D = p.desc[item.x];
         if (FUSED) {
-            engine_fused(D, sdP, red, cb, sbs, coef, &s_flag, &s_tcount, s_mv, s_mi);
+            engine_fused(D, sdP, sA, sBq, &s_bar, fused_items & 1u, &p.sched->status, red, cb, sbs, sbin, &s_nchg,
+                         coef, &s_flag, &s_tcount, s_mv, s_mi);
+            ++fused_items;
             __syncthreads();
             continue;
         }
@@ -790,7 +925,7 @@ __global__ void __launch_bounds__(kMaxEngineThreads, 1) k_engine_step(StepParams
         __syncthreads();
         if (s_last) {
             __threadfence();
-            finish_engine(D, atom, nw, nreal, red, cb, sbs, coef, &s_flag);
+            finish_engine(D, atom, nw, nreal, red, cb, sbs, sbin, &s_nchg, coef, &s_flag);
         }
         __syncthreads();
     }
@@ -840,12 +975,17 @@ __global__ void k_gather_results(const EDesc *desc, const int *ids, EResult *out
 // terms, and y(b) = rho0 2^-s sum_p pair_coef_p z_p(b).  This keeps the
 // O(changed bins x bins) part on the integer pipes, which run many times
 // faster than FP64 on this GPU.
-// Items are (engine, block of kSqRows rows).  A CTA lists each element
-// pair's non-zero deltas, accumulates z_p for its rows (thread = row, T read
-// along rows), forms y and its rows' share of x (y - h); the CTA that
-// finishes an engine's last block adds the shares in block order, decides and
-// commits: counts, Bq -= 2 A S, h -= 2 y, coordinates, and clears dP.
-constexpr int kSqRows = 256;      // rows per item = threads per CTA
+// Items are (engine, block of kSqRows rows).  For each element pair a CTA
+// stages the pair's list of non-zero deltas (written by the histogram pass)
+// in shared memory; kSqGroups thread groups of kSqRows threads (thread = row,
+// T read along rows, kSqUnroll loads in flight) take interleaved chunks of the
+// list, and their partial z_p are added (exactly) before y is formed.  The
+// CTA then takes its rows' share of x (y - h); the CTA that finishes an
+// engine's last block adds the shares in block order, decides and commits:
+// counts, Bq -= 2 A S, h -= 2 y, coordinates, and clears dP.
+constexpr int kSqRows = 64;       // rows per item
+constexpr int kSqGroups = 4;      // event groups per item
+constexpr int kSqThreads = kSqRows * kSqGroups;
 constexpr int kSqMaxBins = 4096;  // histogram bins of an engine with an S(Q) term
 constexpr int kSqBits = 48;       // largest |T| is below 2^48: 2^15 unit deltas fit in an int64 sum
 
@@ -930,11 +1070,14 @@ __device__ void sq_finish(const EDesc &D, int *s_flag, double *s_val)
 
 constexpr int kSqUnroll = 16;  // table loads in flight per thread
 
-__global__ void __launch_bounds__(kSqRows) k_sq_step(SqParams p)
+__global__ void __launch_bounds__(kSqThreads) k_sq_step(SqParams p)
 {
+    extern __shared__ int sq_ev[];  // one element pair's non-zero deltas: (bin << 16) | (delta & 0xffff)
+    __shared__ long long zz[kSqGroups][kSqRows];
     __shared__ double red[kSqRows];
     __shared__ double s_val[3];
     __shared__ int s_item, s_last, s_flag;
+    const int r = threadIdx.x % kSqRows, g = threadIdx.x / kSqRows;
     for (;;) {
         if (threadIdx.x == 0) {
             const unsigned long long k = atomicAdd(&p.sched->claimed, 1ull);
@@ -947,51 +1090,63 @@ __global__ void __launch_bounds__(kSqRows) k_sq_step(SqParams p)
         const int2 item = p.items[it];
         const EDesc &D = p.desc[item.x];
         const int hs = D.hs, np = D.npairs;
-        const int b = item.y * kSqRows + threadIdx.x;
+        const int b = item.y * kSqRows + r;
         const bool row = b < hs;
         const long long *__restrict__ T = D.T + (row ? b : 0);
         double y = 0.0;
         for (int q = 0; q < np; ++q) {
             const int n = __ldcg(D.evn + q);
-            const int *__restrict__ ev = D.evl + q * hs;
             long long z = 0;
             if (n >= 0) {
-                int k = 0;
-                for (; k + kSqUnroll <= n; k += kSqUnroll) {
+                const int *__restrict__ ev = D.evl + q * hs;
+                for (int k = threadIdx.x; k < n; k += kSqThreads) sq_ev[k] = __ldcg(ev + k);
+                __syncthreads();
+                for (int k0 = g * kSqUnroll; k0 < n; k0 += kSqGroups * kSqUnroll) {
+                    const int m = min(kSqUnroll, n - k0);
                     long long t[kSqUnroll];
                     int v[kSqUnroll];
 #pragma unroll
                     for (int u = 0; u < kSqUnroll; ++u) {
-                        const int e = __ldcg(ev + k + u);
-                        v[u] = (int)(short)(e & 0xffff);
-                        t[u] = __ldg(T + (size_t)(e >> 16) * hs);
+                        v[u] = 0;
+                        t[u] = 0;
+                        if (u < m) {
+                            const int e = sq_ev[k0 + u];
+                            v[u] = (int)(short)(e & 0xffff);
+                            t[u] = __ldg(T + (size_t)(e >> 16) * hs);
+                        }
                     }
 #pragma unroll
                     for (int u = 0; u < kSqUnroll; ++u) z += (long long)v[u] * t[u];
                 }
-                for (; k < n; ++k) {
-                    const int e = __ldcg(ev + k);
-                    z += (long long)(short)(e & 0xffff) * __ldg(T + (size_t)(e >> 16) * hs);
-                }
             } else {
                 // a delta beyond 16 bits: read the pair's deltas directly
                 const int *__restrict__ dq = D.dP + q * hs;
-                for (int c = 0; c < hs; ++c) {
+                for (int c = g; c < hs; c += kSqGroups) {
                     const int v = __ldcg(dq + c);
                     if (v)
                         z += (long long)v * __ldg(T + (size_t)c * hs);
                 }
             }
-            y = fma(D.pc[q] * D.yscale, (double)z, y);
+            zz[g][r] = z;
+            __syncthreads();
+            if (g == 0) {
+                long long zt = 0;
+#pragma unroll
+                for (int j = 0; j < kSqGroups; ++j) zt += zz[j][r];
+                y = fma(D.pc[q] * D.yscale, (double)zt, y);
+            }
+            __syncthreads();  // the list and the partial sums are reused
         }
-        double part = 0.0;
-        if (row) {
-            D.y[b] = y;
-            const double sv = __ldcg(D.Sb + b);
-            if (sv != 0.0)
-                part = (D.Rq[b] * sv) * (y - D.h[b]);
+        if (g == 0) {
+            double part = 0.0;
+            if (row) {
+                D.y[b] = y;
+                const double sv = __ldcg(D.Sb + b);
+                if (sv != 0.0)
+                    part = (D.Rq[b] * sv) * (y - D.h[b]);
+            }
+            red[r] = part;
         }
-        red[threadIdx.x] = part;
         __syncthreads();
         for (int st = kSqRows / 2; st > 0; st >>= 1) {
             if ((int)threadIdx.x < st)
@@ -1165,13 +1320,15 @@ struct SqTable {
     size_t bytes = 0;
 };
 
-constexpr int kFusedSmemMax = 96 * 1024;  // shared-memory element-pair deltas of one engine
+constexpr int kFusedSmemMax = 160 * 1024;  // dynamic shared memory of a fused step: element-pair deltas, A, Bq
 constexpr int kFusedMaxAtoms = 49152;     // larger engines are split over several CTAs
 
 struct EngineSet {
     std::vector<Slot> slots;
     int fused = 1;         // batched steps use one CTA per engine where it fits
     int fused_smem = 0;    // dynamic shared memory of batched launches
+    int fused_dp_ints = 0; // its layout: element-pair deltas (ints), then A and Bq (fused_bins doubles each)
+    int fused_bins = 0;
     int nsolo = 0;         // items [0, nsolo): tiles of every engine (one-engine steps)
     int nbatch = 0;        // items [nsolo, nsolo + nbatch): the batched work list
     int nfused = 0;        // of which the first nfused are one-CTA-per-engine items
@@ -1311,12 +1468,17 @@ static int refresh(EngineSet *s)
     // batched list: fused engines largest first, then the tiles of the others
     std::vector<int> fused_ids;
     s->fused_smem = 0;
+    s->fused_dp_ints = 0;
+    s->fused_bins = 0;
     for (int id : s->live) {
         const EDesc &D = s->slots[id].d;
-        const long long smem = 4ll * D.npairs * D.hs;
-        if (s->fused && smem <= kFusedSmemMax && D.n <= kFusedMaxAtoms) {
+        const int dp = (D.npairs * D.hs + 3) & ~3, bins = (D.hs + 1) & ~1;
+        const int dpi = std::max(s->fused_dp_ints, dp), bi = std::max(s->fused_bins, bins);
+        if (s->fused && 4ll * dpi + 16ll * bi <= kFusedSmemMax && D.n <= kFusedMaxAtoms) {
             fused_ids.push_back(id);
-            s->fused_smem = std::max(s->fused_smem, (int)smem);
+            s->fused_dp_ints = dpi;
+            s->fused_bins = bi;
+            s->fused_smem = 4 * dpi + 16 * bi;
         }
     }
     std::stable_sort(fused_ids.begin(), fused_ids.end(),
@@ -1341,7 +1503,7 @@ static int refresh(EngineSet *s)
         s->sq_first[id] = (int)s->sq_host.size();
         s->sq_count[id] = D.sqblk;
         for (int k = 0; k < D.sqblk; ++k) s->sq_host.push_back(make_int2(id, k));
-        s->sq_smem = 0;
+        s->sq_smem = std::max(s->sq_smem, 4 * D.hs);
     }
     if ((int)s->sq_host.size() > s->sq_cap) {
         if (s->sq_items) cudaFree(s->sq_items);
@@ -1399,7 +1561,8 @@ static int launch_items(EngineSet *s, const int2 *items, int count, int eval_onl
         grid = count;
     if (grid < 1)
         return FRMC_OK;
-    StepParams p{s->ddesc, items, count, s->tile, eval_only, s->sched};
+    StepParams p{s->ddesc, items, count, s->tile, eval_only, fused ? s->fused_dp_ints : 0,
+                 fused ? s->fused_bins : 0, s->sched};
     if (fused) {
         FRMC_CUDA(cudaFuncSetAttribute(k_engine_step<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem));
         k_engine_step<true><<<grid, s->threads, dyn_smem, st>>>(p);
@@ -1417,10 +1580,10 @@ static int launch_sq(EngineSet *s, int first, int count, cudaStream_t st)
         return FRMC_OK;
     Context *c;
     FRMC_TRY(get_context(&c));
-    int grid = std::min(count, c->sms * 4);
+    int grid = std::min(count, c->sms * 8);
     SqParams p{s->ddesc, s->sq_items + first, count, s->sched + 1};
     FRMC_CUDA(cudaFuncSetAttribute(k_sq_step, cudaFuncAttributeMaxDynamicSharedMemorySize, s->sq_smem));
-    k_sq_step<<<grid, kSqRows, s->sq_smem, st>>>(p);
+    k_sq_step<<<grid, kSqThreads, s->sq_smem, st>>>(p);
     FRMC_CUDA(cudaGetLastError());
     return FRMC_OK;
 }
@@ -1975,6 +2138,10 @@ int frmc_engines_sync(void *handle)
     if (!s)
         return set_error(FRMC_E_ARG, "null handle");
     FRMC_CUDA(cudaStreamSynchronize(s->stream));
+    unsigned status = 0;
+    FRMC_CUDA(cudaMemcpy(&status, &s->sched[0].status, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    if (status)
+        return set_error(FRMC_E_TIMEOUT, "engine step: a bounded device wait gave up (status 0x%x)", status);
     return FRMC_OK;
 }
 

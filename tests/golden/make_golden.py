@@ -142,6 +142,24 @@ def main():
                                              np.zeros(n, np.int32), 1, mn, mx, b, hs, 1)
     out["saturation"] = dict(n=np.int32(n), minD=mn, maxD=mx, bin=b, hs=hs, full_intra=hi, full_inter=he)
 
+    # G2: half-box ties.  Box-coordinate differences of exactly +-0.49999997
+    # (the float just below 0.5), +-0.5 and neighbours, in a cubic box whose
+    # half side 5.005 is a bin edge.  The reference's round()
+    # (pairs_distances.pyx:31-32) adds the float32 HALF_BOX_LENGTH in float32,
+    # where 0.49999997 + 0.5 rounds to 1.0: the difference wraps to
+    # -0.50000003 (d = 5.0050003, bin 501), where exact arithmetic would keep
+    # it (d = 5.0049997, bin 500).
+    h = np.nextafter(F(0.5), F(0))
+    pts = [(0, 0, 0), (h, 0, 0), (0, h, F(0.3)), (F(0.5), F(0.5), 0), (np.nextafter(F(0.5), F(1)), F(0.2), F(0.7)),
+           (np.nextafter(F(1), F(0)), h, F(0.5)), (F(0.25), F(0.25) + h, F(0.25)), (F(0.75), F(0.75), F(0.75) - h)]
+    rng = np.random.default_rng(707)
+    coords = np.concatenate([np.array(pts, F), rng.random((300, 3)).astype(F)]).astype(F)
+    n = coords.shape[0]
+    Lh = F(10.01)
+    hist_case("half_box_pbc", coords, np.diag([Lh, Lh, Lh]).astype(F), True, np.arange(n, dtype=np.int32),
+              (np.arange(n) % 2).astype(np.int32), 2, grid(6.0),
+              [(np.array([0, 1, 5], np.int32), True), (np.array([1, 2, 3], np.int32), False)])
+
     # H: edge sizes: one atom, zero atoms.
     for nn in (0, 1):
         coords = np.zeros((nn, 3), F)
@@ -223,9 +241,14 @@ def main():
     out["transform"] = dict(basis=B, rbasis=rb, real=real, box=bcc.transform_coordinates(rb, real),
                             back=bcc.transform_coordinates(B, bcc.transform_coordinates(rb, real)))
 
+    only = set(sys.argv[1:])  # names of the cases to (re)write; none = all
+    written = 0
     for name, d in out.items():
+        if only and name not in only:
+            continue
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
-    print("wrote %d golden files" % len(out))
+        written += 1
+    print("wrote %d golden files" % written)
 
 
 if __name__ == "__main__":
