@@ -262,31 +262,19 @@ def run_ours(args):
     E = len(systems)
     K, W = args.steps, args.warmup
     plain_steps = args.plain_steps
-    total_steps = W + 3 * K + plain_steps + 64
+    total_steps = W + 3 * K + plain_steps + 8 * len(EngineSet.TUNE_CANDIDATES) + 64
     cap = total_steps
     moves = [translation_moves(np.random.default_rng([seed, 1000 + e]), s.box_coords.shape[0], total_steps, amp)
              for e, s in enumerate(systems)]
     pairs_per_step = float(sum(2 * (s.box_coords.shape[0] - 1) for s in systems))
 
     # autotune the work list (results are identical under every tuning)
-    tune_cands = [(1024, 256, 2), (1024, 512, 1), (2048, 512, 1), (512, 128, 4), (1024, 256, 4), (2048, 256, 2)]
-    best = None
     es = EngineSet(systems, move_cap=cap)
     es.init()
     for e, (a, v, u) in enumerate(moves):
         es.push_moves(e, a, v, u, 0)
-    done = 0
-    for tn in tune_cands:
-        es.set_tune(*tn)
-        es.step(2, graph=False)
-        t0 = time.perf_counter()
-        es.step(6, graph=False)
-        dt = time.perf_counter() - t0
-        done += 8
-        if best is None or dt < best[0]:
-            best = (dt, tn)
+    tune = es.autotune(steps=6, warmup=2)
     es.close()
-    tune = best[1]
 
     # fresh engines for the measurement
     es = EngineSet(systems, move_cap=cap, tune=tune)

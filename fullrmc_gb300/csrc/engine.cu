@@ -1068,7 +1068,7 @@ __device__ void sq_finish(const EDesc &D, int *s_flag, double *s_val)
     }
 }
 
-constexpr int kSqUnroll = 16;  // table loads in flight per thread
+constexpr int kSqUnroll = 8;  // table loads in flight per thread
 
 __global__ void __launch_bounds__(kSqThreads) k_sq_step(SqParams p)
 {
@@ -1096,7 +1096,7 @@ __global__ void __launch_bounds__(kSqThreads) k_sq_step(SqParams p)
         double y = 0.0;
         for (int q = 0; q < np; ++q) {
             const int n = __ldcg(D.evn + q);
-            long long z = 0;
+            long long z = 0, zp = 0, zn = 0;
             if (n >= 0) {
                 const int *__restrict__ ev = D.evl + q * hs;
                 for (int k = threadIdx.x; k < n; k += kSqThreads) sq_ev[k] = __ldcg(ev + k);
@@ -1115,8 +1115,17 @@ __global__ void __launch_bounds__(kSqThreads) k_sq_step(SqParams p)
                             t[u] = __ldg(T + (size_t)(e >> 16) * hs);
                         }
                     }
+                    // deltas are +-1 but for rare coincident pairs, and every
+                    // thread of the CTA sees the same delta: uniform branches
 #pragma unroll
-                    for (int u = 0; u < kSqUnroll; ++u) z += (long long)v[u] * t[u];
+                    for (int u = 0; u < kSqUnroll; ++u) {
+                        if (v[u] == 1)
+                            zp += t[u];
+                        else if (v[u] == -1)
+                            zn += t[u];
+                        else
+                            z += (long long)v[u] * t[u];
+                    }
                 }
             } else {
                 // a delta beyond 16 bits: read the pair's deltas directly
@@ -1127,7 +1136,7 @@ __global__ void __launch_bounds__(kSqThreads) k_sq_step(SqParams p)
                         z += (long long)v * __ldg(T + (size_t)c * hs);
                 }
             }
-            zz[g][r] = z;
+            zz[g][r] = z + (zp - zn);
             __syncthreads();
             if (g == 0) {
                 long long zt = 0;
@@ -1335,7 +1344,7 @@ struct EngineSet {
     std::vector<int> live;        // live engine ids in work-list order
     std::vector<int> item_first;  // per engine id: first item (or -1)
     std::vector<int> item_count;
-    int tile = 1024, threads = 256, ctas_per_sm = 4;
+    int tile = 1024, threads = 512, ctas_per_sm = 1;  // the usual autotuner choice on GB300
     EDesc *ddesc = nullptr;
     int ddesc_cap = 0;
     int2 *items = nullptr;

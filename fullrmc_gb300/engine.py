@@ -414,6 +414,30 @@ class EngineSet:
     def set_mode(self, fused):
         check(load().frmc_engines_set_mode(self.handle, int(bool(fused))))
 
+    TUNE_CANDIDATES = ((1024, 512, 1), (2048, 512, 1), (1024, 384, 1), (1024, 256, 2), (512, 128, 4),
+                       (1024, 256, 4), (2048, 256, 2))
+
+    def autotune(self, candidates=None, steps=6, warmup=2):
+        """Choose the work-list configuration -- atoms per tile of split
+        engines, threads per CTA, CTAs per SM -- with the shortest batched
+        step for the live engines, by timing `steps` steps after `warmup`
+        steps of each candidate, and keep it.  Results do not depend on the
+        choice, but the timed steps advance every chain, so moves for
+        len(candidates) * (warmup + steps) steps must be pushed.  Returns the
+        chosen (tile, threads, ctas_per_sm)."""
+        import time
+        best = None
+        for tn in candidates or self.TUNE_CANDIDATES:
+            self.set_tune(*tn)
+            self.step(warmup, graph=False)
+            t0 = time.perf_counter()
+            self.step(steps, graph=False)
+            dt = time.perf_counter() - t0
+            if best is None or dt < best[0]:
+                best = (dt, tn)
+        self.set_tune(*best[1])
+        return best[1]
+
     def get_tune(self):
         v = [ctypes.c_int() for _ in range(4)]
         check(load().frmc_engines_get_tune(self.handle, *[ctypes.byref(x) for x in v]))
