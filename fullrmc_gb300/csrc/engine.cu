@@ -66,9 +66,33 @@ struct Sched {
 };
 
 struct EMove {
-    int atom;
-    float v[3];
-    float u;
+    int atom;    // the moved atom (the first atom of a moved group)
+    float v[3];  // its real-space displacement (every atom's, for a group translation)
+    float u;     // uniform number of the tolerance test
+};
+
+// Group moves (engines with group > 1; fullrmc's TranslationGenerator and
+// RotationGenerator on molecule groups, Generators/Translations.py,
+// Generators/Rotations.py): the other atoms of the group and the kind of move.
+// A rotation takes every atom x of the group to (x - c) rot + c, c the
+// group's centroid (float32, atoms added in group order, divided by the
+// group size), with row-vector products summed as (x0 r0k + x1 r1k) + x2 r2k.
+constexpr int kMaxGroup = 16;
+struct EGroup {
+    int kind;       // 0: translation by the move's v, 1: rotation
+    float rot[9];   // row-major 3 x 3
+    int atoms[kMaxGroup - 1];
+};
+
+// The moved atoms of the current step, in shared memory.
+struct MovedGroup {
+    int n;
+    int atom[kMaxGroup];
+    int el[kMaxGroup];
+    int mol[kMaxGroup];
+    float o[kMaxGroup][3];   // box coordinates before the move
+    float nw[kMaxGroup][3];  // box coordinates after
+    float nr[kMaxGroup][3];  // real coordinates after
 };
 
 struct EResult {
@@ -114,6 +138,8 @@ struct EDesc {
     int *evl;           // [npairs][hs] this step's non-zero element-pair deltas, per pair
     int *evn;           // [kMaxP] their counts (-1: a delta beyond 16 bits, read dP instead)
     EMove *moves;
+    EGroup *groups;     // [move_cap] (group > 1)
+    int group;          // atoms per move
     EResult *results;
     EState *st;
 };
@@ -172,6 +198,92 @@ __device__ __forceinline__ float3 to_box(const Basis &RB, float x, float y, floa
     r.y = __fadd_rn(__fadd_rn(__fmul_rn(x, RB.b[1]), __fmul_rn(y, RB.b[4])), __fmul_rn(z, RB.b[7]));
     r.z = __fadd_rn(__fadd_rn(__fmul_rn(x, RB.b[2]), __fmul_rn(y, RB.b[5])), __fmul_rn(z, RB.b[8]));
     return r;
+}
+
+// The moved atoms of `step` into shared memory: box coordinates before, real
+// and box coordinates after the move (new box = transform(reciprocal basis,
+// new real), boundary_conditions_collection.pyx:88-110).  All threads of the
+// CTA call it; the caller synchronises before use.  A single atom is done by
+// thread 0 alone.
+__device__ void load_moved_group(const EDesc &D, long long step, MovedGroup &g)
+{
+    const int G = D.group;
+    const EMove &m = D.moves[step % D.move_cap];
+    if (G == 1) {
+        if (threadIdx.x == 0) {
+            const int a = m.atom;
+            const float4 ob = D.box[a];
+            const float4 orl = D.real[a];
+            const float rx = __fadd_rn(orl.x, m.v[0]), ry = __fadd_rn(orl.y, m.v[1]), rz = __fadd_rn(orl.z, m.v[2]);
+            const float3 nw = D.bm == BM_IBC ? make_float3(rx, ry, rz) : to_box(D.RB, rx, ry, rz);
+            g.n = 1;
+            g.atom[0] = a;
+            g.el[0] = __float_as_int(ob.w);
+            g.mol[0] = D.mol[a];
+            g.o[0][0] = ob.x; g.o[0][1] = ob.y; g.o[0][2] = ob.z;
+            g.nw[0][0] = nw.x; g.nw[0][1] = nw.y; g.nw[0][2] = nw.z;
+            g.nr[0][0] = rx; g.nr[0][1] = ry; g.nr[0][2] = rz;
+        }
+        return;
+    }
+    const EGroup &gm = D.groups[step % D.move_cap];
+    const int t = threadIdx.x;
+    if (t < G) {
+        const int a = t == 0 ? m.atom : gm.atoms[t - 1];
+        const float4 ob = D.box[a];
+        const float4 orl = D.real[a];
+        g.atom[t] = a;
+        g.el[t] = __float_as_int(ob.w);
+        g.mol[t] = D.mol[a];
+        g.o[t][0] = ob.x; g.o[t][1] = ob.y; g.o[t][2] = ob.z;
+        g.nr[t][0] = orl.x; g.nr[t][1] = orl.y; g.nr[t][2] = orl.z;
+    }
+    if (t == 0)
+        g.n = G;
+    __syncthreads();
+    __shared__ float s_c[3];
+    const bool rot = gm.kind == 1;
+    if (rot && t == 0) {
+        float cx = g.nr[0][0], cy = g.nr[0][1], cz = g.nr[0][2];
+        for (int k = 1; k < G; ++k) {
+            cx = __fadd_rn(cx, g.nr[k][0]);
+            cy = __fadd_rn(cy, g.nr[k][1]);
+            cz = __fadd_rn(cz, g.nr[k][2]);
+        }
+        const float fg = (float)G;
+        s_c[0] = __fdiv_rn(cx, fg);
+        s_c[1] = __fdiv_rn(cy, fg);
+        s_c[2] = __fdiv_rn(cz, fg);
+    }
+    __syncthreads();
+    if (t < G) {
+        const float x = g.nr[t][0], y = g.nr[t][1], z = g.nr[t][2];
+        float rx, ry, rz;
+        if (rot) {
+            const float *R = gm.rot;
+            const float dx = __fsub_rn(x, s_c[0]), dy = __fsub_rn(y, s_c[1]), dz = __fsub_rn(z, s_c[2]);
+            rx = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, R[0]), __fmul_rn(dy, R[3])), __fmul_rn(dz, R[6])), s_c[0]);
+            ry = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, R[1]), __fmul_rn(dy, R[4])), __fmul_rn(dz, R[7])), s_c[1]);
+            rz = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, R[2]), __fmul_rn(dy, R[5])), __fmul_rn(dz, R[8])), s_c[2]);
+        } else {
+            rx = __fadd_rn(x, m.v[0]);
+            ry = __fadd_rn(y, m.v[1]);
+            rz = __fadd_rn(z, m.v[2]);
+        }
+        const float3 nw = D.bm == BM_IBC ? make_float3(rx, ry, rz) : to_box(D.RB, rx, ry, rz);
+        g.nr[t][0] = rx; g.nr[t][1] = ry; g.nr[t][2] = rz;
+        g.nw[t][0] = nw.x; g.nw[t][1] = nw.y; g.nw[t][2] = nw.z;
+    }
+}
+
+// Commit of an accepted move: the moved atoms' coordinates.
+__device__ void commit_moved_group(const EDesc &D, const MovedGroup &g)
+{
+    for (int t = threadIdx.x; t < g.n; t += blockDim.x) {
+        const int a = g.atom[t];
+        D.box[a] = make_float4(g.nw[t][0], g.nw[t][1], g.nw[t][2], __int_as_float(g.el[t]));
+        D.real[a] = make_float4(g.nr[t][0], g.nr[t][1], g.nr[t][2], 0.0f);
+    }
 }
 
 // Element-pair index and bin of an oriented flat index.  A count past the
@@ -233,7 +345,7 @@ constexpr int kItemUnroll = 4;
 // touched list (one list reservation per warp and column).  Coordinates of
 // kItemUnroll columns are loaded before any is used.
 template <int BM>
-__device__ void item_delta(const EDesc &Dg, int tile, int atom, float3 o, float3 nw, int ela, int mola, int t)
+__device__ void item_delta(const EDesc &Dg, int tile, const MovedGroup &g, int t)
 {
     const ColView D = col_view(Dg);
     int *__restrict__ delta = Dg.delta;
@@ -241,53 +353,61 @@ __device__ void item_delta(const EDesc &Dg, int tile, int atom, float3 o, float3
     unsigned *tcount = &Dg.st->tcount;
     const int j0 = t * tile;
     const int j1 = min(D.n, j0 + tile);
-    const int arow = ela * D.ne;
+    const int G = g.n;
     const unsigned lane = threadIdx.x & 31u;
     const unsigned lt = (1u << lane) - 1u;
     for (int jb = j0; jb < j1; jb += kItemUnroll * blockDim.x) {
         float4 c[kItemUnroll];
         int mj[kItemUnroll];
+        bool valid[kItemUnroll];
 #pragma unroll
         for (int u = 0; u < kItemUnroll; ++u) {
             const int j = jb + u * blockDim.x + threadIdx.x;
             c[u] = j < j1 ? D.box[j] : make_float4(0.f, 0.f, 0.f, 0.f);
             mj[u] = j < j1 ? D.mol[j] : 0;
+            bool ok = j < j1;
+            for (int q = 0; q < G; ++q) ok &= j != g.atom[q];
+            valid[u] = ok;
         }
-        float s0[kItemUnroll], s1[kItemUnroll];
+        for (int gi = 0; gi < G; ++gi) {
+            const float3 o = make_float3(g.o[gi][0], g.o[gi][1], g.o[gi][2]);
+            const float3 nw = make_float3(g.nw[gi][0], g.nw[gi][1], g.nw[gi][2]);
+            const int ela = g.el[gi], mola = g.mol[gi], arow = ela * D.ne;
+            float s0[kItemUnroll], s1[kItemUnroll];
 #pragma unroll
-        for (int u = 0; u < kItemUnroll; ++u) {
-            s0[u] = pair_s<BM>(o.x, o.y, o.z, c[u].x, c[u].y, c[u].z, D.B);
-            s1[u] = pair_s<BM>(nw.x, nw.y, nw.z, c[u].x, c[u].y, c[u].z, D.B);
-        }
-#pragma unroll
-        for (int u = 0; u < kItemUnroll; ++u) {
-            const int j = jb + u * blockDim.x + threadIdx.x;
-            int f0 = -1, f1 = -1, half = 0, b0 = 0, b1 = 0, elj = 0;
-            column_bins(D, s0[u], s1[u], j < j1 && j != atom, c[u], mj[u], arow, mola, f0, f1, half, b0, b1, elj);
-            const unsigned m0 = __ballot_sync(0xffffffffu, f0 >= 0);
-            const unsigned m1 = __ballot_sync(0xffffffffu, f1 >= 0);
-            if ((m0 | m1) == 0u)
-                continue;
-            unsigned base = 0;
-            if (lane == 0)
-                base = atomicAdd(tcount, __popc(m0) + __popc(m1));
-            base = __shfl_sync(0xffffffffu, base, 0);
-            unsigned pos = base + __popc(m0 & lt) + __popc(m1 & lt);
-            if (f0 >= 0) {
-                atomicSub(delta + half + f0, 1);
-                D.tlist[pos++] = half + f0;
-                int p, b;
-                pair_of_flat(D, f0, ela, elj, b0, p, b);
-                if (p >= 0)
-                    atomicSub(dP + p * D.hs + b, 1);
+            for (int u = 0; u < kItemUnroll; ++u) {
+                s0[u] = pair_s<BM>(o.x, o.y, o.z, c[u].x, c[u].y, c[u].z, D.B);
+                s1[u] = pair_s<BM>(nw.x, nw.y, nw.z, c[u].x, c[u].y, c[u].z, D.B);
             }
-            if (f1 >= 0) {
-                atomicAdd(delta + half + f1, 1);
-                D.tlist[pos] = half + f1;
-                int p, b;
-                pair_of_flat(D, f1, ela, elj, b1, p, b);
-                if (p >= 0)
-                    atomicAdd(dP + p * D.hs + b, 1);
+#pragma unroll
+            for (int u = 0; u < kItemUnroll; ++u) {
+                int f0 = -1, f1 = -1, half = 0, b0 = 0, b1 = 0, elj = 0;
+                column_bins(D, s0[u], s1[u], valid[u], c[u], mj[u], arow, mola, f0, f1, half, b0, b1, elj);
+                const unsigned m0 = __ballot_sync(0xffffffffu, f0 >= 0);
+                const unsigned m1 = __ballot_sync(0xffffffffu, f1 >= 0);
+                if ((m0 | m1) == 0u)
+                    continue;
+                unsigned base = 0;
+                if (lane == 0)
+                    base = atomicAdd(tcount, __popc(m0) + __popc(m1));
+                base = __shfl_sync(0xffffffffu, base, 0);
+                unsigned pos = base + __popc(m0 & lt) + __popc(m1 & lt);
+                if (f0 >= 0) {
+                    atomicSub(delta + half + f0, 1);
+                    D.tlist[pos++] = half + f0;
+                    int p, b;
+                    pair_of_flat(D, f0, ela, elj, b0, p, b);
+                    if (p >= 0)
+                        atomicSub(dP + p * D.hs + b, 1);
+                }
+                if (f1 >= 0) {
+                    atomicAdd(delta + half + f1, 1);
+                    D.tlist[pos] = half + f1;
+                    int p, b;
+                    pair_of_flat(D, f1, ela, elj, b1, p, b);
+                    if (p >= 0)
+                        atomicAdd(dP + p * D.hs + b, 1);
+                }
             }
         }
     }
@@ -555,11 +675,106 @@ __device__ double eval_delta(const EDesc &Dg, int *dP, const double *Ab, const d
     return total;
 }
 
+// Pairs inside a moved group.  fullrmc's before/after-move data is M - F
+// (PairDistributionConstraints.py:1044-1129): M counts each group atom
+// against all atoms, so a pair (a, b) of the group (a before b in group
+// order) appears at [el(a)][el(b)] and [el(b)][el(a)], and F counts the group
+// alone once, at [el(a)][el(b)]: one count per pair remains, at [el(b)][el(a)].
+// Pair t of the G(G-1)/2 pairs gives its before/after bins like a column.
+template <int BM, class V>
+__device__ __forceinline__ void group_pair_bins(const V &D, const MovedGroup &g, int t, int &f0, int &f1, int &half,
+                                                int &b0, int &b1, int &ela, int &elj)
+{
+    int b = 1, a = t;
+    while (a >= b) {
+        a -= b;
+        ++b;
+    }
+    const float s0 = pair_s<BM>(g.o[b][0], g.o[b][1], g.o[b][2], g.o[a][0], g.o[a][1], g.o[a][2], D.B);
+    const float s1 = pair_s<BM>(g.nw[b][0], g.nw[b][1], g.nw[b][2], g.nw[a][0], g.nw[a][1], g.nw[a][2], D.B);
+    ela = g.el[b];
+    half = b0 = b1 = elj = 0;
+    column_bins(D, s0, s1, true, make_float4(0.f, 0.f, 0.f, __int_as_float(g.el[a])), g.mol[a], ela * D.ne, g.mol[b],
+                f0, f1, half, b0, b1, elj);
+}
+
+// The fused path's share of the group's internal pairs (shared-memory deltas).
+template <int BM>
+__device__ void fused_group_internal(const EDesc &Dg, int *sdP, unsigned *s_tcount, const MovedGroup &g)
+{
+    const ColView D = col_view(Dg);
+    const int npair = g.n * (g.n - 1) / 2;
+    for (int t = threadIdx.x; t < npair; t += blockDim.x) {
+        int f0, f1, half, b0, b1, ela, elj;
+        group_pair_bins<BM>(D, g, t, f0, f1, half, b0, b1, ela, elj);
+        const unsigned cnt = (f0 >= 0) + (f1 >= 0);
+        if (!cnt)
+            continue;
+        unsigned pos = atomicAdd(s_tcount, cnt);
+        if (f0 >= 0) {
+            D.tlist[pos++] = (half + f0) << 1;
+            int p, bb;
+            pair_of_flat(D, f0, ela, elj, b0, p, bb);
+            if (p >= 0)
+                atomicSub(sdP + p * D.hs + bb, 1);
+        }
+        if (f1 >= 0) {
+            D.tlist[pos] = ((half + f1) << 1) | 1;
+            int p, bb;
+            pair_of_flat(D, f1, ela, elj, b1, p, bb);
+            if (p >= 0)
+                atomicAdd(sdP + p * D.hs + bb, 1);
+        }
+    }
+}
+
+// The split path's share (global deltas; run by the CTA that evaluates).
+template <int BM>
+__device__ void split_group_internal(const EDesc &Dg, const MovedGroup &g)
+{
+    const ColView D = col_view(Dg);
+    const int npair = g.n * (g.n - 1) / 2;
+    for (int t = threadIdx.x; t < npair; t += blockDim.x) {
+        int f0, f1, half, b0, b1, ela, elj;
+        group_pair_bins<BM>(D, g, t, f0, f1, half, b0, b1, ela, elj);
+        const unsigned cnt = (f0 >= 0) + (f1 >= 0);
+        if (!cnt)
+            continue;
+        unsigned pos = atomicAdd(&Dg.st->tcount, cnt);
+        if (f0 >= 0) {
+            atomicSub(Dg.delta + half + f0, 1);
+            D.tlist[pos++] = half + f0;
+            int p, bb;
+            pair_of_flat(D, f0, ela, elj, b0, p, bb);
+            if (p >= 0)
+                atomicSub(Dg.dP + p * D.hs + bb, 1);
+        }
+        if (f1 >= 0) {
+            atomicAdd(Dg.delta + half + f1, 1);
+            D.tlist[pos] = half + f1;
+            int p, bb;
+            pair_of_flat(D, f1, ela, elj, b1, p, bb);
+            if (p >= 0)
+                atomicAdd(Dg.dP + p * D.hs + bb, 1);
+        }
+    }
+}
+
 constexpr int kCommitUnroll = 4;
 
-__device__ void finish_engine(const EDesc &D, int atom, float3 nw, float4 nreal, double *red, double *cb,
-                              double *sbs, int *sbin, int *s_nchg, double *coef, int *s_flag)
+__device__ void finish_engine(const EDesc &D, const MovedGroup &g, double *red, double *cb, double *sbs, int *sbin,
+                              int *s_nchg, double *coef, int *s_flag)
 {
+    if (g.n > 1) {
+        switch (D.bm) {
+        case BM_IBC: split_group_internal<BM_IBC>(D, g); break;
+        case BM_DIAG: split_group_internal<BM_DIAG>(D, g); break;
+        case BM_XYTRI: split_group_internal<BM_XYTRI>(D, g); break;
+        case BM_LOWER: split_group_internal<BM_LOWER>(D, g); break;
+        default: split_group_internal<BM_GENERAL>(D, g); break;
+        }
+        __syncthreads();
+    }
     const double dsd = eval_delta<false>(D, D.dP, D.A, D.Bq, red, cb, sbs, sbin, s_nchg, coef);
     if (D.sq) {
         // the S(Q) kernel evaluates its term, decides and commits
@@ -615,17 +830,16 @@ __device__ void finish_engine(const EDesc &D, int atom, float3 nw, float4 nreal,
             }
         }
     }
+    if (accept)
+        commit_moved_group(D, g);
     __syncthreads();
     if (threadIdx.x == 0) {
         EState &S = *D.st;
         EResult &r = D.results[S.step % D.move_cap];
         r.chi2_new = chi2_new;
         r.accepted = accept ? 1 : 0;
-        r.atom = atom;
+        r.atom = g.atom[0];
         if (accept) {
-            const float4 ob = D.box[atom];
-            D.box[atom] = make_float4(nw.x, nw.y, nw.z, ob.w);
-            D.real[atom] = nreal;
             S.chi2 = chi2_new;
             S.sd = sd_new;
             S.accepted += 1;
@@ -643,16 +857,17 @@ __device__ void finish_engine(const EDesc &D, int atom, float3 nw, float4 nreal,
 // touches the engine during the step, so there is no cross-CTA hand-off.
 // Columns of the fused path.  Batches of kItemUnroll * blockDim columns are
 // software-pipelined: the next batch's coordinates are loaded before the
-// current batch is binned, and each warp reserves the batch's touched-list
-// entries with one shared-memory atomic.
-template <int BM>
-__device__ void fused_columns(const EDesc &Dg, int *sdP, unsigned *s_tcount, int atom, float3 o, float3 nw, int ela,
-                              int mola)
+// current batch is binned against each moved atom, and each warp reserves the
+// batch's touched-list entries with one shared-memory atomic.  Columns that
+// belong to the moved group are left to group_internal (fullrmc's M - F).
+template <int BM, bool GROUP>
+__device__ void fused_columns(const EDesc &Dg, int *sdP, unsigned *s_tcount, const MovedGroup &g)
 {
     const ColView D = col_view(Dg);
-    const int arow = ela * D.ne;
     const unsigned lane = threadIdx.x & 31u;
     const int step = kItemUnroll * blockDim.x;
+    const int G = GROUP ? g.n : 1;
+    const int atom0 = g.atom[0];
     float4 c[kItemUnroll];
     int mj[kItemUnroll];
 #pragma unroll
@@ -670,51 +885,64 @@ __device__ void fused_columns(const EDesc &Dg, int *sdP, unsigned *s_tcount, int
             cn[u] = j < D.n ? D.box[j] : make_float4(0.f, 0.f, 0.f, 0.f);
             mn[u] = j < D.n ? D.mol[j] : 0;
         }
-        int f0[kItemUnroll], f1[kItemUnroll], half[kItemUnroll], b0[kItemUnroll], b1[kItemUnroll],
-            elj[kItemUnroll];
-        float s0[kItemUnroll], s1[kItemUnroll];
-#pragma unroll
-        for (int u = 0; u < kItemUnroll; ++u) {
-            s0[u] = pair_s<BM>(o.x, o.y, o.z, c[u].x, c[u].y, c[u].z, D.B);
-            s1[u] = pair_s<BM>(nw.x, nw.y, nw.z, c[u].x, c[u].y, c[u].z, D.B);
-        }
-        unsigned mine = 0;
+        bool valid[kItemUnroll];
 #pragma unroll
         for (int u = 0; u < kItemUnroll; ++u) {
             const int j = jb + u * blockDim.x + threadIdx.x;
-            half[u] = b0[u] = b1[u] = elj[u] = 0;
-            column_bins(D, s0[u], s1[u], j < D.n && j != atom, c[u], mj[u], arow, mola, f0[u], f1[u], half[u], b0[u],
-                        b1[u], elj[u]);
-            mine += (f0[u] >= 0) + (f1[u] >= 0);
+            bool ok = j < D.n && j != atom0;
+            if (GROUP)
+                for (int t = 1; t < G; ++t) ok &= j != g.atom[t];
+            valid[u] = ok;
         }
-        unsigned incl = mine;
-#pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-            const unsigned v = __shfl_up_sync(0xffffffffu, incl, off);
-            if (lane >= (unsigned)off) incl += v;
-        }
-        const unsigned tot = __shfl_sync(0xffffffffu, incl, 31);
-        if (tot) {
-            unsigned base = 0;
-            if (lane == 31)
-                base = atomicAdd(s_tcount, tot);
-            base = __shfl_sync(0xffffffffu, base, 31);
-            unsigned pos = base + incl - mine;
+        for (int gi = 0; gi < G; ++gi) {
+            const float3 o = make_float3(g.o[gi][0], g.o[gi][1], g.o[gi][2]);
+            const float3 nw = make_float3(g.nw[gi][0], g.nw[gi][1], g.nw[gi][2]);
+            const int ela = g.el[gi], mola = g.mol[gi], arow = ela * D.ne;
+            int f0[kItemUnroll], f1[kItemUnroll], half[kItemUnroll], b0[kItemUnroll], b1[kItemUnroll],
+                elj[kItemUnroll];
+            float s0[kItemUnroll], s1[kItemUnroll];
 #pragma unroll
             for (int u = 0; u < kItemUnroll; ++u) {
-                if (f0[u] >= 0) {
-                    D.tlist[pos++] = (half[u] + f0[u]) << 1;
-                    int p, b;
-                    pair_of_flat(D, f0[u], ela, elj[u], b0[u], p, b);
-                    if (p >= 0)
-                        atomicSub(sdP + p * D.hs + b, 1);
-                }
-                if (f1[u] >= 0) {
-                    D.tlist[pos++] = ((half[u] + f1[u]) << 1) | 1;
-                    int p, b;
-                    pair_of_flat(D, f1[u], ela, elj[u], b1[u], p, b);
-                    if (p >= 0)
-                        atomicAdd(sdP + p * D.hs + b, 1);
+                s0[u] = pair_s<BM>(o.x, o.y, o.z, c[u].x, c[u].y, c[u].z, D.B);
+                s1[u] = pair_s<BM>(nw.x, nw.y, nw.z, c[u].x, c[u].y, c[u].z, D.B);
+            }
+            unsigned mine = 0;
+#pragma unroll
+            for (int u = 0; u < kItemUnroll; ++u) {
+                half[u] = b0[u] = b1[u] = elj[u] = 0;
+                column_bins(D, s0[u], s1[u], valid[u], c[u], mj[u], arow, mola, f0[u], f1[u], half[u], b0[u], b1[u],
+                            elj[u]);
+                mine += (f0[u] >= 0) + (f1[u] >= 0);
+            }
+            unsigned incl = mine;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const unsigned v = __shfl_up_sync(0xffffffffu, incl, off);
+                if (lane >= (unsigned)off) incl += v;
+            }
+            const unsigned tot = __shfl_sync(0xffffffffu, incl, 31);
+            if (tot) {
+                unsigned base = 0;
+                if (lane == 31)
+                    base = atomicAdd(s_tcount, tot);
+                base = __shfl_sync(0xffffffffu, base, 31);
+                unsigned pos = base + incl - mine;
+#pragma unroll
+                for (int u = 0; u < kItemUnroll; ++u) {
+                    if (f0[u] >= 0) {
+                        D.tlist[pos++] = (half[u] + f0[u]) << 1;
+                        int p, b;
+                        pair_of_flat(D, f0[u], ela, elj[u], b0[u], p, b);
+                        if (p >= 0)
+                            atomicSub(sdP + p * D.hs + b, 1);
+                    }
+                    if (f1[u] >= 0) {
+                        D.tlist[pos++] = ((half[u] + f1[u]) << 1) | 1;
+                        int p, b;
+                        pair_of_flat(D, f1[u], ela, elj[u], b1[u], p, b);
+                        if (p >= 0)
+                            atomicAdd(sdP + p * D.hs + b, 1);
+                    }
                 }
             }
         }
@@ -730,7 +958,7 @@ __device__ void fused_columns(const EDesc &Dg, int *sdP, unsigned *s_tcount, int
 // `bar` while the columns run; parity = this CTA's count of fused items mod 2.
 __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, uint64_t *bar, uint32_t parity,
                              uint32_t *status, double *red, double *cb, double *sbs, int *sbin, int *s_nchg,
-                             double *coef, int *s_flag, unsigned *s_tcount, float *s_mv, int *s_mi)
+                             double *coef, int *s_flag, unsigned *s_tcount, MovedGroup &g)
 {
     if (threadIdx.x == 0) {
         // the previous item's reads of sA / sBq are ordered before this
@@ -740,34 +968,39 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, 
         mbar_arrive_expect_tx(bar, 2 * bytes);
         bulk_g2s(sA, D.A, bytes, bar);
         bulk_g2s(sBq, D.Bq, bytes, bar);
-        const long long step = D.st->step;
-        const EMove m = D.moves[step % D.move_cap];
-        const float4 ob = D.box[m.atom];
-        const float4 orl = D.real[m.atom];
-        const float rx = __fadd_rn(orl.x, m.v[0]), ry = __fadd_rn(orl.y, m.v[1]), rz = __fadd_rn(orl.z, m.v[2]);
-        const float3 nw = D.bm == BM_IBC ? make_float3(rx, ry, rz) : to_box(D.RB, rx, ry, rz);
-        s_mv[0] = ob.x; s_mv[1] = ob.y; s_mv[2] = ob.z;
-        s_mv[3] = nw.x; s_mv[4] = nw.y; s_mv[5] = nw.z;
-        s_mv[6] = rx; s_mv[7] = ry; s_mv[8] = rz;
-        s_mi[0] = m.atom;
-        s_mi[1] = __float_as_int(ob.w);
-        s_mi[2] = D.mol[m.atom];
         *s_tcount = 0u;
     }
+    load_moved_group(D, D.st->step, g);
     const int np = D.npairs;
     const int nph = np * D.hs;
     for (int k = threadIdx.x; k < nph; k += blockDim.x) sdP[k] = 0;
     for (int q = threadIdx.x; q < np; q += blockDim.x) coef[q] = D.pc[q];
     __syncthreads();
-    const int atom = s_mi[0], ela = s_mi[1], mola = s_mi[2];
-    const float3 o = make_float3(s_mv[0], s_mv[1], s_mv[2]);
-    const float3 nw = make_float3(s_mv[3], s_mv[4], s_mv[5]);
-    switch (D.bm) {
-    case BM_IBC: fused_columns<BM_IBC>(D, sdP, s_tcount, atom, o, nw, ela, mola); break;
-    case BM_DIAG: fused_columns<BM_DIAG>(D, sdP, s_tcount, atom, o, nw, ela, mola); break;
-    case BM_XYTRI: fused_columns<BM_XYTRI>(D, sdP, s_tcount, atom, o, nw, ela, mola); break;
-    case BM_LOWER: fused_columns<BM_LOWER>(D, sdP, s_tcount, atom, o, nw, ela, mola); break;
-    default: fused_columns<BM_GENERAL>(D, sdP, s_tcount, atom, o, nw, ela, mola); break;
+    if (g.n == 1) {
+        switch (D.bm) {
+        case BM_IBC: fused_columns<BM_IBC, false>(D, sdP, s_tcount, g); break;
+        case BM_DIAG: fused_columns<BM_DIAG, false>(D, sdP, s_tcount, g); break;
+        case BM_XYTRI: fused_columns<BM_XYTRI, false>(D, sdP, s_tcount, g); break;
+        case BM_LOWER: fused_columns<BM_LOWER, false>(D, sdP, s_tcount, g); break;
+        default: fused_columns<BM_GENERAL, false>(D, sdP, s_tcount, g); break;
+        }
+    } else {
+        switch (D.bm) {
+        case BM_IBC: fused_columns<BM_IBC, true>(D, sdP, s_tcount, g); break;
+        case BM_DIAG: fused_columns<BM_DIAG, true>(D, sdP, s_tcount, g); break;
+        case BM_XYTRI: fused_columns<BM_XYTRI, true>(D, sdP, s_tcount, g); break;
+        case BM_LOWER: fused_columns<BM_LOWER, true>(D, sdP, s_tcount, g); break;
+        default: fused_columns<BM_GENERAL, true>(D, sdP, s_tcount, g); break;
+        }
+    }
+    if (g.n > 1) {
+        switch (D.bm) {
+        case BM_IBC: fused_group_internal<BM_IBC>(D, sdP, s_tcount, g); break;
+        case BM_DIAG: fused_group_internal<BM_DIAG>(D, sdP, s_tcount, g); break;
+        case BM_XYTRI: fused_group_internal<BM_XYTRI>(D, sdP, s_tcount, g); break;
+        case BM_LOWER: fused_group_internal<BM_LOWER>(D, sdP, s_tcount, g); break;
+        default: fused_group_internal<BM_GENERAL>(D, sdP, s_tcount, g); break;
+        }
     }
     __syncthreads();
     mbar_wait(bar, parity, status);
@@ -815,6 +1048,7 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, 
                 Bq[b] = fma(sA[b], sbs[k], sBq[b]);
             }
         }
+        commit_moved_group(D, g);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -822,10 +1056,8 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, 
         EResult &r = D.results[S.step % D.move_cap];
         r.chi2_new = chi2_new;
         r.accepted = accept ? 1 : 0;
-        r.atom = atom;
+        r.atom = g.atom[0];
         if (accept) {
-            D.box[atom] = make_float4(nw.x, nw.y, nw.z, __int_as_float(s_mi[1]));
-            D.real[atom] = make_float4(s_mv[6], s_mv[7], s_mv[8], 0.0f);
             S.chi2 = chi2_new;
             S.sd = sd_new;
             S.accepted += 1;
@@ -845,8 +1077,7 @@ __global__ void __launch_bounds__(kMaxEngineThreads, 1) k_engine_step(StepParams
     __shared__ int sbin[kChunk];
     __shared__ int s_nchg;
     __shared__ double coef[64];
-    __shared__ float s_mv[9];
-    __shared__ int s_mi[3];
+    __shared__ MovedGroup s_group;
     __shared__ unsigned s_tcount;
     __shared__ int s_last, s_flag, s_item;
     __shared__ __align__(8) uint64_t s_bar;
@@ -878,7 +1109,7 @@ __global__ void __launch_bounds__(kMaxEngineThreads, 1) k_engine_step(StepParams
         const EDesc &D = p.desc[item.x];
         if (FUSED) {
             engine_fused(D, sdP, sA, sBq, &s_bar, fused_items & 1u, &p.sched->status, red, cb, sbs, sbin, &s_nchg,
-                         coef, &s_flag, &s_tcount, s_mv, s_mi);
+                         coef, &s_flag, &s_tcount, s_group);
             ++fused_items;
             __syncthreads();
             continue;
@@ -894,24 +1125,14 @@ __global__ void __launch_bounds__(kMaxEngineThreads, 1) k_engine_step(StepParams
             __syncthreads();
             continue;
         }
-        const long long step = D.st->step;
-        const EMove m = D.moves[step % D.move_cap];
-        const int atom = m.atom;
-        const float4 ob = D.box[atom];
-        const float4 orl = D.real[atom];
-        const float4 nreal =
-            make_float4(__fadd_rn(orl.x, m.v[0]), __fadd_rn(orl.y, m.v[1]), __fadd_rn(orl.z, m.v[2]), 0.0f);
-        const float3 nw =
-            D.bm == BM_IBC ? make_float3(nreal.x, nreal.y, nreal.z) : to_box(D.RB, nreal.x, nreal.y, nreal.z);
-        const float3 o = make_float3(ob.x, ob.y, ob.z);
-        const int ela = __float_as_int(ob.w);
-        const int mola = D.mol[atom];
+        load_moved_group(D, D.st->step, s_group);
+        __syncthreads();
         switch (D.bm) {
-        case BM_IBC: item_delta<BM_IBC>(D, p.tile, atom, o, nw, ela, mola, item.y); break;
-        case BM_DIAG: item_delta<BM_DIAG>(D, p.tile, atom, o, nw, ela, mola, item.y); break;
-        case BM_XYTRI: item_delta<BM_XYTRI>(D, p.tile, atom, o, nw, ela, mola, item.y); break;
-        case BM_LOWER: item_delta<BM_LOWER>(D, p.tile, atom, o, nw, ela, mola, item.y); break;
-        default: item_delta<BM_GENERAL>(D, p.tile, atom, o, nw, ela, mola, item.y); break;
+        case BM_IBC: item_delta<BM_IBC>(D, p.tile, s_group, item.y); break;
+        case BM_DIAG: item_delta<BM_DIAG>(D, p.tile, s_group, item.y); break;
+        case BM_XYTRI: item_delta<BM_XYTRI>(D, p.tile, s_group, item.y); break;
+        case BM_LOWER: item_delta<BM_LOWER>(D, p.tile, s_group, item.y); break;
+        default: item_delta<BM_GENERAL>(D, p.tile, s_group, item.y); break;
         }
         // Release: the barrier orders every thread's delta atomics and
         // touched-list stores before thread 0's gpu-scope fence, which is
@@ -925,7 +1146,7 @@ __global__ void __launch_bounds__(kMaxEngineThreads, 1) k_engine_step(StepParams
         __syncthreads();
         if (s_last) {
             __threadfence();
-            finish_engine(D, atom, nw, nreal, red, cb, sbs, sbin, &s_nchg, coef, &s_flag);
+            finish_engine(D, s_group, red, cb, sbs, sbin, &s_nchg, coef, &s_flag);
         }
         __syncthreads();
     }
@@ -996,8 +1217,9 @@ struct SqParams {
     Sched *sched;
 };
 
-__device__ void sq_finish(const EDesc &D, int *s_flag, double *s_val)
+__device__ void sq_finish(const EDesc &D, int *s_flag, double *s_val, MovedGroup &g)
 {
+    load_moved_group(D, D.st->step, g);
     if (threadIdx.x == 0) {
         double dsq = 0.0;
         for (int k = 0; k < D.sqblk; ++k) dsq += __ldcg(D.sqpart + k);
@@ -1040,22 +1262,16 @@ __device__ void sq_finish(const EDesc &D, int *s_flag, double *s_val)
                 D.Bq[b] = fma(-2.0 * D.A[b], sv, D.Bq[b]);
             D.h[b] = fma(-2.0, __ldcg(D.y + b), D.h[b]);
         }
+        commit_moved_group(D, g);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         EState &S = *D.st;
-        const EMove m = D.moves[S.step % D.move_cap];
         EResult &r = D.results[S.step % D.move_cap];
         r.chi2_new = s_val[0];
         r.accepted = accept ? 1 : 0;
-        r.atom = m.atom;
+        r.atom = g.atom[0];
         if (accept) {
-            const float4 ob = D.box[m.atom];
-            const float4 orl = D.real[m.atom];
-            const float rx = __fadd_rn(orl.x, m.v[0]), ry = __fadd_rn(orl.y, m.v[1]), rz = __fadd_rn(orl.z, m.v[2]);
-            const float3 nw = D.bm == BM_IBC ? make_float3(rx, ry, rz) : to_box(D.RB, rx, ry, rz);
-            D.box[m.atom] = make_float4(nw.x, nw.y, nw.z, ob.w);
-            D.real[m.atom] = make_float4(rx, ry, rz, 0.0f);
             S.chi2 = s_val[0];
             S.sd = s_val[1];
             S.sd_sq = s_val[2];
@@ -1077,6 +1293,7 @@ __global__ void __launch_bounds__(kSqThreads) k_sq_step(SqParams p)
     __shared__ double red[kSqRows];
     __shared__ double s_val[3];
     __shared__ int s_item, s_last, s_flag;
+    __shared__ MovedGroup s_group;
     const int r = threadIdx.x % kSqRows, g = threadIdx.x / kSqRows;
     for (;;) {
         if (threadIdx.x == 0) {
@@ -1172,7 +1389,7 @@ __global__ void __launch_bounds__(kSqThreads) k_sq_step(SqParams p)
         __syncthreads();
         if (s_last) {
             __threadfence();
-            sq_finish(D, &s_flag, s_val);
+            sq_finish(D, &s_flag, s_val, s_group);
         }
         __syncthreads();
     }
@@ -1373,8 +1590,10 @@ static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct BlobLayout {
     size_t box, real, mol, counts, delta, rfac, invvol, expd, dw, pc, pi, pj, dP, pidx, tlist, R, A, Bq, Sb, moves,
-        results, st, Rq, rfacq, sqexp, h, y, sqpart, sqv, evl, evn, total;
+        results, st, Rq, rfacq, sqexp, h, y, sqpart, sqv, evl, evn, groups, total;
 };
+
+static int spec_group(const frmc_engine_spec &sp) { return sp.group_size > 1 ? sp.group_size : 1; }
 
 static BlobLayout blob_layout(const frmc_engine_spec &sp)
 {
@@ -1400,7 +1619,8 @@ static BlobLayout blob_layout(const frmc_engine_spec &sp)
     L.pj = take(4 * (size_t)sp.npairs);
     L.dP = take(4 * (size_t)sp.npairs * hs);
     L.pidx = take(4 * (size_t)sp.ne * sp.ne);
-    L.tlist = take(4 * (2 * n + 8));
+    const size_t G = spec_group(sp);
+    L.tlist = take(4 * (2 * G * n + G * G + 8));
     L.R = take(8 * hs);
     L.A = take(8 * hs);
     L.Bq = take(8 * hs);
@@ -1419,6 +1639,7 @@ static BlobLayout blob_layout(const frmc_engine_spec &sp)
     L.sqv = take(8 * nq);
     L.evl = take(sq ? 4 * (size_t)sp.npairs * hs : 0);
     L.evn = take(sq ? 4 * 16 : 0);
+    L.groups = take(G > 1 ? sizeof(EGroup) * (size_t)sp.move_cap : 0);
     L.total = off;
     return L;
 }
@@ -1429,6 +1650,8 @@ static int check_spec(const frmc_engine_spec &sp)
         !sp.real_coords || !sp.el || !sp.mol || !sp.basis || !sp.rbasis || !sp.pair_i || !sp.pair_j ||
         !sp.pair_coef || !sp.rfac || !sp.inv_shell_volume || !sp.experimental || !(sp.variance_squared > 0))
         return set_error(FRMC_E_ARG, "engine spec: missing or invalid field");
+    if (sp.group_size < 0 || sp.group_size > kMaxGroup || spec_group(sp) > sp.n)
+        return set_error(FRMC_E_ARG, "engine spec: group_size must be in [1, %d] and at most n", kMaxGroup);
     if ((double)sp.ne * sp.ne * sp.hs > 2.0e8)
         return set_error(FRMC_E_ARG, "engine spec: histogram too large (ne*ne*hs must stay below 2e8)");
     if (sp.npairs > 64)
@@ -1730,6 +1953,8 @@ static int add_engine(EngineSet *s, const frmc_engine_spec &sp, int *out_id)
     D.Bq = (double *)(b + L.Bq);
     D.Sb = (double *)(b + L.Sb);
     D.moves = (EMove *)(b + L.moves);
+    D.group = spec_group(sp);
+    D.groups = D.group > 1 ? (EGroup *)(b + L.groups) : nullptr;
     D.results = (EResult *)(b + L.results);
     D.st = (EState *)(b + L.st);
     std::vector<double> Rqt;
@@ -1804,6 +2029,8 @@ static int add_engine(EngineSet *s, const frmc_engine_spec &sp, int *out_id)
             ce = cudaMemsetAsync(D.dP, 0, 4 * (size_t)sp.npairs * sp.hs, s->stream);
         if (ce == cudaSuccess)
             ce = cudaMemsetAsync(D.results, 0, sizeof(EResult) * sp.move_cap, s->stream);
+        if (ce == cudaSuccess && D.groups)
+            ce = cudaMemsetAsync(D.groups, 0, sizeof(EGroup) * sp.move_cap, s->stream);
         if (ce == cudaSuccess)
             ce = cudaStreamSynchronize(s->stream);
         if (ce != cudaSuccess)
@@ -2014,6 +2241,9 @@ int frmc_engines_push_moves(void *handle, int32_t e, const int32_t *atoms, const
     if (!s || !valid_id(s, e) || count < 0 || first_step < 0 || from_device)
         return set_error(FRMC_E_ARG, "push_moves: invalid arguments");
     const EDesc &D = s->slots[e].d;
+    if (D.group > 1)
+        return set_error(FRMC_E_ARG, "push_moves: engine %d moves groups of %d atoms (frmc_engines_push_group_moves)",
+                         e, D.group);
     if (count > D.move_cap)
         return set_error(FRMC_E_ARG, "push_moves: %d moves exceed the ring of %d", count, D.move_cap);
     for (int k = 0; k < count; ++k)
@@ -2033,6 +2263,62 @@ int frmc_engines_push_moves(void *handle, int32_t e, const int32_t *atoms, const
         int chunk = (int)std::min<long long>(count - done, D.move_cap - pos);
         FRMC_CUDA(cudaMemcpyAsync(D.moves + pos, mv.data() + done, sizeof(EMove) * chunk, cudaMemcpyHostToDevice,
                                   s->stream));
+        done += chunk;
+        pos = 0;
+    }
+    FRMC_CUDA(cudaStreamSynchronize(s->stream));
+    return FRMC_OK;
+}
+
+int frmc_engines_push_group_moves(void *handle, int32_t e, const int32_t *atoms, const int32_t *kinds,
+                                  const float *params, const float *u, int32_t count, int64_t first_step)
+{
+    EngineSet *s = as_set(handle);
+    if (!s || !valid_id(s, e) || count < 0 || first_step < 0 || (count && (!atoms || !kinds || !params)))
+        return set_error(FRMC_E_ARG, "push_group_moves: invalid arguments");
+    const EDesc &D = s->slots[e].d;
+    const int G = D.group;
+    if (count > D.move_cap)
+        return set_error(FRMC_E_ARG, "push_group_moves: %d moves exceed the ring of %d", count, D.move_cap);
+    std::vector<EMove> mv(count);
+    std::vector<EGroup> gv(G > 1 ? count : 0);
+    for (int k = 0; k < count; ++k) {
+        const int32_t *a = atoms + (size_t)k * G;
+        for (int t = 0; t < G; ++t) {
+            if (a[t] < 0 || a[t] >= D.n)
+                return set_error(FRMC_E_INDEX, "push_group_moves: atom %d out of range", a[t]);
+            for (int r = 0; r < t; ++r)
+                if (a[r] == a[t])
+                    return set_error(FRMC_E_ARG, "push_group_moves: atom %d twice in one group", a[t]);
+        }
+        if (kinds[k] != 0 && kinds[k] != 1)
+            return set_error(FRMC_E_ARG, "push_group_moves: move kind %d (0 translation, 1 rotation)", kinds[k]);
+        if (kinds[k] == 1 && G == 1)
+            return set_error(FRMC_E_ARG, "push_group_moves: a rotation needs a group of at least two atoms");
+        const float *pr = params + (size_t)k * 9;
+        mv[k].atom = a[0];
+        mv[k].v[0] = kinds[k] == 0 ? pr[0] : 0.f;
+        mv[k].v[1] = kinds[k] == 0 ? pr[1] : 0.f;
+        mv[k].v[2] = kinds[k] == 0 ? pr[2] : 0.f;
+        mv[k].u = u ? u[k] : 1.0f;
+        if (G > 1) {
+            EGroup &g = gv[k];
+            memset(&g, 0, sizeof(g));
+            g.kind = kinds[k];
+            if (g.kind == 1)
+                for (int q = 0; q < 9; ++q) g.rot[q] = pr[q];
+            for (int t = 1; t < G; ++t) g.atoms[t - 1] = a[t];
+        }
+    }
+    long long pos = first_step % D.move_cap;
+    int done = 0;
+    while (done < count) {
+        int chunk = (int)std::min<long long>(count - done, D.move_cap - pos);
+        FRMC_CUDA(cudaMemcpyAsync(D.moves + pos, mv.data() + done, sizeof(EMove) * chunk, cudaMemcpyHostToDevice,
+                                  s->stream));
+        if (G > 1)
+            FRMC_CUDA(cudaMemcpyAsync(D.groups + pos, gv.data() + done, sizeof(EGroup) * chunk,
+                                      cudaMemcpyHostToDevice, s->stream));
         done += chunk;
         pos = 0;
     }
@@ -2098,6 +2384,9 @@ int frmc_engines_step_host(void *handle, const int32_t *atoms, const float *vecs
     const int E = (int)s->live.size();
     if (E == 0)
         return FRMC_OK;
+    for (int k = 0; k < E; ++k)
+        if (s->slots[s->live[k]].d.group > 1)
+            return set_error(FRMC_E_ARG, "step_host: engine %d moves groups; push its moves instead", s->live[k]);
     for (int k = 0; k < E; ++k)
         if (atoms[k] < 0 || atoms[k] >= s->slots[s->live[k]].d.n)
             return set_error(FRMC_E_INDEX, "step_host: atom %d out of range for engine %d", atoms[k], s->live[k]);

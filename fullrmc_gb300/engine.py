@@ -39,7 +39,8 @@ class _Spec(ctypes.Structure):
                 ("data_weights", F64P), ("variance_squared", ctypes.c_double), ("tolerance", ctypes.c_double),
                 ("move_cap", ctypes.c_int32), ("sq_table", ctypes.c_int32), ("nq", ctypes.c_int32),
                 ("sq_rfac", F64P), ("sq_inv_shell_volume", F64P), ("sq_experimental", F64P),
-                ("sq_variance_squared", ctypes.c_double), ("sq_rho0", ctypes.c_double)]
+                ("sq_variance_squared", ctypes.c_double), ("sq_rho0", ctypes.c_double),
+                ("group_size", ctypes.c_int32)]
 
 
 _vp = ctypes.c_void_p
@@ -58,6 +59,7 @@ register("frmc_engines_set_mode", [_vp, ctypes.c_int])
 register("frmc_engines_init", [_vp])
 register("frmc_engines_push_moves", [_vp, _i32, I32P, F32P, F32P, _i32, _i64, ctypes.c_int])
 register("frmc_engines_step", [_vp, _i32, _i32, ctypes.c_int, _vp])
+register("frmc_engines_push_group_moves", [_vp, _i32, I32P, I32P, F32P, F32P, _i32, _i64])
 register("frmc_engines_sync", [_vp])
 register("frmc_engines_state", [_vp, _i32, F64P, ctypes.POINTER(_i64), ctypes.POINTER(_i64)])
 register("frmc_engines_results", [_vp, _i32, _i64, _i32, F64P, I32P, I32P])
@@ -240,6 +242,8 @@ class EngineSystem:
     tolerance: float = 0.0
     keep: list = field(default_factory=list, repr=False)
     sq: SQModel | None = None
+    group_size: int = 1              # atoms per move (molecule groups: their size)
+    groups: np.ndarray | None = None  # (n_groups, group_size) atom indexes, for group moves
 
     def chi2_fp64(self, intra, inter):
         """chi2 of the engine's constraints from oriented counts (FP64)."""
@@ -263,6 +267,61 @@ def translation_moves(rng: np.random.Generator, n_atoms: int, count: int, amplit
     v = (v * (rng.random(count) * amplitude).astype(F32)[:, None]).astype(F32)
     u = rng.random(count).astype(F32)
     return atoms, np.ascontiguousarray(v), u
+
+
+def group_moves(rng: np.random.Generator, groups, count: int, amplitude: float, angle: float,
+                p_rotation: float = 0.5):
+    """Moves of whole groups (molecules), like fullrmc's TranslationGenerator
+    (Generators/Translations.py:171-190) and RotationGenerator
+    (Generators/Rotations.py:141-178) on molecule groups: a uniformly chosen
+    group, then with probability `p_rotation` a rotation about the group's
+    centroid by an angle uniform in [-angle, angle] degrees about a uniform
+    random axis, else a translation of length uniform in [0, amplitude) in a
+    uniform direction.  Returns (atoms (count, G), kinds (count,), params
+    (count, 9), u (count,)): params holds the translation vector (first three)
+    or the row-vector rotation matrix (x -> x R), float32."""
+    groups = np.asarray(groups, np.int32)
+    pick = rng.integers(0, groups.shape[0], size=count)
+    atoms = np.ascontiguousarray(groups[pick])
+    kinds = (rng.random(count) < p_rotation).astype(np.int32)
+    params = np.zeros((count, 9), F32)
+    for k in range(count):
+        if kinds[k]:
+            axis = 1.0 - 2.0 * rng.random(3)
+            axis /= np.linalg.norm(axis)
+            th = np.radians((1.0 - 2.0 * rng.random()) * angle)
+            x, y, z = axis
+            c, s_, C = np.cos(th), np.sin(th), 1.0 - np.cos(th)
+            Rcol = np.array([[c + x * x * C, x * y * C - z * s_, x * z * C + y * s_],
+                             [y * x * C + z * s_, c + y * y * C, y * z * C - x * s_],
+                             [z * x * C - y * s_, z * y * C + x * s_, c + z * z * C]])
+            params[k] = Rcol.T.astype(F32).ravel()   # row-vector convention: x R = (Rcol x)^T
+        else:
+            v = 1.0 - 2.0 * rng.random(3)
+            v /= np.linalg.norm(v)
+            params[k, :3] = (v * rng.random() * amplitude).astype(F32)
+    u = rng.random(count).astype(F32)
+    return atoms, kinds, params, u
+
+
+def group_new_real(real, kind, params):
+    """New real coordinates of a group (float32, the engine's operation
+    order): translation real + v, or rotation (x - c) R + c about the
+    centroid c (atoms added in group order, divided by the group size)."""
+    real = np.asarray(real, F32)
+    p = np.asarray(params, F32)
+    if kind == 0:
+        return (real + p[:3]).astype(F32)
+    c = real[0].copy()
+    for k in range(1, real.shape[0]):
+        c = (c + real[k]).astype(F32)
+    c = (c / F32(real.shape[0])).astype(F32)
+    R = p.reshape(3, 3)
+    d = (real - c).astype(F32)
+    out = np.empty_like(real)
+    for k in range(3):
+        out[:, k] = ((d[:, 0] * R[0, k] + d[:, 1] * R[1, k]) + d[:, 2] * R[2, k]) + c[k]
+    return out.astype(F32)
 
 
 def make_spec(system, move_cap, sq_table=-1):
@@ -301,6 +360,7 @@ def make_spec(system, move_cap, sq_table=-1):
     sp.variance_squared = float(m.variance_squared)
     sp.tolerance = float(s.tolerance)
     sp.move_cap = int(move_cap)
+    sp.group_size = int(getattr(s, "group_size", 1) or 1)
     sp.sq_table = -1
     if s.sq is not None:
         q = s.sq
@@ -445,6 +505,16 @@ class EngineSet:
 
     def init(self):
         check(load().frmc_engines_init(self.handle))
+
+    def push_group_moves(self, e, atoms, kinds, params, u, first_step):
+        """Group moves (see group_moves) for steps [first_step, first_step + count)."""
+        atoms = np.ascontiguousarray(atoms, np.int32)
+        kinds = np.ascontiguousarray(kinds, np.int32)
+        params = np.ascontiguousarray(params, F32)
+        u = np.ascontiguousarray(u, F32)
+        check(load().frmc_engines_push_group_moves(self.handle, int(e), atoms.ctypes.data_as(I32P),
+                                                   kinds.ctypes.data_as(I32P), params.ctypes.data_as(F32P),
+                                                   u.ctypes.data_as(F32P), len(kinds), int(first_step)))
 
     def push_moves(self, e, atoms, vecs, u, first_step):
         atoms = np.ascontiguousarray(atoms, np.int32)

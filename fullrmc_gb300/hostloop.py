@@ -126,11 +126,14 @@ class HostPDFChain:
             out[:, k] = (c[:, 0] * M[0, k] + c[:, 1] * M[1, k]) + c[:, 2] * M[2, k]
         return out
 
-    def step(self, atoms, vec, u, force=None):
-        """One move of the atoms ``atoms`` by ``vec``; returns True if accepted.
-        ``force`` (True/False) overrides the decision (used to replay a chain)."""
+    def step(self, atoms, vec, u, force=None, moved_real=None):
+        """One move of the atoms ``atoms`` by ``vec`` (or to ``moved_real``);
+        returns True if accepted.  ``force`` (True/False) overrides the
+        decision (used to replay a chain)."""
         idx = np.ascontiguousarray(np.atleast_1d(atoms), np.int32)
-        moved_real = self.real[idx] + np.asarray(vec, F32)
+        if moved_real is None:
+            moved_real = self.real[idx] + np.asarray(vec, F32)
+        moved_real = np.asarray(moved_real, F32)
         moved_box = self._transform(moved_real) if self.isPBC else moved_real
         before = self._delta(idx)
         saved = np.array(self.box[idx], F32)

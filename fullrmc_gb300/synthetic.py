@@ -10,6 +10,10 @@ workload definitions:
   a = b = c = 103 A, alpha = beta = 90, gamma = 120 degrees, r 0-20 A.
 * ``mixed_engines``: 256 engines, atom counts log-uniform in [1,000, 20,000],
   1-4 species, cubic or triclinic boxes at 0.08-0.10 atoms/A^3, r 0-12 A.
+* ``ring_molecules``: rigid five-membered rings (4 C + 1 O, bond 1.5 A; 8 H
+  at C-H 1.1 A), 13 atoms each, randomly placed and oriented in a cubic box
+  at 0.1 atoms/A^3 (4,000 of them = 52,000 atoms), moved as whole groups;
+  r 0-15 A, dr 0.01 (the G(r) grid is not fixed by the configuration).
 * ``serving_fit``: one fit of the serving stream: atoms log-uniform in
   [2,000, 200,000], 1-3 species, G(r) on r 0-12 A and S(Q) on Q 0.5-25 A^-1
   (dQ 0.01, 2451 points), 2,000-50,000 steps.
@@ -161,3 +165,54 @@ def serving_fit(seed, nmin=2000, nmax=200000, smin=2000, smax=50000, rmax=12.0, 
     B = random_box(rng, n, rng.uniform(0.08, 0.10))
     steps = int(rng.integers(smin, smax + 1))
     return make_system(rng, n, fr, B, rmax, q=q_grid() if sq else None), steps
+
+
+def _ring_template():
+    """One 13-atom ring molecule: 4 C, 1 O on a regular pentagon with 1.5 A
+    bonds, and 2 H on each C at 1.1 A, above and below the ring plane."""
+    R = 1.5 / (2.0 * np.sin(np.radians(36.0)))
+    ang = np.radians(72.0 * np.arange(5))
+    ring = np.stack([R * np.cos(ang), R * np.sin(ang), np.zeros(5)], axis=1)
+    th = np.radians(54.75)
+    hs = []
+    for k in range(4):
+        radial = ring[k] / np.linalg.norm(ring[k])
+        for sgn in (1.0, -1.0):
+            hs.append(ring[k] + 1.1 * (np.cos(th) * radial + sgn * np.sin(th) * np.array([0.0, 0.0, 1.0])))
+    xyz = np.concatenate([ring, np.array(hs)])
+    el = np.array([0, 0, 0, 0, 1] + [2] * 8, np.int32)
+    return xyz - xyz.mean(axis=0), el
+
+
+def _random_rotation(rng):
+    q = rng.normal(size=4)
+    q /= np.linalg.norm(q)
+    a, b, c, d = q
+    return np.array([[a * a + b * b - c * c - d * d, 2 * (b * c - a * d), 2 * (b * d + a * c)],
+                     [2 * (b * c + a * d), a * a - b * b + c * c - d * d, 2 * (c * d - a * b)],
+                     [2 * (b * d - a * c), 2 * (c * d + a * b), a * a - b * b - c * c + d * d]])
+
+
+def ring_molecules(seed=0, nmol=4000, rho=0.1, rmax=15.0):
+    """Molecular system of rigid 13-atom rings moved as groups (see above)."""
+    rng = np.random.default_rng([seed, 13])
+    xyz0, el0 = _ring_template()
+    n = 13 * nmol
+    L = (n / rho) ** (1.0 / 3.0)
+    basis = np.diag([L, L, L]).astype(F32)
+    real = np.empty((n, 3))
+    for m in range(nmol):
+        real[13 * m:13 * m + 13] = xyz0 @ _random_rotation(rng).T + rng.random(3) * L
+    real = real.astype(F32)
+    rbasis = np.linalg.inv(basis.astype(np.float64)).astype(F32)
+    box = transform_f32(rbasis, real)
+    el = np.tile(el0, nmol)
+    mol = np.repeat(np.arange(nmol), 13).astype(np.int32)
+    counts = np.bincount(el, minlength=3)
+    volume = float(L) ** 3
+    weights = normalized_weighting(counts, np.array([6.0, 8.0, 1.0]))
+    r = r_grid(rmax)
+    G = synthetic_G(rng, r, n / volume)
+    model = PDFModel(r=r, G_exp=G, elements_count=counts, weights=weights, volume=volume)
+    return EngineSystem(box_coords=box, real_coords=real, el=el, mol=mol, basis=basis, rbasis=rbasis, isPBC=True,
+                        model=model, group_size=13, groups=np.arange(n, dtype=np.int32).reshape(nmol, 13))

@@ -68,6 +68,9 @@ typedef struct {
     const double *sq_experimental;     /* (nq,) experimental S(Q)               */
     double sq_variance_squared;
     double sq_rho0;                    /* number density: sq_rfac = sq_rho0 r0fac of the table */
+    /* Atoms per move (0 or 1: single-atom moves; up to 16: moves of atom
+     * groups such as molecules, pushed with frmc_engines_push_group_moves). */
+    int32_t group_size;
 } frmc_engine_spec;
 
 /* A G(r) -> S(Q) table shared by the set's engines that use the same r shells
@@ -115,6 +118,16 @@ int frmc_engines_init(void *handle);
  * vecs (count, 3) real-space displacements, u (count,) uniforms (NULL = 1). */
 int frmc_engines_push_moves(void *handle, int32_t e, const int32_t *atoms, const float *vecs, const float *u,
                             int32_t count, int64_t first_step, int from_device);
+/* Group moves for steps [first_step, first_step + count) of an engine with
+ * group_size G: atoms (count, G) distinct per move, kinds (count,) 0 =
+ * translation of every atom by params[0..2], 1 = rotation of the group about
+ * its centroid c (float32 mean of the atoms' real coordinates in the order
+ * given): x -> (x - c) R + c with R = params (3 x 3 row-major, row-vector
+ * convention); params (count, 9); u (count,) uniforms (NULL = 1).  The moves
+ * of fullrmc's TranslationGenerator / RotationGenerator on molecule groups
+ * (Generators/Translations.py, Generators/Rotations.py). */
+int frmc_engines_push_group_moves(void *handle, int32_t e, const int32_t *atoms, const int32_t *kinds,
+                                  const float *params, const float *u, int32_t count, int64_t first_step);
 /* Advance `steps` steps: engine == -1 steps every engine in one launch per
  * step (the batched path); engine >= 0 steps that engine alone.  use_graph
  * captures the launches in a CUDA graph (cached per engine/steps).  Returns
