@@ -20,6 +20,10 @@ Reported beside the headline:
   (46 algorithmic operations per pair distance, SMs x clock x 128 / 46);
 * ``cpu_baseline``: fullrmc's own Cython path (compiled from its sources)
   running the same kind of steps on the host cores, on a bounded sample;
+* ``configs``: single-engine step rates of the other configurations (the
+  5,000-atom alloy; the 100,000-atom triclinic system and its FP64 S(Q)
+  transform; the 52,000-atom molecular system with 13-atom group moves),
+  beside fullrmc's Cython path on a few steps of the same systems;
 * ``serving``: the serving loop on a Poisson stream of fit requests (20 per
   second; 2,000-200,000 atoms log-uniform, 1-3 species, G(r) on r 0-12 A
   plus S(Q) on Q 0.5-25 A^-1 with dQ 0.01, 2,000-50,000 steps each), admitted
@@ -164,6 +168,95 @@ def reference_rate(n_engines_sample, steps, warmup, processes, seed=0, amp=0.1):
     total = sum(max(o[1][k] for o in out) for k in range(warmup, warmup + steps))
     done = n_engines_sample * steps
     return done / total, len(chunks)
+
+
+def _engine_rate(torch, system, steps, seed, group=False):
+    """Steps/s of one engine stepped alone (the plain GPU path, one CUDA
+    graph of `steps` steps), and the engine's initial counts."""
+    from fullrmc_gb300.engine import EngineSet, group_moves, translation_moves
+    es = EngineSet([system], move_cap=steps + 16)
+    es.init()
+    rng = np.random.default_rng(seed)
+    if group:
+        mv = group_moves(rng, system.groups, steps + 16, 0.1, 10.0)
+        es.push_group_moves(0, *mv, 0)
+    else:
+        mv = translation_moves(rng, system.box_coords.shape[0], steps + 16, 0.1)
+        es.push_moves(0, *mv, 0)
+    counts0 = es.counts(0)
+    es.step(8, engine=0, graph=False)
+    es.step(steps, engine=0, graph=True, sync=True)  # capture
+    es.step(8, engine=0, graph=False)
+    # time `steps` further steps (moves: the ring holds steps + 16; re-push)
+    if group:
+        es.push_group_moves(0, *[x[:steps] for x in group_moves(np.random.default_rng(seed + 1), system.groups,
+                                                                  steps, 0.1, 10.0)], es.state(0)[1])
+    else:
+        es.push_moves(0, *[x[:steps] for x in translation_moves(np.random.default_rng(seed + 1),
+                                                                system.box_coords.shape[0], steps, 0.1)],
+                      es.state(0)[1])
+    t0 = time.perf_counter()
+    es.step(steps, engine=0, graph=True, sync=True)
+    dt = time.perf_counter() - t0
+    st = es.state(0)
+    es.close()
+    return steps / dt, counts0, st[2] / max(1, st[1]), mv
+
+
+def _reference_config_rate(system, counts0, mv, steps, group=False):
+    """Steps/s of fullrmc's Cython path (reference-style host loop, ncores=1)
+    on the same system, started from the same initial counts."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import build_ref
+    from fullrmc_gb300.engine import group_new_real
+    from fullrmc_gb300.hostloop import HostPDFChain
+    R = build_ref.import_reference()
+    chain = HostPDFChain(system, R["pairs_histograms"], R["boundary_conditions_collection"])
+    chain.data = (counts0[0].astype(np.float32), counts0[1].astype(np.float32))
+    chain.error = chain.standard_error(*chain.data)
+    t0 = time.perf_counter()
+    for k in range(steps):
+        if group:
+            atoms, kinds, params, u = mv
+            chain.step(atoms[k], None, u[k], moved_real=group_new_real(chain.real[atoms[k]], kinds[k], params[k]))
+        else:
+            a, v, u = mv
+            chain.step(a[k], v[k][None, :], u[k])
+    return steps / (time.perf_counter() - t0)
+
+
+def bench_configs(torch, with_cpu):
+    """Single-engine step rates of the other configurations on the GPU (and,
+    on a bounded sample, of the reference CPU path): the 5,000-atom alloy,
+    the 100,000-atom triclinic system (plus its FP64 S(Q) transform, Q 0.5-30
+    / 0.01), and the 52,000-atom molecular system with 13-atom group moves."""
+    from fullrmc_gb300 import reciprocal_space, synthetic
+    out = {}
+    for name, system, steps, group, cpu_steps in (
+            ("alloy_5000", synthetic.alloy_5000(seed=0), 2000, False, 40),
+            ("triclinic_100k", synthetic.triclinic_100k(seed=0), 1000, False, 8),
+            ("ring_molecules_52000", synthetic.ring_molecules(seed=0, nmol=4000), 400, True, 4)):
+        rate, counts0, acc, mv = _engine_rate(torch, system, steps, seed=5, group=group)
+        d = {"atoms": int(system.box_coords.shape[0]), "atoms_per_move": 13 if group else 1,
+             "gpu_steps_per_s": rate, "steps": steps, "accept_rate": round(float(acc), 4)}
+        if with_cpu:
+            try:
+                d["cpu_reference_steps_per_s"] = _reference_config_rate(system, counts0, mv, cpu_steps, group)
+                d["cpu_sample_steps"] = cpu_steps
+            except Exception as exc:
+                d["cpu_reference_steps_per_s"] = None
+                d["cpu_error"] = str(exc)[:200]
+        out[name] = d
+    # the 100k system's S(Q): FP64 sine transform of its G(r), Q 0.5-30 / 0.01 (2951 points)
+    s = synthetic.triclinic_100k(seed=0)
+    q = (0.5 + 0.01 * np.arange(2951)).astype(np.float32)
+    G = np.asarray(s.model.G_exp, np.float32)
+    reciprocal_space.Gr_to_sq(s.model.r, G, q)
+    t0 = time.perf_counter()
+    for _ in range(5):
+        reciprocal_space.Gr_to_sq(s.model.r, G, q)
+    out["triclinic_100k"]["sq_transform_ms"] = 1e3 * (time.perf_counter() - t0) / 5
+    return out
 
 
 def run_reference(args):
@@ -360,6 +453,9 @@ def run_ours(args):
     d2h = E * 16  # (chi2, accepted, atom) per engine
 
     allp = bench_allpairs(torch, native, dev)
+    configs = None
+    if not args.no_configs and rank == 0:
+        configs = bench_configs(torch, with_cpu=not args.no_cpu)
     serving = None
     if args.serve_seconds > 0 and rank == 0:
         from fullrmc_gb300 import serve
@@ -415,6 +511,7 @@ def run_ours(args):
             "allpairs": dict(allp, roofline_frac=allp["pair_distances_per_s"] / issue_peak,
                              issue_peak_pairs_per_s=issue_peak),
             "serving": serving,
+            "configs": configs,
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": K,
@@ -436,6 +533,7 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="arrival window of the serving stream (0: skip)")
+    ap.add_argument("--no-configs", action="store_true", help="skip the single-engine rates of the other configurations")
     ap.add_argument("--serve-limit", type=float, default=60.0, help="wall-clock limit of the serving run")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -72,6 +72,13 @@ SIGNATURES = {
     "frmc_dev_pack_atoms": [vp, vp, i64, vp, vp],
     "frmc_dev_full_pairs_histograms_noalloc": [vp, vp, i64, F32P, cint, i32, f32, f32, f32, i32, vp, vp, vp],
     "frmc_dev_counts_to_f32": [vp, i64, vp, vp],
+    "frmc_multiple_atomic_distances_coords": [I32P, i64, F32P, i64, F32P, cint, I32P, I32P, i32, F32P, F32P, cint,
+                                              cint, I32P, F32P, I32P, F32P],
+    "frmc_multiple_atomic_distances_dists": [I32P, i64, F32P, i64, I32P, I32P, i32, F32P, F32P, cint, cint, I32P,
+                                             F32P, I32P, F32P],
+    "frmc_single_atomic_distances_dists": [i32, F32P, i64, I32P, I32P, i32, F32P, F32P, I32P, I32P, F32P, F32P, cint,
+                                           cint],
+    "frmc_pair_elements_stats": [I32P, I32P, i64, i32, I32P, I32P],
 }
 _RESTYPE = {"frmc_last_error": ctypes.c_char_p}
 

@@ -544,6 +544,148 @@ static int sine_common(int kind, const float *xs, int64_t nx, const float *ys, c
     return finish(c);
 }
 
+// ----------------------------------------------- atomic distances (host)
+// atomic_distances.pyx: counts and float32 sums of the pairs inside (or
+// outside) per-element-pair limits; see atomic_kernels.cu.
+
+static int atomic_checks(int64_t n, int64_t K, int32_t ne, const int32_t *el, int64_t nel)
+{
+    TRY(check_n(n, "coordinates"));
+    if (K < 0 || K > INT_MAX / 4)
+        return set_error(FRMC_E_ARG, "number of indexes %lld out of range", (long long)K);
+    if (ne < 1 || ne > 16)
+        return set_error(FRMC_E_ARG, "numberOfElements %d out of range (1..16)", ne);
+    for (int64_t i = 0; i < nel; ++i)
+        if (el[i] < 0 || el[i] >= ne)
+            return set_error(FRMC_E_INDEX, "element index %d out of range for %d elements", el[i], ne);
+    return FRMC_OK;
+}
+
+// Device accumulators [dsum 2 ne^2 floats][nsum 2 ne^2 ints], limits
+// [lower ne^2][upper ne^2]; starting values from the given arrays (or 0).
+static int atomic_prepare(Context *c, int32_t ne, const float *lower, const float *upper, const int32_t *nintra0,
+                          const float *dintra0, const int32_t *ninter0, const float *dinter0)
+{
+    const size_t m = (size_t)ne * ne;
+    TRY(c->buf[BUF_ATOMIC_LIMITS].ensure(8 * m + 16));
+    TRY(c->buf[BUF_ATOMIC_ACC].ensure(16 * m + 16));
+    float *lim = c->buf[BUF_ATOMIC_LIMITS].as<float>();
+    TRY(h2d(lim, lower, 4 * m, c->stream));
+    TRY(h2d(lim + m, upper, 4 * m, c->stream));
+    float *acc = c->buf[BUF_ATOMIC_ACC].as<float>();
+    if (dintra0) {
+        TRY(h2d(acc, dintra0, 4 * m, c->stream));
+        TRY(h2d(acc + m, dinter0, 4 * m, c->stream));
+        TRY(h2d(acc + 2 * m, nintra0, 4 * m, c->stream));
+        TRY(h2d(acc + 3 * m, ninter0, 4 * m, c->stream));
+    } else {
+        FRMC_CUDA(cudaMemsetAsync(acc, 0, 16 * m, c->stream));
+    }
+    return FRMC_OK;
+}
+
+static int atomic_finish(Context *c, int32_t ne, int32_t *nintra, float *dintra, int32_t *ninter, float *dinter)
+{
+    const size_t m = (size_t)ne * ne;
+    const float *acc = c->buf[BUF_ATOMIC_ACC].as<float>();
+    TRY(d2h(dintra, acc, 4 * m, c->stream));
+    TRY(d2h(dinter, acc + m, 4 * m, c->stream));
+    TRY(d2h(nintra, acc + 2 * m, 4 * m, c->stream));
+    TRY(d2h(ninter, acc + 3 * m, 4 * m, c->stream));
+    return finish(c);
+}
+
+static int atomic_run(Context *c, const float *dists_dev, int K, int n, int allAtoms, int flags, int ne,
+                      const float *basis, int isPBC)
+{
+    const size_t m = (size_t)ne * ne;
+    float *lim = c->buf[BUF_ATOMIC_LIMITS].as<float>();
+    float *acc = c->buf[BUF_ATOMIC_ACC].as<float>();
+    return atomic_distances_run(c, dists_dev ? nullptr : c->buf[BUF_COORDS].as<float>(), dists_dev,
+                                c->buf[BUF_ROWS].as<int>(), K, n, allAtoms, flags, ne, basis, isPBC,
+                                c->buf[BUF_MOL].as<int>(), c->buf[BUF_EL].as<int>(), lim, lim + m, acc,
+                                reinterpret_cast<int *>(acc + 2 * m), c->stream);
+}
+
+int frmc_multiple_atomic_distances_coords(const int32_t *indexes, int64_t K, const float *boxCoords, int64_t n,
+                                          const float *basis, int isPBC, const int32_t *moleculeIndex,
+                                          const int32_t *elementIndex, int32_t ne, const float *lowerLimit,
+                                          const float *upperLimit, int flags, int allAtoms, int32_t *nintra,
+                                          float *dintra, int32_t *ninter, float *dinter)
+{
+    TRY(atomic_checks(n, K, ne, elementIndex, n));
+    TRY(check_indexes(indexes, K, n));
+    LOCKED_CTX(c);
+    TRY(upload_atoms(c, boxCoords, moleculeIndex, elementIndex, n));
+    TRY(c->buf[BUF_ROWS].ensure(K * 4 + 16));
+    TRY(h2d(c->buf[BUF_ROWS].p, indexes, K * 4, c->stream));
+    TRY(atomic_prepare(c, ne, lowerLimit, upperLimit, nullptr, nullptr, nullptr, nullptr));
+    TRY(atomic_run(c, nullptr, (int)K, (int)n, allAtoms, flags, ne, basis, isPBC));
+    return atomic_finish(c, ne, nintra, dintra, ninter, dinter);
+}
+
+int frmc_multiple_atomic_distances_dists(const int32_t *indexes, int64_t K, const float *distances, int64_t n,
+                                         const int32_t *moleculeIndex, const int32_t *elementIndex, int32_t ne,
+                                         const float *lowerLimit, const float *upperLimit, int flags, int allAtoms,
+                                         int32_t *nintra, float *dintra, int32_t *ninter, float *dinter)
+{
+    TRY(atomic_checks(n, K, ne, elementIndex, n));
+    TRY(check_indexes(indexes, K, n));
+    LOCKED_CTX(c);
+    TRY(c->buf[BUF_EL].ensure(n * 4 + 16));
+    TRY(h2d(c->buf[BUF_EL].p, elementIndex, n * 4, c->stream));
+    TRY(c->buf[BUF_MOL].ensure(n * 4 + 16));
+    TRY(h2d(c->buf[BUF_MOL].p, moleculeIndex, n * 4, c->stream));
+    TRY(c->buf[BUF_AUX0].ensure((size_t)n * K * 4 + 16));
+    TRY(h2d(c->buf[BUF_AUX0].p, distances, (size_t)n * K * 4, c->stream));
+    TRY(c->buf[BUF_ROWS].ensure(K * 4 + 16));
+    TRY(h2d(c->buf[BUF_ROWS].p, indexes, K * 4, c->stream));
+    TRY(atomic_prepare(c, ne, lowerLimit, upperLimit, nullptr, nullptr, nullptr, nullptr));
+    TRY(atomic_run(c, c->buf[BUF_AUX0].as<float>(), (int)K, (int)n, allAtoms, flags, ne, nullptr, 0));
+    return atomic_finish(c, ne, nintra, dintra, ninter, dinter);
+}
+
+int frmc_single_atomic_distances_dists(int32_t atomIndex, const float *distances, int64_t n,
+                                       const int32_t *moleculeIndex, const int32_t *elementIndex, int32_t ne,
+                                       float *dintra, float *dinter, int32_t *nintra, int32_t *ninter,
+                                       const float *lowerLimit, const float *upperLimit, int flags, int allAtoms)
+{
+    TRY(atomic_checks(n, 1, ne, elementIndex, n));
+    if (atomIndex < 0 || atomIndex >= n)
+        return set_error(FRMC_E_INDEX, "atomIndex %d out of range for %lld atoms", atomIndex, (long long)n);
+    LOCKED_CTX(c);
+    TRY(c->buf[BUF_EL].ensure(n * 4 + 16));
+    TRY(h2d(c->buf[BUF_EL].p, elementIndex, n * 4, c->stream));
+    TRY(c->buf[BUF_MOL].ensure(n * 4 + 16));
+    TRY(h2d(c->buf[BUF_MOL].p, moleculeIndex, n * 4, c->stream));
+    TRY(c->buf[BUF_AUX0].ensure((size_t)n * 4 + 16));
+    TRY(h2d(c->buf[BUF_AUX0].p, distances, (size_t)n * 4, c->stream));
+    TRY(c->buf[BUF_ROWS].ensure(16));
+    TRY(h2d(c->buf[BUF_ROWS].p, &atomIndex, 4, c->stream));
+    TRY(atomic_prepare(c, ne, lowerLimit, upperLimit, nintra, dintra, ninter, dinter));
+    TRY(atomic_run(c, c->buf[BUF_AUX0].as<float>(), 1, (int)n, allAtoms, flags, ne, nullptr, 0));
+    return atomic_finish(c, ne, nintra, dintra, ninter, dinter);
+}
+
+int frmc_pair_elements_stats(const int32_t *elementIndex, const int32_t *moleculeIndex, int64_t n, int32_t ne,
+                             int32_t *nintra, int32_t *ninter)
+{
+    TRY(atomic_checks(n, 0, ne, elementIndex, n));
+    const size_t m = (size_t)ne * ne;
+    LOCKED_CTX(c);
+    TRY(c->buf[BUF_EL].ensure(n * 4 + 16));
+    TRY(h2d(c->buf[BUF_EL].p, elementIndex, n * 4, c->stream));
+    TRY(c->buf[BUF_MOL].ensure(n * 4 + 16));
+    TRY(h2d(c->buf[BUF_MOL].p, moleculeIndex, n * 4, c->stream));
+    TRY(c->buf[BUF_ATOMIC_ACC].ensure(8 * m + 16));
+    int *acc = c->buf[BUF_ATOMIC_ACC].as<int>();
+    FRMC_CUDA(cudaMemsetAsync(acc, 0, 8 * m, c->stream));
+    TRY(launch_pair_stats(c->buf[BUF_EL].as<int>(), c->buf[BUF_MOL].as<int>(), (int)n, ne, acc, acc + m, c->stream));
+    TRY(d2h(nintra, acc, 4 * m, c->stream));
+    TRY(d2h(ninter, acc + m, 4 * m, c->stream));
+    return finish(c);
+}
+
 int frmc_gr_to_sq(const float *distances, const float *gr, int64_t nr, const float *qrange, int64_t nq, double rho,
                   double *sq)
 {

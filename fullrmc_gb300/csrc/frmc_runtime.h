@@ -60,6 +60,12 @@ enum BufRole {
     BUF_AUX1,
     BUF_AUX2,
     BUF_STATUS,
+    BUF_ATOMIC_COUNTS,
+    BUF_ATOMIC_TOTALS,
+    BUF_ATOMIC_LIST_B,
+    BUF_ATOMIC_LIST_V,
+    BUF_ATOMIC_ACC,
+    BUF_ATOMIC_LIMITS,
     BUF_COUNT_
 };
 
@@ -128,6 +134,19 @@ int launch_dists_hist(const float *dists, int n, int K, const int *rows, const i
 
 // out[k] = h0[k] + 1.0f added counts[k] times in float32 (h0 may be null = 0).
 int launch_counts_to_f32(const unsigned *counts, const float *h0, float *out, int64_t total, cudaStream_t st);
+
+// Atomic distance constraint sums (atomic_kernels.cu): rows (device, K atom
+// indexes) against every column j of n atoms (j >= row atom unless allAtoms,
+// j != row atom), from box coordinates (device (n, 3)) or given distances
+// (device (n, K)); flags: 1 inter, 2 intra, 4 count within limits, 8 / 16 / 32
+// reduce to upper / lower / nearest limit.  dsum / nsum (device, [2][ne][ne],
+// intra then inter) hold the starting values and receive the sums.
+int atomic_distances_run(Context *c, const float *coords, const float *dists, const int *rows, int K, int n,
+                         int allAtoms, int flags, int ne, const float *basis_host, int isPBC, const int *mol,
+                         const int *el, const float *lower, const float *upper, float *dsum, int *nsum,
+                         cudaStream_t st);
+// pair_elements_stats counts ([2][ne][ne] int, zeroed by the caller).
+int launch_pair_stats(const int *el, const int *mol, int n, int ne, int *nintra, int *ninter, cudaStream_t st);
 
 // Pack AoS coordinates and element indexes into float4 (x, y, z, el bits).
 int launch_pack_atoms(const float *coords, const int *el, int n, float4 *out, cudaStream_t st);

@@ -130,6 +130,42 @@ int frmc_multiple_pairs_histograms_dists(const int32_t *indexes, int64_t K, cons
                                          float minDistance, float maxDistance, float bin, int32_t hs, int allAtoms,
                                          float *hintra, float *hinter);
 
+/* Extensions/atomic_distances.pyx (InterMolecularDistanceConstraint,
+ * Constraints/DistanceConstraints.py:569-697).  For every row atom (indexes,
+ * in order) and every other atom j (j >= the row atom unless allAtoms), pairs
+ * whose distance d passes the limits lowerLimit/upperLimit[el(j)][el(row)]
+ * (flags & 4: lower <= d < upper; otherwise outside) are counted and their
+ * value summed in float32, in the reference's loop order, into
+ * [el(row)][el(j)] of the intra- (same molecule) or inter-molecular arrays.
+ * flags: 1 interMolecular, 2 intraMolecular, 4 countWithinLimits, 8
+ * reduceDistanceToUpper (value |upper - d|), 16 reduceDistanceToLower
+ * (|lower - d|), 32 reduceDistance (the nearer limit).  Outputs are (ne, ne)
+ * (the reference's (ne, ne, 1)).  multiple_atomic_distances_coords
+ * (atomic_distances.pyx:326-417); full_atomic_distances_coords (:500-567) is
+ * the same with indexes = 0..n-1 and allAtoms = 0. */
+int frmc_multiple_atomic_distances_coords(const int32_t *indexes, int64_t K, const float *boxCoords, int64_t n,
+                                          const float *basis, int isPBC, const int32_t *moleculeIndex,
+                                          const int32_t *elementIndex, int32_t ne, const float *lowerLimit,
+                                          const float *upperLimit, int flags, int allAtoms, int32_t *nintra,
+                                          float *dintra, int32_t *ninter, float *dinter);
+/* multiple_atomic_distances_dists (atomic_distances.pyx:419-498): distances
+ * (n, K), column k the distances of atom indexes[k]; full_* (:569-630) with
+ * indexes = 0..K-1, allAtoms = 0. */
+int frmc_multiple_atomic_distances_dists(const int32_t *indexes, int64_t K, const float *distances, int64_t n,
+                                         const int32_t *moleculeIndex, const int32_t *elementIndex, int32_t ne,
+                                         const float *lowerLimit, const float *upperLimit, int flags, int allAtoms,
+                                         int32_t *nintra, float *dintra, int32_t *ninter, float *dinter);
+/* single_atomic_distances_dists (atomic_distances.pyx:128-324): adds into the
+ * given arrays in place. */
+int frmc_single_atomic_distances_dists(int32_t atomIndex, const float *distances, int64_t n,
+                                       const int32_t *moleculeIndex, const int32_t *elementIndex, int32_t ne,
+                                       float *dintra, float *dinter, int32_t *nintra, int32_t *ninter,
+                                       const float *lowerLimit, const float *upperLimit, int flags, int allAtoms);
+/* pair_elements_stats (atomic_distances.pyx:632-672): pairs i < j counted at
+ * [el(i)][el(j)], intra or inter. */
+int frmc_pair_elements_stats(const int32_t *elementIndex, const int32_t *moleculeIndex, int64_t n, int32_t ne,
+                             int32_t *nintra, int32_t *ninter);
+
 /* ---------------------------------------------- reciprocal space (host, FP64)
  * Extensions/reciprocal_space.pyx:42-73 gr_to_sq:
  *   sq[q] = 1 + 4 pi rho sum_r dr r sin(q r)/q (gr[r] - 1), dr = r[1] - r[0]. */

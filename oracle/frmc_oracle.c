@@ -404,3 +404,77 @@ void oracle_transform_coordinates(const float *M, const float *coords,
         out[3 * i + 2] = c[0] * M[2] + c[1] * M[5] + c[2] * M[8];
     }
 }
+
+/* -------------------------------------------------------- atomic distances */
+
+/* atomic_distances.pyx:42-126 (one row atom) as called by :326-417 and
+ * :419-498: rows indexes[k] in order, columns i from start (0 if allAtoms,
+ * else the row atom) to n - 1 in order, float32 sums in that order.  The
+ * distance of column i is d(coords[row], coords[i]) (pairs_distances, row
+ * atom first) or dists[i * K + k].  flags: 1 inter, 2 intra, 4 count within
+ * limits, 8 / 16 / 32 reduce to upper / lower / nearest limit.  Outputs
+ * (ne, ne), added to. */
+void oracle_atomic_distances(const int32_t *indexes, int64_t K, const float *coords, const float *dists,
+                             int64_t n, const float *basis, int isPBC, const int32_t *mol, const int32_t *el,
+                             int32_t ne, const float *lower, const float *upper, int flags, int allAtoms,
+                             float *dintra, float *dinter, int32_t *nintra, int32_t *ninter)
+{
+    for (int64_t k = 0; k < K; ++k) {
+        const int32_t a = indexes[k];
+        const int64_t start = allAtoms ? 0 : a;
+        const int32_t ea = el[a], ma = mol[a];
+        float p[3] = {0.f, 0.f, 0.f};
+        if (!dists) {
+            p[0] = coords[3 * (int64_t)a];
+            p[1] = coords[3 * (int64_t)a + 1];
+            p[2] = coords[3 * (int64_t)a + 2];
+        }
+        for (int64_t i = start; i < n; ++i) {
+            if (i == a)
+                continue;
+            const int32_t mi = mol[i];
+            if (!(flags & 2) && mi == ma)
+                continue;
+            if (!(flags & 1) && mi != ma)
+                continue;
+            float d = dists ? dists[i * K + k] : pair_distance(p, coords + 3 * i, basis, isPBC);
+            const int32_t ei = el[i];
+            const float lo = lower[ei * ne + ea];
+            const float up = upper[ei * ne + ea];
+            if (flags & 4) {
+                if (d < lo)
+                    continue;
+                if (d >= up)
+                    continue;
+            } else if (d >= lo && d < up) {
+                continue;
+            }
+            if (flags & 8)
+                d = fabsf(up - d);
+            else if (flags & 16)
+                d = fabsf(lo - d);
+            else if (flags & 32)
+                d = d > (lo + up) / 2.0f ? fabsf(up - d) : fabsf(lo - d);
+            if (mi == ma) {
+                dintra[ea * ne + ei] += d;
+                nintra[ea * ne + ei] += 1;
+            } else {
+                dinter[ea * ne + ei] += d;
+                ninter[ea * ne + ei] += 1;
+            }
+        }
+    }
+}
+
+/* atomic_distances.pyx:632-657: pairs i < j at [el(i)][el(j)]. */
+void oracle_pair_elements_stats(const int32_t *el, const int32_t *mol, int64_t n, int32_t ne, int32_t *nintra,
+                                int32_t *ninter)
+{
+    for (int64_t i = 0; i + 1 < n; ++i)
+        for (int64_t j = i + 1; j < n; ++j) {
+            if (mol[j] == mol[i])
+                nintra[el[i] * ne + el[j]] += 1;
+            else
+                ninter[el[i] * ne + el[j]] += 1;
+        }
+}

@@ -78,6 +78,9 @@ def _load():
                 "oracle_full_pairs_histograms_coords": [F32P, i64, F32P, cint, I32P, I32P, i32, f32, f32, f32, i32, F32P, F32P],
                 "oracle_multiple_pairs_histograms_dists": [I32P, i64, F32P, i64, I32P, I32P, i32, f32, f32, f32, i32, cint, F32P, F32P],
                 "oracle_transform_coordinates": [F32P, F32P, i64, F32P],
+                "oracle_atomic_distances": [I32P, i64, F32P, F32P, i64, F32P, cint, I32P, I32P, i32, F32P, F32P, cint,
+                                            cint, F32P, F32P, I32P, I32P],
+                "oracle_pair_elements_stats": [I32P, I32P, i64, i32, I32P, I32P],
             }
             for name, args in sig.items():
                 fn = getattr(lib, name)
@@ -345,3 +348,95 @@ def sq_to_Gr_fp64(qValues, rValues, sq):
     dq = q[1] - q[0]
     qs = q * (np.asarray(sq, np.float64) - 1.0)
     return (2.0 / np.pi) * (np.sin(np.outer(r, q)) * dq) @ qs
+
+
+# ----------------------------------------------------------- atomic distances
+def _atomic_flags(inter, intra, within, red_up, red_lo, red):
+    return ((1 if inter else 0) | (2 if intra else 0) | (4 if within else 0) | (8 if red_up else 0) |
+            (16 if red_lo else 0) | (32 if red else 0))
+
+
+def _atomic(indexes, coords, dists, n, basis, isPBC, mol, el, ne, lower, upper, flags, allAtoms, acc=None):
+    ix, m, e = _i(indexes), _i(mol), _i(el)
+    lo, up = _f(lower), _f(upper)
+    if acc is None:
+        acc = (np.zeros((ne, ne, 1), np.int32), np.zeros((ne, ne, 1), np.float32),
+               np.zeros((ne, ne, 1), np.int32), np.zeros((ne, ne, 1), np.float32))
+    ni, di, nn, de = acc
+    c = _f(coords) if coords is not None else None
+    d = _f(dists) if dists is not None else None
+    b = _f(basis) if basis is not None else np.eye(3, dtype=np.float32)
+    _load().oracle_atomic_distances(_p(ix, I32P), ix.shape[0], _p(c) if c is not None else None,
+                                    _p(d) if d is not None else None, n, _p(b), int(bool(isPBC)), _p(m, I32P),
+                                    _p(e, I32P), ne, _p(lo), _p(up), flags, int(bool(allAtoms)), _p(di), _p(de),
+                                    _p(ni, I32P), _p(nn, I32P))
+    return ni, di, nn, de
+
+
+def multiple_atomic_distances_coords(indexes, boxCoords, basis, isPBC, moleculeIndex, elementIndex, numberOfElements,
+                                     lowerLimit, upperLimit, interMolecular=True, intraMolecular=True,
+                                     countWithinLimits=True, reduceDistanceToUpper=False, reduceDistanceToLower=False,
+                                     reduceDistance=False, allAtoms=True, ncores=1):
+    """atomic_distances.pyx:326-417; returns (nintra, dintra, ninter, dinter)."""
+    c = _f(boxCoords)
+    fl = _atomic_flags(interMolecular, intraMolecular, countWithinLimits, reduceDistanceToUpper, reduceDistanceToLower,
+                       reduceDistance)
+    return _atomic(indexes, c, None, c.shape[0], basis, isPBC, moleculeIndex, elementIndex, int(numberOfElements),
+                   lowerLimit, upperLimit, fl, allAtoms)
+
+
+def full_atomic_distances_coords(boxCoords, basis, isPBC, moleculeIndex, elementIndex, numberOfElements, lowerLimit,
+                                 upperLimit, interMolecular=True, intraMolecular=True, reduceDistanceToUpper=False,
+                                 reduceDistanceToLower=False, reduceDistance=False, countWithinLimits=True, ncores=1):
+    """atomic_distances.pyx:500-567."""
+    c = _f(boxCoords)
+    return multiple_atomic_distances_coords(np.arange(c.shape[0], dtype=np.int32), c, basis, isPBC, moleculeIndex,
+                                            elementIndex, numberOfElements, lowerLimit, upperLimit, interMolecular,
+                                            intraMolecular, countWithinLimits, reduceDistanceToUpper,
+                                            reduceDistanceToLower, reduceDistance, allAtoms=False)
+
+
+def multiple_atomic_distances_dists(indexes, distances, moleculeIndex, elementIndex, numberOfElements, lowerLimit,
+                                    upperLimit, interMolecular=True, intraMolecular=True, countWithinLimits=True,
+                                    reduceDistanceToUpper=False, reduceDistanceToLower=False, reduceDistance=False,
+                                    allAtoms=True, ncores=1):
+    """atomic_distances.pyx:419-498 (column i of distances for indexes[i])."""
+    ix = _i(indexes)
+    d = np.ascontiguousarray(_f(distances)[:, :ix.shape[0]])
+    fl = _atomic_flags(interMolecular, intraMolecular, countWithinLimits, reduceDistanceToUpper, reduceDistanceToLower,
+                       reduceDistance)
+    return _atomic(ix, None, d, d.shape[0], None, False, moleculeIndex, elementIndex, int(numberOfElements),
+                   lowerLimit, upperLimit, fl, allAtoms)
+
+
+def full_atomic_distances_dists(distances, moleculeIndex, elementIndex, numberOfElements, lowerLimit, upperLimit,
+                                interMolecular=True, intraMolecular=True, reduceDistanceToUpper=False,
+                                reduceDistanceToLower=False, reduceDistance=False, countWithinLimits=True):
+    """atomic_distances.pyx:569-630."""
+    d = _f(distances)
+    return multiple_atomic_distances_dists(np.arange(d.shape[1], dtype=np.int32), d, moleculeIndex, elementIndex,
+                                           numberOfElements, lowerLimit, upperLimit, interMolecular, intraMolecular,
+                                           countWithinLimits, reduceDistanceToUpper, reduceDistanceToLower,
+                                           reduceDistance, allAtoms=False)
+
+
+def single_atomic_distances_dists(atomIndex, distances, moleculeIndex, elementIndex, dintra, dinter, nintra, ninter,
+                                  lowerLimit, upperLimit, interMolecular=True, intraMolecular=True,
+                                  countWithinLimits=True, reduceDistanceToUpper=False, reduceDistanceToLower=False,
+                                  reduceDistance=False, allAtoms=True, ncores=1):
+    """atomic_distances.pyx:241-324 (in place)."""
+    d = np.ascontiguousarray(_f(distances).reshape(-1, 1))
+    fl = _atomic_flags(interMolecular, intraMolecular, countWithinLimits, reduceDistanceToUpper, reduceDistanceToLower,
+                       reduceDistance)
+    _atomic(np.array([atomIndex], np.int32), None, d, d.shape[0], None, False, moleculeIndex, elementIndex,
+            dintra.shape[0], lowerLimit, upperLimit, fl, allAtoms, acc=(nintra, dintra, ninter, dinter))
+
+
+def pair_elements_stats(elementIndex, moleculeIndex, numberOfElements):
+    """atomic_distances.pyx:659-672."""
+    e, m = _i(elementIndex), _i(moleculeIndex)
+    ne = int(numberOfElements)
+    ni = np.zeros((ne, ne, 1), np.int32)
+    nn = np.zeros((ne, ne, 1), np.int32)
+    _load().oracle_pair_elements_stats(_p(e, I32P), _p(m, I32P), e.shape[0], ne, _p(ni, I32P), _p(nn, I32P))
+    return ni, nn

@@ -233,6 +233,58 @@ def main():
                              gr_to_sq=rs.gr_to_sq(r, gr, q, F(0.08)), Gr_to_sq=sq,
                              sq_to_Gr_raises=np.int32(sq_to_Gr_raises))
 
+    # M: atomic_distances (InterMolecularDistanceConstraint): every flag
+    # combination on a PBC system with 5-atom molecules, the dists variants,
+    # the in-place single-atom call and pair_elements_stats.
+    if "atomic_distances" in R:
+        ad = R["atomic_distances"]
+        rng = np.random.default_rng(808)
+        n, ne = 600, 3
+        c = rng.random((n, 3)).astype(F)
+        B = triclinic_basis(19.0, 18.0, 20.0, 85.0, 95.0, 105.0)
+        mol = (np.arange(n) // 5).astype(np.int32)
+        el = rng.integers(0, ne, size=n).astype(np.int32)
+        lo = (0.8 + 0.4 * rng.random((ne, ne, 1))).astype(F)
+        up = (2.2 + 1.2 * rng.random((ne, ne, 1))).astype(F)
+        idx = np.array([3, 17, 250, 17, 599, 0], np.int32)
+        d = dict(coords=c, basis=B, mol=mol, el=el, ne=np.int32(ne), lower=lo, upper=up, indexes=idx)
+        variants = [dict(), dict(countWithinLimits=False), dict(reduceDistance=True),
+                    dict(reduceDistanceToUpper=True, intraMolecular=False),
+                    dict(reduceDistanceToLower=True, interMolecular=False), dict(allAtoms=False),
+                    dict(countWithinLimits=False, reduceDistance=True, allAtoms=False)]
+        for v, kw in enumerate(variants):
+            for tag, isPBC in (("pbc", True), ("ibc", False)):
+                coords = c if isPBC else (c * F(19.0)).astype(F)
+                res = ad.multiple_atomic_distances_coords(idx, coords, B, isPBC, mol, el, ne, lo, up, **kw)
+                for k, name in enumerate(("nintra", "dintra", "ninter", "dinter")):
+                    d["m%d_%s_%s" % (v, tag, name)] = res[k]
+        for v, kw in enumerate(variants[:3]):
+            kw = {k: x for k, x in kw.items() if k != "allAtoms"}
+            res = ad.full_atomic_distances_coords(c, B, True, mol, el, ne, lo, up, **kw)
+            for k, name in enumerate(("nintra", "dintra", "ninter", "dinter")):
+                d["f%d_%s" % (v, name)] = res[k]
+        dm = pd.pairs_distances_to_multi_indexcoords(idx, c, B, True, True, 1)
+        d["dm"] = dm
+        res = ad.multiple_atomic_distances_dists(idx, dm, mol, el, ne, lo, up, countWithinLimits=False)
+        for k, name in enumerate(("nintra", "dintra", "ninter", "dinter")):
+            d["md_%s" % name] = res[k]
+        sq = pd.pairs_distances_to_multi_indexcoords(np.arange(60, dtype=np.int32), c[:60], B, True, True, 1)
+        d["dsq"] = sq
+        res = ad.full_atomic_distances_dists(sq, mol[:60], el[:60], ne, lo, up, countWithinLimits=False)
+        for k, name in enumerate(("nintra", "dintra", "ninter", "dinter")):
+            d["fd_%s" % name] = res[k]
+        di = rng.random((ne, ne, 1)).astype(F)
+        de = rng.random((ne, ne, 1)).astype(F)
+        ni = rng.integers(0, 5, size=(ne, ne, 1)).astype(np.int32)
+        nn = rng.integers(0, 5, size=(ne, ne, 1)).astype(np.int32)
+        d["s0_dintra"], d["s0_dinter"], d["s0_nintra"], d["s0_ninter"] = di.copy(), de.copy(), ni.copy(), nn.copy()
+        row = pd.pairs_distances_to_indexcoords(42, c, B, True, True, 1)
+        d["srow"] = row
+        ad.single_atomic_distances_dists(42, row, mol, el, di, de, ni, nn, lo, up, reduceDistance=True)
+        d["s_dintra"], d["s_dinter"], d["s_nintra"], d["s_ninter"] = di, de, ni, nn
+        d["stats_intra"], d["stats_inter"] = ad.pair_elements_stats(el, mol, ne)
+        out["atomic_distances"] = d
+
     # L: transform_coordinates (box -> real through the basis, real -> box
     # through its inverse).
     B = triclinic_basis(26.0, 24.0, 25.0, 78.0, 95.0, 110.0)

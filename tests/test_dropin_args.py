@@ -7,6 +7,7 @@ import inspect
 import numpy as np
 import pytest
 
+from fullrmc_gb300 import atomic_distances as ad
 from fullrmc_gb300 import pairs_distances as pd
 from fullrmc_gb300 import pairs_histograms as ph
 from fullrmc_gb300 import reciprocal_space as rs
@@ -42,6 +43,32 @@ REFERENCE_SIGNATURES = {
     rs.gr_to_sq: "distances, gr, qrange, rho",
     rs.Gr_to_sq: "distances, Gr, qrange",
     rs.sq_to_Gr: "qValues, rValues, sq",
+    ad.single_atomic_distances_dists: "atomIndex, distances, moleculeIndex, elementIndex, dintra, dinter, nintra, "
+                                      "ninter, lowerLimit, upperLimit, interMolecular=True, intraMolecular=True, "
+                                      "countWithinLimits=True, reduceDistanceToUpper=False, "
+                                      "reduceDistanceToLower=False, reduceDistance=False, allAtoms=True, ncores=1",
+    ad.single_atomic_distances_dists_serial: "atomIndex, distances, moleculeIndex, elementIndex, dintra, dinter, "
+                                             "nintra, ninter, lowerLimit, upperLimit, interMolecular=True, "
+                                             "intraMolecular=True, countWithinLimits=True, "
+                                             "reduceDistanceToUpper=False, reduceDistanceToLower=False, "
+                                             "reduceDistance=False, allAtoms=True",
+    ad.multiple_atomic_distances_coords: "indexes, boxCoords, basis, isPBC, moleculeIndex, elementIndex, "
+                                         "numberOfElements, lowerLimit, upperLimit, interMolecular=True, "
+                                         "intraMolecular=True, countWithinLimits=True, reduceDistanceToUpper=False, "
+                                         "reduceDistanceToLower=False, reduceDistance=False, allAtoms=True, ncores=1",
+    ad.multiple_atomic_distances_dists: "indexes, distances, moleculeIndex, elementIndex, numberOfElements, "
+                                        "lowerLimit, upperLimit, interMolecular=True, intraMolecular=True, "
+                                        "countWithinLimits=True, reduceDistanceToUpper=False, "
+                                        "reduceDistanceToLower=False, reduceDistance=False, allAtoms=True, ncores=1",
+    ad.full_atomic_distances_coords: "boxCoords, basis, isPBC, moleculeIndex, elementIndex, numberOfElements, "
+                                     "lowerLimit, upperLimit, interMolecular=True, intraMolecular=True, "
+                                     "reduceDistanceToUpper=False, reduceDistanceToLower=False, reduceDistance=False, "
+                                     "countWithinLimits=True, ncores=1",
+    ad.full_atomic_distances_dists: "distances, moleculeIndex, elementIndex, numberOfElements, lowerLimit, "
+                                    "upperLimit, interMolecular=True, intraMolecular=True, "
+                                    "reduceDistanceToUpper=False, reduceDistanceToLower=False, reduceDistance=False, "
+                                    "countWithinLimits=True",
+    ad.pair_elements_stats: "elementIndex, moleculeIndex, numberOfElements",
 }
 
 
@@ -90,3 +117,14 @@ def test_empty_inputs_need_no_device():
     hi, he = ph.full_pairs_histograms_coords(np.zeros((1, 3), F), B, True, M[:1], M[:1], 2, 0.0, 1.0, 0.1, 10)
     assert not hi.any() and not he.any()
     assert ph.full_pairs_histograms_coords(C, B, True, M, M, 0, 0.0, 1.0, 0.1, 10)[0].shape == (0, 0, 10)
+
+
+def test_atomic_limits_shape_is_checked():
+    lo = np.zeros((2, 2, 1), F)
+    with pytest.raises(AssertionError):
+        ad.multiple_atomic_distances_coords(M[:1], C, B, True, M, M, 3, lo, lo)
+    with pytest.raises(AssertionError):
+        ad.multiple_atomic_distances_coords(M[:1], C, B, True, M, M, 2, np.zeros((2, 2, 2), F),
+                                            np.zeros((2, 2, 2), F))
+    with pytest.raises(ValueError, match="dtype mismatch"):
+        ad.multiple_atomic_distances_coords(M[:1], C, B, True, M, M, 2, lo.astype(np.float64), lo)

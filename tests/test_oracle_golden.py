@@ -117,3 +117,49 @@ def test_fp64_transforms_match_reference_float32(oracle_mod):
     # recovers G(r) up to truncation of the q range (smoke check of the formula).
     G = oracle_mod.sq_to_Gr_fp64(q, r, S64)
     assert np.isfinite(G).all()
+
+
+def _atomic_cases(g):
+    """(function name, args, kwargs, golden key prefix) of the atomic_distances golden file."""
+    c, B, mol, el, ne = g["coords"], g["basis"], g["mol"], g["el"], int(g["ne"])
+    lo, up, idx = g["lower"], g["upper"], g["indexes"]
+    variants = [dict(), dict(countWithinLimits=False), dict(reduceDistance=True),
+                dict(reduceDistanceToUpper=True, intraMolecular=False),
+                dict(reduceDistanceToLower=True, interMolecular=False), dict(allAtoms=False),
+                dict(countWithinLimits=False, reduceDistance=True, allAtoms=False)]
+    out = []
+    for v, kw in enumerate(variants):
+        for tag, isPBC in (("pbc", True), ("ibc", False)):
+            coords = c if isPBC else (c * np.float32(19.0)).astype(np.float32)
+            out.append(("multiple_atomic_distances_coords", (idx, coords, B, isPBC, mol, el, ne, lo, up), kw,
+                        "m%d_%s_" % (v, tag)))
+    for v, kw in enumerate(variants[:3]):
+        kw = {k: x for k, x in kw.items() if k != "allAtoms"}
+        out.append(("full_atomic_distances_coords", (c, B, True, mol, el, ne, lo, up), kw, "f%d_" % v))
+    out.append(("multiple_atomic_distances_dists", (idx, g["dm"], mol, el, ne, lo, up),
+                dict(countWithinLimits=False), "md_"))
+    out.append(("full_atomic_distances_dists", (g["dsq"], mol[:60], el[:60], ne, lo, up),
+                dict(countWithinLimits=False), "fd_"))
+    return out
+
+
+def check_atomic_golden(module):
+    """Every atomic_distances golden case through `module`, bit for bit."""
+    g = golden("atomic_distances")
+    for name, args, kw, pre in _atomic_cases(g):
+        res = getattr(module, name)(*args, **kw)
+        for k, key in enumerate(("nintra", "dintra", "ninter", "dinter")):
+            want = g[pre + key]
+            assert res[k].dtype == want.dtype and np.array_equal(res[k], want), (name, kw, pre, key)
+    di, de = g["s0_dintra"].copy(), g["s0_dinter"].copy()
+    ni, nn = g["s0_nintra"].copy(), g["s0_ninter"].copy()
+    module.single_atomic_distances_dists(42, g["srow"], g["mol"], g["el"], di, de, ni, nn, g["lower"], g["upper"],
+                                         reduceDistance=True)
+    for got, key in ((di, "s_dintra"), (de, "s_dinter"), (ni, "s_nintra"), (nn, "s_ninter")):
+        assert np.array_equal(got, g[key]), key
+    si, se = module.pair_elements_stats(g["el"], g["mol"], int(g["ne"]))
+    assert np.array_equal(si, g["stats_intra"]) and np.array_equal(se, g["stats_inter"])
+
+
+def test_oracle_atomic_distances_golden(oracle_mod):
+    check_atomic_golden(oracle_mod)
