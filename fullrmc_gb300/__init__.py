@@ -2,15 +2,15 @@
 
 The package provides drop-in replacements of fullrmc's Cython modules
 ``fullrmc.Core.pairs_distances``, ``fullrmc.Core.pairs_histograms``,
-``fullrmc.Core.reciprocal_space``, ``fullrmc.Core.boundary_conditions_collection``
-and ``fullrmc.Core.atomic_distances`` (same signatures, bit-identical float32
-results), backed by
+``fullrmc.Core.reciprocal_space``, ``fullrmc.Core.boundary_conditions_collection``,
+``fullrmc.Core.atomic_distances`` and ``fullrmc.Core.atomic_coordination``
+(same signatures, bit-identical float32 results), backed by
 ``libfrmc_gpu.so`` (CUDA, sm_103a; C ABI in ``include/frmc_gpu.h``), plus
 device-resident RMC engines (``fullrmc_gb300.engine``) and a serving loop
 (``fullrmc_gb300.serve``).
 
 ``install()`` makes ``import fullrmc.Core.pairs_histograms`` (and the other
-four) resolve to these modules, so fullrmc's constraints run unmodified.
+five) resolve to these modules, so fullrmc's constraints run unmodified.
 """
 from __future__ import annotations
 
@@ -19,8 +19,8 @@ import importlib.abc
 import importlib.util
 import sys
 
-from . import (atomic_distances, boundary_conditions_collection, pairs_distances, pairs_histograms,  # noqa: F401
-               reciprocal_space)
+from . import (atomic_coordination, atomic_distances, boundary_conditions_collection, pairs_distances,  # noqa: F401
+               pairs_histograms, reciprocal_space)
 from ._native import NativeError, device_info, load  # noqa: F401
 
 __version__ = "0.1.0"
@@ -31,6 +31,7 @@ DROPIN_MODULES = {
     "reciprocal_space": reciprocal_space,
     "boundary_conditions_collection": boundary_conditions_collection,
     "atomic_distances": atomic_distances,
+    "atomic_coordination": atomic_coordination,
 }
 
 

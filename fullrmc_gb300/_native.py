@@ -18,6 +18,7 @@ LIB_PATH = os.path.join(_PKG, "_lib", "libfrmc_gpu.so")
 F32P = ctypes.POINTER(ctypes.c_float)
 F64P = ctypes.POINTER(ctypes.c_double)
 I32P = ctypes.POINTER(ctypes.c_int32)
+I64P = ctypes.POINTER(ctypes.c_int64)
 U32P = ctypes.POINTER(ctypes.c_uint32)
 i64 = ctypes.c_int64
 i32 = ctypes.c_int32
@@ -79,6 +80,8 @@ SIGNATURES = {
     "frmc_single_atomic_distances_dists": [i32, F32P, i64, I32P, I32P, i32, F32P, F32P, I32P, I32P, F32P, F32P, cint,
                                            cint],
     "frmc_pair_elements_stats": [I32P, I32P, i64, i32, I32P, I32P],
+    "frmc_coordination_terms": [F32P, i64, F32P, cint, F32P, I64P, I32P, i32, I32P, I64P, i32, I32P, I32P, I32P, i64,
+                                F32P, F32P, F32P, i32],
 }
 _RESTYPE = {"frmc_last_error": ctypes.c_char_p}
 

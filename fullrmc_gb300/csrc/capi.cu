@@ -6,7 +6,9 @@
 // between calls, PairDistributionConstraints.py:1092-1122).
 #include <climits>
 #include <cmath>
+#include <algorithm>
 #include <cstring>
+#include <vector>
 
 #include "frmc_gpu.h"
 #include "frmc_runtime.h"
@@ -683,6 +685,170 @@ int frmc_pair_elements_stats(const int32_t *elementIndex, const int32_t *molecul
     TRY(launch_pair_stats(c->buf[BUF_EL].as<int>(), c->buf[BUF_MOL].as<int>(), (int)n, ne, acc, acc + m, c->stream));
     TRY(d2h(nintra, acc, 4 * m, c->stream));
     TRY(d2h(ninter, acc + m, 4 * m, c->stream));
+    return finish(c);
+}
+
+// ----------------------------------------------- coordination numbers (host)
+// atomic_coordination.pyx: every entry point is a sequence of terms (a row,
+// an index list, a definition); see coord_kernels.cu.  Everything is checked
+// before anything runs, so an index error leaves coordNumData unchanged.
+
+static int coord_index_error(const int32_t *list, int64_t len, int64_t rowlen)
+{
+    for (int64_t e = 0; e < len; ++e)
+        if (list[e] < -rowlen || list[e] >= rowlen)
+            return set_error(FRMC_E_INDEX, "index %d is out of bounds for axis 0 with size %lld", list[e],
+                             (long long)rowlen);
+    return FRMC_OK;
+}
+
+static size_t align16(size_t x)
+{
+    return (x + 15) & ~(size_t)15;
+}
+
+int frmc_coordination_terms(const float *boxCoords, int64_t n, const float *basis, int isPBC, const float *distances,
+                            const int64_t *dist_off, const int32_t *dist_len, int32_t nrows, const int32_t *lists,
+                            const int64_t *list_off, int32_t nlists, const int32_t *term_row,
+                            const int32_t *term_list, const int32_t *term_def, int64_t nterms,
+                            const float *lowerShells, const float *upperShells, float *coordNumData, int32_t ndata)
+{
+    const bool coords = boxCoords != nullptr;
+    TRY(check_n(coords ? n : 0, "coordinates"));
+    if (nterms < 0 || nterms > INT_MAX / 2 || nlists < 0 || ndata < 0 || nrows < 0)
+        return set_error(FRMC_E_ARG, "coordination: negative or too many terms, lists or definitions");
+    if (nterms == 0)
+        return FRMC_OK;
+    if (!coords && !distances)
+        return set_error(FRMC_E_ARG, "coordination: neither coordinates nor distances given");
+    const int64_t npool = nlists ? list_off[nlists] : 0;
+    for (int32_t l = 0; l < nlists; ++l)
+        if (list_off[l] < 0 || list_off[l] > list_off[l + 1] || list_off[l + 1] - list_off[l] > INT_MAX)
+            return set_error(FRMC_E_ARG, "coordination: bad list offsets");
+    int64_t dpool = 0;
+    if (!coords)
+        for (int32_t r = 0; r < nrows; ++r) {
+            if (dist_off[r] < 0 || dist_len[r] < 0)
+                return set_error(FRMC_E_ARG, "coordination: bad distance row offsets");
+            dpool = std::max<int64_t>(dpool, dist_off[r] + dist_len[r]);
+        }
+    // per-list extremes, computed for the lists the terms use
+    std::vector<int32_t> lmin(nlists, INT_MAX), lmax(nlists, INT_MIN);
+    std::vector<char> seen(nlists, 0);
+    std::vector<int> def_count((size_t)ndata + 1, 0);
+    long long nitems = 0;
+    const int chunk = coordination_chunk();
+    for (int64_t t = 0; t < nterms; ++t) {
+        const int32_t l = term_list[t], d = term_def[t], r = term_row[t];
+        if (l < 0 || l >= nlists)
+            return set_error(FRMC_E_ARG, "coordination: term %lld names list %d of %d", (long long)t, l, nlists);
+        if (d < 0 || d >= ndata)
+            return set_error(FRMC_E_INDEX, "definition index %d out of range for %d definitions", d, ndata);
+        const int64_t rows = coords ? n : nrows;
+        if (r < 0 || r >= rows)
+            return set_error(FRMC_E_INDEX, "index %d is out of bounds for axis 0 with size %lld", r,
+                             (long long)rows);
+        const int32_t *lp = lists + list_off[l];
+        const int64_t len = list_off[l + 1] - list_off[l];
+        if (!seen[l]) {
+            seen[l] = 1;
+            for (int64_t e = 0; e < len; ++e) {
+                lmin[l] = std::min(lmin[l], lp[e]);
+                lmax[l] = std::max(lmax[l], lp[e]);
+            }
+        }
+        const int64_t rowlen = coords ? n : dist_len[r];
+        if (len && (lmin[l] < -rowlen || lmax[l] >= rowlen))
+            return coord_index_error(lp, len, rowlen);
+        nitems += (len + chunk - 1) / chunk;
+        def_count[d] += 1;
+    }
+    if (nitems > INT_MAX)
+        return set_error(FRMC_E_ARG, "coordination: too many list entries");
+    int ndefs = 0;
+    for (int32_t d = 0; d < ndata; ++d) ndefs += def_count[d] > 0;
+    // one staging block: terms, items, distance rows, definitions, windows,
+    // accumulators and the zeroed per-term counts
+    const size_t o_terms = 0;
+    const size_t o_items = align16(o_terms + sizeof(CoordTerm) * (size_t)nterms);
+    const size_t o_doff = align16(o_items + sizeof(int2) * (size_t)nitems);
+    const size_t o_dlen = align16(o_doff + 8 * (size_t)(coords ? 0 : nrows));
+    const size_t o_ids = align16(o_dlen + 4 * (size_t)(coords ? 0 : nrows));
+    const size_t o_off = align16(o_ids + 4 * (size_t)ndefs);
+    const size_t o_dterms = align16(o_off + 4 * (size_t)(ndefs + 1));
+    const size_t o_lower = align16(o_dterms + 4 * (size_t)nterms);
+    const size_t o_upper = align16(o_lower + 4 * (size_t)ndata);
+    const size_t o_data = align16(o_upper + 4 * (size_t)ndata);
+    const size_t o_counts = align16(o_data + 4 * (size_t)ndata);
+    const size_t total = align16(o_counts + 4 * (size_t)nterms);
+    std::vector<unsigned char> stage(total, 0);
+    CoordTerm *T = reinterpret_cast<CoordTerm *>(stage.data() + o_terms);
+    int2 *I = reinterpret_cast<int2 *>(stage.data() + o_items);
+    long long k = 0;
+    for (int64_t t = 0; t < nterms; ++t) {
+        const int32_t l = term_list[t];
+        const int64_t len = list_off[l + 1] - list_off[l];
+        T[t] = CoordTerm{term_row[t], term_def[t], (long long)list_off[l], (int)len, 0};
+        for (int64_t e = 0; e < len; e += chunk) I[k++] = make_int2((int)t, (int)e);
+    }
+    if (!coords) {
+        std::memcpy(stage.data() + o_doff, dist_off, 8 * (size_t)nrows);
+        std::memcpy(stage.data() + o_dlen, dist_len, 4 * (size_t)nrows);
+    }
+    int *ids = reinterpret_cast<int *>(stage.data() + o_ids);
+    int *off = reinterpret_cast<int *>(stage.data() + o_off);
+    int *dterms = reinterpret_cast<int *>(stage.data() + o_dterms);
+    std::vector<int> slot((size_t)ndata, -1);
+    int u = 0, acc = 0;
+    for (int32_t d = 0; d < ndata; ++d)
+        if (def_count[d]) {
+            ids[u] = d;
+            off[u] = acc;
+            slot[d] = acc;
+            acc += def_count[d];
+            ++u;
+        }
+    off[ndefs] = acc;
+    for (int64_t t = 0; t < nterms; ++t) dterms[slot[term_def[t]]++] = (int)t;  // stable: call order
+    std::memcpy(stage.data() + o_lower, lowerShells, 4 * (size_t)ndata);
+    std::memcpy(stage.data() + o_upper, upperShells, 4 * (size_t)ndata);
+    std::memcpy(stage.data() + o_data, coordNumData, 4 * (size_t)ndata);
+
+    LOCKED_CTX(c);
+    TRY(c->buf[BUF_COORD_META].ensure(total));
+    unsigned char *meta = c->buf[BUF_COORD_META].as<unsigned char>();
+    TRY(h2d(meta, stage.data(), total, c->stream));
+    TRY(c->buf[BUF_COORD_LISTS].ensure(4 * (size_t)npool + 16));
+    TRY(h2d(c->buf[BUF_COORD_LISTS].p, lists, 4 * (size_t)npool, c->stream));
+    CoordLaunch L;
+    if (coords) {
+        TRY(c->buf[BUF_COORDS].ensure(12 * (size_t)n + 16));
+        TRY(h2d(c->buf[BUF_COORDS].p, boxCoords, 12 * (size_t)n, c->stream));
+        L.coords = c->buf[BUF_COORDS].as<float>();
+        L.basis = basis ? basis : kIdentity;
+        L.isPBC = isPBC;
+        L.n = (int)n;
+    } else {
+        TRY(c->buf[BUF_AUX0].ensure(4 * (size_t)dpool + 16));
+        TRY(h2d(c->buf[BUF_AUX0].p, distances, 4 * (size_t)dpool, c->stream));
+        L.dists = c->buf[BUF_AUX0].as<float>();
+        L.dist_off = reinterpret_cast<const long long *>(meta + o_doff);
+        L.dist_len = reinterpret_cast<const int *>(meta + o_dlen);
+    }
+    L.lists = c->buf[BUF_COORD_LISTS].as<int>();
+    L.terms = reinterpret_cast<const CoordTerm *>(meta + o_terms);
+    L.items = reinterpret_cast<const int2 *>(meta + o_items);
+    L.nitems = nitems;
+    L.lower = reinterpret_cast<const float *>(meta + o_lower);
+    L.upper = reinterpret_cast<const float *>(meta + o_upper);
+    L.counts = reinterpret_cast<int *>(meta + o_counts);
+    L.def_ids = reinterpret_cast<const int *>(meta + o_ids);
+    L.def_off = reinterpret_cast<const int *>(meta + o_off);
+    L.def_terms = reinterpret_cast<const int *>(meta + o_dterms);
+    L.ndefs = ndefs;
+    L.data = reinterpret_cast<float *>(meta + o_data);
+    TRY(coordination_run(L, c->stream));
+    TRY(d2h(coordNumData, meta + o_data, 4 * (size_t)ndata, c->stream));
     return finish(c);
 }
 

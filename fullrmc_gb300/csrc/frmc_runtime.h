@@ -66,6 +66,8 @@ enum BufRole {
     BUF_ATOMIC_LIST_V,
     BUF_ATOMIC_ACC,
     BUF_ATOMIC_LIMITS,
+    BUF_COORD_LISTS,
+    BUF_COORD_META,
     BUF_COUNT_
 };
 
@@ -152,5 +154,38 @@ int launch_pair_stats(const int *el, const int *mol, int n, int ne, int *nintra,
 int launch_pack_atoms(const float *coords, const int *el, int n, float4 *out, cudaStream_t st);
 // The inverse: float4 (x, y, z, el bits) -> AoS coordinates and elements.
 int launch_unpack_atoms(const float4 *atoms, int n, float *coords, int *el, cudaStream_t st);
+
+// Coordination-number terms (coord_kernels.cu).  A term adds to data[def]
+// the number of entries j of one index list (terms[t].begin, terms[t].len in
+// `lists`; negative j counts from the end of the row) with
+// lower[def] <= d(row, j) <= upper[def].
+struct CoordTerm {
+    int row;           // core atom (coordinates) or distance row
+    int def;           // definition: window and accumulator
+    long long begin;   // first entry of the term's list in `lists`
+    int len;           // entries in the list
+    int pad;
+};
+struct CoordLaunch {
+    const float *coords = nullptr;  // device (n, 3) box coordinates, or null
+    const float *basis = nullptr;   // host 3x3 basis (coordinates only)
+    int isPBC = 0;
+    int n = 0;
+    const float *dists = nullptr;   // device distance rows (when coords is null)
+    const long long *dist_off = nullptr;
+    const int *dist_len = nullptr;
+    const int *lists = nullptr;
+    const CoordTerm *terms = nullptr;
+    const int2 *items = nullptr;    // (term, first entry) per CTA
+    long long nitems = 0;
+    const float *lower = nullptr, *upper = nullptr;
+    int *counts = nullptr;          // per term, zeroed
+    const int *def_ids = nullptr, *def_off = nullptr, *def_terms = nullptr;
+    int ndefs = 0;                  // definitions touched
+    float *data = nullptr;          // device accumulators, updated in place
+};
+int coordination_run(const CoordLaunch &L, cudaStream_t st);
+// List entries handled by one CTA of the counting kernel.
+int coordination_chunk();
 
 }  // namespace frmc

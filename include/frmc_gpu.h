@@ -166,6 +166,28 @@ int frmc_single_atomic_distances_dists(int32_t atomIndex, const float *distances
 int frmc_pair_elements_stats(const int32_t *elementIndex, const int32_t *moleculeIndex, int64_t n, int32_t ne,
                              int32_t *nintra, int32_t *ninter);
 
+/* Extensions/atomic_coordination.pyx (AtomicCoordinationNumberConstraint,
+ * Constraints/AtomicCoordinationConstraints.py:476-580).  Every function of
+ * that module is a sequence of terms; this entry point runs any sequence:
+ * for t = 0 .. nterms-1, in order,
+ *   coordNumData[term_def[t]] += (float) min(2^24, count of entries j of list
+ *       term_list[t] with lowerShells[def] <= d(term_row[t], j) <= upperShells[def])
+ * in float32 (atomic_coordination.pyx:31-44 counts, :184-198 and :220-240 add).
+ * List l is lists[list_off[l] .. list_off[l+1]); a negative entry j counts
+ * from the end of the row (numpy indexing, :77, :99).
+ * With boxCoords (n, 3), the row is a core atom and d the minimum-image
+ * distance |bc(box[row] - box[j])| (pairs_distances_to_point, :98-102);
+ * with boxCoords null, the row r is distances[dist_off[r] .. + dist_len[r])
+ * and d its entry j (single_atom_single_shell_totdists, :71-80).
+ * lowerShells, upperShells and coordNumData have ndata entries; coordNumData
+ * is updated in place.  Out-of-range indexes return FRMC_E_INDEX before
+ * anything changes. */
+int frmc_coordination_terms(const float *boxCoords, int64_t n, const float *basis, int isPBC, const float *distances,
+                            const int64_t *dist_off, const int32_t *dist_len, int32_t nrows, const int32_t *lists,
+                            const int64_t *list_off, int32_t nlists, const int32_t *term_row,
+                            const int32_t *term_list, const int32_t *term_def, int64_t nterms,
+                            const float *lowerShells, const float *upperShells, float *coordNumData, int32_t ndata);
+
 /* ---------------------------------------------- reciprocal space (host, FP64)
  * Extensions/reciprocal_space.pyx:42-73 gr_to_sq:
  *   sq[q] = 1 + 4 pi rho sum_r dr r sin(q r)/q (gr[r] - 1), dr = r[1] - r[0]. */

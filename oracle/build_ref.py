@@ -3,8 +3,9 @@
 This script compiles fullrmc's own Cython sources for the pair-distance and
 histogram path -- ``Extensions/pairs_distances.pyx``,
 ``Extensions/pairs_histograms.pyx``, ``Extensions/reciprocal_space.pyx``,
-``Extensions/boundary_conditions_collection.pyx`` and
-``Extensions/atomic_distances.pyx`` -- exactly as they are, into
+``Extensions/boundary_conditions_collection.pyx``,
+``Extensions/atomic_distances.pyx`` and ``Extensions/atomic_coordination.pyx``
+-- exactly as they are, into
 ``oracle/_ref/fullrmc/Core/``, so that ``import fullrmc.Core.pairs_histograms``
 (with ``oracle/_ref`` first on ``sys.path``) loads the reference itself.  The
 reference's own ``Extensions/setup.py:63-121`` builds the same four modules
@@ -41,7 +42,7 @@ SRC_DIR = os.path.join(REF_OUT, "src")
 PKG_DIR = os.path.join(REF_OUT, "fullrmc", "Core")
 REFERENCE_ROOT = os.environ.get("FRMC_REFERENCE_ROOT", "/root/reference")
 MODULES = ("pairs_distances", "pairs_histograms", "reciprocal_space",
-           "boundary_conditions_collection", "atomic_distances")
+           "boundary_conditions_collection", "atomic_distances", "atomic_coordination")
 
 
 def _cythonize() -> bool:

@@ -440,3 +440,118 @@ def pair_elements_stats(elementIndex, moleculeIndex, numberOfElements):
     nn = np.zeros((ne, ne, 1), np.int32)
     _load().oracle_pair_elements_stats(_p(e, I32P), _p(m, I32P), e.shape[0], ne, _p(ni, I32P), _p(nn, I32P))
     return ni, nn
+
+
+# -------------------------------------------------------- atomic coordination
+# Restatement of Extensions/atomic_coordination.pyx, loop for loop, on top of
+# the C distance restatement above (numpy for the window counts).
+def _shell_count(distances, lowerShell, upperShell):
+    """_single_atom_single_shell_dists (atomic_coordination.pyx:31-44): 1.0f
+    added once per distance inside [lowerShell, upperShell]; a float32 sum of
+    ones is exact up to 2^24 and stays at 2^24 beyond."""
+    d = np.asarray(distances, np.float32)
+    lo, up = np.float32(float(lowerShell)), np.float32(float(upperShell))
+    k = int(np.count_nonzero((lo <= d) & (d <= up)))
+    return np.float32(min(k, 1 << 24))
+
+
+def single_atom_single_shell_subdists(distances, lowerShell, upperShell, ncores=1):
+    """atomic_coordination.pyx:55-65."""
+    return float(_shell_count(distances, lowerShell, upperShell))
+
+
+def single_atom_single_shell_totdists(distances, shellIndexes, lowerShell, upperShell, ncores=1):
+    """atomic_coordination.pyx:71-80."""
+    return float(_shell_count(np.asarray(distances)[np.asarray(shellIndexes)], lowerShell, upperShell))
+
+
+def _core_distances(coreIndex, shellIndexes, boxCoords, basis, isPBC):
+    """pairs_distances_to_point(boxCoords[coreIndex], boxCoords[shellIndexes])
+    (atomic_coordination.pyx:98-102)."""
+    c = _f(boxCoords)
+    pts = np.ascontiguousarray(c[np.asarray(shellIndexes)])
+    return pairs_distances_to_point(c[int(coreIndex)], pts, basis, isPBC)
+
+
+def single_atom_single_shell_coords(coreIndex, shellIndexes, boxCoords, basis, isPBC, lowerShell, upperShell,
+                                    ncores=1):
+    """atomic_coordination.pyx:89-108."""
+    return float(_shell_count(_core_distances(coreIndex, shellIndexes, boxCoords, basis, isPBC), lowerShell,
+                              upperShell))
+
+
+def single_atom_multi_shells_totdists(distances, shellsIndexes, lowerShells, upperShells, ncores=1):
+    """atomic_coordination.pyx:116-133."""
+    out = np.zeros(len(shellsIndexes), np.float32)
+    for i in range(len(shellsIndexes)):
+        out[i] = _shell_count(np.asarray(distances)[np.asarray(shellsIndexes[i])], lowerShells[i], upperShells[i])
+    return out
+
+
+def single_atom_multi_shells_coords(coreIndex, shellsIndexes, boxCoords, basis, isPBC, lowerShells, upperShells,
+                                    ncores=1):
+    """atomic_coordination.pyx:139-166."""
+    out = np.zeros(len(shellsIndexes), np.float32)
+    for i in range(len(shellsIndexes)):
+        out[i] = _shell_count(_core_distances(coreIndex, shellsIndexes[i], boxCoords, basis, isPBC), lowerShells[i],
+                              upperShells[i])
+    return out
+
+
+def _add(coordNumData, defIdx, count):
+    """coordNumData[defIdx] += coordNumber in float32."""
+    coordNumData[defIdx] = np.float32(coordNumData[defIdx]) + count
+
+
+def single_atom_coord_number_totdists(atomIndex, distances, coresIndexes, shellsIndexes, lowerShells, upperShells,
+                                      asCoreDefIdxs, inShellDefIdxs, coordNumData, ncores=1):
+    """atomic_coordination.pyx:171-198: both loops walk asCoreDefIdxs."""
+    d = np.asarray(distances)
+    for defIdx in asCoreDefIdxs[atomIndex]:
+        _add(coordNumData, defIdx, _shell_count(d[np.asarray(shellsIndexes[defIdx])], lowerShells[defIdx],
+                                                upperShells[defIdx]))
+    for defIdx in asCoreDefIdxs[atomIndex]:
+        _add(coordNumData, defIdx, _shell_count(d[np.asarray(coresIndexes[defIdx])], lowerShells[defIdx],
+                                                upperShells[defIdx]))
+
+
+def single_atom_coord_number_coords(atomIndex, boxCoords, basis, isPBC, coresIndexes, shellsIndexes, lowerShells,
+                                    upperShells, asCoreDefIdxs, inShellDefIdxs, coordNumData, ncores=1):
+    """atomic_coordination.pyx:207-240."""
+    for defIdx in asCoreDefIdxs[atomIndex]:
+        d = _core_distances(atomIndex, shellsIndexes[defIdx], boxCoords, basis, isPBC)
+        _add(coordNumData, defIdx, _shell_count(d, lowerShells[defIdx], upperShells[defIdx]))
+    for defIdx in inShellDefIdxs[atomIndex]:
+        d = _core_distances(atomIndex, coresIndexes[defIdx], boxCoords, basis, isPBC)
+        _add(coordNumData, defIdx, _shell_count(d, lowerShells[defIdx], upperShells[defIdx]))
+
+
+def multi_atoms_coord_number_totdists(indexes, distances, coresIndexes, shellsIndexes, lowerShells, upperShells,
+                                      asCoreDefIdxs, inShellDefIdxs, coordNumData, ncores=1):
+    """atomic_coordination.pyx:249-278."""
+    for i in range(len(indexes)):
+        single_atom_coord_number_totdists(int(indexes[i]), distances[i], coresIndexes, shellsIndexes, lowerShells,
+                                          upperShells, asCoreDefIdxs, inShellDefIdxs, coordNumData)
+
+
+def multi_atoms_coord_number_coords(indexes, boxCoords, basis, isPBC, coresIndexes, shellsIndexes, lowerShells,
+                                    upperShells, asCoreDefIdxs, inShellDefIdxs, coordNumData, ncores=1):
+    """atomic_coordination.pyx:280-309."""
+    for i in range(len(indexes)):
+        single_atom_coord_number_coords(int(indexes[i]), boxCoords, basis, isPBC, coresIndexes, shellsIndexes,
+                                        lowerShells, upperShells, asCoreDefIdxs, inShellDefIdxs, coordNumData)
+
+
+def all_atoms_coord_number_totdists(distances, coresIndexes, shellsIndexes, lowerShells, upperShells, asCoreDefIdxs,
+                                    inShellDefIdxs, coordNumData, ncores=1):
+    """atomic_coordination.pyx:317-347: the 2-D array reaches a ``list``
+    argument, so the call raises TypeError."""
+    raise TypeError("Argument 'distances' has incorrect type (expected list, got numpy.ndarray)")
+
+
+def all_atoms_coord_number_coords(boxCoords, basis, isPBC, coresIndexes, shellsIndexes, lowerShells, upperShells,
+                                  asCoreDefIdxs, inShellDefIdxs, coordNumData, ncores=1):
+    """atomic_coordination.pyx:349-377."""
+    multi_atoms_coord_number_coords(np.arange(np.asarray(boxCoords).shape[0], dtype=np.int32), boxCoords, basis,
+                                    isPBC, coresIndexes, shellsIndexes, lowerShells, upperShells, asCoreDefIdxs,
+                                    inShellDefIdxs, coordNumData)

@@ -285,6 +285,24 @@ def main():
         d["stats_intra"], d["stats_inter"] = ad.pair_elements_stats(el, mol, ne)
         out["atomic_distances"] = d
 
+    # N: atomic_coordination (AtomicCoordinationNumberConstraint): every
+    # function of the module on the inputs of tests/coordination_cases.py.
+    if "atomic_coordination" in R:
+        sys.path.insert(0, os.path.dirname(HERE))
+        import coordination_cases as cc
+        g = cc.make_inputs()
+        rows = cc.distance_rows(pd, g, g["indexes"])
+        g["rows"] = np.stack(rows)
+        for key, name, args, data in cc.calls(g, rows):
+            g["out_" + key] = cc.run(R["atomic_coordination"], name, args, data)
+        try:
+            R["atomic_coordination"].all_atoms_coord_number_totdists(g["rows"].T.copy(), *cc.unpack(g),
+                                                                     np.zeros(5, F))
+            g["all_tot_raises"] = np.int32(0)
+        except TypeError:
+            g["all_tot_raises"] = np.int32(1)
+        out["atomic_coordination"] = g
+
     # L: transform_coordinates (box -> real through the basis, real -> box
     # through its inverse).
     B = triclinic_basis(26.0, 24.0, 25.0, 78.0, 95.0, 110.0)

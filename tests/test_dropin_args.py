@@ -7,6 +7,7 @@ import inspect
 import numpy as np
 import pytest
 
+from fullrmc_gb300 import atomic_coordination as ac
 from fullrmc_gb300 import atomic_distances as ad
 from fullrmc_gb300 import pairs_distances as pd
 from fullrmc_gb300 import pairs_histograms as ph
@@ -16,6 +17,9 @@ F, I = np.float32, np.int32
 C = np.zeros((4, 3), F)
 B = np.eye(3, dtype=F)
 M = np.zeros(4, I)
+
+_COORD_LISTS = ("coresIndexes, shellsIndexes, lowerShells, upperShells, asCoreDefIdxs, inShellDefIdxs, "
+                 "coordNumData, ncores=1")
 
 REFERENCE_SIGNATURES = {
     ph.single_pairs_histograms: "atomIndex, distances, moleculeIndex, elementIndex, hintra, hinter, minDistance, "
@@ -69,6 +73,19 @@ REFERENCE_SIGNATURES = {
                                     "reduceDistanceToUpper=False, reduceDistanceToLower=False, reduceDistance=False, "
                                     "countWithinLimits=True",
     ad.pair_elements_stats: "elementIndex, moleculeIndex, numberOfElements",
+    ac.single_atom_single_shell_subdists: "distances, lowerShell, upperShell, ncores=1",
+    ac.single_atom_single_shell_totdists: "distances, shellIndexes, lowerShell, upperShell, ncores=1",
+    ac.single_atom_single_shell_coords: "coreIndex, shellIndexes, boxCoords, basis, isPBC, lowerShell, upperShell, "
+                                        "ncores=1",
+    ac.single_atom_multi_shells_totdists: "distances, shellsIndexes, lowerShells, upperShells, ncores=1",
+    ac.single_atom_multi_shells_coords: "coreIndex, shellsIndexes, boxCoords, basis, isPBC, lowerShells, "
+                                        "upperShells, ncores=1",
+    ac.single_atom_coord_number_totdists: "atomIndex, distances, " + _COORD_LISTS,
+    ac.single_atom_coord_number_coords: "atomIndex, boxCoords, basis, isPBC, " + _COORD_LISTS,
+    ac.multi_atoms_coord_number_totdists: "indexes, distances, " + _COORD_LISTS,
+    ac.multi_atoms_coord_number_coords: "indexes, boxCoords, basis, isPBC, " + _COORD_LISTS,
+    ac.all_atoms_coord_number_totdists: "distances, " + _COORD_LISTS,
+    ac.all_atoms_coord_number_coords: "boxCoords, basis, isPBC, " + _COORD_LISTS,
 }
 
 
@@ -128,3 +145,51 @@ def test_atomic_limits_shape_is_checked():
                                             np.zeros((2, 2, 2), F))
     with pytest.raises(ValueError, match="dtype mismatch"):
         ad.multiple_atomic_distances_coords(M[:1], C, B, True, M, M, 2, lo.astype(np.float64), lo)
+
+
+def _coord_lists():
+    cores = [np.array([0, 1], I)]
+    shells = [np.array([2, 3], I)]
+    asCore = [np.array([0], I), np.array([0], I), np.zeros(0, I), np.zeros(0, I)]
+    inShell = [np.zeros(0, I), np.zeros(0, I), np.array([0], I), np.array([0], I)]
+    return cores, shells, [F(0.5)], [F(2.0)], asCore, inShell
+
+
+def test_coordination_argument_checks_need_no_device():
+    L = _coord_lists()
+    data = np.zeros(1, F)
+    with pytest.raises(TypeError, match="expected list"):
+        ac.multi_atoms_coord_number_coords(M[:1], C, B, True, tuple(L[0]), *L[1:], data)
+    with pytest.raises(ValueError, match="dtype mismatch"):
+        ac.multi_atoms_coord_number_coords(M[:1], C, B, True, *L, np.zeros(1))
+    with pytest.raises(ValueError, match="dtype mismatch"):
+        ac.multi_atoms_coord_number_coords(M[:1], C, B, True, L[0], [L[1][0].astype(np.int64)], *L[2:], data)
+    with pytest.raises(ValueError, match="dtype mismatch"):
+        ac.multi_atoms_coord_number_coords(M[:1].astype(np.int64), C, B, True, *L, data)
+    with pytest.raises(IndexError):  # the reference reads outside its list here
+        ac.multi_atoms_coord_number_coords(np.array([-1], I), C, B, True, *L, data)
+    with pytest.raises(IndexError):  # definition 0 on a zero-length coordNumData
+        ac.multi_atoms_coord_number_coords(M[:1], C, B, True, *L, np.zeros(0, F))
+    with pytest.raises(ValueError, match="read-only"):
+        ro = np.zeros(1, F)
+        ro.flags.writeable = False
+        ac.multi_atoms_coord_number_coords(M[:1], C, B, True, *L, ro)
+    with pytest.raises(TypeError, match="expected list"):
+        ac.multi_atoms_coord_number_totdists(M[:1], np.zeros((1, 4), F), *L, data)
+    with pytest.raises(TypeError, match="expected list, got numpy.ndarray"):
+        ac.all_atoms_coord_number_totdists(np.zeros((4, 4), F), *L, data)
+    with pytest.raises(ValueError, match="dtype mismatch"):
+        ac.all_atoms_coord_number_totdists(np.zeros((4, 4)), *L, data)
+    with pytest.raises(ValueError, match="dtype mismatch"):
+        ac.single_atom_single_shell_subdists(np.zeros(3), 0.5, 1.0)
+    with pytest.raises(TypeError):
+        ac.single_atom_single_shell_coords(0.5, M, C, B, True, 0.5, 1.0)
+    with pytest.raises(TypeError):
+        ac.single_atom_multi_shells_totdists(np.zeros(4, F), (M,), np.zeros(1, F), np.zeros(1, F))
+    with pytest.raises(TypeError, match="real number"):
+        ac.multi_atoms_coord_number_coords(M[:1], C, B, True, L[0], L[1], ["0.5"], *L[3:], data)
+    # nothing to do: no device call, data unchanged
+    ac.multi_atoms_coord_number_coords(np.zeros(0, I), C, B, True, *L, data)
+    ac.multi_atoms_coord_number_coords(np.array([2], I), C, B, True, L[0], L[1], L[2], L[3],
+                                       [np.zeros(0, I)] * 4, [np.zeros(0, I)] * 4, data)
+    assert data[0] == 0

@@ -163,3 +163,27 @@ def check_atomic_golden(module):
 
 def test_oracle_atomic_distances_golden(oracle_mod):
     check_atomic_golden(oracle_mod)
+
+
+def check_coordination_golden(module):
+    """Every atomic_coordination golden case through `module`, bit for bit
+    (returned floats as float32, coordNumData after in-place calls)."""
+    import coordination_cases as cc
+    g = golden("atomic_coordination")
+    rows = [np.ascontiguousarray(r) for r in g["rows"]]
+    for key, name, args, data in cc.calls(g, rows):
+        got = cc.run(module, name, args, data)
+        want = g["out_" + key]
+        assert got.dtype == want.dtype and np.array_equal(got.view(np.int32), want.view(np.int32)), (key, got, want)
+    assert int(g["all_tot_raises"]) == 1
+    with pytest.raises(TypeError):
+        module.all_atoms_coord_number_totdists(np.ascontiguousarray(g["rows"].T), *cc.unpack(g),
+                                               np.zeros(len(g["lower"]), np.float32))
+    for name in ("single_atom_single_shell_subdists", "single_atom_single_shell_totdists"):
+        args = (rows[1], g["lower"][1], g["upper"][1]) if name.endswith("subdists") else \
+            (rows[1], cc.unpack(g)[1][1], g["lower"][1], g["upper"][1])
+        assert type(getattr(module, name)(*args)) is float
+
+
+def test_oracle_atomic_coordination_golden(oracle_mod):
+    check_coordination_golden(oracle_mod)
