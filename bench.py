@@ -24,6 +24,10 @@ Reported beside the headline:
   5,000-atom alloy; the 100,000-atom triclinic system and its FP64 S(Q)
   transform; the 52,000-atom molecular system with 13-atom group moves),
   beside fullrmc's Cython path on a few steps of the same systems;
+* ``dropins``: per-call times of the atomic_distances and
+  atomic_coordination drop-ins (the constraints' per-move call on a moved
+  13-atom ring and their full recomputations, 52,000-atom molecular system)
+  beside fullrmc's Cython on the same calls;
 * ``serving``: the serving loop on a Poisson stream of fit requests (20 per
   second; 2,000-200,000 atoms log-uniform, 1-3 species, G(r) on r 0-12 A
   plus S(Q) on Q 0.5-25 A^-1 with dQ 0.01, 2,000-50,000 steps each), admitted
@@ -259,6 +263,92 @@ def bench_configs(torch, with_cpu):
     return out
 
 
+def _call_ms(fn, reps, budget_s=None):
+    """Median wall-clock milliseconds of fn() over reps calls (host buffers,
+    copies and synchronisation included), after one untimed call."""
+    fn()
+    times = []
+    t_start = time.perf_counter()
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        fn()
+        times.append(1e3 * (time.perf_counter() - t0))
+        if budget_s is not None and time.perf_counter() - t_start > budget_s:
+            break
+    return statistics.median(times), len(times)
+
+
+def bench_dropins(with_cpu):
+    """Per-call times of the atomic_distances and atomic_coordination drop-ins
+    through their Python API (host arrays in and out), beside fullrmc's Cython
+    (ncores=1) on the same call: the constraints' per-move call (the 13 atoms
+    of a moved ring) and the full recomputation, on the 52,000-atom molecular
+    system (three species, 13-atom rings)."""
+    from fullrmc_gb300 import atomic_coordination as gac
+    from fullrmc_gb300 import atomic_distances as gad
+    from fullrmc_gb300 import synthetic
+    s = synthetic.ring_molecules(seed=0, nmol=4000)
+    c, B, el, mol = s.box_coords, s.basis, s.el.astype(np.int32), s.mol.astype(np.int32)
+    n, ne = c.shape[0], 3
+    lo = np.full((ne, ne, 1), 1.8, np.float32)
+    up = np.full((ne, ne, 1), 2.6, np.float32)
+    group = np.arange(13 * 1234, 13 * 1235, dtype=np.int32)
+    sub = 20000  # the full recomputation of atomic_distances on the first 20,000 atoms
+    # coordination definitions: (core species, shell species, window)
+    defs = [(0, 1, 1.0, 1.6), (1, 0, 1.0, 1.6), (0, 2, 0.9, 1.3), (0, 0, 1.2, 1.6)]
+    cores = [np.flatnonzero(el == a).astype(np.int32) for a, _, _, _ in defs]
+    shells = [np.flatnonzero(el == b).astype(np.int32) for _, b, _, _ in defs]
+    lower = [np.float32(x) for _, _, x, _ in defs]
+    upper = [np.float32(x) for _, _, _, x in defs]
+    asCore = [[] for _ in range(n)]
+    inShell = [[] for _ in range(n)]
+    for d in range(len(defs)):
+        for a in cores[d]:
+            asCore[a].append(d)
+        for a in shells[d]:
+            inShell[a].append(d)
+    asCore = [np.array(x, np.int32) for x in asCore]
+    inShell = [np.array(x, np.int32) for x in inShell]
+    L = (cores, shells, lower, upper, asCore, inShell)
+    data = np.zeros(len(defs), np.float32)
+
+    def cases(ad, ac):
+        return {
+            "intermolecular_distances_move": (lambda: ad.multiple_atomic_distances_coords(
+                group, c, B, True, mol, el, ne, lo, up, intraMolecular=False, countWithinLimits=True), 50),
+            "intermolecular_distances_full_20000": (lambda: ad.full_atomic_distances_coords(
+                c[:sub], B, True, mol[:sub], el[:sub], ne, lo, up, intraMolecular=False), 5),
+            "coordination_move": (lambda: ac.multi_atoms_coord_number_coords(group, c, B, True, *L, data), 50),
+            "coordination_all_atoms": (lambda: ac.all_atoms_coord_number_coords(c, B, True, *L, data), 5),
+        }
+
+    out = {}
+    for name, (fn, reps) in cases(gad, gac).items():
+        ms, _ = _call_ms(fn, reps)
+        out[name] = {"gpu_ms": ms, "atoms": sub if name.endswith("20000") else n,
+                     "atoms_per_call": 13 if name.endswith("move") else (sub if "20000" in name else n)}
+    if with_cpu:
+        try:
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import build_ref
+            R = build_ref.import_reference()
+            for name, (fn, reps) in cases(R["atomic_distances"], R["atomic_coordination"]).items():
+                if name == "coordination_all_atoms":
+                    # the same call on the first 2,000 atoms, scaled to all atoms
+                    # (the reference loops over atoms in Python)
+                    idx = np.arange(2000, dtype=np.int32)
+                    ms, k = _call_ms(lambda: R["atomic_coordination"].multi_atoms_coord_number_coords(
+                        idx, c, B, True, *L, data), 2)
+                    out[name].update(cpu_reference_ms=ms * n / 2000.0, cpu_sample="2,000 of %d atoms, scaled" % n)
+                else:
+                    ms, k = _call_ms(fn, 2 if reps < 10 else 10, budget_s=20.0)
+                    out[name].update(cpu_reference_ms=ms, cpu_sample="%d calls" % k)
+                out[name]["gpu_over_cpu"] = out[name]["cpu_reference_ms"] / out[name]["gpu_ms"]
+        except Exception as exc:
+            out["cpu_error"] = str(exc)[:200]
+    return out
+
+
 def run_reference(args):
     ws, rank = _dist()
     if rank != 0:
@@ -453,9 +543,10 @@ def run_ours(args):
     d2h = E * 16  # (chi2, accepted, atom) per engine
 
     allp = bench_allpairs(torch, native, dev)
-    configs = None
+    configs = dropins = None
     if not args.no_configs and rank == 0:
         configs = bench_configs(torch, with_cpu=not args.no_cpu)
+        dropins = bench_dropins(with_cpu=not args.no_cpu)
     serving = None
     if args.serve_seconds > 0 and rank == 0:
         from fullrmc_gb300 import serve
@@ -512,6 +603,7 @@ def run_ours(args):
                              issue_peak_pairs_per_s=issue_peak),
             "serving": serving,
             "configs": configs,
+            "dropins": dropins,
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": K,

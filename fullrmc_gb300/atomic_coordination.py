@@ -26,6 +26,8 @@ functions raise ``IndexError`` and leave ``coordNumData`` unchanged.
 """
 from __future__ import annotations
 
+import operator
+
 import numpy as np
 
 from . import _args as A
@@ -164,6 +166,18 @@ class _Terms:
             data[...] = buf
 
 
+def _atom_defs(seq, idx):
+    """seq[a] for every atom a of idx (a Python list of ints already checked
+    against len(seq)), concatenated: (counts per atom, definition indexes)."""
+    K = len(idx)
+    got = operator.itemgetter(*idx)(seq) if K > 1 else (seq[idx[0]],)
+    counts = np.fromiter(map(len, got), np.int64, K)
+    D = np.concatenate(got) if K else np.zeros(0, np.int64)
+    if D.size and D.dtype.kind not in "iu":  # an empty float list widens the dtype: check one by one
+        D = np.concatenate([_def_array(a) for a in got])
+    return counts, np.asarray(D, np.int64).reshape(-1)
+
+
 def _atoms_terms(T, indexes, rows, coresIndexes, shellsIndexes, lowerShells, upperShells, first, second):
     """The terms of the atoms ``indexes`` (row k for atom indexes[k]):
     first[atom]'s definitions against their shells, then second[atom]'s
@@ -171,21 +185,28 @@ def _atoms_terms(T, indexes, rows, coresIndexes, shellsIndexes, lowerShells, upp
     K = len(indexes)
     if K == 0:
         return
-    idx = [int(a) for a in indexes]
-    d1 = [_def_array(_item(first, "list", a)) for a in idx]
-    d2 = [_def_array(_item(second, "list", a)) for a in idx]
-    c1 = np.fromiter((d.shape[0] for d in d1), np.int64, K)
-    c2 = np.fromiter((d.shape[0] for d in d2), np.int64, K)
-    D1 = np.concatenate(d1) if K else np.zeros(0, np.int64)
-    D2 = np.concatenate(d2) if K else np.zeros(0, np.int64)
-    # windows and lists of the definitions used, in first-use order
-    for kind, D, lists, name in ((0, D1, shellsIndexes, "shellIndexes"), (1, D2, coresIndexes, "shellIndexes")):
-        for d in dict.fromkeys(D.tolist()):
-            lo, up = _item(lowerShells, "list", d), _item(upperShells, "list", d)
-            T.window(d, lo, up)
-            T.list_id((kind, d), _item(lists, "list", d), name)
-    lid1 = np.fromiter((T.keys[(0, d)] for d in D1.tolist()), np.int64, D1.shape[0])
-    lid2 = np.fromiter((T.keys[(1, d)] for d in D2.tolist()), np.int64, D2.shape[0])
+    idx = np.asarray(indexes, np.int64)
+    for seq in (first, second):
+        if seq is None:
+            raise TypeError("'NoneType' object is not subscriptable")
+        if idx.min() < 0 or idx.max() >= len(seq):
+            bad = int(idx[(idx < 0) | (idx >= len(seq))][0])
+            raise IndexError("list index %d out of range" % bad)
+    il = idx.tolist()
+    c1, D1 = _atom_defs(first, il)
+    c2, D2 = _atom_defs(second, il)
+    # windows and lists of the definitions used
+    lids = []
+    for kind, D, lists in ((0, D1, shellsIndexes), (1, D2, coresIndexes)):
+        if D.shape[0] == 0:
+            lids.append(D)
+            continue
+        used = np.unique(D)
+        lut = np.empty(int(used[-1]) + 1 - min(0, int(used[0])), np.int64)
+        for d in used.tolist():
+            T.window(d, _item(lowerShells, "list", d), _item(upperShells, "list", d))
+            lut[d] = T.list_id((kind, d), _item(lists, "list", d), "shellIndexes")
+        lids.append(lut[D])
     start = np.zeros(K, np.int64)
     np.cumsum((c1 + c2)[:-1], out=start[1:])
     total = int((c1 + c2).sum())
@@ -193,7 +214,7 @@ def _atoms_terms(T, indexes, rows, coresIndexes, shellsIndexes, lowerShells, upp
     t_lid = np.empty(total, np.int32)
     t_def = np.empty(total, np.int32)
     rows = np.asarray(rows, np.int64)
-    for c, D, lid, base in ((c1, D1, lid1, start), (c2, D2, lid2, start + c1)):
+    for c, D, lid, base in ((c1, D1, lids[0], start), (c2, D2, lids[1], start + c1)):
         if D.shape[0] == 0:
             continue
         o = np.zeros(K, np.int64)
