@@ -535,6 +535,12 @@ constexpr int kMaxP = 10;  // element pairs loaded with unrolled loads (ne <= 4)
 // an S(Q) term, also keep S in the global Sb (zero for unchanged bins).
 // pair_coef_p * v for |v| <= 4 comes from a small table, so a changed bin
 // costs one FP64 add per non-zero element-pair delta.
+// pair_coef_q * v: from the table for |v| <= 4 and the first kMaxP pairs.
+__device__ __forceinline__ double coef_times(const double *tabv, const double *coef, int q, int v)
+{
+    return (q < kMaxP && (unsigned)(v + 4) <= 8u) ? tabv[q * 9 + v + 4] : coef[q] * (double)v;
+}
+
 template <bool SMEM>
 __device__ double eval_delta(const EDesc &Dg, int *dP, const double *Ab, const double *Bqb, double *red, double *cb,
                              double *sbs, int *sbin, int *s_nchg, double *coef)
@@ -597,75 +603,107 @@ __device__ double eval_delta(const EDesc &Dg, int *dP, const double *Ab, const d
                 mine |= 1ull << r;
         }
         __syncthreads();
-        // 2. exclusive scan of the group counts (warp 0)
-        if (threadIdx.x < 32) {
-            const int ngroups = span >> 5;
-            int run = 0;
-            for (int g0 = 0; g0 < ngroups; g0 += 32) {
-                const int gi = g0 + (int)lane;
-                const int v = gi < ngroups ? s_cnt[gi] : 0;
-                int incl = v;
+        // 2. every warp scans the (at most 64) group counts in registers:
+        // ex0 / ex1 are the list offsets of groups `lane` and 32 + `lane`
+        const int ngroups = span >> 5;
+        const int v0 = (int)lane < ngroups ? s_cnt[lane] : 0;
+        const int v1 = (int)lane + 32 < ngroups ? s_cnt[lane + 32] : 0;
+        int i0 = v0, i1 = v1;
 #pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const int t = __shfl_up_sync(0xffffffffu, incl, o);
-                    if ((int)lane >= o)
-                        incl += t;
-                }
-                if (gi < ngroups)
-                    s_cnt[gi] = run + incl - v;
-                run += __shfl_sync(0xffffffffu, incl, 31);
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t0 = __shfl_up_sync(0xffffffffu, i0, o);
+            const int t1 = __shfl_up_sync(0xffffffffu, i1, o);
+            if ((int)lane >= o) {
+                i0 += t0;
+                i1 += t1;
             }
-            if (lane == 0)
-                *s_nchg = run;
         }
-        __syncthreads();
-        // 3. the list, in increasing bin order
+        const int tot0 = __shfl_sync(0xffffffffu, i0, 31);
+        const int ex0 = i0 - v0, ex1 = tot0 + i1 - v1;
+        const int n = tot0 + __shfl_sync(0xffffffffu, i1, 31);
+        if (threadIdx.x == 0)
+            *s_nchg = n;
+        // 3. the list, in increasing bin order (a warp's bins of one round are
+        // one group, so its offset comes from the lane that holds the group)
         r = 0;
         for (int i = threadIdx.x; i < span; i += blockDim.x, ++r) {
+            const int gi = i >> 5;
+            const int base = gi < 32 ? __shfl_sync(0xffffffffu, ex0, gi) : __shfl_sync(0xffffffffu, ex1, gi - 32);
             const bool any = (mine >> r) & 1ull;
             const unsigned bal = __ballot_sync(0xffffffffu, any);
             if (any)
-                sbin[s_cnt[i >> 5] + __popc(bal & ((1u << lane) - 1u))] = c0 + i;
+                sbin[base + __popc(bal & ((1u << lane) - 1u))] = c0 + i;
         }
         __syncthreads();
-        const int n = *s_nchg;
-        // 4. FP64 on the listed bins
-        for (int k = threadIdx.x; k < n; k += blockDim.x) {
-            const int b = sbin[k];
-            const double a = A[b];
-            const double bq = Bq[b];
-            double S = 0.0;
-#pragma unroll
-            for (int q = 0; q < kMaxP; ++q) {
-                if (q >= np)
-                    break;
-                const int v = delta_at(q, b);
-                if (v) {
+        // 4. FP64 on the listed bins.  The first three non-zero (pair, delta)
+        // of a bin are kept in registers (integer work), S starts from the
+        // table entry of the first, and the warp issues one FP64 add per
+        // further term of its busiest lane (the loop is warp-uniform).
+        for (int k0 = (int)(threadIdx.x & ~31u); k0 < n; k0 += blockDim.x) {
+            const int k = k0 + (int)lane;
+            const bool in = k < n;
+            const int b = in ? sbin[k] : 0;
+            int nnz = 0, q0 = 0, v0 = 0, q1 = 0, v1 = 0, q2 = 0, v2 = 0;
+            auto take = [&](int q, int v) {
+                if (sq) {
+                    if (SMEM)
+                        gdP[q * hs + b] = v;
+                    evl[q * hs + atomicAdd(&s_evn[q], 1)] = (b << 16) | (v & 0xffff);
+                    if (v > 32767 || v < -32768)
+                        s_wide = 1;
+                }
+                if (nnz < 3) {
                     if (!SMEM && !sq)
                         dP[(long long)q * hs + b] = 0;
-                    if (sq) {
-                        if (SMEM)
-                            gdP[q * hs + b] = v;
-                        evl[q * hs + atomicAdd(&s_evn[q], 1)] = (b << 16) | (v & 0xffff);
-                        if (v > 32767 || v < -32768)
-                            s_wide = 1;
+                    if (nnz == 0) {
+                        q0 = q;
+                        v0 = v;
+                    } else if (nnz == 1) {
+                        q1 = q;
+                        v1 = v;
+                    } else {
+                        q2 = q;
+                        v2 = v;
                     }
-                    S += (unsigned)(v + 4) <= 8u ? tabv[q * 9 + v + 4] : coef[q] * (double)v;
+                }
+                ++nnz;
+            };
+            if (in) {
+#pragma unroll
+                for (int q = 0; q < kMaxP; ++q) {
+                    if (q < np) {
+                        const int v = delta_at(q, b);
+                        if (v)
+                            take(q, v);
+                    }
+                }
+                for (int q = kMaxP; q < np; ++q) {
+                    const int v = delta_at(q, b);
+                    if (v)
+                        take(q, v);
                 }
             }
-            for (int q = kMaxP; q < np; ++q) {
-                const int v = delta_at(q, b);
-                if (v) {
-                    if (!SMEM)
-                        dP[(long long)q * hs + b] = 0;
-                    const double cf = coef[q];
-                    S += v == 1 ? cf : (v == -1 ? -cf : cf * (double)v);
+            const int wmax = __reduce_max_sync(0xffffffffu, nnz);
+            double S = in ? coef_times(tabv, coef, q0, v0) : 0.0;
+            if (wmax > 1 && nnz > 1)
+                S += coef_times(tabv, coef, q1, v1);
+            if (wmax > 2 && nnz > 2)
+                S += coef_times(tabv, coef, q2, v2);
+            if (nnz > 3)  // more than three element pairs changed in this bin (rare)
+                for (int q = q2 + 1; q < np; ++q) {
+                    const int v = delta_at(q, b);
+                    if (v) {
+                        if (!SMEM && !sq)
+                            dP[(long long)q * hs + b] = 0;
+                        S += coef_times(tabv, coef, q, v);
+                    }
                 }
+            if (in) {
+                cb[k] = S * fma(A[b], S, -Bq[b]);
+                sbs[k] = neg_twice(S);
+                if (big || sq)
+                    Sb[b] = S;
             }
-            cb[k] = S * fma(a, S, -bq);
-            sbs[k] = neg_twice(S);
-            if (big || sq)
-                Sb[b] = S;
         }
         lanes_add_chunk(red, cb, 0, n);
     }
@@ -860,14 +898,76 @@ __device__ void finish_engine(const EDesc &D, const MovedGroup &g, double *red, 
 // current batch is binned against each moved atom, and each warp reserves the
 // batch's touched-list entries with one shared-memory atomic.  Columns that
 // belong to the moved group are left to group_internal (fullrmc's M - F).
+// Per-thread queue of accepted columns in the fused path: kColQueue entries
+// per thread, entry k of thread t at [k * blockDim + t] (conflict-free).
+constexpr int kColQueue = 8;
+
+struct ColQueue {
+    float *s0, *s1;   // squared distances before / after the move
+    unsigned *info;   // el(j) | same molecule << 8 | accepted before << 9 | after << 10 | group atom << 11
+};
+
+// Bins the queued columns of every thread: each pass pops one entry per
+// thread that has one, so the IEEE sqrt / division and the delta atomics run
+// with full warps instead of one diverging lane.
+__device__ __forceinline__ void flush_columns(const ColView &D, const MovedGroup &g, int *sdP, unsigned *s_tcount,
+                                              const ColQueue &q, int &qn)
+{
+    while (__any_sync(0xffffffffu, qn > 0)) {
+        if (qn > 0) {
+            --qn;
+            const int k = qn * (int)blockDim.x + (int)threadIdx.x;
+            const float s0 = q.s0[k], s1 = q.s1[k];
+            const unsigned info = q.info[k];
+            const int elj = (int)(info & 0xffu);
+            const int gi = (int)(info >> 11);
+            const int ela = g.el[gi];
+            const long long half = (info >> 8) & 1u ? 0 : D.total;
+            const long long rowb = (long long)(ela * D.ne + elj) * D.hs;
+            int f0 = -1, f1 = -1, b0 = 0, b1 = 0;
+            if ((info >> 9) & 1u) {
+                b0 = pair_bin(s0, D.minD, D.binw);
+                const long long f = rowb + b0;
+                if ((unsigned long long)f < (unsigned long long)D.total) f0 = (int)f;
+            }
+            if ((info >> 10) & 1u) {
+                b1 = pair_bin(s1, D.minD, D.binw);
+                const long long f = rowb + b1;
+                if ((unsigned long long)f < (unsigned long long)D.total) f1 = (int)f;
+            }
+            if (f0 != f1) {
+                unsigned pos = atomicAdd(s_tcount, (unsigned)((f0 >= 0) + (f1 >= 0)));
+                if (f0 >= 0) {
+                    D.tlist[pos++] = (int)((half + f0) << 1);
+                    int p, bb;
+                    pair_of_flat(D, f0, ela, elj, b0, p, bb);
+                    if (p >= 0)
+                        atomicSub(sdP + p * D.hs + bb, 1);
+                }
+                if (f1 >= 0) {
+                    D.tlist[pos] = (int)(((half + f1) << 1) | 1);
+                    int p, bb;
+                    pair_of_flat(D, f1, ela, elj, b1, p, bb);
+                    if (p >= 0)
+                        atomicAdd(sdP + p * D.hs + bb, 1);
+                }
+            }
+        }
+    }
+}
+
+// The fused path's columns: every column j (not a moved atom) against every
+// moved atom before and after the move.  Squared distances and the window
+// test are branch-free for a batch of columns; accepted columns go to the
+// thread's queue, flushed when a queue is full and at the end.
 template <int BM, bool GROUP>
-__device__ void fused_columns(const EDesc &Dg, int *sdP, unsigned *s_tcount, const MovedGroup &g)
+__device__ void fused_columns(const EDesc &Dg, int *sdP, unsigned *s_tcount, const MovedGroup &g, const ColQueue &q)
 {
     const ColView D = col_view(Dg);
-    const unsigned lane = threadIdx.x & 31u;
     const int step = kItemUnroll * blockDim.x;
     const int G = GROUP ? g.n : 1;
     const int atom0 = g.atom[0];
+    int qn = 0;
     float4 c[kItemUnroll];
     int mj[kItemUnroll];
 #pragma unroll
@@ -895,55 +995,23 @@ __device__ void fused_columns(const EDesc &Dg, int *sdP, unsigned *s_tcount, con
             valid[u] = ok;
         }
         for (int gi = 0; gi < G; ++gi) {
+            if (__any_sync(0xffffffffu, qn > kColQueue - kItemUnroll))
+                flush_columns(D, g, sdP, s_tcount, q, qn);
             const float3 o = make_float3(g.o[gi][0], g.o[gi][1], g.o[gi][2]);
             const float3 nw = make_float3(g.nw[gi][0], g.nw[gi][1], g.nw[gi][2]);
-            const int ela = g.el[gi], mola = g.mol[gi], arow = ela * D.ne;
-            int f0[kItemUnroll], f1[kItemUnroll], half[kItemUnroll], b0[kItemUnroll], b1[kItemUnroll],
-                elj[kItemUnroll];
-            float s0[kItemUnroll], s1[kItemUnroll];
+            const int mola = g.mol[gi];
 #pragma unroll
             for (int u = 0; u < kItemUnroll; ++u) {
-                s0[u] = pair_s<BM>(o.x, o.y, o.z, c[u].x, c[u].y, c[u].z, D.B);
-                s1[u] = pair_s<BM>(nw.x, nw.y, nw.z, c[u].x, c[u].y, c[u].z, D.B);
-            }
-            unsigned mine = 0;
-#pragma unroll
-            for (int u = 0; u < kItemUnroll; ++u) {
-                half[u] = b0[u] = b1[u] = elj[u] = 0;
-                column_bins(D, s0[u], s1[u], valid[u], c[u], mj[u], arow, mola, f0[u], f1[u], half[u], b0[u], b1[u],
-                            elj[u]);
-                mine += (f0[u] >= 0) + (f1[u] >= 0);
-            }
-            unsigned incl = mine;
-#pragma unroll
-            for (int off = 1; off < 32; off <<= 1) {
-                const unsigned v = __shfl_up_sync(0xffffffffu, incl, off);
-                if (lane >= (unsigned)off) incl += v;
-            }
-            const unsigned tot = __shfl_sync(0xffffffffu, incl, 31);
-            if (tot) {
-                unsigned base = 0;
-                if (lane == 31)
-                    base = atomicAdd(s_tcount, tot);
-                base = __shfl_sync(0xffffffffu, base, 31);
-                unsigned pos = base + incl - mine;
-#pragma unroll
-                for (int u = 0; u < kItemUnroll; ++u) {
-                    if (f0[u] >= 0) {
-                        D.tlist[pos++] = (half[u] + f0[u]) << 1;
-                        int p, b;
-                        pair_of_flat(D, f0[u], ela, elj[u], b0[u], p, b);
-                        if (p >= 0)
-                            atomicSub(sdP + p * D.hs + b, 1);
-                    }
-                    if (f1[u] >= 0) {
-                        D.tlist[pos++] = ((half[u] + f1[u]) << 1) | 1;
-                        int p, b;
-                        pair_of_flat(D, f1[u], ela, elj[u], b1[u], p, b);
-                        if (p >= 0)
-                            atomicAdd(sdP + p * D.hs + b, 1);
-                    }
-                }
+                const float s0 = pair_s<BM>(o.x, o.y, o.z, c[u].x, c[u].y, c[u].z, D.B);
+                const float s1 = pair_s<BM>(nw.x, nw.y, nw.z, c[u].x, c[u].y, c[u].z, D.B);
+                const bool a0 = valid[u] & (s0 >= D.s_lo) & (s0 < D.s_hi);
+                const bool a1 = valid[u] & (s1 >= D.s_lo) & (s1 < D.s_hi);
+                const int k = qn * (int)blockDim.x + (int)threadIdx.x;
+                q.s0[k] = s0;
+                q.s1[k] = s1;
+                q.info[k] = ((unsigned)__float_as_int(c[u].w) & 0xffu) | ((mj[u] == mola ? 1u : 0u) << 8) |
+                            ((a0 ? 1u : 0u) << 9) | ((a1 ? 1u : 0u) << 10) | ((unsigned)gi << 11);
+                qn += (a0 | a1) ? 1 : 0;
             }
         }
 #pragma unroll
@@ -952,13 +1020,14 @@ __device__ void fused_columns(const EDesc &Dg, int *sdP, unsigned *s_tcount, con
             mj[u] = mn[u];
         }
     }
+    flush_columns(D, g, sdP, s_tcount, q, qn);
 }
 
 // sA, sBq: shared-memory copies of A and Bq, brought in by bulk copies on
 // `bar` while the columns run; parity = this CTA's count of fused items mod 2.
 __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, uint64_t *bar, uint32_t parity,
                              uint32_t *status, double *red, double *cb, double *sbs, int *sbin, int *s_nchg,
-                             double *coef, int *s_flag, unsigned *s_tcount, MovedGroup &g)
+                             double *coef, int *s_flag, unsigned *s_tcount, MovedGroup &g, const ColQueue &q)
 {
     if (threadIdx.x == 0) {
         // the previous item's reads of sA / sBq are ordered before this
@@ -978,19 +1047,19 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, 
     __syncthreads();
     if (g.n == 1) {
         switch (D.bm) {
-        case BM_IBC: fused_columns<BM_IBC, false>(D, sdP, s_tcount, g); break;
-        case BM_DIAG: fused_columns<BM_DIAG, false>(D, sdP, s_tcount, g); break;
-        case BM_XYTRI: fused_columns<BM_XYTRI, false>(D, sdP, s_tcount, g); break;
-        case BM_LOWER: fused_columns<BM_LOWER, false>(D, sdP, s_tcount, g); break;
-        default: fused_columns<BM_GENERAL, false>(D, sdP, s_tcount, g); break;
+        case BM_IBC: fused_columns<BM_IBC, false>(D, sdP, s_tcount, g, q); break;
+        case BM_DIAG: fused_columns<BM_DIAG, false>(D, sdP, s_tcount, g, q); break;
+        case BM_XYTRI: fused_columns<BM_XYTRI, false>(D, sdP, s_tcount, g, q); break;
+        case BM_LOWER: fused_columns<BM_LOWER, false>(D, sdP, s_tcount, g, q); break;
+        default: fused_columns<BM_GENERAL, false>(D, sdP, s_tcount, g, q); break;
         }
     } else {
         switch (D.bm) {
-        case BM_IBC: fused_columns<BM_IBC, true>(D, sdP, s_tcount, g); break;
-        case BM_DIAG: fused_columns<BM_DIAG, true>(D, sdP, s_tcount, g); break;
-        case BM_XYTRI: fused_columns<BM_XYTRI, true>(D, sdP, s_tcount, g); break;
-        case BM_LOWER: fused_columns<BM_LOWER, true>(D, sdP, s_tcount, g); break;
-        default: fused_columns<BM_GENERAL, true>(D, sdP, s_tcount, g); break;
+        case BM_IBC: fused_columns<BM_IBC, true>(D, sdP, s_tcount, g, q); break;
+        case BM_DIAG: fused_columns<BM_DIAG, true>(D, sdP, s_tcount, g, q); break;
+        case BM_XYTRI: fused_columns<BM_XYTRI, true>(D, sdP, s_tcount, g, q); break;
+        case BM_LOWER: fused_columns<BM_LOWER, true>(D, sdP, s_tcount, g, q); break;
+        default: fused_columns<BM_GENERAL, true>(D, sdP, s_tcount, g, q); break;
         }
     }
     if (g.n > 1) {
@@ -1085,10 +1154,14 @@ __global__ void __launch_bounds__(kMaxEngineThreads, 1) k_engine_step(StepParams
     (void)sdP;
     uint32_t fused_items = 0;
     double *sA = nullptr, *sBq = nullptr;
+    ColQueue cq{};
     if (FUSED) {
         // dynamic layout: element-pair deltas, then A and Bq (16-byte aligned)
         sA = reinterpret_cast<double *>(sdP + p.fused_dp_ints);
         sBq = sA + p.fused_bins;
+        cq.s0 = reinterpret_cast<float *>(sBq + p.fused_bins);
+        cq.s1 = cq.s0 + kColQueue * blockDim.x;
+        cq.info = reinterpret_cast<unsigned *>(cq.s1 + kColQueue * blockDim.x);
         if (threadIdx.x == 0) {
             mbar_init(&s_bar, 1);
             mbar_fence_init();
@@ -1109,7 +1182,7 @@ __global__ void __launch_bounds__(kMaxEngineThreads, 1) k_engine_step(StepParams
         const EDesc &D = p.desc[item.x];
         if (FUSED) {
             engine_fused(D, sdP, sA, sBq, &s_bar, fused_items & 1u, &p.sched->status, red, cb, sbs, sbin, &s_nchg,
-                         coef, &s_flag, &s_tcount, s_group);
+                         coef, &s_flag, &s_tcount, s_group, cq);
             ++fused_items;
             __syncthreads();
             continue;
@@ -1546,7 +1619,7 @@ struct SqTable {
     size_t bytes = 0;
 };
 
-constexpr int kFusedSmemMax = 160 * 1024;  // dynamic shared memory of a fused step: element-pair deltas, A, Bq
+constexpr int kFusedSmemMax = 136 * 1024;  // element-pair deltas, A and Bq of a fused step (the column queue comes on top)
 constexpr int kFusedMaxAtoms = 49152;     // larger engines are split over several CTAs
 
 struct EngineSet {
@@ -1826,7 +1899,8 @@ static int launch_sq(EngineSet *s, int first, int count, cudaStream_t st)
 static int launch_batched(EngineSet *s, cudaStream_t st)
 {
     if (s->nfused > 0)
-        FRMC_TRY(launch_items(s, s->items + s->nsolo, s->nfused, 0, st, s->fused_smem, true));
+        FRMC_TRY(launch_items(s, s->items + s->nsolo, s->nfused, 0, st,
+                              s->fused_smem + kColQueue * s->threads * 12, true));
     if (s->nbatch > s->nfused)
         FRMC_TRY(launch_items(s, s->items + s->nsolo + s->nfused, s->nbatch - s->nfused, 0, st));
     FRMC_TRY(launch_sq(s, 0, (int)s->sq_host.size(), st));
