@@ -93,6 +93,10 @@ struct MovedGroup {
     float o[kMaxGroup][3];   // box coordinates before the move
     float nw[kMaxGroup][3];  // box coordinates after
     float nr[kMaxGroup][3];  // real coordinates after
+    float u;                 // the move's uniform number
+    long long step;          // the engine's step, accepted count, sd and chi2 before this step
+    long long accepted;
+    double sd, chi2;
 };
 
 struct EResult {
@@ -209,6 +213,13 @@ __device__ void load_moved_group(const EDesc &D, long long step, MovedGroup &g)
 {
     const int G = D.group;
     const EMove &m = D.moves[step % D.move_cap];
+    if (threadIdx.x == 0) {
+        g.u = m.u;
+        g.step = step;
+        g.accepted = D.st->accepted;
+        g.sd = D.st->sd;
+        g.chi2 = D.st->chi2;
+    }
     if (G == 1) {
         if (threadIdx.x == 0) {
             const int a = m.atom;
@@ -543,7 +554,7 @@ __device__ __forceinline__ double coef_times(const double *tabv, const double *c
 
 template <bool SMEM>
 __device__ double eval_delta(const EDesc &Dg, int *dP, const double *Ab, const double *Bqb, double *red, double *cb,
-                             double *sbs, int *sbin, int *s_nchg, double *coef)
+                             double *sbs, int *sbin, int *s_nchg, double *coef, const int *nz)
 {
     const int hs = Dg.hs;
     const double *__restrict__ A = Ab;
@@ -588,11 +599,15 @@ __device__ double eval_delta(const EDesc &Dg, int *dP, const double *Ab, const d
             bool any = false;
             if (i < cn) {
                 const int b = c0 + i;
+                if (nz) {
+                    any = nz[b] != 0;
+                } else {
 #pragma unroll
-                for (int q = 0; q < kMaxP; ++q)
-                    if (q < np)
-                        any |= delta_at(q, b) != 0;
-                for (int q = kMaxP; q < np; ++q) any |= delta_at(q, b) != 0;
+                    for (int q = 0; q < kMaxP; ++q)
+                        if (q < np)
+                            any |= delta_at(q, b) != 0;
+                    for (int q = kMaxP; q < np; ++q) any |= delta_at(q, b) != 0;
+                }
                 if ((sq || big) && !any)
                     Sb[b] = 0.0;
             }
@@ -736,9 +751,21 @@ __device__ __forceinline__ void group_pair_bins(const V &D, const MovedGroup &g,
                 f0, f1, half, b0, b1, elj);
 }
 
+// One +-1 on the shared element-pair delta at (pair row idx - b, bin b), and
+// the bin's count of non-zero deltas kept exact: the thread that moves a delta
+// away from zero adds one, the thread that brings it back removes one.
+__device__ __forceinline__ void delta_add(int *sdP, int *nz, int idx, int b, int v)
+{
+    const int old = atomicAdd(sdP + idx, v);
+    if (old == 0)
+        atomicAdd(nz + b, 1);
+    else if (old + v == 0)
+        atomicSub(nz + b, 1);
+}
+
 // The fused path's share of the group's internal pairs (shared-memory deltas).
 template <int BM>
-__device__ void fused_group_internal(const EDesc &Dg, int *sdP, unsigned *s_tcount, const MovedGroup &g)
+__device__ void fused_group_internal(const EDesc &Dg, int *sdP, int *nz, unsigned *s_tcount, const MovedGroup &g)
 {
     const ColView D = col_view(Dg);
     const int npair = g.n * (g.n - 1) / 2;
@@ -754,14 +781,14 @@ __device__ void fused_group_internal(const EDesc &Dg, int *sdP, unsigned *s_tcou
             int p, bb;
             pair_of_flat(D, f0, ela, elj, b0, p, bb);
             if (p >= 0)
-                atomicSub(sdP + p * D.hs + bb, 1);
+                delta_add(sdP, nz, p * D.hs + bb, bb, -1);
         }
         if (f1 >= 0) {
             D.tlist[pos] = ((half + f1) << 1) | 1;
             int p, bb;
             pair_of_flat(D, f1, ela, elj, b1, p, bb);
             if (p >= 0)
-                atomicAdd(sdP + p * D.hs + bb, 1);
+                delta_add(sdP, nz, p * D.hs + bb, bb, 1);
         }
     }
 }
@@ -813,7 +840,7 @@ __device__ void finish_engine(const EDesc &D, const MovedGroup &g, double *red, 
         }
         __syncthreads();
     }
-    const double dsd = eval_delta<false>(D, D.dP, D.A, D.Bq, red, cb, sbs, sbin, s_nchg, coef);
+    const double dsd = eval_delta<false>(D, D.dP, D.A, D.Bq, red, cb, sbs, sbin, s_nchg, coef, nullptr);
     if (D.sq) {
         // the S(Q) kernel evaluates its term, decides and commits
         if (threadIdx.x == 0) {
@@ -905,13 +932,14 @@ constexpr int kColQueue = 8;
 struct ColQueue {
     float *s0, *s1;   // squared distances before / after the move
     unsigned *info;   // el(j) | same molecule << 8 | accepted before << 9 | after << 10 | group atom << 11
+    int *nz;          // per bin: element pairs whose delta is non-zero
 };
 
 // Bins the queued columns of every thread: each pass pops one entry per
 // thread that has one, so the IEEE sqrt / division and the delta atomics run
 // with full warps instead of one diverging lane.
-__device__ __forceinline__ void flush_columns(const ColView &D, const MovedGroup &g, int *sdP, unsigned *s_tcount,
-                                              const ColQueue &q, int &qn)
+__device__ __forceinline__ void flush_columns(const ColView &D, const MovedGroup &g, int *sdP, int *nz,
+                                              unsigned *s_tcount, const ColQueue &q, int &qn)
 {
     while (__any_sync(0xffffffffu, qn > 0)) {
         if (qn > 0) {
@@ -942,14 +970,14 @@ __device__ __forceinline__ void flush_columns(const ColView &D, const MovedGroup
                     int p, bb;
                     pair_of_flat(D, f0, ela, elj, b0, p, bb);
                     if (p >= 0)
-                        atomicSub(sdP + p * D.hs + bb, 1);
+                        delta_add(sdP, nz, p * D.hs + bb, bb, -1);
                 }
                 if (f1 >= 0) {
                     D.tlist[pos] = (int)(((half + f1) << 1) | 1);
                     int p, bb;
                     pair_of_flat(D, f1, ela, elj, b1, p, bb);
                     if (p >= 0)
-                        atomicAdd(sdP + p * D.hs + bb, 1);
+                        delta_add(sdP, nz, p * D.hs + bb, bb, 1);
                 }
             }
         }
@@ -961,7 +989,8 @@ __device__ __forceinline__ void flush_columns(const ColView &D, const MovedGroup
 // test are branch-free for a batch of columns; accepted columns go to the
 // thread's queue, flushed when a queue is full and at the end.
 template <int BM, bool GROUP>
-__device__ void fused_columns(const EDesc &Dg, int *sdP, unsigned *s_tcount, const MovedGroup &g, const ColQueue &q)
+__device__ void fused_columns(const EDesc &Dg, int *sdP, int *nz, unsigned *s_tcount, const MovedGroup &g,
+                              const ColQueue &q)
 {
     const ColView D = col_view(Dg);
     const int step = kItemUnroll * blockDim.x;
@@ -996,7 +1025,7 @@ __device__ void fused_columns(const EDesc &Dg, int *sdP, unsigned *s_tcount, con
         }
         for (int gi = 0; gi < G; ++gi) {
             if (__any_sync(0xffffffffu, qn > kColQueue - kItemUnroll))
-                flush_columns(D, g, sdP, s_tcount, q, qn);
+                flush_columns(D, g, sdP, nz, s_tcount, q, qn);
             const float3 o = make_float3(g.o[gi][0], g.o[gi][1], g.o[gi][2]);
             const float3 nw = make_float3(g.nw[gi][0], g.nw[gi][1], g.nw[gi][2]);
             const int mola = g.mol[gi];
@@ -1020,7 +1049,7 @@ __device__ void fused_columns(const EDesc &Dg, int *sdP, unsigned *s_tcount, con
             mj[u] = mn[u];
         }
     }
-    flush_columns(D, g, sdP, s_tcount, q, qn);
+    flush_columns(D, g, sdP, nz, s_tcount, q, qn);
 }
 
 // sA, sBq: shared-memory copies of A and Bq, brought in by bulk copies on
@@ -1043,37 +1072,38 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, 
     const int np = D.npairs;
     const int nph = np * D.hs;
     for (int k = threadIdx.x; k < nph; k += blockDim.x) sdP[k] = 0;
-    for (int q = threadIdx.x; q < np; q += blockDim.x) coef[q] = D.pc[q];
+    for (int k = threadIdx.x; k < D.hs; k += blockDim.x) q.nz[k] = 0;
+    for (int qq = threadIdx.x; qq < np; qq += blockDim.x) coef[qq] = D.pc[qq];
     __syncthreads();
     if (g.n == 1) {
         switch (D.bm) {
-        case BM_IBC: fused_columns<BM_IBC, false>(D, sdP, s_tcount, g, q); break;
-        case BM_DIAG: fused_columns<BM_DIAG, false>(D, sdP, s_tcount, g, q); break;
-        case BM_XYTRI: fused_columns<BM_XYTRI, false>(D, sdP, s_tcount, g, q); break;
-        case BM_LOWER: fused_columns<BM_LOWER, false>(D, sdP, s_tcount, g, q); break;
-        default: fused_columns<BM_GENERAL, false>(D, sdP, s_tcount, g, q); break;
+        case BM_IBC: fused_columns<BM_IBC, false>(D, sdP, q.nz, s_tcount, g, q); break;
+        case BM_DIAG: fused_columns<BM_DIAG, false>(D, sdP, q.nz, s_tcount, g, q); break;
+        case BM_XYTRI: fused_columns<BM_XYTRI, false>(D, sdP, q.nz, s_tcount, g, q); break;
+        case BM_LOWER: fused_columns<BM_LOWER, false>(D, sdP, q.nz, s_tcount, g, q); break;
+        default: fused_columns<BM_GENERAL, false>(D, sdP, q.nz, s_tcount, g, q); break;
         }
     } else {
         switch (D.bm) {
-        case BM_IBC: fused_columns<BM_IBC, true>(D, sdP, s_tcount, g, q); break;
-        case BM_DIAG: fused_columns<BM_DIAG, true>(D, sdP, s_tcount, g, q); break;
-        case BM_XYTRI: fused_columns<BM_XYTRI, true>(D, sdP, s_tcount, g, q); break;
-        case BM_LOWER: fused_columns<BM_LOWER, true>(D, sdP, s_tcount, g, q); break;
-        default: fused_columns<BM_GENERAL, true>(D, sdP, s_tcount, g, q); break;
+        case BM_IBC: fused_columns<BM_IBC, true>(D, sdP, q.nz, s_tcount, g, q); break;
+        case BM_DIAG: fused_columns<BM_DIAG, true>(D, sdP, q.nz, s_tcount, g, q); break;
+        case BM_XYTRI: fused_columns<BM_XYTRI, true>(D, sdP, q.nz, s_tcount, g, q); break;
+        case BM_LOWER: fused_columns<BM_LOWER, true>(D, sdP, q.nz, s_tcount, g, q); break;
+        default: fused_columns<BM_GENERAL, true>(D, sdP, q.nz, s_tcount, g, q); break;
         }
     }
     if (g.n > 1) {
         switch (D.bm) {
-        case BM_IBC: fused_group_internal<BM_IBC>(D, sdP, s_tcount, g); break;
-        case BM_DIAG: fused_group_internal<BM_DIAG>(D, sdP, s_tcount, g); break;
-        case BM_XYTRI: fused_group_internal<BM_XYTRI>(D, sdP, s_tcount, g); break;
-        case BM_LOWER: fused_group_internal<BM_LOWER>(D, sdP, s_tcount, g); break;
-        default: fused_group_internal<BM_GENERAL>(D, sdP, s_tcount, g); break;
+        case BM_IBC: fused_group_internal<BM_IBC>(D, sdP, q.nz, s_tcount, g); break;
+        case BM_DIAG: fused_group_internal<BM_DIAG>(D, sdP, q.nz, s_tcount, g); break;
+        case BM_XYTRI: fused_group_internal<BM_XYTRI>(D, sdP, q.nz, s_tcount, g); break;
+        case BM_LOWER: fused_group_internal<BM_LOWER>(D, sdP, q.nz, s_tcount, g); break;
+        default: fused_group_internal<BM_GENERAL>(D, sdP, q.nz, s_tcount, g); break;
         }
     }
     __syncthreads();
     mbar_wait(bar, parity, status);
-    const double dsd = eval_delta<true>(D, sdP, sA, sBq, red, cb, sbs, sbin, s_nchg, coef);
+    const double dsd = eval_delta<true>(D, sdP, sA, sBq, red, cb, sbs, sbin, s_nchg, coef, q.nz);
     if (D.sq) {
         // the S(Q) kernel evaluates its term, decides and commits
         if (threadIdx.x == 0) {
@@ -1084,12 +1114,11 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, 
         }
         return;
     }
-    const EState &S0 = *D.st;
-    const double sd_new = S0.sd + dsd;
+    // the state and the move's uniform number were read at set-up
+    const double sd_new = g.sd + dsd;
     const double chi2_new = sd_new / D.var2;
     if (threadIdx.x == 0) {
-        const EMove &m = D.moves[S0.step % D.move_cap];
-        const bool reject = (chi2_new > S0.chi2) && (m.u > D.tol);
+        const bool reject = (chi2_new > g.chi2) && (g.u > D.tol);
         *s_flag = reject ? 0 : 1;
     }
     __syncthreads();
@@ -1122,16 +1151,16 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, 
     __syncthreads();
     if (threadIdx.x == 0) {
         EState &S = *D.st;
-        EResult &r = D.results[S.step % D.move_cap];
+        EResult &r = D.results[g.step % D.move_cap];
         r.chi2_new = chi2_new;
         r.accepted = accept ? 1 : 0;
         r.atom = g.atom[0];
         if (accept) {
             S.chi2 = chi2_new;
             S.sd = sd_new;
-            S.accepted += 1;
+            S.accepted = g.accepted + 1;
         }
-        S.step += 1;
+        S.step = g.step + 1;
     }
 }
 
@@ -1162,6 +1191,7 @@ __global__ void __launch_bounds__(kMaxEngineThreads, 1) k_engine_step(StepParams
         cq.s0 = reinterpret_cast<float *>(sBq + p.fused_bins);
         cq.s1 = cq.s0 + kColQueue * blockDim.x;
         cq.info = reinterpret_cast<unsigned *>(cq.s1 + kColQueue * blockDim.x);
+        cq.nz = reinterpret_cast<int *>(cq.info + kColQueue * blockDim.x);
         if (threadIdx.x == 0) {
             mbar_init(&s_bar, 1);
             mbar_fence_init();
@@ -1779,7 +1809,7 @@ static int refresh(EngineSet *s)
         const EDesc &D = s->slots[id].d;
         const int dp = (D.npairs * D.hs + 3) & ~3, bins = (D.hs + 1) & ~1;
         const int dpi = std::max(s->fused_dp_ints, dp), bi = std::max(s->fused_bins, bins);
-        if (s->fused && 4ll * dpi + 16ll * bi <= kFusedSmemMax && D.n <= kFusedMaxAtoms) {
+        if (s->fused && 4ll * dpi + 20ll * bi <= kFusedSmemMax && D.n <= kFusedMaxAtoms) {
             fused_ids.push_back(id);
             s->fused_dp_ints = dpi;
             s->fused_bins = bi;
@@ -1900,7 +1930,7 @@ static int launch_batched(EngineSet *s, cudaStream_t st)
 {
     if (s->nfused > 0)
         FRMC_TRY(launch_items(s, s->items + s->nsolo, s->nfused, 0, st,
-                              s->fused_smem + kColQueue * s->threads * 12, true));
+                              s->fused_smem + kColQueue * s->threads * 12 + 4 * s->fused_bins, true));
     if (s->nbatch > s->nfused)
         FRMC_TRY(launch_items(s, s->items + s->nsolo + s->nfused, s->nbatch - s->nfused, 0, st));
     FRMC_TRY(launch_sq(s, 0, (int)s->sq_host.size(), st));
