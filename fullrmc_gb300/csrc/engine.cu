@@ -546,12 +546,6 @@ constexpr int kMaxP = 10;  // element pairs loaded with unrolled loads (ne <= 4)
 // an S(Q) term, also keep S in the global Sb (zero for unchanged bins).
 // pair_coef_p * v for |v| <= 4 comes from a small table, so a changed bin
 // costs one FP64 add per non-zero element-pair delta.
-// pair_coef_q * v: from the table for |v| <= 4 and the first kMaxP pairs.
-__device__ __forceinline__ double coef_times(const double *tabv, const double *coef, int q, int v)
-{
-    return (q < kMaxP && (unsigned)(v + 4) <= 8u) ? tabv[q * 9 + v + 4] : coef[q] * (double)v;
-}
-
 template <bool SMEM>
 __device__ double eval_delta(const EDesc &Dg, int *dP, const double *Ab, const double *Bqb, double *red, double *cb,
                              double *sbs, int *sbin, int *s_nchg, double *coef, const int *nz)
@@ -650,75 +644,43 @@ __device__ double eval_delta(const EDesc &Dg, int *dP, const double *Ab, const d
                 sbin[base + __popc(bal & ((1u << lane) - 1u))] = c0 + i;
         }
         __syncthreads();
-        // 4. FP64 on the listed bins.  The first three non-zero (pair, delta)
-        // of a bin are kept in registers (integer work), S starts from the
-        // table entry of the first, and the warp issues one FP64 add per
-        // further term of its busiest lane (the loop is warp-uniform).
-        for (int k0 = (int)(threadIdx.x & ~31u); k0 < n; k0 += blockDim.x) {
-            const int k = k0 + (int)lane;
-            const bool in = k < n;
-            const int b = in ? sbin[k] : 0;
-            int nnz = 0, q0 = 0, v0 = 0, q1 = 0, v1 = 0, q2 = 0, v2 = 0;
-            auto take = [&](int q, int v) {
-                if (sq) {
-                    if (SMEM)
-                        gdP[q * hs + b] = v;
-                    evl[q * hs + atomicAdd(&s_evn[q], 1)] = (b << 16) | (v & 0xffff);
-                    if (v > 32767 || v < -32768)
-                        s_wide = 1;
-                }
-                if (nnz < 3) {
+        // 4. FP64 on the listed bins
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {
+            const int b = sbin[k];
+            const double a = A[b];
+            const double bq = Bq[b];
+            double S = 0.0;
+#pragma unroll
+            for (int q = 0; q < kMaxP; ++q) {
+                if (q >= np)
+                    break;
+                const int v = delta_at(q, b);
+                if (v) {
                     if (!SMEM && !sq)
                         dP[(long long)q * hs + b] = 0;
-                    if (nnz == 0) {
-                        q0 = q;
-                        v0 = v;
-                    } else if (nnz == 1) {
-                        q1 = q;
-                        v1 = v;
-                    } else {
-                        q2 = q;
-                        v2 = v;
+                    if (sq) {
+                        if (SMEM)
+                            gdP[q * hs + b] = v;
+                        evl[q * hs + atomicAdd(&s_evn[q], 1)] = (b << 16) | (v & 0xffff);
+                        if (v > 32767 || v < -32768)
+                            s_wide = 1;
                     }
-                }
-                ++nnz;
-            };
-            if (in) {
-#pragma unroll
-                for (int q = 0; q < kMaxP; ++q) {
-                    if (q < np) {
-                        const int v = delta_at(q, b);
-                        if (v)
-                            take(q, v);
-                    }
-                }
-                for (int q = kMaxP; q < np; ++q) {
-                    const int v = delta_at(q, b);
-                    if (v)
-                        take(q, v);
+                    S += (unsigned)(v + 4) <= 8u ? tabv[q * 9 + v + 4] : coef[q] * (double)v;
                 }
             }
-            const int wmax = __reduce_max_sync(0xffffffffu, nnz);
-            double S = in ? coef_times(tabv, coef, q0, v0) : 0.0;
-            if (wmax > 1 && nnz > 1)
-                S += coef_times(tabv, coef, q1, v1);
-            if (wmax > 2 && nnz > 2)
-                S += coef_times(tabv, coef, q2, v2);
-            if (nnz > 3)  // more than three element pairs changed in this bin (rare)
-                for (int q = q2 + 1; q < np; ++q) {
-                    const int v = delta_at(q, b);
-                    if (v) {
-                        if (!SMEM && !sq)
-                            dP[(long long)q * hs + b] = 0;
-                        S += coef_times(tabv, coef, q, v);
-                    }
+            for (int q = kMaxP; q < np; ++q) {
+                const int v = delta_at(q, b);
+                if (v) {
+                    if (!SMEM)
+                        dP[(long long)q * hs + b] = 0;
+                    const double cf = coef[q];
+                    S += v == 1 ? cf : (v == -1 ? -cf : cf * (double)v);
                 }
-            if (in) {
-                cb[k] = S * fma(A[b], S, -Bq[b]);
-                sbs[k] = neg_twice(S);
-                if (big || sq)
-                    Sb[b] = S;
             }
+            cb[k] = S * fma(a, S, -bq);
+            sbs[k] = neg_twice(S);
+            if (big || sq)
+                Sb[b] = S;
         }
         lanes_add_chunk(red, cb, 0, n);
     }
@@ -1651,6 +1613,7 @@ struct SqTable {
 
 constexpr int kFusedSmemMax = 136 * 1024;  // element-pair deltas, A and Bq of a fused step (the column queue comes on top)
 constexpr int kFusedMaxAtoms = 49152;     // larger engines are split over several CTAs
+constexpr int kSoloFusedAtoms = 16384;    // one-engine steps of engines up to this size use the fused item
 
 struct EngineSet {
     std::vector<Slot> slots;
@@ -1664,6 +1627,7 @@ struct EngineSet {
     std::vector<int> live;        // live engine ids in work-list order
     std::vector<int> item_first;  // per engine id: first item (or -1)
     std::vector<int> item_count;
+    std::vector<int> fused_item;  // per engine id: its one-CTA item in the batched list (or -1)
     int tile = 1024, threads = 512, ctas_per_sm = 1;  // the usual autotuner choice on GB300
     EDesc *ddesc = nullptr;
     int ddesc_cap = 0;
@@ -1818,7 +1782,11 @@ static int refresh(EngineSet *s)
     }
     std::stable_sort(fused_ids.begin(), fused_ids.end(),
                      [s](int a, int b) { return s->slots[a].d.n > s->slots[b].d.n; });
-    for (int id : fused_ids) items.push_back(make_int2(id, -1));
+    s->fused_item.assign(nslots, -1);
+    for (int id : fused_ids) {
+        s->fused_item[id] = (int)items.size();
+        items.push_back(make_int2(id, -1));
+    }
     s->nfused = (int)fused_ids.size();
     for (int id : s->live) {
         if (std::find(fused_ids.begin(), fused_ids.end(), id) != fused_ids.end())
@@ -1923,14 +1891,20 @@ static int launch_sq(EngineSet *s, int first, int count, cudaStream_t st)
     return FRMC_OK;
 }
 
+// Dynamic shared memory of a fused launch: element-pair deltas, A, Bq, the
+// column queue and the per-bin non-zero counts.
+static int fused_dyn_smem(const EngineSet *s)
+{
+    return s->fused_smem + kColQueue * s->threads * 12 + 4 * s->fused_bins;
+}
+
 // The batched work list (every live engine advances one step): the fused
 // engines in one launch, then the tiles of the split ones, then the S(Q)
 // blocks of the engines that have an S(Q) term.
 static int launch_batched(EngineSet *s, cudaStream_t st)
 {
     if (s->nfused > 0)
-        FRMC_TRY(launch_items(s, s->items + s->nsolo, s->nfused, 0, st,
-                              s->fused_smem + kColQueue * s->threads * 12 + 4 * s->fused_bins, true));
+        FRMC_TRY(launch_items(s, s->items + s->nsolo, s->nfused, 0, st, fused_dyn_smem(s), true));
     if (s->nbatch > s->nfused)
         FRMC_TRY(launch_items(s, s->items + s->nsolo + s->nfused, s->nbatch - s->nfused, 0, st));
     FRMC_TRY(launch_sq(s, 0, (int)s->sq_host.size(), st));
@@ -2443,7 +2417,11 @@ int frmc_engines_step(void *handle, int32_t engine, int32_t steps, int use_graph
     auto one = [&](cudaStream_t sx) {
         if (engine < 0)
             return launch_batched(s, sx);
-        FRMC_TRY(launch_items(s, s->items + s->item_first[engine], count, 0, sx));
+        const int fi = s->fused_item[engine];
+        if (fi >= 0 && s->slots[engine].d.n <= kSoloFusedAtoms)  // one CTA beats tiles plus a finisher
+            FRMC_TRY(launch_items(s, s->items + fi, 1, 0, sx, fused_dyn_smem(s), true));
+        else
+            FRMC_TRY(launch_items(s, s->items + s->item_first[engine], count, 0, sx));
         return launch_sq(s, s->sq_first[engine], s->sq_count[engine], sx);
     };
     if (!use_graph) {
