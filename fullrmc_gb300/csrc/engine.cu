@@ -1126,6 +1126,28 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, 
     }
 }
 
+// Warms L2 for a fused item this CTA will probably take later (one grid
+// stride ahead): its descriptor, state, move and the moved atom's lines.  Run
+// by one thread of the second warp while thread 0 walks the same chain for the
+// CTA's current item, so a later item starts from L2 instead of HBM.
+__device__ void warm_item(const StepParams &p, long long idx)
+{
+    if (idx >= p.nitems)
+        return;
+    const int2 item = p.items[idx];
+    const EDesc &D = p.desc[item.x];
+    const long long stp = D.st->step;
+    const long long slot = stp % D.move_cap;
+    const int a = D.moves[slot].atom;
+    prefetch_l2(D.box + a);
+    prefetch_l2(D.real + a);
+    prefetch_l2(D.mol + a);
+    if (D.group > 1)
+        prefetch_l2(D.groups + slot);
+    prefetch_l2(D.A);
+    prefetch_l2(D.Bq);
+}
+
 constexpr int kMaxEngineThreads = 512;  // CTA size limit of the step kernels (128 registers per thread)
 
 template <bool FUSED>
@@ -1172,6 +1194,8 @@ __global__ void __launch_bounds__(kMaxEngineThreads, 1) k_engine_step(StepParams
             break;
         const int2 item = p.items[it];
         const EDesc &D = p.desc[item.x];
+        if (FUSED && fused_items == 0 && threadIdx.x == 32)
+            warm_item(p, (long long)it + gridDim.x);
         if (FUSED) {
             engine_fused(D, sdP, sA, sBq, &s_bar, fused_items & 1u, &p.sched->status, red, cb, sbs, sbin, &s_nchg,
                          coef, &s_flag, &s_tcount, s_group, cq);

@@ -75,6 +75,13 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32
 }
 
 // 1-D bulk copy global -> shared (both 16-byte aligned, bytes % 16 == 0).
+// Hint: bring the line holding p into L2 (no register result, never faults
+// on a valid address).
+__device__ __forceinline__ void prefetch_l2(const void *p)
+{
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 __device__ __forceinline__ void bulk_g2s(void *dst_smem, const void *src_gmem, uint32_t bytes, uint64_t *bar)
 {
     asm volatile(
