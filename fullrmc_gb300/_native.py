@@ -80,6 +80,8 @@ SIGNATURES = {
     "frmc_single_atomic_distances_dists": [i32, F32P, i64, I32P, I32P, i32, F32P, F32P, I32P, I32P, F32P, F32P, cint,
                                            cint],
     "frmc_pair_elements_stats": [I32P, I32P, i64, i32, I32P, I32P],
+    "frmc_shape_function": [F32P, i64, F32P, cint, I32P, I32P, i32, f32, f32, f32, i32, i32, I32P, I32P, F64P, F64P,
+                            F64P, f64, F64P, i32, F64P, i32, F64P, F64P, F64P],
     "frmc_coordination_terms": [F32P, i64, F32P, cint, F32P, I64P, I32P, i32, I32P, I64P, i32, I32P, I32P, I32P, i64,
                                 F32P, F32P, F32P, i32],
 }

@@ -426,6 +426,63 @@ int frmc_full_pairs_histograms_coords(const float *boxCoords, int64_t n, const f
     return counts_out(c, total, nullptr, nullptr, hintra, hinter);
 }
 
+int frmc_shape_function(const float *boxCoords, int64_t n, const float *basis, int isPBC,
+                        const int32_t *moleculeIndex, const int32_t *elementIndex, int32_t ne, float minDistance,
+                        float maxDistance, float bin, int32_t hs, int32_t npairs, const int32_t *pair_i,
+                        const int32_t *pair_j, const double *pair_coef, const double *shellCenters,
+                        const double *shellVolumes, double rho0, const double *qValues, int32_t nq,
+                        const double *rValues, int32_t nr, double *Gr, double *Sq, double *Gshape)
+{
+    int64_t total;
+    TRY(check_n(n, "boxCoords"));
+    TRY(check_hist(ne, hs, &total));
+    if (hs < 2 || nq < 2 || nr < 0 || npairs < 0)
+        return set_error(FRMC_E_ARG, "shape function: needs at least two shells and two q values");
+    for (int32_t p = 0; p < npairs; ++p)
+        if (pair_i[p] < 0 || pair_i[p] >= ne || pair_j[p] < 0 || pair_j[p] >= ne)
+            return set_error(FRMC_E_INDEX, "shape function: element pair %d out of range", p);
+    for (int64_t i = 0; i < n; ++i)
+        if (elementIndex[i] < 0 || elementIndex[i] >= ne)
+            return set_error(FRMC_E_INDEX, "element index %d out of range for %d elements", elementIndex[i], ne);
+    LOCKED_CTX(c);
+    TRY(prepare_counts(c, total));
+    if (n >= 2) {
+        TRY(upload_atoms(c, boxCoords, moleculeIndex, elementIndex, n));
+        TRY(full_counts(c, n, basis, isPBC, ne, minDistance, maxDistance, bin, hs, total,
+                        c->buf[BUF_COUNTS].as<unsigned>()));
+    }
+    // FP64 block: pc, r, vol, q, rv, G, S, Gs, w1, w2 (doubles), then pair_i, pair_j (ints)
+    const size_t nd = (size_t)npairs + 2 * (size_t)hs + (size_t)nq + (size_t)nr + (size_t)hs + (size_t)nq +
+                      (size_t)nr + (size_t)hs + (size_t)nq;
+    TRY(c->buf[BUF_AUX1].ensure(8 * nd + 8 * (size_t)npairs + 64));
+    double *d = c->buf[BUF_AUX1].as<double>();
+    double *pc = d, *r = pc + npairs, *vol = r + hs, *q = vol + hs, *rv = q + nq, *G = rv + nr, *S = G + hs,
+           *Gs = S + nq, *w1 = Gs + nr, *w2 = w1 + hs;
+    int *pij = reinterpret_cast<int *>(w2 + nq);
+    TRY(h2d(pc, pair_coef, 8 * (size_t)npairs, c->stream));
+    TRY(h2d(r, shellCenters, 8 * (size_t)hs, c->stream));
+    TRY(h2d(vol, shellVolumes, 8 * (size_t)hs, c->stream));
+    TRY(h2d(q, qValues, 8 * (size_t)nq, c->stream));
+    TRY(h2d(rv, rValues, 8 * (size_t)nr, c->stream));
+    TRY(h2d(pij, pair_i, 4 * (size_t)npairs, c->stream));
+    TRY(h2d(pij + npairs, pair_j, 4 * (size_t)npairs, c->stream));
+    TRY(launch_shape_function(c->buf[BUF_COUNTS].as<unsigned>(), ne, hs, npairs, pij, pij + npairs, pc, r, vol, rho0,
+                              shellCenters[1] - shellCenters[0], q, nq, qValues[1] - qValues[0], rv, nr, G, S, Gs,
+                              w1, w2, c->stream));
+    if (Gr)
+        TRY(d2h(Gr, G, 8 * (size_t)hs, c->stream));
+    if (Sq)
+        TRY(d2h(Sq, S, 8 * (size_t)nq, c->stream));
+    if (Gshape)
+        TRY(d2h(Gshape, Gs, 8 * (size_t)nr, c->stream));
+    uint32_t status = 0;
+    TRY(d2h(&status, c->buf[BUF_STATUS].p, 4, c->stream));
+    TRY(finish(c));
+    if (status)
+        return set_error(FRMC_E_TIMEOUT, "device wait gave up (status 0x%x)", status);
+    return FRMC_OK;
+}
+
 int frmc_multiple_pairs_histograms_coords(const int32_t *indexes, int64_t K, const float *boxCoords, int64_t n,
                                           const float *basis, int isPBC, const int32_t *moleculeIndex,
                                           const int32_t *elementIndex, int32_t ne, float minDistance,

@@ -188,4 +188,12 @@ int coordination_run(const CoordLaunch &L, cudaStream_t st);
 // List entries handled by one CTA of the counting kernel.
 int coordination_chunk();
 
+// ShapeFunction in FP64 (fp64_kernels.cu): G on the shells from the oriented
+// uint32 counts, S on q, and the shape function on rv; w1 (hs) and w2 (nq)
+// are scratch.  Every array is on the device.
+int launch_shape_function(const unsigned *counts, int ne, int hs, int npairs, const int *pi, const int *pj,
+                          const double *pc, const double *r, const double *vol, double rho0, double dr,
+                          const double *q, int nq, double dq, const double *rv, int nr, double *G, double *S,
+                          double *Gs, double *w1, double *w2, cudaStream_t st);
+
 }  // namespace frmc

@@ -123,6 +123,23 @@ int frmc_full_pairs_histograms_coords(const float *boxCoords, int64_t n, const f
                                       const int32_t *moleculeIndex, const int32_t *elementIndex, int32_t ne,
                                       float minDistance, float maxDistance, float bin, int32_t hs, float *hintra,
                                       float *hinter);
+/* ShapeFunction (Constraints/Collection.py:15-160) in FP64: the all-pairs
+ * counts of a StructureFactorConstraint's histogram (minDistance, maxDistance,
+ * bin, hs), its total G on the shells
+ *   G(b) = 4 pi r_b rho0 (sum_p pair_coef[p] n_p(b) / shellVolumes[b] - 1)
+ * (n_p: intra + inter counts of element pair (pair_i, pair_j), both
+ * orientations for unlike elements; pair_coef = w_ij V / N_ij;
+ * StructureFactorConstraints.py:836-896), S(q) = 1 + sum_b G(b) dr sin(q r_b) / q
+ * (:302-312, 772-773; dr = r_1 - r_0) and the shape function
+ *   Gshape(r) = 2/pi sum_q dq q (S(q) - 1) sin(q r)   (Collection.py:131-139).
+ * The counts are exact (the reference's float32 histogram stops at 2^24 per
+ * bin).  Gr (hs), Sq (nq) and Gshape (nr) may each be NULL. */
+int frmc_shape_function(const float *boxCoords, int64_t n, const float *basis, int isPBC,
+                        const int32_t *moleculeIndex, const int32_t *elementIndex, int32_t ne, float minDistance,
+                        float maxDistance, float bin, int32_t hs, int32_t npairs, const int32_t *pair_i,
+                        const int32_t *pair_j, const double *pair_coef, const double *shellCenters,
+                        const double *shellVolumes, double rho0, const double *qValues, int32_t nq,
+                        const double *rValues, int32_t nr, double *Gr, double *Sq, double *Gshape);
 /* pairs_histograms.pyx:225-281 multiple_pairs_histograms_dists: distances is
  * (n, K) row-major, column k belongs to atom indexes[k]. */
 int frmc_multiple_pairs_histograms_dists(const int32_t *indexes, int64_t K, const float *distances, int64_t n,

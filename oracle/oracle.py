@@ -555,3 +555,77 @@ def all_atoms_coord_number_coords(boxCoords, basis, isPBC, coresIndexes, shellsI
     multi_atoms_coord_number_coords(np.arange(np.asarray(boxCoords).shape[0], dtype=np.int32), boxCoords, basis,
                                     isPBC, coresIndexes, shellsIndexes, lowerShells, upperShells, asCoreDefIdxs,
                                     inShellDefIdxs, coordNumData)
+
+
+# -------------------------------------------------------------- shape function
+def _normalized_weights(counts, b):
+    """w_ij = (2 - delta_ij) c_i c_j b_i b_j / (sum_k c_k b_k)^2, the element-pair
+    weights of PairDistributionConstraints.py:66-86 (pdbparser's
+    get_normalized_weighting, not installed, implements this definition)."""
+    n = np.asarray(counts, np.float64)
+    bb = np.asarray(b, np.float64)
+    c = n / n.sum()
+    s = (c * bb).sum()
+    return np.outer(c * bb, c * bb) / (s * s) * (2.0 - np.eye(len(n)))
+
+
+def shape_function_grids(qmin, qmax, dq, rmin, rmax, dr):
+    """Collection.py:64-75 (Q) and StructureFactorConstraints.py:336-350, 502-575 (edges)."""
+    F = np.float32
+    Q = np.arange(F(qmin), F(qmax), F(dq)).astype(F)
+    mn, mx, b = F(rmin), F(rmax), F(dr)
+    edges = np.arange(mn, F(mx + b), b).astype(F)
+    centers = ((edges[:-1] + edges[1:]) / F(2.0)).astype(F)
+    return Q, edges, centers, b
+
+
+def shape_function_fp64(boxCoords, basis, isPBC, mol, el, counts, b, volume, rValues, qmin, qmax, dq, rmin, rmax,
+                        dr):
+    """The ShapeFunction chain in float64 on the oracle's histogram:
+    (Gshape on rValues, G on the shells, S on Q)."""
+    Q, edges, centers, bin_ = shape_function_grids(qmin, qmax, dq, rmin, rmax, dr)
+    hs = len(edges) - 1
+    intra, inter = full_pairs_histograms_coords(boxCoords, basis, isPBC, mol, el, len(counts), edges[0], edges[-1],
+                                                bin_, hs)
+    e = edges.astype(np.float64)
+    vol = 4.0 / 3.0 * np.pi * (e[1:] ** 3 - e[:-1] ** 3)
+    w = _normalized_weights(counts, b)
+    rho0 = float(np.asarray(boxCoords).shape[0]) / float(volume)
+    G = total_Gr_fp64(intra, inter, counts, w, volume, vol, centers, rho0)
+    S = sq_from_Gr_fp64(G, gr2sq_matrix_fp64(centers, Q))
+    return sq_to_Gr_fp64(Q, rValues, S), G, S
+
+
+def shape_function_f32_port(boxCoords, basis, isPBC, mol, el, counts, b, volume, rValues, qmin, qmax, dq, rmin,
+                            rmax, dr):
+    """The reference's own float32 arithmetic (StructureFactorConstraints.py:
+    302-312, 346-350, 836-896 and Collection.py:131-139), for a loose check of
+    the formulas: Gshape on rValues (float32)."""
+    F = np.float32
+    PI = F(np.pi)
+    Q, edges, centers, bin_ = shape_function_grids(qmin, qmax, dq, rmin, rmax, dr)
+    hs = len(edges) - 1
+    intra, inter = full_pairs_histograms_coords(boxCoords, basis, isPBC, mol, el, len(counts), edges[0], edges[-1],
+                                                bin_, hs)
+    vol = F(4.0 / 3.) * PI * ((edges[1:]) ** 3 - edges[0:-1] ** 3)
+    w = _normalized_weights(counts, b).astype(F)
+    gr = np.zeros(hs, F)
+    V = float(volume)
+    for i in range(len(counts)):
+        for j in range(i, len(counts)):
+            ni, nj = int(counts[i]), int(counts[j])
+            Nij = ni * (ni - 1) / 2.0 if i == j else ni * nj
+            nij = intra[i, j] + inter[i, j] if i == j else intra[i, j] + intra[j, i] + inter[i, j] + inter[j, i]
+            gr += w[i, j] * (nij / vol) / (Nij / V)
+    rho0 = F(np.asarray(boxCoords).shape[0] / V)
+    Gr = (F(4.) * PI * centers * rho0) * (gr - 1)
+    drr = centers[1] - centers[0]
+    qr = centers.reshape((-1, 1)) * (np.ones((len(centers), 1), dtype=F) * Q)
+    M = drr * (np.sin(qr) / Q)
+    Sq = np.sum(Gr.reshape((-1, 1)) * M, axis=0) + 1
+    out = np.zeros(len(rValues), F)
+    qsq_1 = Q * (Sq - 1)
+    dqq = Q[1] - Q[0]
+    for k, r in enumerate(np.asarray(rValues, F)):
+        out[k] = (2. / PI) * np.sum(qsq_1 * (dqq * np.sin(Q * r)))
+    return out
