@@ -27,6 +27,7 @@ Reported beside the headline:
 * ``dropins``: per-call times of the atomic_distances and
   atomic_coordination drop-ins (the constraints' per-move call on a moved
   13-atom ring and their full recomputations, 52,000-atom molecular system)
+  and of the ShapeFunction (100,000-atom finite cluster, every pair binned)
   beside fullrmc's Cython on the same calls;
 * ``serving``: the serving loop on a Poisson stream of fit requests (20 per
   second; 2,000-200,000 atoms log-uniform, 1-3 species, G(r) on r 0-12 A
@@ -279,7 +280,7 @@ def _call_ms(fn, reps, budget_s=None):
 
 
 def bench_dropins(with_cpu):
-    """Per-call times of the atomic_distances and atomic_coordination drop-ins
+    """Per-call times of the atomic_distances, atomic_coordination and shape-function paths
     through their Python API (host arrays in and out), beside fullrmc's Cython
     (ncores=1) on the same call: the constraints' per-move call (the 13 atoms
     of a moved ring) and the full recomputation, on the 52,000-atom molecular
@@ -323,6 +324,25 @@ def bench_dropins(with_cpu):
         }
 
     out = {}
+    # ShapeFunction of a 100,000-atom finite cluster (infinite boundary
+    # conditions): every pair binned (r 0-110 A, dr 1), S(q) on q 0.001-1
+    # (dq 0.005) and the shape function on r 0.005-20 (0.01)
+    from fullrmc_gb300 import shape_function as gsf
+    rng = np.random.default_rng(77)
+    pts = rng.normal(size=(300000, 3))
+    pts = pts[np.linalg.norm(pts, axis=1) < 2.0][:100000]
+    cl = (pts * 25.0).astype(np.float32)
+    cel = rng.integers(0, 3, size=cl.shape[0]).astype(np.int32)
+    cmol = np.arange(cl.shape[0], dtype=np.int32)
+    ccount = np.bincount(cel, minlength=3)
+    cvol = 4.0 / 3.0 * np.pi * 50.0 ** 3
+    rv = (0.005 + 0.01 * np.arange(2000)).astype(np.float32)
+    sgrid = dict(qmin=0.001, qmax=1.0, dq=0.005, rmin=0.0, rmax=110.0, dr=1.0)
+    eye = np.eye(3, dtype=np.float32)
+    ms, _ = _call_ms(lambda: gsf.gr_shape_function(cl, eye, False, cmol, cel, ccount, [6.0, 8.0, 14.0], cvol, rv,
+                                                   **sgrid), 5)
+    out["shape_function_100000"] = {"gpu_ms": ms, "atoms": int(cl.shape[0]),
+                                    "pairs": int(cl.shape[0]) * (int(cl.shape[0]) - 1) // 2}
     for name, (fn, reps) in cases(gad, gac).items():
         ms, _ = _call_ms(fn, reps)
         out[name] = {"gpu_ms": ms, "atoms": sub if name.endswith("20000") else n,
@@ -344,6 +364,16 @@ def bench_dropins(with_cpu):
                     ms, k = _call_ms(fn, 2 if reps < 10 else 10, budget_s=20.0)
                     out[name].update(cpu_reference_ms=ms, cpu_sample="%d calls" % k)
                 out[name]["gpu_over_cpu"] = out[name]["cpu_reference_ms"] / out[name]["gpu_ms"]
+            # the reference's ShapeFunction cost is its all-pairs float32
+            # histogram: timed on the first 10,000 atoms, scaled by pairs
+            sub_n = 10000
+            Q, edges, centers, mn, mx, b, hs = gsf.shape_function_grids(**sgrid)
+            ms, k = _call_ms(lambda: R["pairs_histograms"].full_pairs_histograms_coords(
+                cl[:sub_n], eye, False, cmol[:sub_n], cel[:sub_n], 3, mn, mx, b, hs, 1), 1)
+            d = out["shape_function_100000"]
+            d.update(cpu_reference_ms=ms * d["pairs"] / (sub_n * (sub_n - 1) / 2),
+                     cpu_sample="all-pairs histogram of 10,000 of the atoms, scaled by pairs")
+            d["gpu_over_cpu"] = d["cpu_reference_ms"] / d["gpu_ms"]
         except Exception as exc:
             out["cpu_error"] = str(exc)[:200]
     return out
