@@ -183,6 +183,7 @@ __device__ __forceinline__ ColView col_view(const EDesc &D)
 
 struct StepParams {
     const EDesc *desc;
+    const EDesc *fdesc;  // fused launches: the descriptors in work-list order (fdesc[k] is item k's engine)
     const int2 *items;
     int nitems;
     int tile;
@@ -1134,8 +1135,7 @@ __device__ void warm_item(const StepParams &p, long long idx)
 {
     if (idx >= p.nitems)
         return;
-    const int2 item = p.items[idx];
-    const EDesc &D = p.desc[item.x];
+    const EDesc &D = p.fdesc[idx];
     const long long stp = D.st->step;
     const long long slot = stp % D.move_cap;
     const int a = D.moves[slot].atom;
@@ -1184,7 +1184,13 @@ __global__ void __launch_bounds__(kMaxEngineThreads, 1) k_engine_step(StepParams
     }
     for (;;) {
         if (threadIdx.x == 0) {
-            const unsigned long long k = atomicAdd(&p.sched->claimed, 1ull);
+            // fused launches: item blockIdx.x first (the list is largest
+            // first), then items gridDim.x, gridDim.x + 1, ... by claim
+            unsigned long long k;
+            if (FUSED)
+                k = fused_items == 0 ? blockIdx.x : gridDim.x + atomicAdd(&p.sched->claimed, 1ull);
+            else
+                k = atomicAdd(&p.sched->claimed, 1ull);
             s_item = k < (unsigned long long)p.nitems ? (int)k : -1;
         }
         __syncthreads();
@@ -1192,8 +1198,8 @@ __global__ void __launch_bounds__(kMaxEngineThreads, 1) k_engine_step(StepParams
         __syncthreads();
         if (it < 0)
             break;
-        const int2 item = p.items[it];
-        const EDesc &D = p.desc[item.x];
+        const int2 item = FUSED ? make_int2(0, -1) : p.items[it];
+        const EDesc &D = FUSED ? p.fdesc[it] : p.desc[item.x];
         if (FUSED && fused_items == 0 && threadIdx.x == 32)
             warm_item(p, (long long)it + gridDim.x);
         if (FUSED) {
@@ -1655,6 +1661,8 @@ struct EngineSet {
     int tile = 1024, threads = 512, ctas_per_sm = 1;  // the usual autotuner choice on GB300
     EDesc *ddesc = nullptr;
     int ddesc_cap = 0;
+    EDesc *fdesc = nullptr;        // descriptors of the fused items, in work-list order
+    int fdesc_cap = 0;
     int2 *items = nullptr;
     int items_cap = 0;
     int nitems = 0;
@@ -1839,6 +1847,13 @@ static int refresh(EngineSet *s)
         FRMC_CUDA(cudaMalloc(&s->sq_items, sizeof(int2) * cap));
         s->sq_cap = cap;
     }
+    if ((int)fused_ids.size() > s->fdesc_cap) {
+        if (s->fdesc) cudaFree(s->fdesc);
+        s->fdesc = nullptr;
+        int cap = std::max((int)fused_ids.size(), 2 * s->fdesc_cap);
+        FRMC_CUDA(cudaMalloc(&s->fdesc, sizeof(EDesc) * cap));
+        s->fdesc_cap = cap;
+    }
     if (nslots > s->ddesc_cap) {
         if (s->ddesc) cudaFree(s->ddesc);
         s->ddesc = nullptr;
@@ -1865,6 +1880,12 @@ static int refresh(EngineSet *s)
     FRMC_CUDA(cudaStreamSynchronize(s->stream));
     if (nslots)
         FRMC_CUDA(cudaMemcpy(s->ddesc, hd.data(), sizeof(EDesc) * nslots, cudaMemcpyHostToDevice));
+    if (!fused_ids.empty()) {
+        std::vector<EDesc> fd;
+        fd.reserve(fused_ids.size());
+        for (int id : fused_ids) fd.push_back(s->slots[id].d);
+        FRMC_CUDA(cudaMemcpy(s->fdesc, fd.data(), sizeof(EDesc) * fd.size(), cudaMemcpyHostToDevice));
+    }
     if (!items.empty())
         FRMC_CUDA(cudaMemcpy(s->items, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice));
     if (!s->live.empty())
@@ -1888,7 +1909,8 @@ static int launch_items(EngineSet *s, const int2 *items, int count, int eval_onl
         grid = count;
     if (grid < 1)
         return FRMC_OK;
-    StepParams p{s->ddesc, items, count, s->tile, eval_only, fused ? s->fused_dp_ints : 0,
+    const EDesc *fd = fused ? s->fdesc + (items - (s->items + s->nsolo)) : nullptr;
+    StepParams p{s->ddesc, fd, items, count, s->tile, eval_only, fused ? s->fused_dp_ints : 0,
                  fused ? s->fused_bins : 0, s->sched};
     if (fused) {
         FRMC_CUDA(cudaFuncSetAttribute(k_engine_step<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem));
@@ -2171,7 +2193,7 @@ static void free_set(EngineSet *s)
         if (sl.blob) cudaFree(sl.blob);
     for (auto &t : s->tables)
         if (t.blob) cudaFree(t.blob);
-    void *ptrs[] = {s->ddesc, s->items, s->dlive, s->dstage_m, s->dstage_r, s->sched, s->sq_items};
+    void *ptrs[] = {s->ddesc, s->fdesc, s->items, s->dlive, s->dstage_m, s->dstage_r, s->sched, s->sq_items};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (s->hstage_m) cudaFreeHost(s->hstage_m);
