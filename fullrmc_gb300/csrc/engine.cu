@@ -32,10 +32,14 @@
 // bit-identical results alone or batched with any other chains, under any
 // tile or CTA configuration.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <map>
 #include <vector>
+
+#include <cublas_v2.h>
+#include <cuda_fp16.h>
 
 #include "frmc_gpu_engine.h"
 #include "frmc_math.cuh"
@@ -140,7 +144,16 @@ struct EDesc {
     double *sqpart;     // [sqblk] this step's partial sums of x (y - h)
     double *sqv;        // [nq] S(Q) written by the evaluation kernel
     int *evl;           // [npairs][hs] this step's non-zero element-pair deltas, per pair
-    int *evn;           // [kMaxP] their counts (-1: a delta beyond 16 bits, read dP instead)
+    int *evn;           // [kMaxP] their counts n (-1 - n: a delta beyond kSqGemmMaxDelta, sum the
+                        // list exactly; INT_MIN: a delta beyond 16 bits, sum the deltas dP)
+    // y on the tensor cores: X holds this step's element-pair deltas as fp16
+    // (column q of the engine at X + q xld, bins down the column), the table
+    // in kSqLimbs balanced base-256 digits multiplies all engines' columns in
+    // one GEMM, and Y (column q at Y + q yld, digit l's rows at l hsp) holds
+    // the digit products, exact integers in fp32.
+    __half *X;
+    const float *Y;
+    int xld, yld, hsp;
     EMove *moves;
     EGroup *groups;     // [move_cap] (group > 1)
     int group;          // atoms per move
@@ -530,6 +543,12 @@ __device__ double eval_full(const EDesc &D, double *red, double *cb)
 // in shared memory (chunk) or global memory (Sb) for the commit.  Sums use the
 // fixed lane order, so the result does not depend on the CTA size.
 constexpr int kMaxP = 10;  // element pairs loaded with unrolled loads (ne <= 4)
+// T in kSqLimbs balanced base-256 digits t_l in [-128, 127] (7 digits cover
+// |T| < 2^48).  With |delta| <= kSqGemmMaxDelta and at most 4096 (kSqMaxBins) bins,
+// every digit product sum is an integer of magnitude <= 128 * 32 * 4096 =
+// 2^24, so fp16 inputs with fp32 accumulation give it exactly.
+constexpr int kSqLimbs = 7;
+constexpr int kSqGemmMaxDelta = 32;
 
 // SMEM: the element-pair deltas are this CTA's shared-memory copy (one CTA per
 // engine); otherwise they are the engine's global array, filled by several
@@ -663,8 +682,9 @@ __device__ double eval_delta(const EDesc &Dg, int *dP, const double *Ab, const d
                         if (SMEM)
                             gdP[q * hs + b] = v;
                         evl[q * hs + atomicAdd(&s_evn[q], 1)] = (b << 16) | (v & 0xffff);
-                        if (v > 32767 || v < -32768)
-                            s_wide = 1;
+                        Dg.X[q * Dg.xld + b] = __int2half_rn(v);
+                        if (v > kSqGemmMaxDelta || v < -kSqGemmMaxDelta)
+                            s_wide = (v > 32767 || v < -32768) ? 2 : max(s_wide, 1);
                     }
                     S += (unsigned)(v + 4) <= 8u ? tabv[q * 9 + v + 4] : coef[q] * (double)v;
                 }
@@ -687,7 +707,7 @@ __device__ double eval_delta(const EDesc &Dg, int *dP, const double *Ab, const d
     }
     const double total = lanes_total(red);
     if (sq && (int)threadIdx.x < np)
-        Dg.evn[threadIdx.x] = s_wide ? -1 : s_evn[threadIdx.x];
+        Dg.evn[threadIdx.x] = s_wide == 0 ? s_evn[threadIdx.x] : (s_wide == 1 ? -1 - s_evn[threadIdx.x] : INT_MIN);
     return total;
 }
 
@@ -1314,10 +1334,13 @@ struct SqParams {
 
 __device__ void sq_finish(const EDesc &D, int *s_flag, double *s_val, MovedGroup &g)
 {
+    __shared__ double s_part[kSqMaxBins / kSqRows];
+    for (int k = threadIdx.x; k < D.sqblk; k += blockDim.x) s_part[k] = __ldcg(D.sqpart + k);
     load_moved_group(D, D.st->step, g);
+    __syncthreads();
     if (threadIdx.x == 0) {
         double dsq = 0.0;
-        for (int k = 0; k < D.sqblk; ++k) dsq += __ldcg(D.sqpart + k);
+        for (int k = 0; k < D.sqblk; ++k) dsq += s_part[k];
         const EState &S0 = *D.st;
         const double sd_new = S0.sd + S0.dsd;
         const double sq_new = S0.sd_sq + dsq;
@@ -1350,6 +1373,9 @@ __device__ void sq_finish(const EDesc &D, int *s_flag, double *s_val, MovedGroup
     }
     const int nph = D.npairs * D.hs;
     for (int k = threadIdx.x; k < nph; k += blockDim.x) D.dP[k] = 0;
+    // the engine's fp16 delta columns are adjacent: clear them for the next step
+    const int nx = D.npairs * D.xld;
+    for (int k = threadIdx.x; k < nx; k += blockDim.x) D.X[k] = __float2half_rn(0.0f);
     if (accept) {
         for (int b = threadIdx.x; b < D.hs; b += blockDim.x) {
             const double sv = D.Sb[b];
@@ -1379,16 +1405,19 @@ __device__ void sq_finish(const EDesc &D, int *s_flag, double *s_val, MovedGroup
     }
 }
 
-constexpr int kSqUnroll = 8;  // table loads in flight per thread
-
+// The S(Q) term of one step over (engine, block of kSqRows rows) items: the
+// CTA's four thread groups take the element pairs q = g, g + 4, ... and form
+// z_q(b) for the block's rows -- from the GEMM's digit products, or for a
+// step with a large delta the exact integer sum over the pair's list (or its
+// deltas) -- then y(b) = yscale sum_q pair_coef_q z_q(b) in q order, the
+// block's share of x (y - h) by a fixed tree.  k_sq_commit then decides and
+// commits, one CTA per engine.
 __global__ void __launch_bounds__(kSqThreads) k_sq_step(SqParams p)
 {
-    extern __shared__ int sq_ev[];  // one element pair's non-zero deltas: (bin << 16) | (delta & 0xffff)
-    __shared__ long long zz[kSqGroups][kSqRows];
+    __shared__ long long zq[kMaxP][kSqRows];
+    __shared__ int s_n[kMaxP];
     __shared__ double red[kSqRows];
-    __shared__ double s_val[3];
-    __shared__ int s_item, s_last, s_flag;
-    __shared__ MovedGroup s_group;
+    __shared__ int s_item;
     const int r = threadIdx.x % kSqRows, g = threadIdx.x / kSqRows;
     for (;;) {
         if (threadIdx.x == 0) {
@@ -1404,63 +1433,47 @@ __global__ void __launch_bounds__(kSqThreads) k_sq_step(SqParams p)
         const int hs = D.hs, np = D.npairs;
         const int b = item.y * kSqRows + r;
         const bool row = b < hs;
-        const long long *__restrict__ T = D.T + (row ? b : 0);
-        double y = 0.0;
-        for (int q = 0; q < np; ++q) {
-            const int n = __ldcg(D.evn + q);
-            long long z = 0, zp = 0, zn = 0;
-            if (n >= 0) {
-                const int *__restrict__ ev = D.evl + q * hs;
-                for (int k = threadIdx.x; k < n; k += kSqThreads) sq_ev[k] = __ldcg(ev + k);
-                __syncthreads();
-                for (int k0 = g * kSqUnroll; k0 < n; k0 += kSqGroups * kSqUnroll) {
-                    const int m = min(kSqUnroll, n - k0);
-                    long long t[kSqUnroll];
-                    int v[kSqUnroll];
+        if (threadIdx.x < np)
+            s_n[threadIdx.x] = __ldcg(D.evn + threadIdx.x);
+        __syncthreads();
+        for (int q = g; q < np; q += kSqGroups) {
+            const int n = s_n[q];
+            long long z = 0;
+            if (row) {
+                if (n >= 0) {
+                    // sum_l 256^l Y_l(b): the digit products are exact
+                    // integers; the sum is taken modulo 2^64 (|z| < 2^63)
+                    const float *__restrict__ Yq = D.Y + (size_t)q * D.yld + b;
+                    float yl[kSqLimbs];
 #pragma unroll
-                    for (int u = 0; u < kSqUnroll; ++u) {
-                        v[u] = 0;
-                        t[u] = 0;
-                        if (u < m) {
-                            const int e = sq_ev[k0 + u];
-                            v[u] = (int)(short)(e & 0xffff);
-                            t[u] = __ldg(T + (size_t)(e >> 16) * hs);
-                        }
+                    for (int l = 0; l < kSqLimbs; ++l) yl[l] = __ldcg(Yq + (size_t)l * D.hsp);
+                    unsigned long long acc = 0;
+#pragma unroll
+                    for (int l = 0; l < kSqLimbs; ++l) acc += (unsigned long long)(long long)yl[l] << (8 * l);
+                    z = (long long)acc;
+                } else if (n != INT_MIN) {
+                    const int *__restrict__ ev = D.evl + q * hs;
+                    for (int k = 0; k < -1 - n; ++k) {
+                        const int e = __ldcg(ev + k);
+                        z += (long long)(short)(e & 0xffff) * __ldg(D.T + (size_t)(e >> 16) * hs + b);
                     }
-                    // deltas are +-1 but for rare coincident pairs, and every
-                    // thread of the CTA sees the same delta: uniform branches
-#pragma unroll
-                    for (int u = 0; u < kSqUnroll; ++u) {
-                        if (v[u] == 1)
-                            zp += t[u];
-                        else if (v[u] == -1)
-                            zn += t[u];
-                        else
-                            z += (long long)v[u] * t[u];
+                } else {
+                    const int *__restrict__ dq = D.dP + q * hs;
+                    for (int c = 0; c < hs; ++c) {
+                        const int v = __ldcg(dq + c);
+                        if (v)
+                            z += (long long)v * __ldg(D.T + (size_t)c * hs + b);
                     }
                 }
-            } else {
-                // a delta beyond 16 bits: read the pair's deltas directly
-                const int *__restrict__ dq = D.dP + q * hs;
-                for (int c = g; c < hs; c += kSqGroups) {
-                    const int v = __ldcg(dq + c);
-                    if (v)
-                        z += (long long)v * __ldg(T + (size_t)c * hs);
-                }
             }
-            zz[g][r] = z + (zp - zn);
-            __syncthreads();
-            if (g == 0) {
-                long long zt = 0;
-#pragma unroll
-                for (int j = 0; j < kSqGroups; ++j) zt += zz[j][r];
-                y = fma(D.pc[q] * D.yscale, (double)zt, y);
-            }
-            __syncthreads();  // the list and the partial sums are reused
+            zq[q][r] = z;
         }
+        __syncthreads();
         if (g == 0) {
             double part = 0.0;
             if (row) {
+                double y = 0.0;
+                for (int q = 0; q < np; ++q) y = fma(D.pc[q] * D.yscale, (double)zq[q][r], y);
                 D.y[b] = y;
                 const double sv = __ldcg(D.Sb + b);
                 if (sv != 0.0)
@@ -1474,18 +1487,8 @@ __global__ void __launch_bounds__(kSqThreads) k_sq_step(SqParams p)
                 red[threadIdx.x] += red[threadIdx.x + st];
             __syncthreads();
         }
-        // release: y and the share are visible before the block is counted
-        if (threadIdx.x == 0) {
+        if (threadIdx.x == 0)
             D.sqpart[item.y] = red[0];
-            __threadfence();
-            const unsigned prev = atomicAdd(&D.st->sq_done, 1u);
-            s_last = (prev == (unsigned)D.sqblk - 1u) ? 1 : 0;
-        }
-        __syncthreads();
-        if (s_last) {
-            __threadfence();
-            sq_finish(D, &s_flag, s_val, s_group);
-        }
         __syncthreads();
     }
     if (threadIdx.x == 0) {
@@ -1497,6 +1500,19 @@ __global__ void __launch_bounds__(kSqThreads) k_sq_step(SqParams p)
             __threadfence();
         }
     }
+}
+
+// One CTA per engine (the item of its first row block; the others return):
+// sum the blocks' shares, decide and commit.
+__global__ void __launch_bounds__(kSqThreads) k_sq_commit(SqParams p)
+{
+    __shared__ double s_val[3];
+    __shared__ int s_flag;
+    __shared__ MovedGroup s_group;
+    const int2 item = p.items[blockIdx.x];
+    if (item.y != 0)
+        return;
+    sq_finish(p.desc[item.x], &s_flag, s_val, s_group);
 }
 
 // S(Q) of engine `id`'s current counts (StructureFactorConstraints.py:780-822
@@ -1576,6 +1592,24 @@ __global__ void k_sq_quantize(double *K, const double *R0, int hs, int s)
     }
 }
 
+// The GEMM operand: TL[(l hsp + b) + c (kSqLimbs hsp)] = digit l of T[c][b]
+// (balanced base 256, so T = sum_l 256^l digit_l), zero outside hs x hs.
+__global__ void k_sq_limbs(const long long *T, int hs, int hsp, __half *TL)
+{
+    const long long n = (long long)hsp * hsp;
+    const long long ld = (long long)kSqLimbs * hsp;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(k / hsp), b = (int)(k - (long long)c * hsp);
+        long long v = (b < hs && c < hs) ? T[(long long)c * hs + b] : 0;
+#pragma unroll
+        for (int l = 0; l < kSqLimbs; ++l) {
+            const long long d = ((v + 128) & 255) - 128;
+            v = (v - d) >> 8;
+            TL[(long long)l * hsp + b + c * ld] = __int2half_rn((int)d);
+        }
+    }
+}
+
 // K[b][c] = sum_q (M[b][q] M[c][q]) w_q in increasing q: 64 x 64 tiles of K
 // per CTA, 4 x 4 per thread, M staged through shared memory 16 Q points at a
 // time.  The product M[b][q] M[c][q] is formed before the weight, so K is
@@ -1627,6 +1661,7 @@ __global__ void __launch_bounds__(256) k_sq_gram(const double *M, const double *
 struct Slot {
     bool live = false;
     bool initialized = false;
+    int sq_table = -1;  // S(Q) table of the engine (or -1)
     EDesc d;
     void *blob = nullptr;
     size_t bytes = 0;
@@ -1639,6 +1674,13 @@ struct SqTable {
     double *M = nullptr, *w = nullptr, *R0 = nullptr;
     long long *T = nullptr;
     size_t bytes = 0;
+    int hsp = 0;           // hs rounded up to a multiple of 8
+    __half *TL = nullptr;  // [kSqLimbs hsp][hsp] digits of T, column-major GEMM operand
+    // this step's fp16 deltas of every engine on the table (hsp x ncols,
+    // column-major) and their digit products (kSqLimbs hsp x ncols)
+    __half *X = nullptr;
+    float *Y = nullptr;
+    int ncols = 0, cap = 0;
 };
 
 constexpr int kFusedSmemMax = 136 * 1024;  // element-pair deltas, A and Bq of a fused step (the column queue comes on top)
@@ -1663,6 +1705,8 @@ struct EngineSet {
     int ddesc_cap = 0;
     EDesc *fdesc = nullptr;        // descriptors of the fused items, in work-list order
     int fdesc_cap = 0;
+    cublasHandle_t blas = nullptr; // the S(Q) terms' GEMM (created on first use)
+    void *blas_ws = nullptr;       // its fixed workspace (graph capture allocates nothing)
     int2 *items = nullptr;
     int items_cap = 0;
     int nitems = 0;
@@ -1677,6 +1721,7 @@ struct EngineSet {
     std::vector<SqTable> tables;
     std::vector<int2> sq_host;     // (engine, row block) of every live engine with an S(Q) term
     std::vector<int> sq_first, sq_count;
+    std::vector<int> sq_xcol;      // per engine id: its first delta column in its table's X
     int2 *sq_items = nullptr;
     int sq_cap = 0;
     int sq_smem = 0;               // dynamic shared memory of the S(Q) kernel
@@ -1838,7 +1883,6 @@ static int refresh(EngineSet *s)
         s->sq_first[id] = (int)s->sq_host.size();
         s->sq_count[id] = D.sqblk;
         for (int k = 0; k < D.sqblk; ++k) s->sq_host.push_back(make_int2(id, k));
-        s->sq_smem = std::max(s->sq_smem, 4 * D.hs);
     }
     if ((int)s->sq_host.size() > s->sq_cap) {
         if (s->sq_items) cudaFree(s->sq_items);
@@ -1874,6 +1918,63 @@ static int refresh(EngineSet *s)
         int cap = std::max((int)s->live.size(), 2 * s->dlive_cap);
         FRMC_CUDA(cudaMalloc(&s->dlive, sizeof(int) * cap));
         s->dlive_cap = cap;
+    }
+    // S(Q) GEMM columns: each live engine with an S(Q) term owns npairs
+    // adjacent fp16 delta columns of its table's X and the matching digit-
+    // product columns of Y.  X is all zero between steps (the finisher clears
+    // its columns), so columns can be dealt afresh here.
+    s->sq_xcol.assign(nslots, -1);
+    for (auto &t : s->tables) t.ncols = 0;
+    for (int id : s->live) {
+        Slot &sl = s->slots[id];
+        if (!sl.d.sq)
+            continue;
+        SqTable &t = s->tables[sl.sq_table];
+        s->sq_xcol[id] = t.ncols;
+        t.ncols += sl.d.npairs;
+    }
+    FRMC_CUDA(cudaStreamSynchronize(s->stream));
+    bool any_sq = false;
+    for (const auto &t : s->tables) any_sq |= t.ncols > 0;
+    if (any_sq && !s->blas) {
+        // created here, never inside a stream capture; the workspace is fixed
+        // so that captured GEMMs allocate nothing
+        const cublasStatus_t cs = cublasCreate(&s->blas);
+        if (cs != CUBLAS_STATUS_SUCCESS) {
+            s->blas = nullptr;
+            return set_error(FRMC_E_CUDA, "cublasCreate failed (status %d)", (int)cs);
+        }
+        const size_t ws = 32u << 20;
+        FRMC_CUDA(cudaMalloc(&s->blas_ws, ws));
+        if (cublasSetWorkspace(s->blas, s->blas_ws, ws) != CUBLAS_STATUS_SUCCESS ||
+            cublasSetMathMode(s->blas, (cublasMath_t)(CUBLAS_DEFAULT_MATH |
+                                                       CUBLAS_MATH_DISALLOW_REDUCED_PRECISION_REDUCTION)) !=
+                CUBLAS_STATUS_SUCCESS)
+            return set_error(FRMC_E_CUDA, "cuBLAS workspace / math mode");
+    }
+    for (auto &t : s->tables) {
+        if (t.ncols <= t.cap)
+            continue;
+        if (t.X) cudaFree(t.X);
+        if (t.Y) cudaFree(t.Y);
+        t.X = nullptr;
+        t.Y = nullptr;
+        const int cap = std::max(t.ncols, 2 * t.cap);
+        FRMC_CUDA(cudaMalloc(&t.X, sizeof(__half) * (size_t)t.hsp * cap));
+        FRMC_CUDA(cudaMemset(t.X, 0, sizeof(__half) * (size_t)t.hsp * cap));
+        FRMC_CUDA(cudaMalloc(&t.Y, sizeof(float) * (size_t)kSqLimbs * t.hsp * cap));
+        t.cap = cap;
+    }
+    for (int id : s->live) {
+        Slot &sl = s->slots[id];
+        if (!sl.d.sq)
+            continue;
+        const SqTable &t = s->tables[sl.sq_table];
+        sl.d.hsp = t.hsp;
+        sl.d.xld = t.hsp;
+        sl.d.yld = kSqLimbs * t.hsp;
+        sl.d.X = t.X + (size_t)s->sq_xcol[id] * t.hsp;
+        sl.d.Y = t.Y + (size_t)s->sq_xcol[id] * kSqLimbs * t.hsp;
     }
     std::vector<EDesc> hd(nslots);
     for (int k = 0; k < nslots; ++k) hd[k] = s->slots[k].d;
@@ -1923,16 +2024,49 @@ static int launch_items(EngineSet *s, const int2 *items, int count, int eval_onl
 }
 
 // S(Q) row blocks [first, first + count) of the set's S(Q) item list.
-static int launch_sq(EngineSet *s, int first, int count, cudaStream_t st)
+// The digit products of every table's delta columns (engine >= 0: that
+// engine's columns only): Y = TL X, fp16 in, fp32 accumulate -- the products
+// are exact integers (see kSqLimbs).
+static int sq_gemm(EngineSet *s, int engine, cudaStream_t st)
+{
+    if (!s->blas)
+        return set_error(FRMC_E_STATE, "S(Q) GEMM before the engine set was refreshed");
+    if (cublasSetStream(s->blas, st) != CUBLAS_STATUS_SUCCESS)
+        return set_error(FRMC_E_CUDA, "cublasSetStream failed");
+    const float one = 1.0f, zero = 0.0f;
+    for (int ti = 0; ti < (int)s->tables.size(); ++ti) {
+        const SqTable &t = s->tables[ti];
+        int col0 = 0, ncol = t.ncols;
+        if (engine >= 0) {
+            if (s->slots[engine].sq_table != ti)
+                continue;
+            col0 = s->sq_xcol[engine];
+            ncol = s->slots[engine].d.npairs;
+        }
+        if (ncol <= 0)
+            continue;
+        const int M = kSqLimbs * t.hsp;
+        const cublasStatus_t bs = cublasGemmEx(
+            s->blas, CUBLAS_OP_N, CUBLAS_OP_N, M, ncol, t.hsp, &one, t.TL, CUDA_R_16F, M,
+            t.X + (size_t)col0 * t.hsp, CUDA_R_16F, t.hsp, &zero, t.Y + (size_t)col0 * M, CUDA_R_32F, M,
+            CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
+        if (bs != CUBLAS_STATUS_SUCCESS)
+            return set_error(FRMC_E_CUDA, "cublasGemmEx failed (%d)", (int)bs);
+    }
+    return FRMC_OK;
+}
+
+static int launch_sq(EngineSet *s, int first, int count, cudaStream_t st, int engine = -1)
 {
     if (count <= 0)
         return FRMC_OK;
+    FRMC_TRY(sq_gemm(s, engine, st));
     Context *c;
     FRMC_TRY(get_context(&c));
-    int grid = std::min(count, c->sms * 8);
+    const int grid = std::min(count, c->sms * 8);
     SqParams p{s->ddesc, s->sq_items + first, count, s->sched + 1};
-    FRMC_CUDA(cudaFuncSetAttribute(k_sq_step, cudaFuncAttributeMaxDynamicSharedMemorySize, s->sq_smem));
-    k_sq_step<<<grid, kSqThreads, s->sq_smem, st>>>(p);
+    k_sq_step<<<grid, kSqThreads, 0, st>>>(p);
+    k_sq_commit<<<count, kSqThreads, 0, st>>>(p);
     FRMC_CUDA(cudaGetLastError());
     return FRMC_OK;
 }
@@ -2176,6 +2310,7 @@ static int add_engine(EngineSet *s, const frmc_engine_spec &sp, int *out_id)
         s->slots.push_back(Slot());
     }
     sl.live = true;
+    sl.sq_table = sp.sq_table;
     s->slots[id] = sl;
     s->live.push_back(id);
     std::sort(s->live.begin(), s->live.end());
@@ -2191,8 +2326,14 @@ static void free_set(EngineSet *s)
     drop_graphs(s);
     for (auto &sl : s->slots)
         if (sl.blob) cudaFree(sl.blob);
-    for (auto &t : s->tables)
+    for (auto &t : s->tables) {
         if (t.blob) cudaFree(t.blob);
+        if (t.TL) cudaFree(t.TL);
+        if (t.X) cudaFree(t.X);
+        if (t.Y) cudaFree(t.Y);
+    }
+    if (s->blas) cublasDestroy(s->blas);
+    if (s->blas_ws) cudaFree(s->blas_ws);
     void *ptrs[] = {s->ddesc, s->fdesc, s->items, s->dlive, s->dstage_m, s->dstage_r, s->sched, s->sq_items};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -2468,7 +2609,7 @@ int frmc_engines_step(void *handle, int32_t engine, int32_t steps, int use_graph
             FRMC_TRY(launch_items(s, s->items + fi, 1, 0, sx, fused_dyn_smem(s), true));
         else
             FRMC_TRY(launch_items(s, s->items + s->item_first[engine], count, 0, sx));
-        return launch_sq(s, s->sq_first[engine], s->sq_count[engine], sx);
+        return launch_sq(s, s->sq_first[engine], s->sq_count[engine], sx, engine);
     };
     if (!use_graph) {
         for (int k = 0; k < steps; ++k) FRMC_TRY(one(st));
@@ -2696,10 +2837,20 @@ int frmc_engines_sq_table(void *handle, int32_t hs, int32_t nq, const double *M,
         k_sq_quantize<<<c->sms * 2, 256, 0, s->stream>>>(K, t.R0, hs, t.s);
         ce = cudaGetLastError();
     }
+    if (ce == cudaSuccess) {
+        t.hsp = (hs + 7) & ~7;
+        ce = cudaMalloc(&t.TL, sizeof(__half) * (size_t)kSqLimbs * t.hsp * t.hsp);
+    }
+    if (ce == cudaSuccess) {
+        k_sq_limbs<<<c->sms * 4, 256, 0, s->stream>>>(t.T, hs, t.hsp, t.TL);
+        ce = cudaGetLastError();
+        t.bytes += sizeof(__half) * (size_t)kSqLimbs * t.hsp * t.hsp;
+    }
     if (ce == cudaSuccess)
         ce = cudaStreamSynchronize(s->stream);
     if (ce != cudaSuccess) {
         cudaFree(t.blob);
+        if (t.TL) cudaFree(t.TL);
         return cuda_fail(ce, "S(Q) table");
     }
     s->tables.push_back(t);
