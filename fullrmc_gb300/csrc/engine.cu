@@ -154,6 +154,8 @@ struct EDesc {
     __half *X;
     const float *Y;
     int xld, yld, hsp;
+    int sq_gemm_max;    // largest |delta| taken through the GEMM (kSqGemmMaxDelta; lower values,
+                        // down to 0 = never and -1 = the dense integer loop, exist for tests)
     EMove *moves;
     EGroup *groups;     // [move_cap] (group > 1)
     int group;          // atoms per move
@@ -683,8 +685,8 @@ __device__ double eval_delta(const EDesc &Dg, int *dP, const double *Ab, const d
                             gdP[q * hs + b] = v;
                         evl[q * hs + atomicAdd(&s_evn[q], 1)] = (b << 16) | (v & 0xffff);
                         Dg.X[q * Dg.xld + b] = __int2half_rn(v);
-                        if (v > kSqGemmMaxDelta || v < -kSqGemmMaxDelta)
-                            s_wide = (v > 32767 || v < -32768) ? 2 : max(s_wide, 1);
+                        if (v > Dg.sq_gemm_max || v < -Dg.sq_gemm_max)
+                            s_wide = (v > 32767 || v < -32768 || Dg.sq_gemm_max < 0) ? 2 : max(s_wide, 1);
                     }
                     S += (unsigned)(v + 4) <= 8u ? tabv[q * 9 + v + 4] : coef[q] * (double)v;
                 }
@@ -2223,6 +2225,7 @@ static int add_engine(EngineSet *s, const frmc_engine_spec &sp, int *out_id)
         D.var2q = sp.sq_variance_squared;
         D.M = tab->M;
         D.T = tab->T;
+        D.sq_gemm_max = kSqGemmMaxDelta;
         D.wq = tab->w;
         D.yscale = std::ldexp(sp.sq_rho0, -tab->s);
         D.Rq = (double *)(b + L.Rq);
@@ -2462,6 +2465,16 @@ int frmc_engines_set_tune(void *handle, int tile, int threads, int ctas_per_sm)
     s->ctas_per_sm = ctas_per_sm;
     s->dirty = true;
     return refresh(s);
+}
+
+int frmc_engines_set_sq_gemm_limit(void *handle, int32_t limit)
+{
+    EngineSet *s = as_set(handle);
+    if (!s || limit < -1 || limit > kSqGemmMaxDelta)
+        return set_error(FRMC_E_ARG, "engines_set_sq_gemm_limit: limit must be in [-1, %d]", kSqGemmMaxDelta);
+    for (auto &sl : s->slots) sl.d.sq_gemm_max = limit;
+    s->dirty = true;
+    return FRMC_OK;
 }
 
 int frmc_engines_set_mode(void *handle, int fused)

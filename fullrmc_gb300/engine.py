@@ -56,6 +56,7 @@ register("frmc_engines_destroy", [_vp])
 register("frmc_engines_set_tune", [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int])
 register("frmc_engines_get_tune", [_vp] + [ctypes.POINTER(ctypes.c_int)] * 4)
 register("frmc_engines_set_mode", [_vp, ctypes.c_int])
+register("frmc_engines_set_sq_gemm_limit", [_vp, ctypes.c_int32])
 register("frmc_engines_init", [_vp])
 register("frmc_engines_push_moves", [_vp, _i32, I32P, F32P, F32P, _i32, _i64, ctypes.c_int])
 register("frmc_engines_step", [_vp, _i32, _i32, ctypes.c_int, _vp])
@@ -473,6 +474,12 @@ class EngineSet:
 
     def set_mode(self, fused):
         check(load().frmc_engines_set_mode(self.handle, int(bool(fused))))
+
+    def set_sq_gemm_limit(self, limit):
+        """Largest element-pair delta the S(Q) product takes through the GEMM
+        (default 32); 0 forces the exact sum over the list of deltas and -1
+        the dense integer loop (all three give the same integers)."""
+        check(load().frmc_engines_set_sq_gemm_limit(self.handle, int(limit)))
 
     TUNE_CANDIDATES = ((1024, 512, 1), (2048, 512, 1), (1024, 384, 1), (1024, 256, 2), (512, 128, 4),
                        (1024, 256, 4), (2048, 256, 2))

@@ -112,6 +112,12 @@ int frmc_engines_get_tune(void *handle, int *tile, int *threads, int *ctas_per_s
  * fit in shared memory (fused = 1, the default), else every engine is split
  * over atom tiles (fused = 0).  Results are identical either way. */
 int frmc_engines_set_mode(void *handle, int fused);
+/* The S(Q) term's product y = T x runs as one fp16 GEMM over digits of T when
+ * every element-pair delta of the step is at most `limit` in magnitude
+ * (default and maximum 32, where the GEMM is exact), else as an exact integer
+ * sum over the step's list of deltas; -1 takes the dense integer loop.  All
+ * three give the same integers; the lower limits exist to test that. */
+int frmc_engines_set_sq_gemm_limit(void *handle, int32_t limit);
 /* All-pairs histograms of the initial coordinates and the initial chi2. */
 int frmc_engines_init(void *handle);
 /* Moves for steps [first_step, first_step + count) of engine e: atoms (count,),

@@ -52,10 +52,12 @@ def _oracle_chi2(oracle_mod, s, intra, inter):
     return s.model.chi2_fp64(intra, inter) + sd_sq / s.sq.variance_squared
 
 
-def _run(systems, moves, steps, mode="batched", fused=1, graph=True, chunk=None, tune=None):
+def _run(systems, moves, steps, mode="batched", fused=1, graph=True, chunk=None, tune=None, gemm_limit=None):
     from fullrmc_gb300.engine import EngineSet
     es = EngineSet(systems, move_cap=max(64, steps), tune=tune)
     es.set_mode(fused)
+    if gemm_limit is not None:
+        es.set_sq_gemm_limit(gemm_limit)
     es.init()
     for e, (a, v, u) in enumerate(moves):
         es.push_moves(e, a[:steps], v[:steps], u[:steps], 0)
@@ -140,6 +142,20 @@ def test_sq_chains_identical_solo_batched_fused_split():
     _same(base, _run(systems, mv, steps, mode="solo", chunk=7))
     _same(base, _run(systems, mv, steps, fused=0, graph=False))
     _same(base, _run(systems, mv, steps, tune=(128, 128, 8), chunk=13))
+
+
+def test_sq_gemm_digits_give_the_integer_sums_exactly():
+    """The tensor-core product (fp16 digits of T times fp16 deltas, fp32
+    accumulation) yields the same integers as the exact sum over the list of
+    deltas (limit 0) and the dense integer loop (limit -1): the chains agree
+    bit for bit, fused and tile-split."""
+    systems = _systems(3, seed=17, nmin=800, nmax=2600)
+    steps = 40
+    mv = _moves(systems, steps, seed=6, amp=0.5)
+    base = _run(systems, mv, steps)
+    _same(base, _run(systems, mv, steps, gemm_limit=0))
+    _same(base, _run(systems, mv, steps, gemm_limit=-1, graph=False))
+    _same(base, _run(systems, mv, steps, gemm_limit=1, fused=0))
 
 
 def test_sq_and_plain_engines_mixed():
