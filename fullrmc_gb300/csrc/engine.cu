@@ -57,7 +57,7 @@ struct EState {
     long long accepted;
     unsigned done;      // items of the current step finished
     unsigned tcount;    // entries in the touched-bin list of the current step
-    unsigned sq_done;   // S(Q) row blocks of the current step finished
+    unsigned sq_done;   // reserved (zero)
     int fmt;            // touched-list format of the step: 1 = (flat << 1) | sign, 0 = flat
 };
 
@@ -1310,19 +1310,18 @@ __global__ void k_gather_results(const EDesc *desc, const int *ids, EResult *out
 // y is formed from the integer deltas and the fixed-point table T (K scaled
 // by the shells' 4 pi r / volume and 2^s): z_p(b) = sum_c T[c][b] dP_p(c) is
 // an exact int64 sum, so its value does not depend on the order of the
-// terms, and y(b) = rho0 2^-s sum_p pair_coef_p z_p(b).  This keeps the
-// O(changed bins x bins) part on the integer pipes, which run many times
-// faster than FP64 on this GPU.
-// Items are (engine, block of kSqRows rows).  For each element pair a CTA
-// stages the pair's list of non-zero deltas (written by the histogram pass)
-// in shared memory; kSqGroups thread groups of kSqRows threads (thread = row,
-// T read along rows, kSqUnroll loads in flight) take interleaved chunks of the
-// list, and their partial z_p are added (exactly) before y is formed.  The
-// CTA then takes its rows' share of x (y - h); the CTA that finishes an
-// engine's last block adds the shares in block order, decides and commits:
-// counts, Bq -= 2 A S, h -= 2 y, coordinates, and clears dP.
+// terms, and y(b) = rho0 2^-s sum_p pair_coef_p z_p(b).
+// The O(changed bins x bins) product runs on the tensor cores: T's balanced
+// base-256 digits (fp16) times every engine's fp16 delta columns in one GEMM
+// (sq_gemm), whose fp32 results are exact integers (see kSqLimbs); a step with
+// a delta beyond the GEMM's limit sums its list of deltas exactly instead.
+// k_sq_step takes (engine, block of kSqRows rows) items, combines the digits
+// per element pair (kSqGroups thread groups share the pairs) and forms the
+// rows' share of x (y - h); k_sq_commit adds the shares in block order,
+// decides and commits: counts, Bq -= 2 A S, h -= 2 y, coordinates, and clears
+// dP and the delta columns.
 constexpr int kSqRows = 64;       // rows per item
-constexpr int kSqGroups = 4;      // event groups per item
+constexpr int kSqGroups = 4;      // thread groups (element pairs) per item
 constexpr int kSqThreads = kSqRows * kSqGroups;
 constexpr int kSqMaxBins = 4096;  // histogram bins of an engine with an S(Q) term
 constexpr int kSqBits = 48;       // largest |T| is below 2^48: 2^15 unit deltas fit in an int64 sum
@@ -1726,7 +1725,6 @@ struct EngineSet {
     std::vector<int> sq_xcol;      // per engine id: its first delta column in its table's X
     int2 *sq_items = nullptr;
     int sq_cap = 0;
-    int sq_smem = 0;               // dynamic shared memory of the S(Q) kernel
     cudaStream_t stream = nullptr;
     std::map<std::pair<int, int>, cudaGraphExec_t> graphs;
     bool dirty = true;
@@ -1877,7 +1875,6 @@ static int refresh(EngineSet *s)
     s->sq_host.clear();
     s->sq_first.assign(nslots, -1);
     s->sq_count.assign(nslots, 0);
-    s->sq_smem = 0;
     for (int id : s->live) {
         const EDesc &D = s->slots[id].d;
         if (!D.sq)
