@@ -2358,7 +2358,14 @@ int frmc_engine_footprint(const frmc_engine_spec *spec, int64_t *bytes)
 {
     if (!spec || !bytes)
         return set_error(FRMC_E_ARG, "engine_footprint: null argument");
-    *bytes = (int64_t)blob_layout(*spec).total;
+    int64_t b = (int64_t)blob_layout(*spec).total;
+    if (spec->sq_table >= 0) {
+        // the engine's columns of its table's fp16 deltas and fp32 digit
+        // products (counted twice: the shared buffers grow by doubling)
+        const int64_t hsp = (spec->hs + 7) & ~7;
+        b += 2 * (int64_t)spec->npairs * hsp * (int64_t)(sizeof(__half) + sizeof(float) * kSqLimbs);
+    }
+    *bytes = b;
     return FRMC_OK;
 }
 
