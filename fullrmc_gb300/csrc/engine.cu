@@ -1713,10 +1713,14 @@ struct EngineSet {
     int nitems = 0;
     int *dlive = nullptr;
     int dlive_cap = 0;
-    EMove *hstage_m = nullptr;     // pinned
-    EResult *hstage_r = nullptr;   // pinned
-    EMove *dstage_m = nullptr;
-    EResult *dstage_r = nullptr;
+    // step_host staging, two slots so that a host can submit a step before
+    // it reads the previous one's results
+    EMove *hstage_m[2] = {nullptr, nullptr};     // pinned
+    EResult *hstage_r[2] = {nullptr, nullptr};   // pinned
+    EMove *dstage_m[2] = {nullptr, nullptr};
+    EResult *dstage_r[2] = {nullptr, nullptr};
+    cudaEvent_t stage_ev[2] = {nullptr, nullptr};
+    bool stage_busy[2] = {false, false};
     int stage_cap = 0;
     Sched *sched = nullptr;        // [0]: histogram step kernels, [1]: S(Q) kernel
     std::vector<SqTable> tables;
@@ -1727,6 +1731,8 @@ struct EngineSet {
     int sq_cap = 0;
     cudaStream_t stream = nullptr;
     std::map<std::pair<int, int>, cudaGraphExec_t> graphs;
+    cudaGraphExec_t host_graph[2] = {nullptr, nullptr};  // step_host per slot: copy in, scatter,
+    int host_graph_E[2] = {0, 0};                        // step, gather, copy out
     bool dirty = true;
 };
 
@@ -1822,6 +1828,12 @@ static void drop_graphs(EngineSet *s)
 {
     for (auto &kv : s->graphs) cudaGraphExecDestroy(kv.second);
     s->graphs.clear();
+    for (int k = 0; k < 2; ++k) {
+        if (s->host_graph[k])
+            cudaGraphExecDestroy(s->host_graph[k]);
+        s->host_graph[k] = nullptr;
+        s->host_graph_E[k] = 0;
+    }
 }
 
 // Rebuild the work list over live engines and upload descriptors.
@@ -2334,11 +2346,16 @@ static void free_set(EngineSet *s)
     }
     if (s->blas) cublasDestroy(s->blas);
     if (s->blas_ws) cudaFree(s->blas_ws);
-    void *ptrs[] = {s->ddesc, s->fdesc, s->items, s->dlive, s->dstage_m, s->dstage_r, s->sched, s->sq_items};
+    void *ptrs[] = {s->ddesc, s->fdesc, s->items, s->dlive, s->sched, s->sq_items};
     for (void *p : ptrs)
         if (p) cudaFree(p);
-    if (s->hstage_m) cudaFreeHost(s->hstage_m);
-    if (s->hstage_r) cudaFreeHost(s->hstage_r);
+    for (int k = 0; k < 2; ++k) {
+        if (s->dstage_m[k]) cudaFree(s->dstage_m[k]);
+        if (s->dstage_r[k]) cudaFree(s->dstage_r[k]);
+        if (s->hstage_m[k]) cudaFreeHost(s->hstage_m[k]);
+        if (s->hstage_r[k]) cudaFreeHost(s->hstage_r[k]);
+        if (s->stage_ev[k]) cudaEventDestroy(s->stage_ev[k]);
+    }
     if (s->stream)
         cudaStreamDestroy(s->stream);
     delete s;
@@ -2660,12 +2677,19 @@ int frmc_engines_step(void *handle, int32_t engine, int32_t steps, int use_graph
     return FRMC_OK;
 }
 
-int frmc_engines_step_host(void *handle, const int32_t *atoms, const float *vecs, const float *u, double *chi2_new,
-                           int32_t *accepted)
+// One batched step from host arrays into staging slot `slot` (0 or 1): the
+// moves are written to the slot's pinned buffer, and one CUDA graph copies
+// them in, scatters them into the rings, steps, gathers the results and
+// copies them back; the slot's event marks its completion.
+static int step_host_submit(EngineSet *s, const int32_t *atoms, const float *vecs, const float *u, int slot)
 {
-    EngineSet *s = as_set(handle);
-    if (!s)
-        return set_error(FRMC_E_ARG, "null handle");
+    if (slot < 0 || slot > 1)
+        return set_error(FRMC_E_ARG, "step_host: slot must be 0 or 1");
+    if (s->stage_busy[slot])
+        return set_error(FRMC_E_STATE, "step_host: slot %d holds a step whose results were not collected", slot);
+    const bool other_busy = s->stage_busy[1 - slot];
+    if (s->dirty && other_busy)
+        return set_error(FRMC_E_STATE, "step_host: the engine set changed while a step is in flight");
     FRMC_TRY(refresh(s));
     const int E = (int)s->live.size();
     if (E == 0)
@@ -2677,23 +2701,32 @@ int frmc_engines_step_host(void *handle, const int32_t *atoms, const float *vecs
         if (atoms[k] < 0 || atoms[k] >= s->slots[s->live[k]].d.n)
             return set_error(FRMC_E_INDEX, "step_host: atom %d out of range for engine %d", atoms[k], s->live[k]);
     if (E > s->stage_cap) {
-        if (s->hstage_m) cudaFreeHost(s->hstage_m);
-        if (s->hstage_r) cudaFreeHost(s->hstage_r);
-        if (s->dstage_m) cudaFree(s->dstage_m);
-        if (s->dstage_r) cudaFree(s->dstage_r);
-        s->hstage_m = nullptr;
-        s->hstage_r = nullptr;
-        s->dstage_m = nullptr;
-        s->dstage_r = nullptr;
-        int cap = std::max(E, 2 * s->stage_cap);
-        FRMC_CUDA(cudaMallocHost(&s->hstage_m, sizeof(EMove) * cap));
-        FRMC_CUDA(cudaMallocHost(&s->hstage_r, sizeof(EResult) * cap));
-        FRMC_CUDA(cudaMalloc(&s->dstage_m, sizeof(EMove) * cap));
-        FRMC_CUDA(cudaMalloc(&s->dstage_r, sizeof(EResult) * cap));
+        if (other_busy)
+            return set_error(FRMC_E_STATE, "step_host: the staging must grow while a step is in flight");
+        FRMC_CUDA(cudaStreamSynchronize(s->stream));
+        drop_graphs(s);  // the captured copies name the staging buffers
+        const int cap = std::max(E, 2 * s->stage_cap);
+        for (int k = 0; k < 2; ++k) {
+            if (s->hstage_m[k]) cudaFreeHost(s->hstage_m[k]);
+            if (s->hstage_r[k]) cudaFreeHost(s->hstage_r[k]);
+            if (s->dstage_m[k]) cudaFree(s->dstage_m[k]);
+            if (s->dstage_r[k]) cudaFree(s->dstage_r[k]);
+            s->hstage_m[k] = nullptr;
+            s->hstage_r[k] = nullptr;
+            s->dstage_m[k] = nullptr;
+            s->dstage_r[k] = nullptr;
+            FRMC_CUDA(cudaMallocHost(&s->hstage_m[k], sizeof(EMove) * cap));
+            FRMC_CUDA(cudaMallocHost(&s->hstage_r[k], sizeof(EResult) * cap));
+            FRMC_CUDA(cudaMalloc(&s->dstage_m[k], sizeof(EMove) * cap));
+            FRMC_CUDA(cudaMalloc(&s->dstage_r[k], sizeof(EResult) * cap));
+            if (!s->stage_ev[k])
+                FRMC_CUDA(cudaEventCreateWithFlags(&s->stage_ev[k], cudaEventDisableTiming));
+        }
         s->stage_cap = cap;
     }
+    EMove *hm = s->hstage_m[slot];
     for (int k = 0; k < E; ++k) {
-        EMove &m = s->hstage_m[k];
+        EMove &m = hm[k];
         m.atom = atoms[k];
         m.v[0] = vecs[3 * k];
         m.v[1] = vecs[3 * k + 1];
@@ -2701,19 +2734,91 @@ int frmc_engines_step_host(void *handle, const int32_t *atoms, const float *vecs
         m.u = u ? u[k] : 1.0f;
     }
     cudaStream_t st = s->stream;
-    FRMC_CUDA(cudaMemcpyAsync(s->dstage_m, s->hstage_m, sizeof(EMove) * E, cudaMemcpyHostToDevice, st));
-    k_scatter_moves<<<(E + 127) / 128, 128, 0, st>>>(s->ddesc, s->dlive, s->dstage_m, E);
-    FRMC_CUDA(cudaGetLastError());
-    FRMC_TRY(launch_batched(s, st));
-    k_gather_results<<<(E + 127) / 128, 128, 0, st>>>(s->ddesc, s->dlive, s->dstage_r, E);
-    FRMC_CUDA(cudaGetLastError());
-    FRMC_CUDA(cudaMemcpyAsync(s->hstage_r, s->dstage_r, sizeof(EResult) * E, cudaMemcpyDeviceToHost, st));
-    FRMC_CUDA(cudaStreamSynchronize(st));
+    auto body = [&](cudaStream_t sx) -> int {
+        FRMC_CUDA(cudaMemcpyAsync(s->dstage_m[slot], hm, sizeof(EMove) * E, cudaMemcpyHostToDevice, sx));
+        k_scatter_moves<<<(E + 127) / 128, 128, 0, sx>>>(s->ddesc, s->dlive, s->dstage_m[slot], E);
+        FRMC_CUDA(cudaGetLastError());
+        FRMC_TRY(launch_batched(s, sx));
+        k_gather_results<<<(E + 127) / 128, 128, 0, sx>>>(s->ddesc, s->dlive, s->dstage_r[slot], E);
+        FRMC_CUDA(cudaGetLastError());
+        FRMC_CUDA(cudaMemcpyAsync(s->hstage_r[slot], s->dstage_r[slot], sizeof(EResult) * E, cudaMemcpyDeviceToHost,
+                                  sx));
+        return FRMC_OK;
+    };
+    if (!s->host_graph[slot] || s->host_graph_E[slot] != E) {
+        if (s->host_graph[slot])
+            cudaGraphExecDestroy(s->host_graph[slot]);
+        s->host_graph[slot] = nullptr;
+        cudaStream_t cap;
+        FRMC_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        cudaGraph_t g;
+        cudaError_t ce = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+        int rc = FRMC_OK;
+        if (ce == cudaSuccess) {
+            rc = body(cap);
+            ce = cudaStreamEndCapture(cap, &g);
+        }
+        cudaStreamDestroy(cap);
+        if (rc)
+            return rc;
+        if (ce != cudaSuccess)
+            return cuda_fail(ce, "step_host graph capture");
+        ce = cudaGraphInstantiate(&s->host_graph[slot], g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) {
+            s->host_graph[slot] = nullptr;
+            return cuda_fail(ce, "step_host graph instantiate");
+        }
+        s->host_graph_E[slot] = E;
+    }
+    FRMC_CUDA(cudaGraphLaunch(s->host_graph[slot], st));
+    FRMC_CUDA(cudaEventRecord(s->stage_ev[slot], st));
+    s->stage_busy[slot] = true;
+    return FRMC_OK;
+}
+
+static int step_host_collect(EngineSet *s, int slot, double *chi2_new, int32_t *accepted)
+{
+    if (slot < 0 || slot > 1 || !s->stage_busy[slot])
+        return set_error(FRMC_E_STATE, "step_host: slot %d holds no submitted step", slot);
+    FRMC_CUDA(cudaEventSynchronize(s->stage_ev[slot]));
+    s->stage_busy[slot] = false;
+    const int E = (int)s->live.size();
+    const EResult *hr = s->hstage_r[slot];
     for (int k = 0; k < E; ++k) {
-        if (chi2_new) chi2_new[k] = s->hstage_r[k].chi2_new;
-        if (accepted) accepted[k] = s->hstage_r[k].accepted;
+        if (chi2_new) chi2_new[k] = hr[k].chi2_new;
+        if (accepted) accepted[k] = hr[k].accepted;
     }
     return FRMC_OK;
+}
+
+int frmc_engines_step_host(void *handle, const int32_t *atoms, const float *vecs, const float *u, double *chi2_new,
+                           int32_t *accepted)
+{
+    EngineSet *s = as_set(handle);
+    if (!s)
+        return set_error(FRMC_E_ARG, "null handle");
+    if (s->live.empty())
+        return FRMC_OK;
+    FRMC_TRY(step_host_submit(s, atoms, vecs, u, 0));
+    return s->stage_busy[0] ? step_host_collect(s, 0, chi2_new, accepted) : FRMC_OK;
+}
+
+int frmc_engines_step_host_submit(void *handle, const int32_t *atoms, const float *vecs, const float *u,
+                                  int32_t slot)
+{
+    EngineSet *s = as_set(handle);
+    if (!s)
+        return set_error(FRMC_E_ARG, "null handle");
+    return step_host_submit(s, atoms, vecs, u, slot);
+}
+
+int frmc_engines_step_host_collect(void *handle, int32_t slot, double *chi2_new, int32_t *accepted)
+{
+    EngineSet *s = as_set(handle);
+    if (!s)
+        return set_error(FRMC_E_ARG, "null handle");
+    return step_host_collect(s, slot, chi2_new, accepted);
 }
 
 int frmc_engines_sync(void *handle)

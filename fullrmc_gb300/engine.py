@@ -52,6 +52,8 @@ register("frmc_engines_add", [_vp, ctypes.POINTER(_Spec), ctypes.POINTER(_i32)])
 register("frmc_engines_remove", [_vp, _i32])
 register("frmc_engines_live", [_vp, I32P, _i32, ctypes.POINTER(_i32)])
 register("frmc_engines_step_host", [_vp, I32P, F32P, F32P, F64P, I32P])
+register("frmc_engines_step_host_submit", [_vp, I32P, F32P, F32P, ctypes.c_int32])
+register("frmc_engines_step_host_collect", [_vp, ctypes.c_int32, F64P, I32P])
 register("frmc_engines_destroy", [_vp])
 register("frmc_engines_set_tune", [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int])
 register("frmc_engines_get_tune", [_vp] + [ctypes.POINTER(ctypes.c_int)] * 4)
@@ -466,6 +468,25 @@ class EngineSet:
         check(load().frmc_engines_step_host(self.handle, atoms.ctypes.data_as(I32P), vecs.ctypes.data_as(F32P),
                                             u.ctypes.data_as(F32P), c2.ctypes.data_as(F64P),
                                             acc.ctypes.data_as(I32P)))
+        return c2, acc
+
+    def step_host_submit(self, atoms, vecs, u, slot):
+        """Submit one batched step from host arrays into staging slot 0 or 1
+        (step_host in two halves: a host may submit step k + 1 before it
+        collects step k)."""
+        atoms = np.ascontiguousarray(atoms, np.int32)
+        vecs = np.ascontiguousarray(vecs, F32)
+        u = np.ascontiguousarray(u, F32)
+        check(load().frmc_engines_step_host_submit(self.handle, atoms.ctypes.data_as(I32P),
+                                                   vecs.ctypes.data_as(F32P), u.ctypes.data_as(F32P), int(slot)))
+
+    def step_host_collect(self, slot):
+        """Wait for the step in `slot`; returns (chi2_new, accepted) in live-id order."""
+        E = len(self.systems)
+        c2 = np.empty(E, np.float64)
+        acc = np.empty(E, np.int32)
+        check(load().frmc_engines_step_host_collect(self.handle, int(slot), c2.ctypes.data_as(F64P),
+                                                    acc.ctypes.data_as(I32P)))
         return c2, acc
 
     # ------------------------------------------------------------ control

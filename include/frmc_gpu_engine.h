@@ -146,6 +146,15 @@ int frmc_engines_step(void *handle, int32_t engine, int32_t steps, int use_graph
  * accepted may be NULL).  Synchronous. */
 int frmc_engines_step_host(void *handle, const int32_t *atoms, const float *vecs, const float *u, double *chi2_new,
                            int32_t *accepted);
+/* The same in two halves, so that a host can submit step k + 1 before it
+ * reads step k: submit writes the moves into staging slot `slot` (0 or 1)
+ * and enqueues the copy in, the step and the copy of the results out;
+ * collect waits for that slot's step and returns its results.  A slot takes
+ * one step at a time, steps run in submission order, and the engine set must
+ * not change while a step is in flight. */
+int frmc_engines_step_host_submit(void *handle, const int32_t *atoms, const float *vecs, const float *u,
+                                  int32_t slot);
+int frmc_engines_step_host_collect(void *handle, int32_t slot, double *chi2_new, int32_t *accepted);
 int frmc_engines_sync(void *handle);
 int frmc_engines_state(void *handle, int32_t e, double *chi2, int64_t *step, int64_t *accepted);
 /* Per-step results of steps [first_step, first_step + count). */

@@ -143,6 +143,39 @@ def test_step_host_matches_ring_steps():
     es.close()
 
 
+def test_step_host_two_slots_match_ring_steps():
+    """Submitting step k + 1 before collecting step k (two staging slots)
+    gives the same chains as pushed moves; misuse of a slot is refused."""
+    from fullrmc_gb300._native import NativeError
+    from fullrmc_gb300.engine import EngineSet
+    systems = _systems(count=5, seed=14)
+    steps = 41
+    mv = _moves(systems, steps, seed=9)
+    ring = _run(systems, mv, steps, "batched")
+    es = EngineSet(systems, move_cap=4)
+    es.init()
+    A = np.ascontiguousarray(np.stack([m[0] for m in mv]).T)
+    V = np.ascontiguousarray(np.stack([m[1] for m in mv]).transpose(1, 0, 2))
+    U = np.ascontiguousarray(np.stack([m[2] for m in mv]).T)
+    out = {}
+    es.step_host_submit(A[0], V[0], U[0], 0)
+    with pytest.raises(NativeError):
+        es.step_host_submit(A[1], V[1], U[1], 0)  # slot 0 not collected yet
+    for k in range(1, steps):
+        es.step_host_submit(A[k], V[k], U[k], k % 2)
+        out[k - 1] = es.step_host_collect((k - 1) % 2)
+    out[steps - 1] = es.step_host_collect((steps - 1) % 2)
+    with pytest.raises(NativeError):
+        es.step_host_collect(0)  # nothing in flight
+    for k in range(steps):
+        c2, acc = out[k]
+        for e in range(len(systems)):
+            assert c2[e] == ring[e]["chi2"][k] and acc[e] == ring[e]["acc"][k]
+    for e in range(len(systems)):
+        assert es.state(e) == ring[e]["state"]
+    es.close()
+
+
 def test_add_remove_keeps_other_chains_exact():
     """Engines added and removed between steps (the serving pattern) do not
     change the results of the others."""
