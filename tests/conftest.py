@@ -26,7 +26,7 @@ def golden_names(prefix=""):
 
 
 HIST_CASES = ["cubic_pbc_ne2", "triclinic120_ne3", "general_triclinic_ne4_mol", "ibc_ne2", "bin_overflow_ibc",
-              "bin_edges_ibc", "half_box_pbc"]
+              "bin_edges_ibc", "half_box_pbc", "niti_pdb"]
 DIST_CASES = ["dist_cubic_pbc_ne2", "dist_general_triclinic_ne4_mol", "dist_ibc_ne2"]
 
 

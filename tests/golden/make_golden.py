@@ -160,6 +160,37 @@ def main():
               (np.arange(n) % 2).astype(np.int32), 2, grid(6.0),
               [(np.array([0, 1, 5], np.int32), True), (np.array([1, 2, 3], np.int32), False)])
 
+    # G2: real data -- the reference's own NiTi example (6,750 atoms, cubic
+    # 45.75 A, Examples/atomicNiTi/system.pdb) on the r grid of its
+    # experimental.gr, box coordinates through the reference's
+    # transform_coordinates as fullrmc's Engine makes them.
+    niti = os.path.join(build_ref.REFERENCE_ROOT, "Examples", "atomicNiTi")
+    if os.path.exists(os.path.join(niti, "system.pdb")):
+        real, names, L = [], [], None
+        with open(os.path.join(niti, "system.pdb")) as fh:
+            for line in fh:
+                if line.startswith("CRYST1"):
+                    L = float(line[6:15])
+                elif line.startswith(("ATOM", "HETATM")):
+                    real.append((float(line[30:38]), float(line[38:46]), float(line[46:54])))
+                    names.append(line[76:78].strip().lower())
+        real = np.array(real, F)
+        kinds = sorted(set(names))
+        el = np.array([kinds.index(x) for x in names], np.int32)
+        B = np.diag([L, L, L]).astype(F)
+        box = bcc.transform_coordinates(np.linalg.inv(B.astype(np.float64)).astype(F), real)
+        x = np.loadtxt(os.path.join(niti, "experimental.gr"))[:, 0].astype(F)
+        b = F(x[1] - x[0])
+        lims = (F(x[0] - b / F(2)), F(x[-1] + b / F(2)), b, np.int32(len(x)))
+        n = real.shape[0]
+        hist_case("niti_pdb", box, B, True, np.arange(n, dtype=np.int32), el, len(kinds), lims,
+                  [(np.array([0, 3374, 3375, 6749], np.int32), True),
+                   (np.arange(0, n, 519, dtype=np.int32), False)])
+        out["niti_pdb"]["real"] = real
+        out["niti_pdb"]["rbasis"] = np.linalg.inv(B.astype(np.float64)).astype(F)
+        out["niti_pdb"]["G_exp"] = np.loadtxt(os.path.join(niti, "experimental.gr"))[:, 1].astype(F)
+        out["niti_pdb"]["r"] = x
+
     # H: edge sizes: one atom, zero atoms.
     for nn in (0, 1):
         coords = np.zeros((nn, 3), F)

@@ -221,3 +221,39 @@ def test_fused_and_split_batched_paths_agree():
                          counts=es.counts(e), coords=es.coords(e)) for e in range(len(systems))])
         es.close()
     _same(out[0], out[1])
+
+
+def test_real_data_chain_replays_on_oracle(oracle_mod):
+    """fullrmc's own NiTi example (6,750 atoms, its experimental G(r) as the
+    target): a device chain of single-atom moves replays on the oracle with
+    every chi2 within 1e-10 and identical final counts and coordinates."""
+    from conftest import golden
+    from fullrmc_gb300.engine import EngineSystem, PDFModel, normalized_weighting
+    from fullrmc_gb300.hostloop import HostPDFChain
+    g = golden("niti_pdb")
+    el = g["el"]
+    counts = np.bincount(el, minlength=int(g["ne"]))
+    L = float(g["basis"][0, 0])
+    model = PDFModel(r=g["r"], G_exp=g["G_exp"].astype(np.float64), elements_count=counts,
+                     weights=normalized_weighting(counts, [10.3, -3.44]), volume=L ** 3)
+    s = EngineSystem(box_coords=g["coords"], real_coords=g["real"], el=el, mol=g["mol"], basis=g["basis"],
+                     rbasis=g["rbasis"], isPBC=True, model=model)
+    steps = 120
+    mv = _moves([s], steps, seed=21, amp=0.1)
+    res = _run([s], mv, steps, "batched")[0]
+    chain = HostPDFChain(s, oracle_mod, oracle_mod)
+    chain.compute_data()
+    assert np.array_equal(chain.data[1], g["full_inter"])
+    chi2 = res["chi2_0"]
+    assert abs(chi2 - model.chi2_fp64(*chain.data)) <= 1e-10 * abs(chi2)
+    a, v, u = mv[0]
+    for k in range(steps):
+        acc = bool(res["acc"][k])
+        chain.step(a[k], v[k][None, :], u[k], force=acc)
+        c_new = model.chi2_fp64(chain.last[0], chain.last[1])
+        assert abs(c_new - res["chi2"][k]) <= 1e-10 * abs(c_new), k
+        if acc:
+            chi2 = res["chi2"][k]
+    assert np.array_equal(res["counts"][1].astype(np.float32), chain.data[1])
+    assert np.array_equal(res["coords"][0], chain.box)
+    assert 0 < int(res["acc"].sum()) < steps
