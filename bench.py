@@ -260,7 +260,14 @@ def bench_configs(torch, with_cpu):
     t0 = time.perf_counter()
     for _ in range(5):
         reciprocal_space.Gr_to_sq(s.model.r, G, q)
-    out["triclinic_100k"]["sq_transform_ms"] = 1e3 * (time.perf_counter() - t0) / 5
+    t = (time.perf_counter() - t0) / 5
+    terms = float(q.size) * float(np.asarray(s.model.r).size)
+    d = out["triclinic_100k"]
+    d["sq_transform_ms"] = 1e3 * t
+    d["sq_transform_terms"] = int(terms)
+    # per term w * sin(q r) accumulated: the product q r and one FMA (3 FP64
+    # flops, the sine's own arithmetic not counted); host copies included
+    d["sq_transform_fp64_gflops"] = 3.0 * terms / t * 1e-9
     return out
 
 

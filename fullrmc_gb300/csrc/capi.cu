@@ -22,7 +22,7 @@ int launch_from_to(const float *from, const float *to, int n, int isPBC, const f
                    cudaStream_t st);
 int launch_transform(const float *M, const float *coords, int n, float *out, cudaStream_t st);
 int launch_sine(int kind, const float *xs, int nx, const float *ys, const float *f, int ny, double rho, double *out,
-                cudaStream_t st);
+                double *scratch, cudaStream_t st);
 
 static FullTune g_full_tune;
 static std::mutex g_tune_mu;
@@ -598,7 +598,9 @@ static int sine_common(int kind, const float *xs, int64_t nx, const float *ys, c
     TRY(h2d(dxs, xs, nx * 4, c->stream));
     TRY(h2d(dys, ys, ny * 4, c->stream));
     TRY(h2d(df, f, ny * 4, c->stream));
-    TRY(launch_sine(kind, dxs, (int)nx, dys, df, (int)ny, rho, c->buf[BUF_OUT].as<double>(), c->stream));
+    TRY(c->buf[BUF_AUX2].ensure(8 * (size_t)(nx + 2 * ny) + 16));
+    TRY(launch_sine(kind, dxs, (int)nx, dys, df, (int)ny, rho, c->buf[BUF_OUT].as<double>(),
+                    c->buf[BUF_AUX2].as<double>(), c->stream));
     TRY(d2h(out, c->buf[BUF_OUT].p, nx * 8, c->stream));
     return finish(c);
 }

@@ -10,8 +10,8 @@
 //
 // The float32 inputs are promoted exactly, so every sine argument q*r is the
 // exact double product; only the summation order differs from a float64
-// numpy evaluation.  One thread per output point; the summation grid is
-// staged through shared memory in chunks.
+// numpy evaluation.  One CTA per output point (k_sine_rows), so a grid of a
+// few thousand points fills every SM.
 #include <cmath>
 
 #include "frmc_runtime.h"
@@ -19,58 +19,6 @@
 namespace frmc {
 
 enum SineKind : int { SK_GR_TO_SQ = 0, SK_BIGGR_TO_SQ = 1, SK_SQ_TO_GR = 2 };
-
-constexpr int kSineChunk = 256;
-
-__global__ void __launch_bounds__(256) k_sine(int kind, const float *__restrict__ xs, int nx,
-                                              const float *__restrict__ ys, const float *__restrict__ f, int ny,
-                                              double rho, double *__restrict__ out)
-{
-    __shared__ double sy[kSineChunk], sw[kSineChunk];
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    const double x = m < nx ? (double)xs[m] : 0.0;
-    const double dy = (double)ys[1] - (double)ys[0];
-    double acc = 0.0;
-    for (int l0 = 0; l0 < ny; l0 += kSineChunk) {
-        __syncthreads();
-        for (int l = threadIdx.x; l < kSineChunk && l0 + l < ny; l += blockDim.x) {
-            const double y = (double)ys[l0 + l];
-            const double v = (double)f[l0 + l];
-            double w;
-            if (kind == SK_GR_TO_SQ)
-                w = dy * y * (v - 1.0);
-            else if (kind == SK_BIGGR_TO_SQ)
-                w = dy * v;
-            else
-                w = dy * y * (v - 1.0);
-            sy[l] = y;
-            sw[l] = w;
-        }
-        __syncthreads();
-        const int lc = min(kSineChunk, ny - l0);
-        for (int l = 0; l < lc; ++l) acc = fma(sw[l], sin(x * sy[l]), acc);
-    }
-    if (m >= nx)
-        return;
-    if (kind == SK_GR_TO_SQ)
-        out[m] = 1.0 + (4.0 * M_PI * rho) * (acc / x);
-    else if (kind == SK_BIGGR_TO_SQ)
-        out[m] = 1.0 + acc / x;
-    else
-        out[m] = (2.0 / M_PI) * acc;
-}
-
-int launch_sine(int kind, const float *xs, int nx, const float *ys, const float *f, int ny, double rho, double *out,
-                cudaStream_t st)
-{
-    if (nx <= 0)
-        return FRMC_OK;
-    if (ny < 2)
-        return set_error(FRMC_E_ARG, "sine transform needs at least two grid points");
-    k_sine<<<(nx + 255) / 256, 256, 0, st>>>(kind, xs, nx, ys, f, ny, rho, out);
-    FRMC_CUDA(cudaGetLastError());
-    return FRMC_OK;
-}
 
 // ----------------------------------------------------------------- shape function
 // fullrmc's ShapeFunction (Constraints/Collection.py:15-160) on the device in
@@ -141,6 +89,43 @@ __global__ void __launch_bounds__(kSineRowThreads) k_sine_rows(const double *__r
         const double s = (part[0] + part[1]) + (part[2] + part[3]);
         out[m] = add + mul * (div ? s / xm : s);
     }
+}
+
+// The sine transforms with one CTA per output point (k_sine_rows): the
+// float32 grids are promoted exactly and the summand weights formed first.
+__global__ void k_sine_prep(int kind, const float *__restrict__ xs, int nx, const float *__restrict__ ys,
+                            const float *__restrict__ f, int ny, double *__restrict__ xd, double *__restrict__ yd,
+                            double *__restrict__ w)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nx)
+        xd[i] = (double)xs[i];
+    if (i < ny) {
+        const double dy = (double)ys[1] - (double)ys[0];
+        const double y = (double)ys[i], v = (double)f[i];
+        yd[i] = y;
+        w[i] = kind == SK_BIGGR_TO_SQ ? dy * v : dy * y * (v - 1.0);
+    }
+}
+
+int launch_sine(int kind, const float *xs, int nx, const float *ys, const float *f, int ny, double rho, double *out,
+                double *scratch, cudaStream_t st)
+{
+    if (nx <= 0)
+        return FRMC_OK;
+    if (ny < 2)
+        return set_error(FRMC_E_ARG, "sine transform needs at least two grid points");
+    double *xd = scratch, *yd = xd + nx, *w = yd + ny;
+    const int n = nx > ny ? nx : ny;
+    k_sine_prep<<<(n + 255) / 256, 256, 0, st>>>(kind, xs, nx, ys, f, ny, xd, yd, w);
+    if (kind == SK_GR_TO_SQ)
+        k_sine_rows<<<nx, kSineRowThreads, 0, st>>>(xd, yd, w, ny, 1.0, 4.0 * M_PI * rho, 1, out);
+    else if (kind == SK_BIGGR_TO_SQ)
+        k_sine_rows<<<nx, kSineRowThreads, 0, st>>>(xd, yd, w, ny, 1.0, 1.0, 1, out);
+    else
+        k_sine_rows<<<nx, kSineRowThreads, 0, st>>>(xd, yd, w, ny, 0.0, 2.0 / M_PI, 0, out);
+    FRMC_CUDA(cudaGetLastError());
+    return FRMC_OK;
 }
 
 int launch_shape_function(const unsigned *counts, int ne, int hs, int npairs, const int *pi, const int *pj,
