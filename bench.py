@@ -125,6 +125,26 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def _host_cpu():
+    """The host CPU as /proc/cpuinfo names it (x86 "model name"; Arm
+    implementer/part codes), with the logical core count."""
+    name = None
+    try:
+        with open("/proc/cpuinfo") as f:
+            info = f.read()
+        for key in ("model name", "Model", "CPU part"):
+            for line in info.splitlines():
+                if line.split(":")[0].strip() == key:
+                    name = "%s %s" % ("CPU part" if key == "CPU part" else "", line.split(":", 1)[1].strip())
+                    break
+            if name:
+                break
+    except OSError:
+        pass
+    import platform
+    return "%s (%s), %d logical cores" % ((name or "unknown").strip(), platform.machine(), os.cpu_count() or 1)
+
+
 def _dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -410,7 +430,7 @@ def run_reference(args):
             "impl": "reference",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": kind,
                              "sample": "fullrmc Cython (ncores=1) in %d processes, %d engines, %d timed steps"
-                                       % (procs, sample, args.steps)},
+                                       % (procs, sample, args.steps), "host": _host_cpu()},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -508,6 +528,9 @@ def run_ours(args):
         for _ in range(W):
             es.step(1, graph=False, sync=False, stream=sp)
         torch.cuda.synchronize()
+        # columns the one-CTA steps sweep: all atoms of an engine without a
+        # column grid, the selected cells' atoms with one
+        swept0 = sum(es.swept(e) for e in range(E))
         if ws > 1:
             torch.distributed.barrier()
         clocks = ClockSampler(dev.index)
@@ -524,6 +547,7 @@ def run_ours(args):
         torch.cuda.nvtx.range_pop()
         torch.cuda.synchronize()
         step_ms = [a.elapsed_time(b) for a, b in ev]
+        swept_per_step = (sum(es.swept(e) for e in range(E)) - swept0) / K
         # steady state: K steps back to back in one CUDA graph (state stays in L2)
         g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         es.step(K, graph=True, sync=False, stream=sp)  # capture + warm
@@ -558,6 +582,7 @@ def run_ours(args):
         p1.record(st)
         torch.cuda.synchronize()
     plain_rate = len(sample) * (plain_steps - 1) / (p0.elapsed_time(p1) * 1e-3)
+    grid_engines = sum(1 for e in range(E) if es.cells(e) > 0)
     es.close()
 
     # e2e: public API with host buffers; every step uploads all engines' moves
@@ -618,7 +643,8 @@ def run_ours(args):
             build_ref.import_reference()
             rate, procs = reference_rate(4, 6, 2, 1, seed=seed, amp=amp)
             cpu = {"value": rate, "unit": UNIT, "cores": 1, "kind": "reference",
-                   "sample": "fullrmc Cython (ncores=1): 4 engines of this workload x 6 timed steps, 1 core"}
+                   "sample": "fullrmc Cython (ncores=1): 4 engines of this workload x 6 timed steps, 1 core",
+                   "host": _host_cpu()}
         except Exception as exc:
             cpu = {"value": None, "unit": UNIT, "cores": 1, "kind": "reference", "sample": "failed: %s" % exc}
 
@@ -642,8 +668,14 @@ def run_ours(args):
             "roofline": {"bound": "issue", "achieved": step_pairs_rate / 1e9, "peak": issue_peak / 1e9,
                          "unit": "Gpair/s", "frac": step_pairs_rate / issue_peak, "traffic": traffic,
                          "kernel": "k_engine_step", "pairs_per_launch": pairs_per_step,
+                         "pairs_evaluated_per_launch": 2.0 * swept_per_step,
+                         "evaluated_frac": 2.0 * swept_per_step / (ms_per_step * 1e-3) / issue_peak,
+                         "column_grid_engines": grid_engines,
                          "peak_basis": "%d SMs x %.0f MHz (%s) x 128 lanes / %d ops per pair"
-                                       % (sms, fmax / 1e6, peaks_kind, OPS_PER_PAIR)},
+                                       % (sms, fmax / 1e6, peaks_kind, OPS_PER_PAIR),
+                         "note": "achieved counts the reference's pair evaluations (2 (n - 1) per engine and "
+                                 "step); engines with a column grid evaluate only the columns of the cells a "
+                                 "moved atom may reach (pairs_evaluated_per_launch)"},
             "allpairs": dict(allp, roofline_frac=allp["pair_distances_per_s"] / issue_peak,
                              issue_peak_pairs_per_s=issue_peak),
             "serving": serving,

@@ -55,6 +55,7 @@ struct EState {
     double dsd;         // change of sd proposed this step (engines with S(Q))
     long long step;
     long long accepted;
+    unsigned long long swept;  // columns swept by one-CTA steps (all atoms, or the selected cells')
     unsigned done;      // items of the current step finished
     unsigned tcount;    // entries in the touched-bin list of the current step
     unsigned sq_done;   // reserved (zero)
@@ -82,6 +83,7 @@ struct EMove {
 // group's centroid (float32, atoms added in group order, divided by the
 // group size), with row-vector products summed as (x0 r0k + x1 r1k) + x2 r2k.
 constexpr int kMaxGroup = 16;
+constexpr int kMaxCells = 512;  // cells of an engine's column grid
 struct EGroup {
     int kind;       // 0: translation by the move's v, 1: rotation
     float rot[9];   // row-major 3 x 3
@@ -97,6 +99,8 @@ struct MovedGroup {
     float o[kMaxGroup][3];   // box coordinates before the move
     float nw[kMaxGroup][3];  // box coordinates after
     float nr[kMaxGroup][3];  // real coordinates after
+    int slot[kMaxGroup];     // cell-sorted position and cell of each moved atom (engines with a grid)
+    int cell[kMaxGroup];
     float u;                 // the move's uniform number
     long long step;          // the engine's step, accepted count, sd and chi2 before this step
     long long accepted;
@@ -156,6 +160,21 @@ struct EDesc {
     int xld, yld, hsp;
     int sq_gemm_max;    // largest |delta| taken through the GEMM (kSqGemmMaxDelta; lower values,
                         // down to 0 = never and -1 = the dense integer loop, exist for tests)
+    // Column grid (nc > 0): the atoms sorted by cell, so that a step sweeps
+    // only the cells whose bounding box may come within maxD of a moved atom.
+    // cbox / cmol mirror box / mol in cell order, csl[i] = (position, cell)
+    // of atom i, cstart[c] the first position of cell c; clo / chi bound the
+    // box coordinates of each cell's atoms and only grow (an accepted move
+    // widens its atom's cell).  The lower bound of the minimum-image distance
+    // from per-axis gaps m (fractional, or real for free boundaries) is
+    // sum_k (m_k cw_k)^2 (cmode 0: orthorhombic box, free boundaries) or
+    // max(max_k (m_k cw_k)^2, clam2 |m|^2) (cmode 1: cw_k the cell's
+    // perpendicular widths, clam2 the smallest eigenvalue of B B^T).
+    int nc, cmode, cpbc;
+    float cw[3], clam2, cthr2;
+    float4 *cbox, *clo, *chi;
+    int *cmol, *cstart;
+    int2 *csl;
     EMove *moves;
     EGroup *groups;     // [move_cap] (group > 1)
     int group;          // atoms per move
@@ -250,6 +269,11 @@ __device__ void load_moved_group(const EDesc &D, long long step, MovedGroup &g)
             g.o[0][0] = ob.x; g.o[0][1] = ob.y; g.o[0][2] = ob.z;
             g.nw[0][0] = nw.x; g.nw[0][1] = nw.y; g.nw[0][2] = nw.z;
             g.nr[0][0] = rx; g.nr[0][1] = ry; g.nr[0][2] = rz;
+            if (D.nc > 0) {
+                const int2 sl = D.csl[a];
+                g.slot[0] = sl.x;
+                g.cell[0] = sl.y;
+            }
         }
         return;
     }
@@ -264,6 +288,11 @@ __device__ void load_moved_group(const EDesc &D, long long step, MovedGroup &g)
         g.mol[t] = D.mol[a];
         g.o[t][0] = ob.x; g.o[t][1] = ob.y; g.o[t][2] = ob.z;
         g.nr[t][0] = orl.x; g.nr[t][1] = orl.y; g.nr[t][2] = orl.z;
+        if (D.nc > 0) {
+            const int2 sl = D.csl[a];
+            g.slot[t] = sl.x;
+            g.cell[t] = sl.y;
+        }
     }
     if (t == 0)
         g.n = G;
@@ -303,13 +332,32 @@ __device__ void load_moved_group(const EDesc &D, long long step, MovedGroup &g)
     }
 }
 
-// Commit of an accepted move: the moved atoms' coordinates.
+// Commit of an accepted move: the moved atoms' coordinates, their copies in
+// cell order and their cells' bounds (one thread, as atoms of a group may
+// share a cell).
 __device__ void commit_moved_group(const EDesc &D, const MovedGroup &g)
 {
     for (int t = threadIdx.x; t < g.n; t += blockDim.x) {
         const int a = g.atom[t];
-        D.box[a] = make_float4(g.nw[t][0], g.nw[t][1], g.nw[t][2], __int_as_float(g.el[t]));
+        const float4 nb = make_float4(g.nw[t][0], g.nw[t][1], g.nw[t][2], __int_as_float(g.el[t]));
+        D.box[a] = nb;
         D.real[a] = make_float4(g.nr[t][0], g.nr[t][1], g.nr[t][2], 0.0f);
+        if (D.nc > 0)
+            D.cbox[g.slot[t]] = nb;
+    }
+    if (D.nc > 0 && threadIdx.x == 0) {
+        for (int t = 0; t < g.n; ++t) {
+            const int c = g.cell[t];
+            float4 lo = D.clo[c], hi = D.chi[c];
+            lo.x = fminf(lo.x, g.nw[t][0]);
+            lo.y = fminf(lo.y, g.nw[t][1]);
+            lo.z = fminf(lo.z, g.nw[t][2]);
+            hi.x = fmaxf(hi.x, g.nw[t][0]);
+            hi.y = fmaxf(hi.y, g.nw[t][1]);
+            hi.z = fmaxf(hi.z, g.nw[t][2]);
+            D.clo[c] = lo;
+            D.chi[c] = hi;
+        }
     }
 }
 
@@ -969,43 +1017,161 @@ __device__ __forceinline__ void flush_columns(const ColView &D, const MovedGroup
     }
 }
 
+// Gap m >= 0 between the ranges [a, b] of coordinate differences and the
+// nearest difference the distance can reach: the nearest integer with
+// periodic boundaries (the minimum image subtracts round(diff)), zero with
+// free boundaries.
+__device__ __forceinline__ float cell_gap(float a, float b, int pbc)
+{
+    if (!pbc)
+        return a > 0.f ? a : (b < 0.f ? -b : 0.f);
+    const float n = floorf(b);
+    return n >= a ? 0.f : fminf(a - n, n + 1.f - b);
+}
+
+// The cells of the column grid that a moved atom may reach: for each cell,
+// a lower bound of the distance from the bounding box of the moved atoms'
+// positions (before and after the move) to the cell's box; a cell whose
+// bound is not below maxD + margin holds only columns out of range before
+// and after the move, which change no bin.  lo, hi, st0, st1: cell
+// threadIdx.x's bounds and start positions, loaded by the caller ahead of
+// the barrier.  Writes P[c], the exclusive prefix of the selected cells'
+// atom counts (P[nc] = the total), and Bse[c] = cstart[c] - P[c] (wsum: 32
+// ints of scratch); returns the number of columns to sweep.  Column v of the sweep is atom
+// Bse[c] + v of the cell order, c the last cell with P[c] <= v.
+__device__ int cell_select(const EDesc &D, const MovedGroup &g, float4 lo, float4 hi, int st0, int st1, int *P,
+                           int *Bse, int *wsum)
+{
+    float plo[3], phi[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        plo[k] = fminf(g.o[0][k], g.nw[0][k]);
+        phi[k] = fmaxf(g.o[0][k], g.nw[0][k]);
+    }
+    for (int t = 1; t < g.n; ++t)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            plo[k] = fminf(plo[k], fminf(g.o[t][k], g.nw[t][k]));
+            phi[k] = fmaxf(phi[k], fmaxf(g.o[t][k], g.nw[t][k]));
+        }
+    const int nc = D.nc;
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int carry = 0;
+    for (int c0 = 0; c0 < nc; c0 += blockDim.x) {
+        const int c = c0 + (int)threadIdx.x;
+        if (c0 > 0 && c < nc) {
+            lo = D.clo[c];
+            hi = D.chi[c];
+            st0 = D.cstart[c];
+            st1 = D.cstart[c + 1];
+        }
+        int take = 0;
+        if (c < nc && st1 > st0) {
+            const float f0 = cell_gap(plo[0] - hi.x, phi[0] - lo.x, D.cpbc);
+            const float f1 = cell_gap(plo[1] - hi.y, phi[1] - lo.y, D.cpbc);
+            const float f2 = cell_gap(plo[2] - hi.z, phi[2] - lo.z, D.cpbc);
+            const float m0 = f0 * D.cw[0], m1 = f1 * D.cw[1], m2 = f2 * D.cw[2];
+            float lb2 = m0 * m0 + m1 * m1 + m2 * m2;
+            if (D.cmode != 0)
+                lb2 = fmaxf(fmaxf(m0 * m0, m1 * m1), fmaxf(m2 * m2, D.clam2 * (f0 * f0 + f1 * f1 + f2 * f2)));
+            take = lb2 < D.cthr2 ? st1 - st0 : 0;
+        }
+        // exclusive scan of the selected counts: warps by shuffles, then
+        // every thread adds the totals of the warps before its own
+        int inc = take;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, inc, o);
+            if ((int)lane >= o)
+                inc += v;
+        }
+        if (lane == 31)
+            wsum[warp] = inc;
+        __syncthreads();
+        int before = carry, total = 0;
+        for (unsigned w = 0; w < nw; ++w) {
+            const int x = wsum[w];
+            before += w < warp ? x : 0;
+            total += x;
+        }
+        if (c < nc) {
+            const int ex = before + inc - take;
+            P[c] = ex;
+            Bse[c] = st0 - ex;
+        }
+        carry += total;
+        if (threadIdx.x == 0 && c0 + (int)blockDim.x >= nc)
+            P[nc] = carry;
+        __syncthreads();
+    }
+    return carry;
+}
+
+// Position in cell order of sweep column v (P[lo] <= v < P[lo + 1]).
+__device__ __forceinline__ int cell_column(const int *P, const int *Bse, int nc, int v)
+{
+    int lo = 0, hi = nc;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (P[mid] <= v)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return Bse[lo] + v;
+}
+
 // The fused path's columns: every column j (not a moved atom) against every
 // moved atom before and after the move.  Squared distances and the window
 // test are branch-free for a batch of columns; accepted columns go to the
 // thread's queue, flushed when a queue is full and at the end.
-template <int BM, bool GROUP>
+//
+// With a column grid (CELL) the sweep runs over the ncol columns of the
+// selected cells in cell order (cell_select, cell_column): the copies cbox /
+// cmol, and the moved atoms recognised by their cell-order positions.
+template <int BM, bool GROUP, bool CELL>
 __device__ void fused_columns(const EDesc &Dg, int *sdP, int *nz, unsigned *s_tcount, const MovedGroup &g,
-                              const ColQueue &q)
+                              const ColQueue &q, int ncol, const int *cP, const int *cB)
 {
-    const ColView D = col_view(Dg);
+    ColView D = col_view(Dg);
+    if (CELL) {
+        D.box = Dg.cbox;
+        D.mol = Dg.cmol;
+    }
+    const int nc = Dg.nc;
     const int step = kItemUnroll * blockDim.x;
     const int G = GROUP ? g.n : 1;
-    const int atom0 = g.atom[0];
+    const int self0 = CELL ? g.slot[0] : g.atom[0];
     int qn = 0;
     float4 c[kItemUnroll];
     int mj[kItemUnroll];
+    int jc[kItemUnroll];  // the columns' indexes (cell order with a grid)
 #pragma unroll
     for (int u = 0; u < kItemUnroll; ++u) {
-        const int j = u * blockDim.x + threadIdx.x;
-        c[u] = j < D.n ? D.box[j] : make_float4(0.f, 0.f, 0.f, 0.f);
-        mj[u] = j < D.n ? D.mol[j] : 0;
+        const int v = u * blockDim.x + threadIdx.x;
+        const int j = v < ncol ? (CELL ? cell_column(cP, cB, nc, v) : v) : -1;
+        jc[u] = j;
+        c[u] = j >= 0 ? D.box[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        mj[u] = j >= 0 ? D.mol[j] : 0;
     }
-    for (int jb = 0; jb < D.n; jb += step) {
+    for (int jb = 0; jb < ncol; jb += step) {
         float4 cn[kItemUnroll];
-        int mn[kItemUnroll];
+        int mn[kItemUnroll], jn[kItemUnroll];
 #pragma unroll
         for (int u = 0; u < kItemUnroll; ++u) {
-            const int j = jb + step + u * blockDim.x + threadIdx.x;
-            cn[u] = j < D.n ? D.box[j] : make_float4(0.f, 0.f, 0.f, 0.f);
-            mn[u] = j < D.n ? D.mol[j] : 0;
+            const int v = jb + step + u * blockDim.x + threadIdx.x;
+            const int j = v < ncol ? (CELL ? cell_column(cP, cB, nc, v) : v) : -1;
+            jn[u] = j;
+            cn[u] = j >= 0 ? D.box[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+            mn[u] = j >= 0 ? D.mol[j] : 0;
         }
         bool valid[kItemUnroll];
 #pragma unroll
         for (int u = 0; u < kItemUnroll; ++u) {
-            const int j = jb + u * blockDim.x + threadIdx.x;
-            bool ok = j < D.n && j != atom0;
+            const int j = jc[u];
+            bool ok = j >= 0 && j != self0;
             if (GROUP)
-                for (int t = 1; t < G; ++t) ok &= j != g.atom[t];
+                for (int t = 1; t < G; ++t) ok &= j != (CELL ? g.slot[t] : g.atom[t]);
             valid[u] = ok;
         }
         for (int gi = 0; gi < G; ++gi) {
@@ -1032,6 +1198,7 @@ __device__ void fused_columns(const EDesc &Dg, int *sdP, int *nz, unsigned *s_tc
         for (int u = 0; u < kItemUnroll; ++u) {
             c[u] = cn[u];
             mj[u] = mn[u];
+            jc[u] = jn[u];
         }
     }
     flush_columns(D, g, sdP, nz, s_tcount, q, qn);
@@ -1043,6 +1210,9 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, 
                              uint32_t *status, double *red, double *cb, double *sbs, int *sbin, int *s_nchg,
                              double *coef, int *s_flag, unsigned *s_tcount, MovedGroup &g, const ColQueue &q)
 {
+    // the column grid's prefix and bases live in cb until the evaluation
+    static_assert(sizeof(double) * kChunk >= sizeof(int) * (2 * kMaxCells + 33), "cell arrays exceed cb");
+    int *cP = reinterpret_cast<int *>(cb), *cB = cP + kMaxCells + 1;
     if (threadIdx.x == 0) {
         // the previous item's reads of sA / sBq are ordered before this
         // item's bulk copies by the barrier at the item boundary
@@ -1053,6 +1223,16 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, 
         bulk_g2s(sBq, D.Bq, bytes, bar);
         *s_tcount = 0u;
     }
+    // this thread's cell of the column grid, read ahead of the barrier
+    const int nc = D.nc;
+    float4 clo = make_float4(0.f, 0.f, 0.f, 0.f), chi = clo;
+    int cs0 = 0, cs1 = 0;
+    if ((int)threadIdx.x < nc) {
+        clo = D.clo[threadIdx.x];
+        chi = D.chi[threadIdx.x];
+        cs0 = D.cstart[threadIdx.x];
+        cs1 = D.cstart[threadIdx.x + 1];
+    }
     load_moved_group(D, D.st->step, g);
     const int np = D.npairs;
     const int nph = np * D.hs;
@@ -1060,23 +1240,31 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, 
     for (int k = threadIdx.x; k < D.hs; k += blockDim.x) q.nz[k] = 0;
     for (int qq = threadIdx.x; qq < np; qq += blockDim.x) coef[qq] = D.pc[qq];
     __syncthreads();
+    const int ncol = nc > 0 ? cell_select(D, g, clo, chi, cs0, cs1, cP, cB, cB + kMaxCells) : D.n;
+    if (threadIdx.x == 0)
+        atomicAdd(&D.st->swept, (unsigned long long)ncol);
+#define FRMC_COLUMNS(G_, C_)                                                                           \
+    switch (D.bm) {                                                                                    \
+    case BM_IBC: fused_columns<BM_IBC, G_, C_>(D, sdP, q.nz, s_tcount, g, q, ncol, cP, cB); break;     \
+    case BM_DIAG: fused_columns<BM_DIAG, G_, C_>(D, sdP, q.nz, s_tcount, g, q, ncol, cP, cB); break;   \
+    case BM_XYTRI: fused_columns<BM_XYTRI, G_, C_>(D, sdP, q.nz, s_tcount, g, q, ncol, cP, cB); break; \
+    case BM_LOWER: fused_columns<BM_LOWER, G_, C_>(D, sdP, q.nz, s_tcount, g, q, ncol, cP, cB); break; \
+    default: fused_columns<BM_GENERAL, G_, C_>(D, sdP, q.nz, s_tcount, g, q, ncol, cP, cB); break;     \
+    }
     if (g.n == 1) {
-        switch (D.bm) {
-        case BM_IBC: fused_columns<BM_IBC, false>(D, sdP, q.nz, s_tcount, g, q); break;
-        case BM_DIAG: fused_columns<BM_DIAG, false>(D, sdP, q.nz, s_tcount, g, q); break;
-        case BM_XYTRI: fused_columns<BM_XYTRI, false>(D, sdP, q.nz, s_tcount, g, q); break;
-        case BM_LOWER: fused_columns<BM_LOWER, false>(D, sdP, q.nz, s_tcount, g, q); break;
-        default: fused_columns<BM_GENERAL, false>(D, sdP, q.nz, s_tcount, g, q); break;
+        if (nc > 0) {
+            FRMC_COLUMNS(false, true)
+        } else {
+            FRMC_COLUMNS(false, false)
         }
     } else {
-        switch (D.bm) {
-        case BM_IBC: fused_columns<BM_IBC, true>(D, sdP, q.nz, s_tcount, g, q); break;
-        case BM_DIAG: fused_columns<BM_DIAG, true>(D, sdP, q.nz, s_tcount, g, q); break;
-        case BM_XYTRI: fused_columns<BM_XYTRI, true>(D, sdP, q.nz, s_tcount, g, q); break;
-        case BM_LOWER: fused_columns<BM_LOWER, true>(D, sdP, q.nz, s_tcount, g, q); break;
-        default: fused_columns<BM_GENERAL, true>(D, sdP, q.nz, s_tcount, g, q); break;
+        if (nc > 0) {
+            FRMC_COLUMNS(true, true)
+        } else {
+            FRMC_COLUMNS(true, false)
         }
     }
+#undef FRMC_COLUMNS
     if (g.n > 1) {
         switch (D.bm) {
         case BM_IBC: fused_group_internal<BM_IBC>(D, sdP, q.nz, s_tcount, g); break;
@@ -1663,6 +1851,10 @@ struct Slot {
     bool live = false;
     bool initialized = false;
     int sq_table = -1;  // S(Q) table of the engine (or -1)
+    // cost of a one-CTA step in column units: the columns a step sweeps (all
+    // atoms, or with a column grid the estimate, counted 4 times: a grid
+    // column is gathered and mostly in range), times the atoms a move moves
+    long long cost = 0;
     EDesc d;
     void *blob = nullptr;
     size_t bytes = 0;
@@ -1684,13 +1876,14 @@ struct SqTable {
     int ncols = 0, cap = 0;
 };
 
-constexpr int kFusedSmemMax = 136 * 1024;  // element-pair deltas, A and Bq of a fused step (the column queue comes on top)
-constexpr int kFusedMaxAtoms = 49152;     // larger engines are split over several CTAs
-constexpr int kSoloFusedAtoms = 16384;    // one-engine steps of engines up to this size use the fused item
+constexpr int kFusedSmemMax = 135 * 1024;  // element-pair deltas, A and Bq of a fused step (the column queue comes on top)
+constexpr long long kFusedMaxCost = 49152;  // engines of a higher step cost (Slot::cost) are split over several CTAs
+constexpr long long kSoloFusedCost = 16384;  // one-engine steps up to this cost use the fused item
 
 struct EngineSet {
     std::vector<Slot> slots;
     int fused = 1;         // batched steps use one CTA per engine where it fits
+    int cells = 1;         // engines added from now on get a column grid where it pays
     int fused_smem = 0;    // dynamic shared memory of batched launches
     int fused_dp_ints = 0; // its layout: element-pair deltas (ints), then A and Bq (fused_bins doubles each)
     int fused_bins = 0;
@@ -1740,7 +1933,8 @@ static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct BlobLayout {
     size_t box, real, mol, counts, delta, rfac, invvol, expd, dw, pc, pi, pj, dP, pidx, tlist, R, A, Bq, Sb, moves,
-        results, st, Rq, rfacq, sqexp, h, y, sqpart, sqv, evl, evn, groups, total;
+        results, st, Rq, rfacq, sqexp, h, y, sqpart, sqv, evl, evn, groups, cbox, cmol, csl, cstart, clo, chi,
+        total;
 };
 
 static int spec_group(const frmc_engine_spec &sp) { return sp.group_size > 1 ? sp.group_size : 1; }
@@ -1790,6 +1984,12 @@ static BlobLayout blob_layout(const frmc_engine_spec &sp)
     L.evl = take(sq ? 4 * (size_t)sp.npairs * hs : 0);
     L.evn = take(sq ? 4 * 16 : 0);
     L.groups = take(G > 1 ? sizeof(EGroup) * (size_t)sp.move_cap : 0);
+    L.cbox = take(16 * n);
+    L.cmol = take(4 * n);
+    L.csl = take(8 * n);
+    L.cstart = take(4 * (size_t)(kMaxCells + 1));
+    L.clo = take(16 * (size_t)kMaxCells);
+    L.chi = take(16 * (size_t)kMaxCells);
     L.total = off;
     return L;
 }
@@ -1853,7 +2053,7 @@ static int refresh(EngineSet *s)
         for (int t = 0; t < D.ntiles; ++t) items.push_back(make_int2(id, t));
     }
     s->nsolo = (int)items.size();
-    // batched list: fused engines largest first, then the tiles of the others
+    // batched list: fused engines costliest first, then the tiles of the others
     std::vector<int> fused_ids;
     s->fused_smem = 0;
     s->fused_dp_ints = 0;
@@ -1862,7 +2062,7 @@ static int refresh(EngineSet *s)
         const EDesc &D = s->slots[id].d;
         const int dp = (D.npairs * D.hs + 3) & ~3, bins = (D.hs + 1) & ~1;
         const int dpi = std::max(s->fused_dp_ints, dp), bi = std::max(s->fused_bins, bins);
-        if (s->fused && 4ll * dpi + 20ll * bi <= kFusedSmemMax && D.n <= kFusedMaxAtoms) {
+        if (s->fused && 4ll * dpi + 20ll * bi <= kFusedSmemMax && s->slots[id].cost <= kFusedMaxCost) {
             fused_ids.push_back(id);
             s->fused_dp_ints = dpi;
             s->fused_bins = bi;
@@ -1870,7 +2070,7 @@ static int refresh(EngineSet *s)
         }
     }
     std::stable_sort(fused_ids.begin(), fused_ids.end(),
-                     [s](int a, int b) { return s->slots[a].d.n > s->slots[b].d.n; });
+                     [s](int a, int b) { return s->slots[a].cost > s->slots[b].cost; });
     s->fused_item.assign(nslots, -1);
     for (int id : fused_ids) {
         s->fused_item[id] = (int)items.size();
@@ -2167,6 +2367,187 @@ static int init_engine(EngineSet *s, int id)
     return FRMC_OK;
 }
 
+// Column grid of an engine (the cell fields of EDesc): the atoms sorted by
+// cell of a grid over the range of their box coordinates, with cells of at
+// least maxD / 2 across in real space and at most kMaxCells of them; no grid
+// where a moved atom would reach most cells anyway.  The distance bound's
+// margin (1e-2 A + 1e-4 maxD + a few float32 ulps of the coordinates) is far
+// above the float32 rounding of the reference's distance.
+struct CellGrid {
+    int nc = 0, cmode = 0, cpbc = 0;
+    double sweep = 0.0;  // estimated columns a step sweeps (the mean over sample atoms)
+    float cw[3] = {1.f, 1.f, 1.f}, clam2 = 0.f, cthr2 = 0.f;
+    std::vector<float4> cbox, clo, chi;
+    std::vector<int> cmol, cstart;
+    std::vector<int2> csl;
+};
+
+static void build_cells(const frmc_engine_spec &sp, int bm, CellGrid &G)
+{
+    const int n = sp.n;
+    const bool pbc = bm != BM_IBC;
+    double w[3] = {1.0, 1.0, 1.0}, lam = 0.0;
+    int mode = 0;
+    if (pbc) {
+        double B[9];
+        for (int k = 0; k < 9; ++k) B[k] = sp.basis[k];
+        if (bm == BM_DIAG) {
+            for (int k = 0; k < 3; ++k) w[k] = std::fabs(B[4 * k]);
+        } else {
+            mode = 1;
+            // columns of B^-1 (box = real B^-1): |real| >= |box_k| / |column k|
+            const double c00 = B[4] * B[8] - B[5] * B[7], c01 = B[5] * B[6] - B[3] * B[8],
+                         c02 = B[3] * B[7] - B[4] * B[6];
+            const double det = B[0] * c00 + B[1] * c01 + B[2] * c02;
+            if (!(std::fabs(det) > 0.0))
+                return;
+            double I[9];  // I[r*3 + c] = (B^-1)[r][c]
+            I[0] = c00 / det;
+            I[1] = (B[2] * B[7] - B[1] * B[8]) / det;
+            I[2] = (B[1] * B[5] - B[2] * B[4]) / det;
+            I[3] = c01 / det;
+            I[4] = (B[0] * B[8] - B[2] * B[6]) / det;
+            I[5] = (B[2] * B[3] - B[0] * B[5]) / det;
+            I[6] = c02 / det;
+            I[7] = (B[1] * B[6] - B[0] * B[7]) / det;
+            I[8] = (B[0] * B[4] - B[1] * B[3]) / det;
+            for (int k = 0; k < 3; ++k)
+                w[k] = 1.0 / std::sqrt(I[k] * I[k] + I[3 + k] * I[3 + k] + I[6 + k] * I[6 + k]);
+            // smallest eigenvalue of M = B B^T (|real|^2 = box M box^T), by
+            // the trigonometric solution of the symmetric 3 x 3 eigenproblem
+            double M[9];
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j)
+                    M[3 * i + j] = B[3 * i] * B[3 * j] + B[3 * i + 1] * B[3 * j + 1] + B[3 * i + 2] * B[3 * j + 2];
+            const double p1 = M[1] * M[1] + M[2] * M[2] + M[5] * M[5];
+            if (p1 == 0.0) {
+                lam = std::min(M[0], std::min(M[4], M[8]));
+            } else {
+                const double q = (M[0] + M[4] + M[8]) / 3.0;
+                const double p2 = (M[0] - q) * (M[0] - q) + (M[4] - q) * (M[4] - q) + (M[8] - q) * (M[8] - q) + 2 * p1;
+                const double pp = std::sqrt(p2 / 6.0);
+                double Q[9];
+                for (int k = 0; k < 9; ++k) Q[k] = (M[k] - (k % 4 == 0 ? q : 0.0)) / pp;
+                double r = 0.5 * (Q[0] * (Q[4] * Q[8] - Q[5] * Q[7]) - Q[1] * (Q[3] * Q[8] - Q[5] * Q[6]) +
+                                  Q[2] * (Q[3] * Q[7] - Q[4] * Q[6]));
+                r = std::max(-1.0, std::min(1.0, r));
+                lam = q + 2.0 * pp * std::cos(std::acos(r) / 3.0 + 2.0 * M_PI / 3.0);
+            }
+            lam = std::max(0.0, 0.999 * lam);
+        }
+    }
+    double lo[3], hi[3];
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = INFINITY;
+        hi[k] = -INFINITY;
+    }
+    for (int i = 0; i < n; ++i)
+        for (int k = 0; k < 3; ++k) {
+            const double x = sp.box_coords[3 * (size_t)i + k];
+            lo[k] = std::min(lo[k], x);
+            hi[k] = std::max(hi[k], x);
+        }
+    const double maxD = sp.maxDistance;
+    if (!(maxD > 0.0) || !std::isfinite(lo[0] + lo[1] + lo[2] + hi[0] + hi[1] + hi[2]))
+        return;
+    double ext[3], vol = 1.0;
+    int nk[3];
+    const double Lc = std::max(0.5 * maxD, 1e-3);
+    for (int k = 0; k < 3; ++k) {
+        ext[k] = (hi[k] - lo[k]) * w[k];
+        nk[k] = (int)std::max(1.0, std::min(64.0, std::floor(ext[k] / Lc)));
+        vol *= std::max(ext[k], 1e-9);
+    }
+    while (nk[0] * nk[1] * nk[2] > kMaxCells) {
+        int k = nk[0] >= nk[1] && nk[0] >= nk[2] ? 0 : (nk[1] >= nk[2] ? 1 : 2);
+        --nk[k];
+    }
+    const int nc = nk[0] * nk[1] * nk[2];
+    double diag2 = 0.0;
+    for (int k = 0; k < 3; ++k) diag2 += (ext[k] / nk[k]) * (ext[k] / nk[k]);
+    const double R = (maxD + 0.5 * std::sqrt(diag2)) * (mode ? 1.1 : 1.0);
+    if (nc < 8 || 4.0 / 3.0 * M_PI * R * R * R > 0.6 * vol)
+        return;
+    std::vector<int> cell(n), count(nc + 1, 0);
+    for (int i = 0; i < n; ++i) {
+        int ck[3];
+        for (int k = 0; k < 3; ++k) {
+            const double span = hi[k] - lo[k];
+            const double x = sp.box_coords[3 * (size_t)i + k];
+            int c = span > 0.0 ? (int)std::floor((x - lo[k]) / span * nk[k]) : 0;
+            ck[k] = std::max(0, std::min(nk[k] - 1, c));
+        }
+        cell[i] = ck[0] + nk[0] * (ck[1] + nk[1] * ck[2]);
+        ++count[cell[i]];
+    }
+    G.cstart.assign(nc + 1, 0);
+    for (int c = 0; c < nc; ++c) G.cstart[c + 1] = G.cstart[c] + count[c];
+    std::vector<int> fill(G.cstart.begin(), G.cstart.end() - 1);
+    G.cbox.resize(n);
+    G.cmol.resize(n);
+    G.csl.resize(n);
+    G.clo.assign(nc, make_float4(INFINITY, INFINITY, INFINITY, 0.f));
+    G.chi.assign(nc, make_float4(-INFINITY, -INFINITY, -INFINITY, 0.f));
+    for (int i = 0; i < n; ++i) {
+        const int c = cell[i], pos = fill[c]++;
+        const float x = sp.box_coords[3 * (size_t)i], y = sp.box_coords[3 * (size_t)i + 1],
+                    z = sp.box_coords[3 * (size_t)i + 2];
+        G.cbox[pos] = make_float4(x, y, z, int_bits_as_float(sp.el[i]));
+        G.cmol[pos] = sp.mol[i];
+        G.csl[i] = make_int2(pos, c);
+        float4 &l = G.clo[c], &h = G.chi[c];
+        l.x = std::min(l.x, x); l.y = std::min(l.y, y); l.z = std::min(l.z, z);
+        h.x = std::max(h.x, x); h.y = std::max(h.y, y); h.z = std::max(h.z, z);
+    }
+    for (int c = 0; c < nc; ++c)
+        if (!count[c]) {
+            G.clo[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+            G.chi[c] = G.clo[c];
+        }
+    double slack = 0.0;
+    for (int k = 0; k < 3; ++k) slack += w[k] * std::max(1.0, std::max(std::fabs(lo[k]), std::fabs(hi[k])));
+    const double thr = maxD * (1.0 + 1e-4) + 1e-2 + 4e-6 * slack;
+    G.nc = nc;
+    G.cmode = mode;
+    G.cpbc = pbc ? 1 : 0;
+    for (int k = 0; k < 3; ++k) G.cw[k] = (float)w[k];
+    G.clam2 = (float)lam;
+    G.cthr2 = (float)(thr * thr);
+    // the columns a step would sweep, averaged over up to 32 atoms taken as
+    // the moved atom (the device's test, in double)
+    const int ns = std::min(n, 32);
+    double sum = 0.0;
+    for (int k = 0; k < ns; ++k) {
+        const int i = (int)((long long)k * n / ns);
+        const double p[3] = {sp.box_coords[3 * (size_t)i], sp.box_coords[3 * (size_t)i + 1],
+                             sp.box_coords[3 * (size_t)i + 2]};
+        for (int c = 0; c < nc; ++c) {
+            if (!count[c])
+                continue;
+            const double clo[3] = {G.clo[c].x, G.clo[c].y, G.clo[c].z}, chi[3] = {G.chi[c].x, G.chi[c].y, G.chi[c].z};
+            double f[3], lb2 = 0.0, mx = 0.0, f2 = 0.0;
+            for (int a = 0; a < 3; ++a) {
+                const double lo_d = p[a] - chi[a], hi_d = p[a] - clo[a];
+                if (!pbc) {
+                    f[a] = lo_d > 0 ? lo_d : (hi_d < 0 ? -hi_d : 0.0);
+                } else {
+                    const double nn = std::floor(hi_d);
+                    f[a] = nn >= lo_d ? 0.0 : std::min(lo_d - nn, nn + 1.0 - hi_d);
+                }
+                const double m = f[a] * w[a];
+                lb2 += m * m;
+                mx = std::max(mx, m * m);
+                f2 += f[a] * f[a];
+            }
+            if (mode != 0)
+                lb2 = std::max(mx, lam * f2);
+            if (lb2 < thr * thr)
+                sum += count[c];
+        }
+    }
+    G.sweep = sum / ns;
+}
+
 static int add_engine(EngineSet *s, const frmc_engine_spec &sp, int *out_id)
 {
     FRMC_TRY(check_spec(sp));
@@ -2226,6 +2607,21 @@ static int add_engine(EngineSet *s, const frmc_engine_spec &sp, int *out_id)
     D.groups = D.group > 1 ? (EGroup *)(b + L.groups) : nullptr;
     D.results = (EResult *)(b + L.results);
     D.st = (EState *)(b + L.st);
+    CellGrid cg;
+    if (s->cells)
+        build_cells(sp, D.bm, cg);
+    D.nc = cg.nc;
+    D.cmode = cg.cmode;
+    D.cpbc = cg.cpbc;
+    for (int k = 0; k < 3; ++k) D.cw[k] = cg.cw[k];
+    D.clam2 = cg.clam2;
+    D.cthr2 = cg.cthr2;
+    D.cbox = (float4 *)(b + L.cbox);
+    D.cmol = (int *)(b + L.cmol);
+    D.csl = (int2 *)(b + L.csl);
+    D.cstart = (int *)(b + L.cstart);
+    D.clo = (float4 *)(b + L.clo);
+    D.chi = (float4 *)(b + L.chi);
     std::vector<double> Rqt;
     if (tab) {
         D.sq = 1;
@@ -2288,6 +2684,14 @@ static int add_engine(EngineSet *s, const frmc_engine_spec &sp, int *out_id)
     up(D.pidx, pidx.data(), 4 * pidx.size());
     up(D.R, Rt.data(), 8 * Rt.size());
     up(D.A, At.data(), 8 * At.size());
+    if (cg.nc > 0) {
+        up(D.cbox, cg.cbox.data(), 16 * cg.cbox.size());
+        up(D.cmol, cg.cmol.data(), 4 * cg.cmol.size());
+        up(D.csl, cg.csl.data(), 8 * cg.csl.size());
+        up(D.cstart, cg.cstart.data(), 4 * cg.cstart.size());
+        up(D.clo, cg.clo.data(), 16 * cg.clo.size());
+        up(D.chi, cg.chi.data(), 16 * cg.chi.size());
+    }
     if (tab) {
         up(D.Rq, Rqt.data(), 8 * Rqt.size());
         up(D.rfacq, sp.sq_rfac, 8 * (size_t)sp.hs);
@@ -2323,6 +2727,7 @@ static int add_engine(EngineSet *s, const frmc_engine_spec &sp, int *out_id)
     }
     sl.live = true;
     sl.sq_table = sp.sq_table;
+    sl.cost = (cg.nc > 0 ? 4 * (long long)std::ceil(cg.sweep) : (long long)sp.n) * spec_group(sp);
     s->slots[id] = sl;
     s->live.push_back(id);
     std::sort(s->live.begin(), s->live.end());
@@ -2498,6 +2903,32 @@ int frmc_engines_set_sq_gemm_limit(void *handle, int32_t limit)
     return FRMC_OK;
 }
 
+int frmc_engines_set_cells(void *handle, int32_t on)
+{
+    EngineSet *s = as_set(handle);
+    if (!s)
+        return set_error(FRMC_E_ARG, "null handle");
+    s->cells = on ? 1 : 0;
+    return FRMC_OK;
+}
+
+int frmc_engines_cells(void *handle, int32_t e, int32_t *ncells, int64_t *swept)
+{
+    EngineSet *s = as_set(handle);
+    if (!s || !ncells)
+        return set_error(FRMC_E_ARG, "null argument");
+    if (e < 0 || e >= (int)s->slots.size() || !s->slots[e].live)
+        return set_error(FRMC_E_ARG, "engines_cells: no engine %d", e);
+    *ncells = s->slots[e].d.nc;
+    if (swept) {
+        FRMC_CUDA(cudaStreamSynchronize(s->stream));
+        EState S;
+        FRMC_CUDA(cudaMemcpy(&S, s->slots[e].d.st, sizeof(EState), cudaMemcpyDeviceToHost));
+        *swept = (int64_t)S.swept;
+    }
+    return FRMC_OK;
+}
+
 int frmc_engines_set_mode(void *handle, int fused)
 {
     EngineSet *s = as_set(handle);
@@ -2639,7 +3070,7 @@ int frmc_engines_step(void *handle, int32_t engine, int32_t steps, int use_graph
         if (engine < 0)
             return launch_batched(s, sx);
         const int fi = s->fused_item[engine];
-        if (fi >= 0 && s->slots[engine].d.n <= kSoloFusedAtoms)  // one CTA beats tiles plus a finisher
+        if (fi >= 0 && s->slots[engine].cost <= kSoloFusedCost)  // one CTA beats tiles plus a finisher
             FRMC_TRY(launch_items(s, s->items + fi, 1, 0, sx, fused_dyn_smem(s), true));
         else
             FRMC_TRY(launch_items(s, s->items + s->item_first[engine], count, 0, sx));

@@ -58,6 +58,8 @@ register("frmc_engines_destroy", [_vp])
 register("frmc_engines_set_tune", [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int])
 register("frmc_engines_get_tune", [_vp] + [ctypes.POINTER(ctypes.c_int)] * 4)
 register("frmc_engines_set_mode", [_vp, ctypes.c_int])
+register("frmc_engines_set_cells", [_vp, ctypes.c_int32])
+register("frmc_engines_cells", [_vp, _i32, ctypes.POINTER(_i32), ctypes.POINTER(_i64)])
 register("frmc_engines_set_sq_gemm_limit", [_vp, ctypes.c_int32])
 register("frmc_engines_init", [_vp])
 register("frmc_engines_push_moves", [_vp, _i32, I32P, F32P, F32P, _i32, _i64, ctypes.c_int])
@@ -391,17 +393,21 @@ def footprint(system, move_cap):
 class EngineSet:
     """A set of device-resident engines stepped together or one at a time."""
 
-    def __init__(self, systems=(), move_cap: int = 4096, tune=None):
+    def __init__(self, systems=(), move_cap: int = 4096, tune=None, cells: bool = True):
+        """cells: give engines a column grid where it pays (the one-CTA step
+        then sweeps only the cells a moved atom may reach; results are
+        identical either way)."""
         load()
         self.move_cap = int(move_cap)
         self.systems = {}
         self.tables = {}
         h = ctypes.c_void_p()
         systems = list(systems)
-        if any(s.sq is not None for s in systems):
+        if not cells or any(s.sq is not None for s in systems):
             # S(Q) tables must exist before their engines: add one by one
             check(load().frmc_engines_new(ctypes.byref(h)))
             self.handle = h
+            check(load().frmc_engines_set_cells(h, 1 if cells else 0))
             for s in systems:
                 self.add(s)
         elif systems:
@@ -492,6 +498,19 @@ class EngineSet:
     # ------------------------------------------------------------ control
     def set_tune(self, tile, threads, ctas_per_sm):
         check(load().frmc_engines_set_tune(self.handle, int(tile), int(threads), int(ctas_per_sm)))
+
+    def cells(self, e):
+        """Number of cells of engine e's column grid (0: no grid)."""
+        v = _i32()
+        check(load().frmc_engines_cells(self.handle, int(e), ctypes.byref(v), None))
+        return v.value
+
+    def swept(self, e):
+        """Columns engine e's one-CTA steps swept since init (all its atoms
+        per step without a grid, the selected cells' atoms with one)."""
+        v, w = _i32(), _i64()
+        check(load().frmc_engines_cells(self.handle, int(e), ctypes.byref(v), ctypes.byref(w)))
+        return w.value
 
     def set_mode(self, fused):
         check(load().frmc_engines_set_mode(self.handle, int(bool(fused))))

@@ -113,6 +113,16 @@ int frmc_engines_get_tune(void *handle, int *tile, int *threads, int *ctas_per_s
  * fit in shared memory (fused = 1, the default), else every engine is split
  * over atom tiles (fused = 0).  Results are identical either way. */
 int frmc_engines_set_mode(void *handle, int fused);
+/* Column grids (on = 1, the default): an engine added afterwards gets its
+ * atoms sorted into at most 512 cells where that pays, and the one-CTA step
+ * sweeps only the cells whose bounding box may come within maxDistance of a
+ * moved atom (a lower bound of the minimum-image distance with a margin far
+ * above float32 rounding, so every skipped pair is out of range before and
+ * after the move).  Results are identical with and without grids.
+ * frmc_engines_cells reports an engine's number of cells (0: no grid) and,
+ * when swept is not null, the columns its one-CTA steps swept since init. */
+int frmc_engines_set_cells(void *handle, int32_t on);
+int frmc_engines_cells(void *handle, int32_t e, int32_t *ncells, int64_t *swept);
 /* The S(Q) term's product y = T x runs as one fp16 GEMM over digits of T when
  * every element-pair delta of the step is at most `limit` in magnitude
  * (default and maximum 32, where the GEMM is exact), else as an exact integer
