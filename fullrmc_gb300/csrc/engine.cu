@@ -225,6 +225,12 @@ struct StepParams {
     int fused_dp_ints;  // fused launches: ints of the element-pair deltas (a multiple of 4)
     int fused_bins;     // fused launches: doubles of each of A and Bq (even)
     Sched *sched;
+    // host-buffer steps of fused engines (else null): item k's move is
+    // hmoves[fpos[k]] and its result goes to hres[fpos[k]], both in mapped
+    // pinned host memory
+    const EMove *hmoves;
+    EResult *hres;
+    const int *fpos;
 };
 
 constexpr int kRedLanes = 64;
@@ -244,10 +250,10 @@ __device__ __forceinline__ float3 to_box(const Basis &RB, float x, float y, floa
 // new real), boundary_conditions_collection.pyx:88-110).  All threads of the
 // CTA call it; the caller synchronises before use.  A single atom is done by
 // thread 0 alone.
-__device__ void load_moved_group(const EDesc &D, long long step, MovedGroup &g)
+__device__ void load_moved_group(const EDesc &D, long long step, MovedGroup &g, const EMove *staged = nullptr)
 {
     const int G = D.group;
-    const EMove &m = D.moves[step % D.move_cap];
+    const EMove &m = staged ? *staged : D.moves[step % D.move_cap];
     if (threadIdx.x == 0) {
         g.u = m.u;
         g.step = step;
@@ -1208,7 +1214,8 @@ __device__ void fused_columns(const EDesc &Dg, int *sdP, int *nz, unsigned *s_tc
 // `bar` while the columns run; parity = this CTA's count of fused items mod 2.
 __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, uint64_t *bar, uint32_t parity,
                              uint32_t *status, double *red, double *cb, double *sbs, int *sbin, int *s_nchg,
-                             double *coef, int *s_flag, unsigned *s_tcount, MovedGroup &g, const ColQueue &q)
+                             double *coef, int *s_flag, unsigned *s_tcount, MovedGroup &g, const ColQueue &q,
+                             const EMove *hm, EResult *hr)
 {
     // the column grid's prefix and bases live in cb until the evaluation
     static_assert(sizeof(double) * kChunk >= sizeof(int) * (2 * kMaxCells + 33), "cell arrays exceed cb");
@@ -1233,7 +1240,7 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, 
         cs0 = D.cstart[threadIdx.x];
         cs1 = D.cstart[threadIdx.x + 1];
     }
-    load_moved_group(D, D.st->step, g);
+    load_moved_group(D, D.st->step, g, hm);
     const int np = D.npairs;
     const int nph = np * D.hs;
     for (int k = threadIdx.x; k < nph; k += blockDim.x) sdP[k] = 0;
@@ -1328,6 +1335,8 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, 
         r.chi2_new = chi2_new;
         r.accepted = accept ? 1 : 0;
         r.atom = g.atom[0];
+        if (hr)
+            *hr = r;
         if (accept) {
             S.chi2 = chi2_new;
             S.sd = sd_new;
@@ -1348,7 +1357,7 @@ __device__ void warm_item(const StepParams &p, long long idx)
     const EDesc &D = p.fdesc[idx];
     const long long stp = D.st->step;
     const long long slot = stp % D.move_cap;
-    const int a = D.moves[slot].atom;
+    const int a = p.hmoves ? p.hmoves[p.fpos[idx]].atom : D.moves[slot].atom;
     prefetch_l2(D.box + a);
     prefetch_l2(D.real + a);
     prefetch_l2(D.mol + a);
@@ -1413,8 +1422,10 @@ __global__ void __launch_bounds__(kMaxEngineThreads, 1) k_engine_step(StepParams
         if (FUSED && fused_items == 0 && threadIdx.x == 32)
             warm_item(p, (long long)it + gridDim.x);
         if (FUSED) {
+            const int hp = p.hmoves ? p.fpos[it] : 0;
             engine_fused(D, sdP, sA, sBq, &s_bar, fused_items & 1u, &p.sched->status, red, cb, sbs, sbin, &s_nchg,
-                         coef, &s_flag, &s_tcount, s_group, cq);
+                         coef, &s_flag, &s_tcount, s_group, cq, p.hmoves ? p.hmoves + hp : nullptr,
+                         p.hres ? p.hres + hp : nullptr);
             ++fused_items;
             __syncthreads();
             continue;
@@ -1899,6 +1910,7 @@ struct EngineSet {
     int ddesc_cap = 0;
     EDesc *fdesc = nullptr;        // descriptors of the fused items, in work-list order
     int fdesc_cap = 0;
+    int *fpos = nullptr;           // per fused item: its engine's index in live order (host-buffer steps)
     cublasHandle_t blas = nullptr; // the S(Q) terms' GEMM (created on first use)
     void *blas_ws = nullptr;       // its fixed workspace (graph capture allocates nothing)
     int2 *items = nullptr;
@@ -2107,6 +2119,9 @@ static int refresh(EngineSet *s)
         s->fdesc = nullptr;
         int cap = std::max((int)fused_ids.size(), 2 * s->fdesc_cap);
         FRMC_CUDA(cudaMalloc(&s->fdesc, sizeof(EDesc) * cap));
+        if (s->fpos) cudaFree(s->fpos);
+        s->fpos = nullptr;
+        FRMC_CUDA(cudaMalloc(&s->fpos, sizeof(int) * cap));
         s->fdesc_cap = cap;
     }
     if (nslots > s->ddesc_cap) {
@@ -2197,6 +2212,11 @@ static int refresh(EngineSet *s)
         fd.reserve(fused_ids.size());
         for (int id : fused_ids) fd.push_back(s->slots[id].d);
         FRMC_CUDA(cudaMemcpy(s->fdesc, fd.data(), sizeof(EDesc) * fd.size(), cudaMemcpyHostToDevice));
+        std::vector<int> live_pos(nslots, -1), fp;
+        for (int k = 0; k < (int)s->live.size(); ++k) live_pos[s->live[k]] = k;
+        fp.reserve(fused_ids.size());
+        for (int id : fused_ids) fp.push_back(live_pos[id]);
+        FRMC_CUDA(cudaMemcpy(s->fpos, fp.data(), sizeof(int) * fp.size(), cudaMemcpyHostToDevice));
     }
     if (!items.empty())
         FRMC_CUDA(cudaMemcpy(s->items, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice));
@@ -2212,7 +2232,8 @@ static int refresh(EngineSet *s)
 }
 
 static int launch_items(EngineSet *s, const int2 *items, int count, int eval_only, cudaStream_t st,
-                        int dyn_smem = 0, bool fused = false)
+                        int dyn_smem = 0, bool fused = false, const EMove *hmoves = nullptr,
+                        EResult *hres = nullptr)
 {
     Context *c;
     FRMC_TRY(get_context(&c));
@@ -2221,9 +2242,15 @@ static int launch_items(EngineSet *s, const int2 *items, int count, int eval_onl
         grid = count;
     if (grid < 1)
         return FRMC_OK;
-    const EDesc *fd = fused ? s->fdesc + (items - (s->items + s->nsolo)) : nullptr;
+    const long long first = items - (s->items + s->nsolo);
+    const EDesc *fd = fused ? s->fdesc + first : nullptr;
     StepParams p{s->ddesc, fd, items, count, s->tile, eval_only, fused ? s->fused_dp_ints : 0,
-                 fused ? s->fused_bins : 0, s->sched};
+                 fused ? s->fused_bins : 0, s->sched, nullptr, nullptr, nullptr};
+    if (fused && hmoves) {
+        p.hmoves = hmoves;
+        p.hres = hres;
+        p.fpos = s->fpos + first;
+    }
     if (fused) {
         FRMC_CUDA(cudaFuncSetAttribute(k_engine_step<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem));
         k_engine_step<true><<<grid, s->threads, dyn_smem, st>>>(p);
@@ -2751,7 +2778,7 @@ static void free_set(EngineSet *s)
     }
     if (s->blas) cublasDestroy(s->blas);
     if (s->blas_ws) cudaFree(s->blas_ws);
-    void *ptrs[] = {s->ddesc, s->fdesc, s->items, s->dlive, s->sched, s->sq_items};
+    void *ptrs[] = {s->ddesc, s->fdesc, s->fpos, s->items, s->dlive, s->sched, s->sq_items};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int k = 0; k < 2; ++k) {
@@ -3146,8 +3173,10 @@ static int step_host_submit(EngineSet *s, const int32_t *atoms, const float *vec
             s->hstage_r[k] = nullptr;
             s->dstage_m[k] = nullptr;
             s->dstage_r[k] = nullptr;
-            FRMC_CUDA(cudaMallocHost(&s->hstage_m[k], sizeof(EMove) * cap));
-            FRMC_CUDA(cudaMallocHost(&s->hstage_r[k], sizeof(EResult) * cap));
+            // mapped: a step of fused engines reads its moves and writes its
+            // results here directly
+            FRMC_CUDA(cudaHostAlloc((void **)&s->hstage_m[k], sizeof(EMove) * cap, cudaHostAllocMapped));
+            FRMC_CUDA(cudaHostAlloc((void **)&s->hstage_r[k], sizeof(EResult) * cap, cudaHostAllocMapped));
             FRMC_CUDA(cudaMalloc(&s->dstage_m[k], sizeof(EMove) * cap));
             FRMC_CUDA(cudaMalloc(&s->dstage_r[k], sizeof(EResult) * cap));
             if (!s->stage_ev[k])
@@ -3165,7 +3194,17 @@ static int step_host_submit(EngineSet *s, const int32_t *atoms, const float *vec
         m.u = u ? u[k] : 1.0f;
     }
     cudaStream_t st = s->stream;
+    // every live engine fused and none with an S(Q) term: one kernel reads
+    // the moves from the mapped staging buffer and writes the results there
+    const bool direct = s->nfused == s->nbatch && s->sq_host.empty() && s->nfused == E;
     auto body = [&](cudaStream_t sx) -> int {
+        if (direct) {
+            EMove *dm = nullptr;
+            EResult *dr = nullptr;
+            FRMC_CUDA(cudaHostGetDevicePointer((void **)&dm, s->hstage_m[slot], 0));
+            FRMC_CUDA(cudaHostGetDevicePointer((void **)&dr, s->hstage_r[slot], 0));
+            return launch_items(s, s->items + s->nsolo, s->nfused, 0, sx, fused_dyn_smem(s), true, dm, dr);
+        }
         FRMC_CUDA(cudaMemcpyAsync(s->dstage_m[slot], hm, sizeof(EMove) * E, cudaMemcpyHostToDevice, sx));
         k_scatter_moves<<<(E + 127) / 128, 128, 0, sx>>>(s->ddesc, s->dlive, s->dstage_m[slot], E);
         FRMC_CUDA(cudaGetLastError());

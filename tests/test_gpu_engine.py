@@ -143,9 +143,12 @@ def test_step_host_matches_ring_steps():
     es.close()
 
 
-def test_step_host_two_slots_match_ring_steps():
+@pytest.mark.parametrize("fused", [1, 0])
+def test_step_host_two_slots_match_ring_steps(fused):
     """Submitting step k + 1 before collecting step k (two staging slots)
-    gives the same chains as pushed moves; misuse of a slot is refused."""
+    gives the same chains as pushed moves -- one kernel on the mapped staging
+    buffers when every engine runs in one CTA, copies and tile-split steps
+    otherwise; misuse of a slot is refused."""
     from fullrmc_gb300._native import NativeError
     from fullrmc_gb300.engine import EngineSet
     systems = _systems(count=5, seed=14)
@@ -153,6 +156,7 @@ def test_step_host_two_slots_match_ring_steps():
     mv = _moves(systems, steps, seed=9)
     ring = _run(systems, mv, steps, "batched")
     es = EngineSet(systems, move_cap=4)
+    es.set_mode(fused)
     es.init()
     A = np.ascontiguousarray(np.stack([m[0] for m in mv]).T)
     V = np.ascontiguousarray(np.stack([m[1] for m in mv]).transpose(1, 0, 2))
@@ -173,6 +177,11 @@ def test_step_host_two_slots_match_ring_steps():
             assert c2[e] == ring[e]["chi2"][k] and acc[e] == ring[e]["acc"][k]
     for e in range(len(systems)):
         assert es.state(e) == ring[e]["state"]
+        c2, a, at = es.results(e, steps - 4, 4)  # the ring keeps the last move_cap results
+        assert np.array_equal(c2.view(np.int64), ring[e]["chi2"][steps - 4:].view(np.int64))
+        assert np.array_equal(at, ring[e]["atoms"][steps - 4:])
+        assert all(np.array_equal(x, y) for x, y in zip(es.counts(e), ring[e]["counts"]))
+        assert all(np.array_equal(x, y) for x, y in zip(es.coords(e), ring[e]["coords"]))
     es.close()
 
 
