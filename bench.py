@@ -664,7 +664,10 @@ def run_ours(args):
                       "batched_over_plain": value / ws / plain_rate},
             "steady_graph": {"ms_per_step": graph_ms, "steps_per_s": E / (graph_ms * 1e-3),
                              "note": "K steps in one CUDA graph, no L2 flush"},
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "path": "frmc_engines_step_host_submit/collect from numpy arrays; the moves go through "
+                            "mapped pinned host memory, which the step kernel reads, and it writes the "
+                            "results there (zero-copy over NVLink-C2C)"},
             "roofline": {"bound": "issue", "achieved": step_pairs_rate / 1e9, "peak": issue_peak / 1e9,
                          "unit": "Gpair/s", "frac": step_pairs_rate / issue_peak, "traffic": traffic,
                          "kernel": "k_engine_step", "pairs_per_launch": pairs_per_step,

@@ -3377,6 +3377,60 @@ int frmc_engines_coords(void *handle, int32_t e, float *box_coords, float *real_
     return FRMC_OK;
 }
 
+int frmc_engines_regrid(void *handle, int32_t e)
+{
+    EngineSet *s = as_set(handle);
+    if (!s || !valid_id(s, e))
+        return set_error(FRMC_E_ARG, "engines_regrid: invalid engine");
+    Slot &sl = s->slots[e];
+    EDesc &D = sl.d;
+    if (!s->cells)
+        return FRMC_OK;
+    FRMC_CUDA(cudaStreamSynchronize(s->stream));
+    std::vector<float4> b(D.n);
+    std::vector<int> mol(D.n), el(D.n);
+    std::vector<float> box(3 * (size_t)D.n);
+    FRMC_CUDA(cudaMemcpy(b.data(), D.box, sizeof(float4) * D.n, cudaMemcpyDeviceToHost));
+    FRMC_CUDA(cudaMemcpy(mol.data(), D.mol, sizeof(int) * D.n, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < D.n; ++i) {
+        box[3 * (size_t)i] = b[i].x;
+        box[3 * (size_t)i + 1] = b[i].y;
+        box[3 * (size_t)i + 2] = b[i].z;
+        int v;
+        std::memcpy(&v, &b[i].w, 4);
+        el[i] = v;
+    }
+    frmc_engine_spec sp;
+    std::memset(&sp, 0, sizeof(sp));
+    sp.n = D.n;
+    sp.isPBC = D.bm != BM_IBC;
+    sp.box_coords = box.data();
+    sp.el = el.data();
+    sp.mol = mol.data();
+    sp.basis = D.B.b;
+    sp.maxDistance = D.maxD;
+    sp.group_size = D.group;
+    CellGrid cg;
+    build_cells(sp, D.bm, cg);
+    if (cg.nc > 0) {
+        FRMC_CUDA(cudaMemcpy(D.cbox, cg.cbox.data(), 16 * cg.cbox.size(), cudaMemcpyHostToDevice));
+        FRMC_CUDA(cudaMemcpy(D.cmol, cg.cmol.data(), 4 * cg.cmol.size(), cudaMemcpyHostToDevice));
+        FRMC_CUDA(cudaMemcpy(D.csl, cg.csl.data(), 8 * cg.csl.size(), cudaMemcpyHostToDevice));
+        FRMC_CUDA(cudaMemcpy(D.cstart, cg.cstart.data(), 4 * cg.cstart.size(), cudaMemcpyHostToDevice));
+        FRMC_CUDA(cudaMemcpy(D.clo, cg.clo.data(), 16 * cg.clo.size(), cudaMemcpyHostToDevice));
+        FRMC_CUDA(cudaMemcpy(D.chi, cg.chi.data(), 16 * cg.chi.size(), cudaMemcpyHostToDevice));
+    }
+    D.nc = cg.nc;
+    D.cmode = cg.cmode;
+    D.cpbc = cg.cpbc;
+    for (int k = 0; k < 3; ++k) D.cw[k] = cg.cw[k];
+    D.clam2 = cg.clam2;
+    D.cthr2 = cg.cthr2;
+    sl.cost = (cg.nc > 0 ? 4 * (long long)std::ceil(cg.sweep) : (long long)D.n) * D.group;
+    s->dirty = true;  // descriptors and the work list are rebuilt before the next step
+    return FRMC_OK;
+}
+
 int frmc_engines_sq_table(void *handle, int32_t hs, int32_t nq, const double *M, const double *weights,
                           const double *r0fac, int32_t *table)
 {

@@ -60,6 +60,7 @@ register("frmc_engines_get_tune", [_vp] + [ctypes.POINTER(ctypes.c_int)] * 4)
 register("frmc_engines_set_mode", [_vp, ctypes.c_int])
 register("frmc_engines_set_cells", [_vp, ctypes.c_int32])
 register("frmc_engines_cells", [_vp, _i32, ctypes.POINTER(_i32), ctypes.POINTER(_i64)])
+register("frmc_engines_regrid", [_vp, _i32])
 register("frmc_engines_set_sq_gemm_limit", [_vp, ctypes.c_int32])
 register("frmc_engines_init", [_vp])
 register("frmc_engines_push_moves", [_vp, _i32, I32P, F32P, F32P, _i32, _i64, ctypes.c_int])
@@ -504,6 +505,10 @@ class EngineSet:
         v = _i32()
         check(load().frmc_engines_cells(self.handle, int(e), ctypes.byref(v), None))
         return v.value
+
+    def regrid(self, e):
+        """Rebuild engine e's column grid from its current coordinates."""
+        check(load().frmc_engines_regrid(self.handle, int(e)))
 
     def swept(self, e):
         """Columns engine e's one-CTA steps swept since init (all its atoms

@@ -122,6 +122,10 @@ int frmc_engines_set_mode(void *handle, int fused);
  * frmc_engines_cells reports an engine's number of cells (0: no grid) and,
  * when swept is not null, the columns its one-CTA steps swept since init. */
 int frmc_engines_set_cells(void *handle, int32_t on);
+/* Rebuild engine e's column grid from its current coordinates (cell bounds
+ * only grow as atoms move; a long run with large moves can re-tighten them).
+ * Results are unchanged. */
+int frmc_engines_regrid(void *handle, int32_t e);
 int frmc_engines_cells(void *handle, int32_t e, int32_t *ncells, int64_t *swept);
 /* The S(Q) term's product y = T x runs as one fp16 GEMM over digits of T when
  * every element-pair delta of the step is at most `limit` in magnitude

@@ -170,3 +170,30 @@ def test_large_grid_engine_runs_fused_and_equals_split_path():
     assert 0 < with_grid[0]["swept"] < 0.2 * steps * 60000   # one-CTA steps
     assert without[0]["swept"] == 0                           # tile-split steps
     _same(with_grid, without)
+
+
+def test_regrid_mid_chain_keeps_results():
+    """Rebuilding the grids from the current coordinates halfway through a
+    chain of large moves (their cells have widened) changes nothing."""
+    from fullrmc_gb300.engine import EngineSet
+    systems = _systems()[:4]
+    steps = 120
+    mv = _moves(systems, steps, seed=13, amp=4.0)
+    without, _ = _run(systems, mv, steps, cells=False)
+    es = EngineSet(systems, move_cap=max(64, steps), cells=True)
+    es.init()
+    for e, (a, v, u) in enumerate(mv):
+        es.push_moves(e, a, v, u, 0)
+    es.step(steps // 2, engine=-1)
+    for e in range(len(systems)):
+        es.regrid(e)
+    assert all(es.cells(e) > 0 for e in range(len(systems)))
+    es.step(steps - steps // 2, engine=-1)
+    for e in range(len(systems)):
+        c2, a, at = es.results(e, 0, steps)
+        assert np.array_equal(a, without[e]["acc"])
+        assert np.array_equal(c2.view(np.int64), without[e]["chi2"].view(np.int64))
+        assert es.state(e) == without[e]["state"]
+        for k in (0, 1):
+            assert np.array_equal(es.counts(e)[k], without[e]["counts"][k])
+    es.close()
