@@ -804,9 +804,11 @@ __device__ __forceinline__ void delta_add(int *sdP, int *nz, int idx, int b, int
 
 // The fused path's share of the group's internal pairs (shared-memory deltas).
 template <int BM>
-__device__ void fused_group_internal(const EDesc &Dg, int *sdP, int *nz, unsigned *s_tcount, const MovedGroup &g)
+__device__ void fused_group_internal(const EDesc &Dg, int *sdP, int *nz, unsigned *s_tcount, const MovedGroup &g,
+                                     const int *pidx)
 {
-    const ColView D = col_view(Dg);
+    ColView D = col_view(Dg);
+    D.pidx = pidx;
     const int npair = g.n * (g.n - 1) / 2;
     for (int t = threadIdx.x; t < npair; t += blockDim.x) {
         int f0, f1, half, b0, b1, ela, elj;
@@ -967,60 +969,75 @@ __device__ void finish_engine(const EDesc &D, const MovedGroup &g, double *red, 
 // Per-thread queue of accepted columns in the fused path: kColQueue entries
 // per thread, entry k of thread t at [k * blockDim + t] (conflict-free).
 constexpr int kColQueue = 8;
+constexpr int kMaxEngineThreads = 512;  // CTA size limit of the step kernels (128 registers per thread)
 
 struct ColQueue {
     float *s0, *s1;   // squared distances before / after the move
     unsigned *info;   // el(j) | same molecule << 8 | accepted before << 9 | after << 10 | group atom << 11
     int *nz;          // per bin: element pairs whose delta is non-zero
+    unsigned short *list;  // per warp: 32 * kColQueue queue indexes, the warp's entries packed
 };
 
-// Bins the queued columns of every thread: each pass pops one entry per
-// thread that has one, so the IEEE sqrt / division and the delta atomics run
-// with full warps instead of one diverging lane.
+// Bins the queued columns of a warp: the lanes' entries are packed into one
+// list (a warp scan of the queue lengths), and each pass bins 32 of them, so
+// the IEEE sqrt / division and the delta atomics run with full warps however
+// unevenly the entries fell on the lanes.
 __device__ __forceinline__ void flush_columns(const ColView &D, const MovedGroup &g, int *sdP, int *nz,
                                               unsigned *s_tcount, const ColQueue &q, int &qn)
 {
-    while (__any_sync(0xffffffffu, qn > 0)) {
-        if (qn > 0) {
-            --qn;
-            const int k = qn * (int)blockDim.x + (int)threadIdx.x;
-            const float s0 = q.s0[k], s1 = q.s1[k];
-            const unsigned info = q.info[k];
-            const int elj = (int)(info & 0xffu);
-            const int gi = (int)(info >> 11);
-            const int ela = g.el[gi];
-            const long long half = (info >> 8) & 1u ? 0 : D.total;
-            const long long rowb = (long long)(ela * D.ne + elj) * D.hs;
-            int f0 = -1, f1 = -1, b0 = 0, b1 = 0;
-            if ((info >> 9) & 1u) {
-                b0 = pair_bin(s0, D.minD, D.binw);
-                const long long f = rowb + b0;
-                if ((unsigned long long)f < (unsigned long long)D.total) f0 = (int)f;
+    const unsigned lane = threadIdx.x & 31u;
+    unsigned short *lst = q.list + (threadIdx.x >> 5) * (32 * kColQueue);
+    int inc = qn;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, inc, o);
+        if ((int)lane >= o)
+            inc += v;
+    }
+    const int total = __shfl_sync(0xffffffffu, inc, 31);
+    const int ex = inc - qn;
+    for (int j = 0; j < qn; ++j) lst[ex + j] = (unsigned short)(j * (int)blockDim.x + (int)threadIdx.x);
+    qn = 0;
+    __syncwarp();
+    for (int e = (int)lane; e < total; e += 32) {
+        const int k = lst[e];
+        const float s0 = q.s0[k], s1 = q.s1[k];
+        const unsigned info = q.info[k];
+        const int elj = (int)(info & 0xffu);
+        const int gi = (int)(info >> 11);
+        const int ela = g.el[gi];
+        const long long half = (info >> 8) & 1u ? 0 : D.total;
+        const long long rowb = (long long)(ela * D.ne + elj) * D.hs;
+        int f0 = -1, f1 = -1, b0 = 0, b1 = 0;
+        if ((info >> 9) & 1u) {
+            b0 = pair_bin(s0, D.minD, D.binw);
+            const long long f = rowb + b0;
+            if ((unsigned long long)f < (unsigned long long)D.total) f0 = (int)f;
+        }
+        if ((info >> 10) & 1u) {
+            b1 = pair_bin(s1, D.minD, D.binw);
+            const long long f = rowb + b1;
+            if ((unsigned long long)f < (unsigned long long)D.total) f1 = (int)f;
+        }
+        if (f0 != f1) {
+            unsigned pos = atomicAdd(s_tcount, (unsigned)((f0 >= 0) + (f1 >= 0)));
+            if (f0 >= 0) {
+                D.tlist[pos++] = (int)((half + f0) << 1);
+                int p, bb;
+                pair_of_flat(D, f0, ela, elj, b0, p, bb);
+                if (p >= 0)
+                    delta_add(sdP, nz, p * D.hs + bb, bb, -1);
             }
-            if ((info >> 10) & 1u) {
-                b1 = pair_bin(s1, D.minD, D.binw);
-                const long long f = rowb + b1;
-                if ((unsigned long long)f < (unsigned long long)D.total) f1 = (int)f;
-            }
-            if (f0 != f1) {
-                unsigned pos = atomicAdd(s_tcount, (unsigned)((f0 >= 0) + (f1 >= 0)));
-                if (f0 >= 0) {
-                    D.tlist[pos++] = (int)((half + f0) << 1);
-                    int p, bb;
-                    pair_of_flat(D, f0, ela, elj, b0, p, bb);
-                    if (p >= 0)
-                        delta_add(sdP, nz, p * D.hs + bb, bb, -1);
-                }
-                if (f1 >= 0) {
-                    D.tlist[pos] = (int)(((half + f1) << 1) | 1);
-                    int p, bb;
-                    pair_of_flat(D, f1, ela, elj, b1, p, bb);
-                    if (p >= 0)
-                        delta_add(sdP, nz, p * D.hs + bb, bb, 1);
-                }
+            if (f1 >= 0) {
+                D.tlist[pos] = (int)(((half + f1) << 1) | 1);
+                int p, bb;
+                pair_of_flat(D, f1, ela, elj, b1, p, bb);
+                if (p >= 0)
+                    delta_add(sdP, nz, p * D.hs + bb, bb, 1);
             }
         }
     }
+    __syncwarp();  // the list and the queue slots are refilled after this
 }
 
 // Gap m >= 0 between the ranges [a, b] of coordinate differences and the
@@ -1137,9 +1154,10 @@ __device__ __forceinline__ int cell_column(const int *P, const int *Bse, int nc,
 // cmol, and the moved atoms recognised by their cell-order positions.
 template <int BM, bool GROUP, bool CELL>
 __device__ void fused_columns(const EDesc &Dg, int *sdP, int *nz, unsigned *s_tcount, const MovedGroup &g,
-                              const ColQueue &q, int ncol, const int *cP, const int *cB)
+                              const ColQueue &q, int ncol, const int *cP, const int *cB, const int *pidx)
 {
     ColView D = col_view(Dg);
+    D.pidx = pidx;
     if (CELL) {
         D.box = Dg.cbox;
         D.mol = Dg.cmol;
@@ -1214,12 +1232,23 @@ __device__ void fused_columns(const EDesc &Dg, int *sdP, int *nz, unsigned *s_tc
 // `bar` while the columns run; parity = this CTA's count of fused items mod 2.
 __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, uint64_t *bar, uint32_t parity,
                              uint32_t *status, double *red, double *cb, double *sbs, int *sbin, int *s_nchg,
-                             double *coef, int *s_flag, unsigned *s_tcount, MovedGroup &g, const ColQueue &q,
+                             double *coef, int *s_flag, unsigned *s_tcount, MovedGroup &g, const ColQueue &q0,
                              const EMove *hm, EResult *hr)
 {
-    // the column grid's prefix and bases live in cb until the evaluation
-    static_assert(sizeof(double) * kChunk >= sizeof(int) * (2 * kMaxCells + 33), "cell arrays exceed cb");
+    // the column grid's prefix and bases, and the warps' packed queue lists,
+    // live in cb until the evaluation
+    constexpr int kCellInts = 2 * kMaxCells + 34;
     int *cP = reinterpret_cast<int *>(cb), *cB = cP + kMaxCells + 1;
+    ColQueue q = q0;
+    q.list = reinterpret_cast<unsigned short *>(cP + kCellInts);
+    // and the element-pair index table [ne][ne] (binning reads it per pair)
+    constexpr int kListInts = 32 * kColQueue * (kMaxEngineThreads / 32) / 2, kPidxSmem = 256;
+    static_assert(sizeof(double) * kChunk >= sizeof(int) * (kCellInts + kListInts + kPidxSmem), "cb too small");
+    int *spidx = cP + kCellInts + kListInts;
+    const int nee = D.ne * D.ne;
+    const int *pidx = nee <= kPidxSmem ? spidx : D.pidx;
+    if (nee <= kPidxSmem)
+        for (int k = threadIdx.x; k < nee; k += blockDim.x) spidx[k] = D.pidx[k];
     if (threadIdx.x == 0) {
         // the previous item's reads of sA / sBq are ordered before this
         // item's bulk copies by the barrier at the item boundary
@@ -1252,11 +1281,11 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, 
         atomicAdd(&D.st->swept, (unsigned long long)ncol);
 #define FRMC_COLUMNS(G_, C_)                                                                           \
     switch (D.bm) {                                                                                    \
-    case BM_IBC: fused_columns<BM_IBC, G_, C_>(D, sdP, q.nz, s_tcount, g, q, ncol, cP, cB); break;     \
-    case BM_DIAG: fused_columns<BM_DIAG, G_, C_>(D, sdP, q.nz, s_tcount, g, q, ncol, cP, cB); break;   \
-    case BM_XYTRI: fused_columns<BM_XYTRI, G_, C_>(D, sdP, q.nz, s_tcount, g, q, ncol, cP, cB); break; \
-    case BM_LOWER: fused_columns<BM_LOWER, G_, C_>(D, sdP, q.nz, s_tcount, g, q, ncol, cP, cB); break; \
-    default: fused_columns<BM_GENERAL, G_, C_>(D, sdP, q.nz, s_tcount, g, q, ncol, cP, cB); break;     \
+    case BM_IBC: fused_columns<BM_IBC, G_, C_>(D, sdP, q.nz, s_tcount, g, q, ncol, cP, cB, pidx); break;     \
+    case BM_DIAG: fused_columns<BM_DIAG, G_, C_>(D, sdP, q.nz, s_tcount, g, q, ncol, cP, cB, pidx); break;   \
+    case BM_XYTRI: fused_columns<BM_XYTRI, G_, C_>(D, sdP, q.nz, s_tcount, g, q, ncol, cP, cB, pidx); break; \
+    case BM_LOWER: fused_columns<BM_LOWER, G_, C_>(D, sdP, q.nz, s_tcount, g, q, ncol, cP, cB, pidx); break; \
+    default: fused_columns<BM_GENERAL, G_, C_>(D, sdP, q.nz, s_tcount, g, q, ncol, cP, cB, pidx); break;     \
     }
     if (g.n == 1) {
         if (nc > 0) {
@@ -1274,11 +1303,11 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, 
 #undef FRMC_COLUMNS
     if (g.n > 1) {
         switch (D.bm) {
-        case BM_IBC: fused_group_internal<BM_IBC>(D, sdP, q.nz, s_tcount, g); break;
-        case BM_DIAG: fused_group_internal<BM_DIAG>(D, sdP, q.nz, s_tcount, g); break;
-        case BM_XYTRI: fused_group_internal<BM_XYTRI>(D, sdP, q.nz, s_tcount, g); break;
-        case BM_LOWER: fused_group_internal<BM_LOWER>(D, sdP, q.nz, s_tcount, g); break;
-        default: fused_group_internal<BM_GENERAL>(D, sdP, q.nz, s_tcount, g); break;
+        case BM_IBC: fused_group_internal<BM_IBC>(D, sdP, q.nz, s_tcount, g, pidx); break;
+        case BM_DIAG: fused_group_internal<BM_DIAG>(D, sdP, q.nz, s_tcount, g, pidx); break;
+        case BM_XYTRI: fused_group_internal<BM_XYTRI>(D, sdP, q.nz, s_tcount, g, pidx); break;
+        case BM_LOWER: fused_group_internal<BM_LOWER>(D, sdP, q.nz, s_tcount, g, pidx); break;
+        default: fused_group_internal<BM_GENERAL>(D, sdP, q.nz, s_tcount, g, pidx); break;
         }
     }
     __syncthreads();
@@ -1367,7 +1396,6 @@ __device__ void warm_item(const StepParams &p, long long idx)
     prefetch_l2(D.Bq);
 }
 
-constexpr int kMaxEngineThreads = 512;  // CTA size limit of the step kernels (128 registers per thread)
 
 template <bool FUSED>
 __global__ void __launch_bounds__(kMaxEngineThreads, 1) k_engine_step(StepParams p)
