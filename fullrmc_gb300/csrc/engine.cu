@@ -2437,60 +2437,73 @@ struct CellGrid {
     std::vector<int2> csl;
 };
 
+// Per-axis factors and smallest eigenvalue of the distance bound (see the
+// cell fields of EDesc): for a box, w_k = 1 / |column k of B^-1| (cmode 1)
+// or |B_kk| for an orthorhombic box (cmode 0); free boundaries: w = 1.
+// Returns false for a singular basis.
+static bool cell_metric(const float *basis, int bm, double w[3], double *lam, int *mode)
+{
+    w[0] = w[1] = w[2] = 1.0;
+    *lam = 0.0;
+    *mode = 0;
+    if (bm == BM_IBC)
+        return true;
+    double B[9];
+    for (int k = 0; k < 9; ++k) B[k] = basis[k];
+    if (bm == BM_DIAG) {
+        for (int k = 0; k < 3; ++k) w[k] = std::fabs(B[4 * k]);
+        return w[0] > 0.0 && w[1] > 0.0 && w[2] > 0.0;
+    }
+    *mode = 1;
+    // columns of B^-1 (box = real B^-1): |real| >= |box_k| / |column k|
+    const double c00 = B[4] * B[8] - B[5] * B[7], c01 = B[5] * B[6] - B[3] * B[8], c02 = B[3] * B[7] - B[4] * B[6];
+    const double det = B[0] * c00 + B[1] * c01 + B[2] * c02;
+    if (!(std::fabs(det) > 0.0))
+        return false;
+    double I[9];  // I[r*3 + c] = (B^-1)[r][c]
+    I[0] = c00 / det;
+    I[1] = (B[2] * B[7] - B[1] * B[8]) / det;
+    I[2] = (B[1] * B[5] - B[2] * B[4]) / det;
+    I[3] = c01 / det;
+    I[4] = (B[0] * B[8] - B[2] * B[6]) / det;
+    I[5] = (B[2] * B[3] - B[0] * B[5]) / det;
+    I[6] = c02 / det;
+    I[7] = (B[1] * B[6] - B[0] * B[7]) / det;
+    I[8] = (B[0] * B[4] - B[1] * B[3]) / det;
+    for (int k = 0; k < 3; ++k) w[k] = 1.0 / std::sqrt(I[k] * I[k] + I[3 + k] * I[3 + k] + I[6 + k] * I[6 + k]);
+    // smallest eigenvalue of M = B B^T (|real|^2 = box M box^T), by the
+    // trigonometric solution of the symmetric 3 x 3 eigenproblem
+    double M[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            M[3 * i + j] = B[3 * i] * B[3 * j] + B[3 * i + 1] * B[3 * j + 1] + B[3 * i + 2] * B[3 * j + 2];
+    const double p1 = M[1] * M[1] + M[2] * M[2] + M[5] * M[5];
+    double l;
+    if (p1 == 0.0) {
+        l = std::min(M[0], std::min(M[4], M[8]));
+    } else {
+        const double q = (M[0] + M[4] + M[8]) / 3.0;
+        const double p2 = (M[0] - q) * (M[0] - q) + (M[4] - q) * (M[4] - q) + (M[8] - q) * (M[8] - q) + 2 * p1;
+        const double pp = std::sqrt(p2 / 6.0);
+        double Q[9];
+        for (int k = 0; k < 9; ++k) Q[k] = (M[k] - (k % 4 == 0 ? q : 0.0)) / pp;
+        double r = 0.5 * (Q[0] * (Q[4] * Q[8] - Q[5] * Q[7]) - Q[1] * (Q[3] * Q[8] - Q[5] * Q[6]) +
+                          Q[2] * (Q[3] * Q[7] - Q[4] * Q[6]));
+        r = std::max(-1.0, std::min(1.0, r));
+        l = q + 2.0 * pp * std::cos(std::acos(r) / 3.0 + 2.0 * M_PI / 3.0);
+    }
+    *lam = std::max(0.0, 0.999 * l);
+    return true;
+}
+
 static void build_cells(const frmc_engine_spec &sp, int bm, CellGrid &G)
 {
     const int n = sp.n;
     const bool pbc = bm != BM_IBC;
-    double w[3] = {1.0, 1.0, 1.0}, lam = 0.0;
-    int mode = 0;
-    if (pbc) {
-        double B[9];
-        for (int k = 0; k < 9; ++k) B[k] = sp.basis[k];
-        if (bm == BM_DIAG) {
-            for (int k = 0; k < 3; ++k) w[k] = std::fabs(B[4 * k]);
-        } else {
-            mode = 1;
-            // columns of B^-1 (box = real B^-1): |real| >= |box_k| / |column k|
-            const double c00 = B[4] * B[8] - B[5] * B[7], c01 = B[5] * B[6] - B[3] * B[8],
-                         c02 = B[3] * B[7] - B[4] * B[6];
-            const double det = B[0] * c00 + B[1] * c01 + B[2] * c02;
-            if (!(std::fabs(det) > 0.0))
-                return;
-            double I[9];  // I[r*3 + c] = (B^-1)[r][c]
-            I[0] = c00 / det;
-            I[1] = (B[2] * B[7] - B[1] * B[8]) / det;
-            I[2] = (B[1] * B[5] - B[2] * B[4]) / det;
-            I[3] = c01 / det;
-            I[4] = (B[0] * B[8] - B[2] * B[6]) / det;
-            I[5] = (B[2] * B[3] - B[0] * B[5]) / det;
-            I[6] = c02 / det;
-            I[7] = (B[1] * B[6] - B[0] * B[7]) / det;
-            I[8] = (B[0] * B[4] - B[1] * B[3]) / det;
-            for (int k = 0; k < 3; ++k)
-                w[k] = 1.0 / std::sqrt(I[k] * I[k] + I[3 + k] * I[3 + k] + I[6 + k] * I[6 + k]);
-            // smallest eigenvalue of M = B B^T (|real|^2 = box M box^T), by
-            // the trigonometric solution of the symmetric 3 x 3 eigenproblem
-            double M[9];
-            for (int i = 0; i < 3; ++i)
-                for (int j = 0; j < 3; ++j)
-                    M[3 * i + j] = B[3 * i] * B[3 * j] + B[3 * i + 1] * B[3 * j + 1] + B[3 * i + 2] * B[3 * j + 2];
-            const double p1 = M[1] * M[1] + M[2] * M[2] + M[5] * M[5];
-            if (p1 == 0.0) {
-                lam = std::min(M[0], std::min(M[4], M[8]));
-            } else {
-                const double q = (M[0] + M[4] + M[8]) / 3.0;
-                const double p2 = (M[0] - q) * (M[0] - q) + (M[4] - q) * (M[4] - q) + (M[8] - q) * (M[8] - q) + 2 * p1;
-                const double pp = std::sqrt(p2 / 6.0);
-                double Q[9];
-                for (int k = 0; k < 9; ++k) Q[k] = (M[k] - (k % 4 == 0 ? q : 0.0)) / pp;
-                double r = 0.5 * (Q[0] * (Q[4] * Q[8] - Q[5] * Q[7]) - Q[1] * (Q[3] * Q[8] - Q[5] * Q[6]) +
-                                  Q[2] * (Q[3] * Q[7] - Q[4] * Q[6]));
-                r = std::max(-1.0, std::min(1.0, r));
-                lam = q + 2.0 * pp * std::cos(std::acos(r) / 3.0 + 2.0 * M_PI / 3.0);
-            }
-            lam = std::max(0.0, 0.999 * lam);
-        }
-    }
+    double w[3], lam;
+    int mode;
+    if (!cell_metric(sp.basis, bm, w, &lam, &mode))
+        return;
     double lo[3], hi[3];
     for (int k = 0; k < 3; ++k) {
         lo[k] = INFINITY;
@@ -3402,6 +3415,17 @@ int frmc_engines_coords(void *handle, int32_t e, float *box_coords, float *real_
             real_coords[3 * i + 2] = r[i].z;
         }
     }
+    return FRMC_OK;
+}
+
+int frmc_cell_metric(const float *basis, int32_t isPBC, double *w, double *lam, int32_t *mode)
+{
+    if (!basis || !w || !lam || !mode)
+        return set_error(FRMC_E_ARG, "cell_metric: null argument");
+    int m = 0;
+    if (!cell_metric(basis, isPBC ? basis_mode(basis, 1) : BM_IBC, w, lam, &m))
+        return set_error(FRMC_E_ARG, "cell_metric: singular basis");
+    *mode = m;
     return FRMC_OK;
 }
 

@@ -126,6 +126,12 @@ int frmc_engines_set_cells(void *handle, int32_t on);
  * only grow as atoms move; a long run with large moves can re-tighten them).
  * Results are unchanged. */
 int frmc_engines_regrid(void *handle, int32_t e);
+/* The column grids' distance bound for a basis (host only, no device use):
+ * w[k] and lam such that the reference's minimum-image distance of box
+ * difference g satisfies |g B| >= |g_k| w[k] and |g B|^2 >= lam |g|^2
+ * (mode 1), or |g B|^2 >= sum (g_k w[k])^2 (mode 0: orthorhombic box, or free
+ * boundaries with w = 1). */
+int frmc_cell_metric(const float *basis, int32_t isPBC, double *w, double *lam, int32_t *mode);
 int frmc_engines_cells(void *handle, int32_t e, int32_t *ncells, int64_t *swept);
 /* The S(Q) term's product y = T x runs as one fp16 GEMM over digits of T when
  * every element-pair delta of the step is at most `limit` in magnitude
