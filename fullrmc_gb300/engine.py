@@ -61,6 +61,7 @@ register("frmc_engines_set_mode", [_vp, ctypes.c_int])
 register("frmc_engines_set_cells", [_vp, ctypes.c_int32])
 register("frmc_engines_cells", [_vp, _i32, ctypes.POINTER(_i32), ctypes.POINTER(_i64)])
 register("frmc_engines_regrid", [_vp, _i32])
+register("frmc_cell_metric", [F32P, _i32, F64P, F64P, ctypes.POINTER(_i32)])
 register("frmc_engines_set_sq_gemm_limit", [_vp, ctypes.c_int32])
 register("frmc_engines_init", [_vp])
 register("frmc_engines_push_moves", [_vp, _i32, I32P, F32P, F32P, _i32, _i64, ctypes.c_int])
@@ -389,6 +390,18 @@ def footprint(system, move_cap):
     b = ctypes.c_int64()
     check(load().frmc_engine_footprint(ctypes.byref(sp), ctypes.byref(b)))
     return b.value
+
+
+def cell_metric(basis, isPBC):
+    """(w, lam, mode) of the column grids' distance bound for a basis (host
+    only): |g B| >= |g_k| w_k and |g B|^2 >= lam |g|^2 (mode 1), or
+    |g B|^2 >= sum (g_k w_k)^2 (mode 0)."""
+    B = np.ascontiguousarray(basis, F32)
+    w = np.empty(3, np.float64)
+    lam, mode = ctypes.c_double(), _i32()
+    check(load().frmc_cell_metric(B.ctypes.data_as(F32P), int(bool(isPBC)), w.ctypes.data_as(F64P),
+                                  ctypes.byref(lam), ctypes.byref(mode)))
+    return w, lam.value, mode.value
 
 
 class EngineSet:
