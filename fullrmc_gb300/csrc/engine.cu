@@ -172,6 +172,10 @@ struct EDesc {
     // perpendicular widths, clam2 the smallest eigenvalue of B B^T).
     int nc, cmode, cpbc;
     float cw[3], clam2, cthr2;
+    // one-CTA steps keep the element-pair deltas as biased 16-bit halves of
+    // 32-bit words (dpk = 1) when no delta can pass 32767 in magnitude
+    // (atoms x moved atoms + moved-atom pairs < 32000)
+    int dpk;
     float4 *cbox, *clo, *chi;
     int *cmol, *cstart;
     int2 *csl;
@@ -188,7 +192,7 @@ struct EDesc {
 struct ColView {
     Basis B;
     float s_lo, s_hi, minD, binw;
-    int n, ne, hs;
+    int n, ne, hs, dpk;
     long long total;
     const float4 *__restrict__ box;
     const int *__restrict__ mol;
@@ -207,6 +211,7 @@ __device__ __forceinline__ ColView col_view(const EDesc &D)
     v.n = D.n;
     v.ne = D.ne;
     v.hs = D.hs;
+    v.dpk = D.dpk;
     v.total = D.total;
     v.box = D.box;
     v.mol = D.mol;
@@ -622,6 +627,15 @@ constexpr int kSqGemmMaxDelta = 32;
 // an S(Q) term, also keep S in the global Sb (zero for unchanged bins).
 // pair_coef_p * v for |v| <= 4 comes from a small table, so a changed bin
 // costs one FP64 add per non-zero element-pair delta.
+// Element-pair delta idx of a CTA's shared deltas (either layout).
+__device__ __forceinline__ int delta_get(const int *sdP, int idx, int dpk)
+{
+    if (dpk)
+        return (int)((reinterpret_cast<const unsigned *>(sdP)[idx >> 1] >> ((unsigned)(idx & 1) << 4)) & 0xffffu) -
+               32768;
+    return sdP[idx];
+}
+
 template <bool SMEM>
 __device__ double eval_delta(const EDesc &Dg, int *dP, const double *Ab, const double *Bqb, double *red, double *cb,
                              double *sbs, int *sbin, int *s_nchg, double *coef, const int *nz)
@@ -656,8 +670,9 @@ __device__ double eval_delta(const EDesc &Dg, int *dP, const double *Ab, const d
     __syncthreads();
     const bool big = hs > kChunk;
     const unsigned lane = threadIdx.x & 31u;
+    const int dpk = Dg.dpk;
     auto delta_at = [&](int q, int b) -> int {
-        return SMEM ? dP[q * hs + b] : __ldcg(dP + (long long)q * hs + b);
+        return SMEM ? delta_get(dP, q * hs + b, dpk) : __ldcg(dP + (long long)q * hs + b);
     };
     for (int c0 = 0; c0 < hs; c0 += kChunk) {
         const int cn = min(kChunk, hs - c0);
@@ -793,9 +808,18 @@ __device__ __forceinline__ void group_pair_bins(const V &D, const MovedGroup &g,
 // One +-1 on the shared element-pair delta at (pair row idx - b, bin b), and
 // the bin's count of non-zero deltas kept exact: the thread that moves a delta
 // away from zero adds one, the thread that brings it back removes one.
-__device__ __forceinline__ void delta_add(int *sdP, int *nz, int idx, int b, int v)
+__device__ __forceinline__ void delta_add(int *sdP, int *nz, int idx, int b, int v, int dpk)
 {
-    const int old = atomicAdd(sdP + idx, v);
+    int old;
+    if (dpk) {
+        // delta idx is the half (idx & 1) of word idx >> 1, stored + 32768, so
+        // adding v << 16 or v never carries or borrows across the halves
+        const unsigned sh = (unsigned)(idx & 1) << 4;
+        const unsigned w = atomicAdd(reinterpret_cast<unsigned *>(sdP) + (idx >> 1), (unsigned)v << sh);
+        old = (int)((w >> sh) & 0xffffu) - 32768;
+    } else {
+        old = atomicAdd(sdP + idx, v);
+    }
     if (old == 0)
         atomicAdd(nz + b, 1);
     else if (old + v == 0)
@@ -822,14 +846,14 @@ __device__ void fused_group_internal(const EDesc &Dg, int *sdP, int *nz, unsigne
             int p, bb;
             pair_of_flat(D, f0, ela, elj, b0, p, bb);
             if (p >= 0)
-                delta_add(sdP, nz, p * D.hs + bb, bb, -1);
+                delta_add(sdP, nz, p * D.hs + bb, bb, -1, D.dpk);
         }
         if (f1 >= 0) {
             D.tlist[pos] = ((half + f1) << 1) | 1;
             int p, bb;
             pair_of_flat(D, f1, ela, elj, b1, p, bb);
             if (p >= 0)
-                delta_add(sdP, nz, p * D.hs + bb, bb, 1);
+                delta_add(sdP, nz, p * D.hs + bb, bb, 1, D.dpk);
         }
     }
 }
@@ -970,6 +994,22 @@ __device__ void finish_engine(const EDesc &D, const MovedGroup &g, double *red, 
 // per thread, entry k of thread t at [k * blockDim + t] (conflict-free).
 constexpr int kColQueue = 8;
 constexpr int kMaxEngineThreads = 512;  // CTA size limit of the step kernels (128 registers per thread)
+// The one-CTA step keeps the column grid's prefix and bases, the warps'
+// packed queue lists and the element-pair index table in the evaluation
+// scratch cb until the evaluation: ints at [0, kCellInts), the lists, then
+// kPidxSmem ints.
+constexpr int kCellInts = 2 * kMaxCells + 34, kPidxSmem = 256;
+__host__ __device__ constexpr int list_ints(int threads) { return 32 * kColQueue * (threads / 32) / 2; }
+// Doubles of the one-CTA step's evaluation scratch cb (and bins of sbs /
+// sbin): the changed bins of one chunk, at least the cell, list and table
+// ints above.
+__host__ __device__ constexpr int fused_bins_cap(int fused_bins) { return fused_bins < kChunk ? fused_bins : kChunk; }
+__host__ __device__ constexpr int fused_cb_cap(int fused_bins, int threads)
+{
+    return fused_bins_cap(fused_bins) > (kCellInts + list_ints(threads) + kPidxSmem + 1) / 2
+               ? fused_bins_cap(fused_bins)
+               : (kCellInts + list_ints(threads) + kPidxSmem + 1) / 2;
+}
 
 struct ColQueue {
     float *s0, *s1;   // squared distances before / after the move
@@ -1026,14 +1066,14 @@ __device__ __forceinline__ void flush_columns(const ColView &D, const MovedGroup
                 int p, bb;
                 pair_of_flat(D, f0, ela, elj, b0, p, bb);
                 if (p >= 0)
-                    delta_add(sdP, nz, p * D.hs + bb, bb, -1);
+                    delta_add(sdP, nz, p * D.hs + bb, bb, -1, D.dpk);
             }
             if (f1 >= 0) {
                 D.tlist[pos] = (int)(((half + f1) << 1) | 1);
                 int p, bb;
                 pair_of_flat(D, f1, ela, elj, b1, p, bb);
                 if (p >= 0)
-                    delta_add(sdP, nz, p * D.hs + bb, bb, 1);
+                    delta_add(sdP, nz, p * D.hs + bb, bb, 1, D.dpk);
             }
         }
     }
@@ -1235,16 +1275,15 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, 
                              double *coef, int *s_flag, unsigned *s_tcount, MovedGroup &g, const ColQueue &q0,
                              const EMove *hm, EResult *hr)
 {
-    // the column grid's prefix and bases, and the warps' packed queue lists,
-    // live in cb until the evaluation
-    constexpr int kCellInts = 2 * kMaxCells + 34;
+    // the column grid's prefix and bases, the warps' packed queue lists and
+    // the element-pair index table (binning reads it per pair) live in cb
+    // until the evaluation
+    static_assert(sizeof(double) * kChunk >= sizeof(int) * (kCellInts + list_ints(kMaxEngineThreads) + kPidxSmem),
+                  "cb too small");
     int *cP = reinterpret_cast<int *>(cb), *cB = cP + kMaxCells + 1;
     ColQueue q = q0;
     q.list = reinterpret_cast<unsigned short *>(cP + kCellInts);
-    // and the element-pair index table [ne][ne] (binning reads it per pair)
-    constexpr int kListInts = 32 * kColQueue * (kMaxEngineThreads / 32) / 2, kPidxSmem = 256;
-    static_assert(sizeof(double) * kChunk >= sizeof(int) * (kCellInts + kListInts + kPidxSmem), "cb too small");
-    int *spidx = cP + kCellInts + kListInts;
+    int *spidx = cP + kCellInts + list_ints(blockDim.x);
     const int nee = D.ne * D.ne;
     const int *pidx = nee <= kPidxSmem ? spidx : D.pidx;
     if (nee <= kPidxSmem)
@@ -1272,7 +1311,12 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, 
     load_moved_group(D, D.st->step, g, hm);
     const int np = D.npairs;
     const int nph = np * D.hs;
-    for (int k = threadIdx.x; k < nph; k += blockDim.x) sdP[k] = 0;
+    if (D.dpk) {
+        const int words = (nph + 1) >> 1;
+        for (int k = threadIdx.x; k < words; k += blockDim.x) sdP[k] = (int)0x80008000u;
+    } else {
+        for (int k = threadIdx.x; k < nph; k += blockDim.x) sdP[k] = 0;
+    }
     for (int k = threadIdx.x; k < D.hs; k += blockDim.x) q.nz[k] = 0;
     for (int qq = threadIdx.x; qq < np; qq += blockDim.x) coef[qq] = D.pc[qq];
     __syncthreads();
@@ -1401,9 +1445,13 @@ template <bool FUSED>
 __global__ void __launch_bounds__(kMaxEngineThreads, 1) k_engine_step(StepParams p)
 {
     __shared__ double red[kRedLanes];
-    __shared__ double cb[kChunk];
-    __shared__ double sbs[kChunk];
-    __shared__ int sbin[kChunk];
+    // the evaluation scratch: static for tile-split steps, in the dynamic
+    // layout (sized by the launch's bins) for one-CTA steps
+    __shared__ double cb_s[FUSED ? 1 : kChunk];
+    __shared__ double sbs_s[FUSED ? 1 : kChunk];
+    __shared__ int sbin_s[FUSED ? 1 : kChunk];
+    double *cb = cb_s, *sbs = sbs_s;
+    int *sbin = sbin_s;
     __shared__ int s_nchg;
     __shared__ double coef[64];
     __shared__ MovedGroup s_group;
@@ -1423,6 +1471,9 @@ __global__ void __launch_bounds__(kMaxEngineThreads, 1) k_engine_step(StepParams
         cq.s1 = cq.s0 + kColQueue * blockDim.x;
         cq.info = reinterpret_cast<unsigned *>(cq.s1 + kColQueue * blockDim.x);
         cq.nz = reinterpret_cast<int *>(cq.info + kColQueue * blockDim.x);
+        cb = reinterpret_cast<double *>(cq.nz + p.fused_bins);  // fused_bins is even: 8-byte aligned
+        sbs = cb + fused_cb_cap(p.fused_bins, blockDim.x);
+        sbin = reinterpret_cast<int *>(sbs + fused_bins_cap(p.fused_bins));
         if (threadIdx.x == 0) {
             mbar_init(&s_bar, 1);
             mbar_fence_init();
@@ -1915,7 +1966,18 @@ struct SqTable {
     int ncols = 0, cap = 0;
 };
 
-constexpr int kFusedSmemMax = 135 * 1024;  // element-pair deltas, A and Bq of a fused step (the column queue comes on top)
+// dynamic shared memory of a one-CTA step at the largest CTA (the static
+// part, about 4 KB, comes on top of it within the 227 KB an SM offers)
+constexpr long long kFusedDynMax = 221 * 1024;
+
+// Dynamic shared memory of a one-CTA step: element-pair deltas, A and Bq,
+// the column queue, the per-bin non-zero counts, the evaluation scratch.
+static long long fused_dyn_bytes(long long dp_ints, int bins, int threads)
+{
+    return 4 * dp_ints + 16ll * bins + (long long)kColQueue * threads * 12 + 4ll * bins +
+           8ll * fused_cb_cap(bins, threads) + 12ll * fused_bins_cap(bins);
+}
+
 constexpr long long kFusedMaxCost = 49152;  // engines of a higher step cost (Slot::cost) are split over several CTAs
 constexpr long long kSoloFusedCost = 16384;  // one-engine steps up to this cost use the fused item
 
@@ -1923,7 +1985,6 @@ struct EngineSet {
     std::vector<Slot> slots;
     int fused = 1;         // batched steps use one CTA per engine where it fits
     int cells = 1;         // engines added from now on get a column grid where it pays
-    int fused_smem = 0;    // dynamic shared memory of batched launches
     int fused_dp_ints = 0; // its layout: element-pair deltas (ints), then A and Bq (fused_bins doubles each)
     int fused_bins = 0;
     int nsolo = 0;         // items [0, nsolo): tiles of every engine (one-engine steps)
@@ -1933,7 +1994,7 @@ struct EngineSet {
     std::vector<int> item_first;  // per engine id: first item (or -1)
     std::vector<int> item_count;
     std::vector<int> fused_item;  // per engine id: its one-CTA item in the batched list (or -1)
-    int tile = 1024, threads = 512, ctas_per_sm = 1;  // the usual autotuner choice on GB300
+    int tile = 1024, threads = 256, ctas_per_sm = 2;  // the usual autotuner choice on GB300
     EDesc *ddesc = nullptr;
     int ddesc_cap = 0;
     EDesc *fdesc = nullptr;        // descriptors of the fused items, in work-list order
@@ -2095,18 +2156,18 @@ static int refresh(EngineSet *s)
     s->nsolo = (int)items.size();
     // batched list: fused engines costliest first, then the tiles of the others
     std::vector<int> fused_ids;
-    s->fused_smem = 0;
     s->fused_dp_ints = 0;
     s->fused_bins = 0;
     for (int id : s->live) {
         const EDesc &D = s->slots[id].d;
-        const int dp = (D.npairs * D.hs + 3) & ~3, bins = (D.hs + 1) & ~1;
+        const int dpw = D.dpk ? (D.npairs * D.hs + 1) / 2 : D.npairs * D.hs;  // words of the deltas
+        const int dp = (dpw + 3) & ~3, bins = (D.hs + 1) & ~1;
         const int dpi = std::max(s->fused_dp_ints, dp), bi = std::max(s->fused_bins, bins);
-        if (s->fused && 4ll * dpi + 20ll * bi <= kFusedSmemMax && s->slots[id].cost <= kFusedMaxCost) {
+        if (s->fused && fused_dyn_bytes(dpi, bi, kMaxEngineThreads) <= kFusedDynMax &&
+            s->slots[id].cost <= kFusedMaxCost) {
             fused_ids.push_back(id);
             s->fused_dp_ints = dpi;
             s->fused_bins = bi;
-            s->fused_smem = 4 * dpi + 16 * bi;
         }
     }
     std::stable_sort(fused_ids.begin(), fused_ids.end(),
@@ -2261,8 +2322,10 @@ static int refresh(EngineSet *s)
 
 static int launch_items(EngineSet *s, const int2 *items, int count, int eval_only, cudaStream_t st,
                         int dyn_smem = 0, bool fused = false, const EMove *hmoves = nullptr,
-                        EResult *hres = nullptr)
+                        EResult *hres = nullptr, int threads = 0)
 {
+    if (threads <= 0)
+        threads = s->threads;
     Context *c;
     FRMC_TRY(get_context(&c));
     int grid = c->sms * s->ctas_per_sm;
@@ -2281,9 +2344,12 @@ static int launch_items(EngineSet *s, const int2 *items, int count, int eval_onl
     }
     if (fused) {
         FRMC_CUDA(cudaFuncSetAttribute(k_engine_step<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem));
-        k_engine_step<true><<<grid, s->threads, dyn_smem, st>>>(p);
+        // all shared memory: two CTAs of 256 threads fit one SM where their layouts do
+        FRMC_CUDA(cudaFuncSetAttribute(k_engine_step<true>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                       (int)cudaSharedmemCarveoutMaxShared));
+        k_engine_step<true><<<grid, threads, dyn_smem, st>>>(p);
     } else {
-        k_engine_step<false><<<grid, s->threads, 0, st>>>(p);
+        k_engine_step<false><<<grid, threads, 0, st>>>(p);
     }
     FRMC_CUDA(cudaGetLastError());
     return FRMC_OK;
@@ -2341,7 +2407,7 @@ static int launch_sq(EngineSet *s, int first, int count, cudaStream_t st, int en
 // column queue and the per-bin non-zero counts.
 static int fused_dyn_smem(const EngineSet *s)
 {
-    return s->fused_smem + kColQueue * s->threads * 12 + 4 * s->fused_bins;
+    return (int)fused_dyn_bytes(s->fused_dp_ints, s->fused_bins, s->threads);
 }
 
 // The batched work list (every live engine advances one step): the fused
@@ -2651,6 +2717,10 @@ static int add_engine(EngineSet *s, const frmc_engine_spec &sp, int *out_id)
     D.var2 = sp.variance_squared;
     D.tol = sp.tolerance;
     D.has_dw = sp.data_weights ? 1 : 0;
+    {
+        const long long G = spec_group(sp);
+        D.dpk = (long long)sp.n * G + G * G < 32000 ? 1 : 0;
+    }
     D.box = (float4 *)(b + L.box);
     D.real = (float4 *)(b + L.real);
     D.mol = (int *)(b + L.mol);
@@ -3139,9 +3209,13 @@ int frmc_engines_step(void *handle, int32_t engine, int32_t steps, int use_graph
             return launch_batched(s, sx);
         const int fi = s->fused_item[engine];
         if (fi >= 0 && s->slots[engine].cost <= kSoloFusedCost)  // one CTA beats tiles plus a finisher
-            FRMC_TRY(launch_items(s, s->items + fi, 1, 0, sx, fused_dyn_smem(s), true));
+            // one engine alone: the largest CTA (its layout fits by the fused check)
+            FRMC_TRY(launch_items(s, s->items + fi, 1, 0, sx,
+                                  (int)fused_dyn_bytes(s->fused_dp_ints, s->fused_bins, kMaxEngineThreads), true,
+                                  nullptr, nullptr, kMaxEngineThreads));
         else
-            FRMC_TRY(launch_items(s, s->items + s->item_first[engine], count, 0, sx));
+            FRMC_TRY(launch_items(s, s->items + s->item_first[engine], count, 0, sx, 0, false, nullptr, nullptr,
+                                  kMaxEngineThreads));
         return launch_sq(s, s->sq_first[engine], s->sq_count[engine], sx, engine);
     };
     if (!use_graph) {

@@ -539,7 +539,7 @@ class EngineSet:
         the dense integer loop (all three give the same integers)."""
         check(load().frmc_engines_set_sq_gemm_limit(self.handle, int(limit)))
 
-    TUNE_CANDIDATES = ((1024, 512, 1), (2048, 512, 1), (1024, 384, 1), (1024, 256, 2), (512, 128, 4),
+    TUNE_CANDIDATES = ((1024, 256, 2), (1024, 512, 1), (2048, 512, 1), (1024, 384, 1), (512, 128, 4),
                        (1024, 256, 4), (2048, 256, 2))
 
     def autotune(self, candidates=None, steps=6, warmup=2):

@@ -315,7 +315,10 @@ def benchmark_stream(seconds, wall_limit, seed=0, rate=20.0, budget_gib=16, plai
     for i, t in enumerate(arr):
         system, steps = synthetic.serving_fit(seed * 100000 + i)
         reqs.append(FitRequest(i, system, steps, seed=seed * 100000 + i, arrival=t))
-    es = EngineSet([], move_cap=cap)
+    # fits average 44,000 atoms (up to 200,000): 512-thread CTAs, one per SM
+    # (two 256-thread CTAs per SM pay off for the smaller engines of the
+    # batching workload)
+    es = EngineSet([], move_cap=cap, tune=(1024, 512, 1))
     srv = Server(es, lambda s: footprint(s, cap), budget_gib << 30, max_k=32)
     # warm the kernels and the shared S(Q) table outside the timed stream
     warm = Server(es, lambda s: footprint(s, cap), budget_gib << 30, max_k=32)
