@@ -307,13 +307,15 @@ def _call_ms(fn, reps, budget_s=None):
 
 
 def bench_dropins(with_cpu):
-    """Per-call times of the atomic_distances, atomic_coordination and shape-function paths
-    through their Python API (host arrays in and out), beside fullrmc's Cython
-    (ncores=1) on the same call: the constraints' per-move call (the 13 atoms
-    of a moved ring) and the full recomputation, on the 52,000-atom molecular
-    system (three species, 13-atom rings)."""
+    """Per-call times of the pairs_histograms, atomic_distances,
+    atomic_coordination and shape-function paths through their Python API
+    (host arrays in and out), beside fullrmc's Cython (ncores=1) on the same
+    call: the constraints' per-move call (one atom of the 5,000-atom alloy,
+    or the 13 atoms of a moved ring) and the full recomputation, on the
+    52,000-atom molecular system (three species, 13-atom rings)."""
     from fullrmc_gb300 import atomic_coordination as gac
     from fullrmc_gb300 import atomic_distances as gad
+    from fullrmc_gb300 import pairs_histograms as gph
     from fullrmc_gb300 import synthetic
     s = synthetic.ring_molecules(seed=0, nmol=4000)
     c, B, el, mol = s.box_coords, s.basis, s.el.astype(np.int32), s.mol.astype(np.int32)
@@ -340,8 +342,23 @@ def bench_dropins(with_cpu):
     L = (cores, shells, lower, upper, asCore, inShell)
     data = np.zeros(len(defs), np.float32)
 
-    def cases(ad, ac):
+    s5 = synthetic.alloy_5000(seed=0)
+    m5 = s5.model
+    h5 = dict(boxCoords=s5.box_coords, basis=s5.basis, isPBC=True, moleculeIndex=s5.mol.astype(np.int32),
+              elementIndex=s5.el.astype(np.int32), numberOfElements=len(m5.elements_count),
+              minDistance=np.float32(m5.minDistance), maxDistance=np.float32(m5.maxDistance),
+              bin=np.float32(m5.bin), histSize=int(m5.hs))
+    hg = dict(boxCoords=c, basis=B, isPBC=True, moleculeIndex=mol, elementIndex=el, numberOfElements=ne,
+              minDistance=np.float32(-0.005), maxDistance=np.float32(15.005), bin=np.float32(0.01), histSize=1501)
+    one = np.array([1234], np.int32)
+
+    def cases(ad, ac, ph):
         return {
+            # the PDF constraint's per-move histogram (fullrmc calls it for the
+            # moved atoms before and after each move): one atom of the 5,000-atom
+            # alloy, and a 13-atom ring of the 52,000-atom molecular system
+            "pairs_histograms_move_5000": (lambda: ph.multiple_pairs_histograms_coords(one, **h5), 50),
+            "pairs_histograms_group_52000": (lambda: ph.multiple_pairs_histograms_coords(group, **hg), 50),
             "intermolecular_distances_move": (lambda: ad.multiple_atomic_distances_coords(
                 group, c, B, True, mol, el, ne, lo, up, intraMolecular=False, countWithinLimits=True), 50),
             "intermolecular_distances_full_20000": (lambda: ad.full_atomic_distances_coords(
@@ -370,16 +387,18 @@ def bench_dropins(with_cpu):
                                                    **sgrid), 5)
     out["shape_function_100000"] = {"gpu_ms": ms, "atoms": int(cl.shape[0]),
                                     "pairs": int(cl.shape[0]) * (int(cl.shape[0]) - 1) // 2}
-    for name, (fn, reps) in cases(gad, gac).items():
+    for name, (fn, reps) in cases(gad, gac, gph).items():
         ms, _ = _call_ms(fn, reps)
-        out[name] = {"gpu_ms": ms, "atoms": sub if name.endswith("20000") else n,
-                     "atoms_per_call": 13 if name.endswith("move") else (sub if "20000" in name else n)}
+        atoms = 5000 if name.endswith("_5000") else (sub if name.endswith("20000") else n)
+        per = 1 if name.endswith("move_5000") else (13 if ("move" in name or "group" in name) else atoms)
+        out[name] = {"gpu_ms": ms, "atoms": atoms, "atoms_per_call": per}
     if with_cpu:
         try:
             sys.path.insert(0, os.path.join(ROOT, "oracle"))
             import build_ref
             R = build_ref.import_reference()
-            for name, (fn, reps) in cases(R["atomic_distances"], R["atomic_coordination"]).items():
+            for name, (fn, reps) in cases(R["atomic_distances"], R["atomic_coordination"],
+                                          R["pairs_histograms"]).items():
                 if name == "coordination_all_atoms":
                     # the same call on the first 2,000 atoms, scaled to all atoms
                     # (the reference loops over atoms in Python)
