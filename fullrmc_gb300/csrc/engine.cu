@@ -981,15 +981,16 @@ __device__ void finish_engine(const EDesc &D, const MovedGroup &g, double *red, 
 }
 
 // Fused path: one CTA advances one engine by one step.  The element-pair
-// deltas live in this CTA's shared memory (sdP, npairs * hs ints), changes are
-// listed as (oriented bin, sign) in the engine's touched list, and an accepted
-// move is committed with fire-and-forget atomics on the counts.  No other CTA
-// touches the engine during the step, so there is no cross-CTA hand-off.
+// deltas live in this CTA's shared memory (sdP: npairs * hs ints, or biased
+// 16-bit halves of words), changes are listed as (oriented bin, sign) in the
+// engine's touched list, and an accepted move is committed with
+// fire-and-forget atomics on the counts.  No other CTA touches the engine
+// during the step, so there is no cross-CTA hand-off.
 // Columns of the fused path.  Batches of kItemUnroll * blockDim columns are
 // software-pipelined: the next batch's coordinates are loaded before the
-// current batch is binned against each moved atom, and each warp reserves the
-// batch's touched-list entries with one shared-memory atomic.  Columns that
-// belong to the moved group are left to group_internal (fullrmc's M - F).
+// current batch's squared distances are taken against each moved atom; the
+// columns in range go to a per-thread queue that whole warps bin.  Columns
+// that belong to the moved group are left to group_internal (fullrmc's M - F).
 // Per-thread queue of accepted columns in the fused path: kColQueue entries
 // per thread, entry k of thread t at [k * blockDim + t] (conflict-free).
 constexpr int kColQueue = 8;
