@@ -154,13 +154,23 @@ static int full_counts(Context *c, int64_t n, const float *basis, int isPBC, int
                             &tn, c->stream);
 }
 
-static int prepare_counts(Context *c, int64_t total)
+// Zeroed counts for a call (skipping the memset where the previous call's
+// conversion left them zero) and, unless the call's kernels never set it, a
+// zero device status word.
+static int prepare_counts(Context *c, int64_t total, bool status = true)
 {
-    TRY(c->buf[BUF_COUNTS].ensure(2 * total * 4 + 16));
-    TRY(c->buf[BUF_OUT].ensure(2 * total * 4 + 16));
+    const size_t need = 2 * (size_t)total * 4;
+    const void *before = c->buf[BUF_COUNTS].p;
+    TRY(c->buf[BUF_COUNTS].ensure(need + 16));
+    if (c->buf[BUF_COUNTS].p != before)
+        c->counts_clean = 0;
+    TRY(c->buf[BUF_OUT].ensure(need + 16));
     TRY(c->buf[BUF_STATUS].ensure(16));
-    FRMC_CUDA(cudaMemsetAsync(c->buf[BUF_COUNTS].p, 0, 2 * total * 4, c->stream));
-    FRMC_CUDA(cudaMemsetAsync(c->buf[BUF_STATUS].p, 0, 4, c->stream));
+    if (c->counts_clean < need)
+        FRMC_CUDA(cudaMemsetAsync(c->buf[BUF_COUNTS].p, 0, need, c->stream));
+    c->counts_clean = 0;  // in use until a conversion resets them
+    if (status)
+        FRMC_CUDA(cudaMemsetAsync(c->buf[BUF_STATUS].p, 0, 4, c->stream));
     return FRMC_OK;
 }
 
@@ -189,6 +199,22 @@ static int counts_out(Context *c, int64_t total, const float *h0intra, const flo
     if (status)
         return set_error(FRMC_E_TIMEOUT, "device wait gave up (status 0x%x)", status);
     return FRMC_OK;
+}
+
+// Host-buffer calls with at most this many rows read the caller's arrays
+// directly where the device accesses pageable memory (each row reads every
+// column once, so a few rows cost less than a copy).
+constexpr int64_t kDirectRows = 4;
+
+// counts_out for pageable-access devices after kernels without device waits
+// (no status to read): one conversion kernel writes the caller's float32
+// histograms directly and leaves the counts zero for the next call.
+static int counts_out_direct(Context *c, int64_t total, float *hintra, float *hinter)
+{
+    unsigned *cnt = c->buf[BUF_COUNTS].as<unsigned>();
+    TRY(launch_counts_pair_to_f32_zero(cnt, total, hintra, hinter, c->stream));
+    c->counts_clean = 2 * (size_t)total * 4;
+    return finish(c);
 }
 
 }  // namespace frmc
@@ -504,11 +530,20 @@ int frmc_multiple_pairs_histograms_coords(const int32_t *indexes, int64_t K, con
     }
     const float *B = isPBC ? basis : kIdentity;
     LOCKED_CTX(c);
+    const bool direct = c->pageable && K <= kDirectRows;
+    TRY(prepare_counts(c, total, !direct));  // the row kernels have no device waits
+    unsigned *cnt = c->buf[BUF_COUNTS].as<unsigned>();
+    if (direct) {
+        // the per-move call (fullrmc's moved atoms, PairDistributionConstraints.py:1016-1026):
+        // the kernels read the caller's arrays and write its histograms in place
+        TRY(launch_rows_hist(boxCoords, elementIndex, moleculeIndex, (int)n, indexes, (int)K, allAtoms,
+                             basis_mode(B, isPBC), make_basis(B), minDistance, maxDistance, bin, ne, hs, cnt,
+                             cnt + total, c->stream));
+        return counts_out_direct(c, total, hintra, hinter);
+    }
     TRY(upload_atoms(c, boxCoords, moleculeIndex, elementIndex, n));
-    TRY(prepare_counts(c, total));
     TRY(c->buf[BUF_ROWS].ensure(K * 4 + 16));
     TRY(h2d(c->buf[BUF_ROWS].p, indexes, K * 4, c->stream));
-    unsigned *cnt = c->buf[BUF_COUNTS].as<unsigned>();
     TRY(launch_rows_hist(c->buf[BUF_COORDS].as<float>(), c->buf[BUF_EL].as<int>(), c->buf[BUF_MOL].as<int>(), (int)n,
                          c->buf[BUF_ROWS].as<int>(), (int)K, allAtoms, basis_mode(B, isPBC), make_basis(B),
                          minDistance, maxDistance, bin, ne, hs, cnt, cnt + total, c->stream));

@@ -75,6 +75,12 @@ struct Context {
     int device = -1;
     int sms = 0;
     int max_smem_optin = 0;
+    // the device reads and writes pageable host memory coherently
+    // (cudaDevAttrPageableMemoryAccess, e.g. through NVLink-C2C on Grace):
+    // small host-buffer calls then pass the caller's arrays to the kernels
+    // instead of copying them (FRMC_HOST_DIRECT=0 turns this off)
+    int pageable = 0;
+    size_t counts_clean = 0;  // leading bytes of BUF_COUNTS known to be zero
     cudaStream_t stream = nullptr;
     std::mutex mu;  // serialises host-buffer entry points on this device
     DevBuf buf[BUF_COUNT_];
@@ -135,6 +141,7 @@ int launch_dists_hist(const float *dists, int n, int K, const int *rows, const i
                       unsigned *inter, cudaStream_t st);
 
 // out[k] = h0[k] + 1.0f added counts[k] times in float32 (h0 may be null = 0).
+int launch_counts_pair_to_f32_zero(unsigned *counts, int64_t total, float *out0, float *out1, cudaStream_t st);
 int launch_counts_to_f32(const unsigned *counts, const float *h0, float *out, int64_t total, cudaStream_t st);
 
 // Atomic distance constraint sums (atomic_kernels.cu): rows (device, K atom

@@ -582,6 +582,38 @@ int launch_dists_hist(const float *dists, int n, int K, const int *rows, const i
     return FRMC_OK;
 }
 
+// Both histograms of fresh counts (no starting values: a count c becomes
+// min(c, 2^24) as float32, as sequential float32 additions of 1.0 from zero
+// give) into two separate outputs, and the counts reset to zero for the next
+// call.
+__global__ void k_counts_pair_to_f32_zero(unsigned *__restrict__ counts, long long total, float *__restrict__ out0,
+                                          float *__restrict__ out1)
+{
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < 2 * total;
+         k += (long long)gridDim.x * blockDim.x) {
+        const unsigned c = counts[k];
+        const float h = c >= 16777216u ? 16777216.0f : (float)c;
+        if (k < total)
+            out0[k] = h;
+        else
+            out1[k - total] = h;
+        if (c)
+            counts[k] = 0u;
+    }
+}
+
+int launch_counts_pair_to_f32_zero(unsigned *counts, int64_t total, float *out0, float *out1, cudaStream_t st)
+{
+    if (total <= 0)
+        return FRMC_OK;
+    long long blocks = (2 * total + 255) / 256;
+    if (blocks > 4096)
+        blocks = 4096;
+    k_counts_pair_to_f32_zero<<<(int)blocks, 256, 0, st>>>(counts, total, out0, out1);
+    FRMC_CUDA(cudaGetLastError());
+    return FRMC_OK;
+}
+
 int launch_counts_to_f32(const unsigned *counts, const float *h0, float *out, int64_t total, cudaStream_t st)
 {
     if (total <= 0)

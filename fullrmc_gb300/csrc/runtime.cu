@@ -4,6 +4,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <cstdlib>
 #include <map>
 
 #include "frmc_runtime.h"
@@ -73,6 +74,15 @@ int get_context(Context **out)
     c->device = dev;
     FRMC_CUDA(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, dev));
     FRMC_CUDA(cudaDeviceGetAttribute(&c->max_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
+            cudaGetLastError();
+            v = 0;
+        }
+        const char *env = std::getenv("FRMC_HOST_DIRECT");
+        c->pageable = (v == 1 && !(env && env[0] == '0')) ? 1 : 0;
+    }
     FRMC_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     g_ctx[dev] = c;
     *out = c;
