@@ -202,9 +202,9 @@ static int counts_out(Context *c, int64_t total, const float *h0intra, const flo
 }
 
 // Host-buffer calls with at most this many rows read the caller's arrays
-// directly where the device accesses pageable memory (each row reads every
-// column once, so a few rows cost less than a copy).
-constexpr int64_t kDirectRows = 4;
+// directly where the device accesses pageable memory: the row kernel reads
+// every column once per 64 rows, so up to 64 rows read no more than a copy.
+constexpr int64_t kDirectRows = 64;
 
 // counts_out for pageable-access devices after kernels without device waits
 // (no status to read): one conversion kernel writes the caller's float32
