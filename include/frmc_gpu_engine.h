@@ -89,9 +89,9 @@ int frmc_engines_sq(void *handle, int32_t e, double *sq);
  * sd_sq of the S(Q) term (0 without one); chi2 = sd / variance_squared +
  * sd_sq / sq_variance_squared. */
 int frmc_engines_terms(void *handle, int32_t e, double *sd, double *sd_sq);
-/* Device bytes one engine of this spec occupies (its state, tables and rings,
- * and with an S(Q) term its share of the table's GEMM delta and product
- * buffers; the shared S(Q) table itself is not included). */
+/* Device bytes one engine of this spec occupies (its state, tables, rings and
+ * column grid, and with an S(Q) term its share of the table's GEMM delta and
+ * product buffers; the shared S(Q) table itself is not included). */
 int frmc_engine_footprint(const frmc_engine_spec *spec, int64_t *bytes);
 /* An empty engine set on the current device. */
 int frmc_engines_new(void **handle);
