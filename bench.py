@@ -604,10 +604,10 @@ def run_ours(args):
     grid_engines = sum(1 for e in range(E) if es.cells(e) > 0)
     es.close()
 
-    # e2e: public API with host buffers; every step uploads all engines' moves
-    # from pinned memory in one copy and reads all engines' chi2 and decisions
-    # back in one copy.  Two staging slots: the host submits step k + 1
-    # before it collects step k's results.
+    # e2e: public API with host buffers; every step passes all engines' moves
+    # from numpy arrays and reads all engines' chi2 and decisions back into
+    # numpy arrays (one result pair per slot).  Two staging slots: the host
+    # submits step k + 1 before it collects step k's results.
     es2 = EngineSet(systems, move_cap=4, tune=tune)
     es2.init()
     hm = [translation_moves(np.random.default_rng([seed, 5000 + e]), s.box_coords.shape[0], W + K, amp)
@@ -615,16 +615,17 @@ def run_ours(args):
     A = np.ascontiguousarray(np.stack([m[0] for m in hm]).T)        # (steps, engines)
     V = np.ascontiguousarray(np.stack([m[1] for m in hm]).transpose(1, 0, 2))
     U = np.ascontiguousarray(np.stack([m[2] for m in hm]).T)
+    res = [(np.empty(E, np.float64), np.empty(E, np.int32)) for _ in range(2)]
     accepted_e2e = 0
     for k in range(W + K):
         if k == W:
             if k > 0:
-                accepted_e2e += int(es2.step_host_collect((k - 1) % 2)[1].sum())
+                accepted_e2e += int(es2.step_host_collect((k - 1) % 2, res[(k - 1) % 2])[1].sum())
             t0 = time.perf_counter()
         es2.step_host_submit(A[k], V[k], U[k], k % 2)
         if k > W or (k > 0 and k < W):
-            accepted_e2e += int(es2.step_host_collect((k - 1) % 2)[1].sum())
-    accepted_e2e += int(es2.step_host_collect((W + K - 1) % 2)[1].sum())
+            accepted_e2e += int(es2.step_host_collect((k - 1) % 2, res[(k - 1) % 2])[1].sum())
+    accepted_e2e += int(es2.step_host_collect((W + K - 1) % 2, res[(W + K - 1) % 2])[1].sum())
     t_e2e = time.perf_counter() - t0
     es2.close()
     e2e_value = E * K / t_e2e

@@ -52,8 +52,10 @@ register("frmc_engines_add", [_vp, ctypes.POINTER(_Spec), ctypes.POINTER(_i32)])
 register("frmc_engines_remove", [_vp, _i32])
 register("frmc_engines_live", [_vp, I32P, _i32, ctypes.POINTER(_i32)])
 register("frmc_engines_step_host", [_vp, I32P, F32P, F32P, F64P, I32P])
-register("frmc_engines_step_host_submit", [_vp, I32P, F32P, F32P, ctypes.c_int32])
-register("frmc_engines_step_host_collect", [_vp, ctypes.c_int32, F64P, I32P])
+# host-step array arguments as raw addresses (ndarray.ctypes.data): these
+# calls run once per step, where building ctypes pointer objects shows up
+register("frmc_engines_step_host_submit", [_vp, _vp, _vp, _vp, ctypes.c_int32])
+register("frmc_engines_step_host_collect", [_vp, ctypes.c_int32, _vp, _vp])
 register("frmc_engines_destroy", [_vp])
 register("frmc_engines_set_tune", [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int])
 register("frmc_engines_get_tune", [_vp] + [ctypes.POINTER(ctypes.c_int)] * 4)
@@ -480,11 +482,15 @@ class EngineSet:
     def step_host(self, atoms, vecs, u):
         """One batched step of all live engines from host arrays (live-id order);
         returns (chi2_new, accepted)."""
+        E = len(self.systems)
         atoms = np.ascontiguousarray(atoms, np.int32)
         vecs = np.ascontiguousarray(vecs, F32)
         u = np.ascontiguousarray(u, F32)
-        c2 = np.empty(len(atoms), np.float64)
-        acc = np.empty(len(atoms), np.int32)
+        if atoms.size != E or vecs.size != 3 * E or u.size != E:
+            raise ValueError("step_host: need %d atoms, (%d, 3) vectors and %d numbers, got %s, %s, %s"
+                             % (E, E, E, atoms.shape, vecs.shape, u.shape))
+        c2 = np.empty(E, np.float64)
+        acc = np.empty(E, np.int32)
         check(load().frmc_engines_step_host(self.handle, atoms.ctypes.data_as(I32P), vecs.ctypes.data_as(F32P),
                                             u.ctypes.data_as(F32P), c2.ctypes.data_as(F64P),
                                             acc.ctypes.data_as(I32P)))
@@ -494,19 +500,29 @@ class EngineSet:
         """Submit one batched step from host arrays into staging slot 0 or 1
         (step_host in two halves: a host may submit step k + 1 before it
         collects step k)."""
+        E = len(self.systems)
         atoms = np.ascontiguousarray(atoms, np.int32)
         vecs = np.ascontiguousarray(vecs, F32)
         u = np.ascontiguousarray(u, F32)
-        check(load().frmc_engines_step_host_submit(self.handle, atoms.ctypes.data_as(I32P),
-                                                   vecs.ctypes.data_as(F32P), u.ctypes.data_as(F32P), int(slot)))
+        if atoms.size != E or vecs.size != 3 * E or u.size != E:
+            raise ValueError("step_host_submit: need %d atoms, (%d, 3) vectors and %d numbers, got %s, %s, %s"
+                             % (E, E, E, atoms.shape, vecs.shape, u.shape))
+        check(load().frmc_engines_step_host_submit(self.handle, atoms.ctypes.data, vecs.ctypes.data,
+                                                   u.ctypes.data, int(slot)))
 
-    def step_host_collect(self, slot):
-        """Wait for the step in `slot`; returns (chi2_new, accepted) in live-id order."""
+    def step_host_collect(self, slot, out=None):
+        """Wait for the step in `slot`; returns (chi2_new, accepted) in live-id
+        order, into `out` = (float64 array, int32 array) of the live-engine
+        count when given."""
         E = len(self.systems)
-        c2 = np.empty(E, np.float64)
-        acc = np.empty(E, np.int32)
-        check(load().frmc_engines_step_host_collect(self.handle, int(slot), c2.ctypes.data_as(F64P),
-                                                    acc.ctypes.data_as(I32P)))
+        if out is None:
+            c2, acc = np.empty(E, np.float64), np.empty(E, np.int32)
+        else:
+            c2, acc = out
+            if (c2.dtype != np.float64 or acc.dtype != np.int32 or c2.size != E or acc.size != E
+                    or not c2.flags.c_contiguous or not acc.flags.c_contiguous):
+                raise ValueError("step_host_collect: out must be contiguous float64 and int32 arrays of %d" % E)
+        check(load().frmc_engines_step_host_collect(self.handle, int(slot), c2.ctypes.data, acc.ctypes.data))
         return c2, acc
 
     # ------------------------------------------------------------ control

@@ -162,12 +162,19 @@ def test_step_host_two_slots_match_ring_steps(fused):
     V = np.ascontiguousarray(np.stack([m[1] for m in mv]).transpose(1, 0, 2))
     U = np.ascontiguousarray(np.stack([m[2] for m in mv]).T)
     out = {}
+    with pytest.raises(ValueError):
+        es.step_host_submit(A[0][:-1], V[0], U[0], 0)  # one engine's move missing
     es.step_host_submit(A[0], V[0], U[0], 0)
     with pytest.raises(NativeError):
         es.step_host_submit(A[1], V[1], U[1], 0)  # slot 0 not collected yet
+    bufs = [(np.empty(len(systems), np.float64), np.empty(len(systems), np.int32)) for _ in range(2)]
     for k in range(1, steps):
         es.step_host_submit(A[k], V[k], U[k], k % 2)
-        out[k - 1] = es.step_host_collect((k - 1) % 2)
+        if k % 3:
+            out[k - 1] = es.step_host_collect((k - 1) % 2)
+        else:  # into caller-owned arrays
+            c2, acc = es.step_host_collect((k - 1) % 2, bufs[(k - 1) % 2])
+            out[k - 1] = (c2.copy(), acc.copy())
     out[steps - 1] = es.step_host_collect((steps - 1) % 2)
     with pytest.raises(NativeError):
         es.step_host_collect(0)  # nothing in flight
