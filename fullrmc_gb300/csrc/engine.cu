@@ -2016,6 +2016,7 @@ struct EngineSet {
     EResult *dstage_r[2] = {nullptr, nullptr};
     cudaEvent_t stage_ev[2] = {nullptr, nullptr};
     bool stage_busy[2] = {false, false};
+    int stage_E[2] = {0, 0};       // engines of the step each busy slot holds
     int stage_cap = 0;
     Sched *sched = nullptr;        // [0]: histogram step kernels, [1]: S(Q) kernel
     std::vector<SqTable> tables;
@@ -2975,6 +2976,8 @@ int frmc_engines_add(void *handle, const frmc_engine_spec *spec, int32_t *id)
     EngineSet *s = as_set(handle);
     if (!s || !spec || !id)
         return set_error(FRMC_E_ARG, "engines_add: null argument");
+    if (s->stage_busy[0] || s->stage_busy[1])
+        return set_error(FRMC_E_STATE, "engines_add: a host step is in flight; collect it first");
     int k;
     FRMC_TRY(add_engine(s, *spec, &k));
     int rc = init_engine(s, k);
@@ -2991,6 +2994,8 @@ int frmc_engines_remove(void *handle, int32_t id)
     EngineSet *s = as_set(handle);
     if (!s || !valid_id(s, id))
         return set_error(FRMC_E_ARG, "engines_remove: invalid engine %d", id);
+    if (s->stage_busy[0] || s->stage_busy[1])
+        return set_error(FRMC_E_STATE, "engines_remove: a host step is in flight; collect it first");
     FRMC_CUDA(cudaStreamSynchronize(s->stream));
     FRMC_CUDA(cudaDeviceSynchronize());
     cudaFree(s->slots[id].blob);
@@ -3360,6 +3365,7 @@ static int step_host_submit(EngineSet *s, const int32_t *atoms, const float *vec
     FRMC_CUDA(cudaGraphLaunch(s->host_graph[slot], st));
     FRMC_CUDA(cudaEventRecord(s->stage_ev[slot], st));
     s->stage_busy[slot] = true;
+    s->stage_E[slot] = E;
     return FRMC_OK;
 }
 
@@ -3369,7 +3375,9 @@ static int step_host_collect(EngineSet *s, int slot, double *chi2_new, int32_t *
         return set_error(FRMC_E_STATE, "step_host: slot %d holds no submitted step", slot);
     FRMC_CUDA(cudaEventSynchronize(s->stage_ev[slot]));
     s->stage_busy[slot] = false;
-    const int E = (int)s->live.size();
+    // the engines of the submitted step (add and remove are refused while a
+    // slot is busy, so this is also the live count)
+    const int E = s->stage_E[slot];
     const EResult *hr = s->hstage_r[slot];
     for (int k = 0; k < E; ++k) {
         if (chi2_new) chi2_new[k] = hr[k].chi2_new;

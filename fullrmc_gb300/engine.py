@@ -416,6 +416,7 @@ class EngineSet:
         load()
         self.move_cap = int(move_cap)
         self.systems = {}
+        self._stage_E = [None, None]
         self.tables = {}
         h = ctypes.c_void_p()
         systems = list(systems)
@@ -509,12 +510,14 @@ class EngineSet:
                              % (E, E, E, atoms.shape, vecs.shape, u.shape))
         check(load().frmc_engines_step_host_submit(self.handle, atoms.ctypes.data, vecs.ctypes.data,
                                                    u.ctypes.data, int(slot)))
+        self._stage_E[int(slot)] = E
 
     def step_host_collect(self, slot, out=None):
         """Wait for the step in `slot`; returns (chi2_new, accepted) in live-id
         order, into `out` = (float64 array, int32 array) of the live-engine
-        count when given."""
-        E = len(self.systems)
+        count when given.  Engines cannot be added or removed while a step is
+        in flight (the library refuses), so the count is the submitted one."""
+        E = self._stage_E[int(slot)] if slot in (0, 1) and self._stage_E[int(slot)] is not None else len(self.systems)
         if out is None:
             c2, acc = np.empty(E, np.float64), np.empty(E, np.int32)
         else:
@@ -523,6 +526,7 @@ class EngineSet:
                     or not c2.flags.c_contiguous or not acc.flags.c_contiguous):
                 raise ValueError("step_host_collect: out must be contiguous float64 and int32 arrays of %d" % E)
         check(load().frmc_engines_step_host_collect(self.handle, int(slot), c2.ctypes.data, acc.ctypes.data))
+        self._stage_E[int(slot)] = None
         return c2, acc
 
     # ------------------------------------------------------------ control

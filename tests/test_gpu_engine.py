@@ -167,6 +167,12 @@ def test_step_host_two_slots_match_ring_steps(fused):
     es.step_host_submit(A[0], V[0], U[0], 0)
     with pytest.raises(NativeError):
         es.step_host_submit(A[1], V[1], U[1], 0)  # slot 0 not collected yet
+    # the set cannot change while a step is in flight
+    with pytest.raises(NativeError):
+        es.add(systems[0])
+    with pytest.raises(NativeError):
+        es.remove(0)
+    assert len(es.live()) == len(systems) and es.E == len(systems)
     bufs = [(np.empty(len(systems), np.float64), np.empty(len(systems), np.int32)) for _ in range(2)]
     for k in range(1, steps):
         es.step_host_submit(A[k], V[k], U[k], k % 2)
