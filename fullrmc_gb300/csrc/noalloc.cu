@@ -9,6 +9,7 @@
 // its uint32 counts and its status word in one fixed array of device memory
 // reserved when the library is loaded (below).  Every GPU that loads the
 // library holds that array until the process exits.
+#include <climits>
 #include <cstdio>
 #include <mutex>
 
@@ -71,7 +72,8 @@ int frmc_dev_full_pairs_histograms_noalloc(const void *atoms4, const int32_t *mo
                                            float maxDistance, float bin, int32_t hs, float *hintra, float *hinter,
                                            void *stream)
 {
-    if (n < 0 || n > (int64_t)(1 << 30))
+    // the same atom limit as frmc_dev_full_hist_counts
+    if (n < 0 || n > (int64_t)(INT_MAX / 4))
         return set_error(FRMC_E_ARG, "no-allocation histogram: %lld atoms out of range", (long long)n);
     if (ne < 0 || hs < 0)
         return set_error(FRMC_E_ARG, "no-allocation histogram: negative histogram shape (%d, %d)", ne, hs);

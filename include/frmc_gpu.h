@@ -258,10 +258,12 @@ int frmc_dev_multiple_hist_counts(const int32_t *indexes, int64_t K, const float
  * histograms equal those of full_pairs_histograms_coords.  The uint32
  * counts live in one fixed device array of 2^20 counts (4 MiB) that every GPU
  * loading the library holds until exit: 2*ne*ne*hs above 1048576 returns
- * FRMC_E_ARG.  The first call on a device resolves that array's address and
- * should come before any stream capture.  All calls share the array, so calls
- * that overlap on the GPU (other streams, other threads) race.  Synchronises
- * `stream` before returning. */
+ * FRMC_E_ARG, and so does n above INT_MAX / 4 (the limit of
+ * frmc_dev_full_hist_counts).  The first call on a device is its set-up: it
+ * resolves that array's device address, so make it before any stream capture
+ * begins.  All calls share the array, so calls that overlap on the GPU (other
+ * streams, other threads) race.  Every call copies its status word back and
+ * synchronises `stream` before returning. */
 int frmc_dev_full_pairs_histograms_noalloc(const void *atoms4, const int32_t *moleculeIndex, int64_t n,
                                            const float *basis_host, int isPBC, int32_t ne, float minDistance,
                                            float maxDistance, float bin, int32_t hs, float *hintra, float *hinter,
