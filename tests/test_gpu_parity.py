@@ -228,3 +228,38 @@ def test_index_errors(gpu):
         gpu.pairs_histograms.multiple_pairs_histograms_coords(indexes=np.array([100], np.int32), **a)
     with pytest.raises(IndexError):
         gpu.pairs_distances.pairs_distances_to_indexcoords(-1, a["boxCoords"], a["basis"], True)
+
+
+_COPY_BRANCH = r"""
+import sys
+import numpy as np
+sys.path[:0] = [ROOT, ROOT + "/oracle", ROOT + "/tests"]
+import fullrmc_gb300
+import oracle
+from fullrmc_gb300 import pairs_histograms as ph
+from test_gpu_parity import _system
+a = _system(31, 5000, 2, "xytri", molsize=13, rmax=15.0)
+for k in (1, 13, 64, 65):
+    idx = np.random.default_rng(k).choice(5000, size=k, replace=False).astype(np.int32)
+    for allAtoms in (True, False):
+        got = ph.multiple_pairs_histograms_coords(indexes=idx, allAtoms=allAtoms, **a)
+        want = oracle.multiple_pairs_histograms_coords(indexes=idx, allAtoms=allAtoms, **a)
+        assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1]), (k, allAtoms)
+print("copy branch ok")
+"""
+
+
+def test_multiple_copy_branch_vs_oracle(gpu):
+    """With FRMC_HOST_DIRECT=0 the per-move call copies its inputs to the
+    device instead of letting the kernels read the caller's arrays (the path
+    of devices without coherent pageable-memory access); run in a fresh
+    process, since the switch is read when the library's context is made."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, FRMC_HOST_DIRECT="0")
+    r = subprocess.run([sys.executable, "-c", "ROOT = %r\n" % root + _COPY_BRANCH], env=env, cwd=root,
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "copy branch ok" in r.stdout
