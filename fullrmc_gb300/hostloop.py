@@ -32,7 +32,9 @@ PI = F32(np.pi)
 
 
 class HostPDFChain:
-    def __init__(self, system, hist_module, transform_module=None):
+    def __init__(self, system, hist_module, transform_module=None, weights=None):
+        """`weights`: float32 element-pair weights w[i][j] to use instead of
+        the system model's (e.g. those a fullrmc constraint computed)."""
         self.h = hist_module
         self.t = transform_module
         s = system
@@ -53,10 +55,12 @@ class HostPDFChain:
         edges = np.asarray(m.edges, F32)
         self.shellVolumes = F32(4.0 / 3.0) * PI * (edges[1:] ** 3 - edges[0:-1] ** 3)
         self.volume = F32(m.volume)
-        self.rho0 = F32(sum(self.counts) / float(m.volume))
+        # fullrmc's number density: float32 atoms / float32 volume (Engine.py:2274)
+        self.rho0 = F32(sum(self.counts)) / F32(m.volume)
         self.exp = np.asarray(m.G_exp, F32)
         self.varianceSquared = F32(m.variance_squared)
-        self.weights = {(i, j): F32(m.weights[i][j]) for i in range(self.ne) for j in range(i, self.ne)}
+        w = m.weights if weights is None else weights
+        self.weights = {(i, j): F32(w[i][j]) for i in range(self.ne) for j in range(i, self.ne)}
         self.data = None
         self.error = None
         self.accepted = 0
