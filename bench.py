@@ -145,6 +145,29 @@ def _host_cpu():
     return "%s (%s), %d logical cores" % ((name or "unknown").strip(), platform.machine(), os.cpu_count() or 1)
 
 
+def workload_config(ws, engines=256, amp=0.1, seed=0):
+    """The `config` object of both arms: the batching workload as generated
+    (the same dict whichever arm prints it)."""
+    from fullrmc_gb300 import synthetic
+    systems = synthetic.mixed_engines(seed=seed, count=engines)
+    return {"workload": WORKLOAD, "engines": engines, "engines_total": ws * engines,
+            "atoms_total": int(sum(s.box_coords.shape[0] for s in systems)),
+            "atoms": "log-uniform 1000-20000", "species": "1-4", "rmax": 12.0, "dr": 0.01,
+            "move": "single-atom translation <= %.1f A" % amp,
+            "l2": "256 MiB buffer written between timed steps",
+            "parallelism": "engines sharded per GPU" if ws > 1 else "single GPU"}
+
+
+def stratified(systems, count):
+    """`count` engine indexes spread evenly over the engines sorted by atom
+    count (the sample's size distribution follows the population's)."""
+    order = np.argsort([s.box_coords.shape[0] for s in systems], kind="stable")
+    if count >= len(order):
+        return sorted(int(e) for e in order)
+    pick = np.floor((np.arange(count) + 0.5) * len(order) / count).astype(int)
+    return sorted(int(order[k]) for k in pick)
+
+
 def _dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -179,19 +202,25 @@ def _ref_worker(args):
     return len(idxs), times
 
 
-def reference_rate(n_engines_sample, steps, warmup, processes, seed=0, amp=0.1):
-    """Aggregate steps/s of the reference CPU path: `processes` host processes
-    each step their own engines (the engines are independent); a timed step
-    lasts as long as the slowest process."""
+def reference_rate(engines, steps, warmup, processes, seed=0, amp=0.1):
+    """Aggregate steps/s of the reference CPU path over the engine indexes
+    `engines`: `processes` host processes each step their own engines (the
+    engines are independent; engines are dealt largest first to the least
+    loaded process); a timed step lasts as long as the slowest process."""
     import multiprocessing as mp
-    engines = list(range(n_engines_sample))
-    chunks = [engines[i::processes] for i in range(processes)]
-    chunks = [c for c in chunks if c]
+    from fullrmc_gb300 import synthetic
+    sizes = [s.box_coords.shape[0] for s in synthetic.mixed_engines(seed=seed, count=max(engines) + 1)]
+    chunks = [[] for _ in range(max(1, min(processes, len(engines))))]
+    load = [0] * len(chunks)
+    for e in sorted(engines, key=lambda e: -sizes[e]):
+        k = load.index(min(load))
+        chunks[k].append(e)
+        load[k] += sizes[e]
     ctx = mp.get_context("spawn")
     with ctx.Pool(len(chunks)) as pool:
         out = pool.map(_ref_worker, [(c, warmup + steps, seed, amp) for c in chunks])
     total = sum(max(o[1][k] for o in out) for k in range(warmup, warmup + steps))
-    done = n_engines_sample * steps
+    done = len(engines) * steps
     return done / total, len(chunks)
 
 
@@ -250,6 +279,29 @@ def _reference_config_rate(system, counts0, mv, steps, group=False):
     return steps / (time.perf_counter() - t0)
 
 
+def _dropin_loop_rate(system, steps):
+    """Steps/s of the plain drop-in: fullrmc's step with a
+    PairDistributionConstraint (hostloop.HostPDFChain: M and F histograms
+    before and after the move, the moved box coordinates through
+    transform_coordinates, float32 G(r) and standard error on the host) with
+    the GPU modules in place of the Cython ones, host arrays in and out."""
+    import fullrmc_gb300
+    from fullrmc_gb300.engine import translation_moves
+    from fullrmc_gb300.hostloop import HostPDFChain
+    chain = HostPDFChain(system, fullrmc_gb300.pairs_histograms, fullrmc_gb300.boundary_conditions_collection)
+    chain.compute_data()
+    a, v, u = translation_moves(np.random.default_rng(17), system.box_coords.shape[0], steps + 50, 0.1)
+    for k in range(50):
+        chain.step(a[k], v[k][None, :], u[k])
+    t0 = time.perf_counter()
+    for k in range(50, 50 + steps):
+        chain.step(a[k], v[k][None, :], u[k])
+    dt = time.perf_counter() - t0
+    return {"plain_dropin_steps_per_s": steps / dt, "plain_dropin_steps": steps,
+            "plain_dropin_path": "fullrmc's PDF step on the drop-in modules: 4 histogram calls and 1 coordinate "
+                                 "transform per step, host arrays, float32 G(r) on the host"}
+
+
 def bench_configs(torch, with_cpu):
     """Single-engine step rates of the other configurations on the GPU (and,
     on a bounded sample, of the reference CPU path): the 5,000-atom alloy,
@@ -264,6 +316,8 @@ def bench_configs(torch, with_cpu):
         rate, counts0, acc, mv = _engine_rate(torch, system, steps, seed=5, group=group)
         d = {"atoms": int(system.box_coords.shape[0]), "atoms_per_move": 13 if group else 1,
              "gpu_steps_per_s": rate, "steps": steps, "accept_rate": round(float(acc), 4)}
+        if name == "alloy_5000":
+            d.update(_dropin_loop_rate(system, 2000))
         if with_cpu:
             try:
                 d["cpu_reference_steps_per_s"] = _reference_config_rate(system, counts0, mv, cpu_steps, group)
@@ -439,17 +493,18 @@ def run_reference(args):
         print(json.dumps({"impl": "reference", "unavailable": "fullrmc Cython could not be built here: %s" % exc}))
         return 0
     cores = os.cpu_count() or 1
-    sample = min(2 * cores, 256)
-    value, procs = reference_rate(sample, args.steps, args.warmup, cores)
+    engines = list(range(256))  # every engine of the workload
+    value, procs = reference_rate(engines, args.steps, args.warmup, cores)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * 256 / value, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "engines": 256, "atoms": "log-uniform 1000-20000",
-                       "rmax": 12.0, "dr": 0.01, "sample": "%d of the 256 engines, one move each per step" % sample},
+            "config": workload_config(ws),
             "impl": "reference",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": kind,
-                             "sample": "fullrmc Cython (ncores=1) in %d processes, %d engines, %d timed steps"
-                                       % (procs, sample, args.steps), "host": _host_cpu()},
+                             "sample": "fullrmc Cython (ncores=1) in %d processes: all 256 engines of the workload "
+                                       "(the GPU arm's engines), each moved once per step, %d timed steps; a step "
+                                       "lasts as long as the slowest process" % (procs, args.steps),
+                             "host": _host_cpu()},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -526,6 +581,7 @@ def run_ours(args):
     moves = [translation_moves(np.random.default_rng([seed, 1000 + e]), s.box_coords.shape[0], total_steps, amp)
              for e, s in enumerate(systems)]
     pairs_per_step = float(sum(2 * (s.box_coords.shape[0] - 1) for s in systems))
+    mean_atoms = float(np.mean([s.box_coords.shape[0] for s in systems]))
 
     # autotune the work list (results are identical under every tuning)
     es = EngineSet(systems, move_cap=cap)
@@ -602,7 +658,29 @@ def run_ours(args):
         torch.cuda.synchronize()
     plain_rate = len(sample) * (plain_steps - 1) / (p0.elapsed_time(p1) * 1e-3)
     grid_engines = sum(1 for e in range(E) if es.cells(e) > 0)
+    # same accepts: the first W + 3K steps of every engine were batched steps;
+    # replay them with the same moves one engine at a time on fresh engines
+    # and compare every decision and every chi2 bit pattern
+    batched_steps = W + 3 * K
+    batched_res = [es.results(e, 0, batched_steps) for e in range(E)]
     es.close()
+    es3 = EngineSet(systems, move_cap=batched_steps + 8, tune=tune)
+    es3.init()
+    for e, (a, v, u) in enumerate(moves):
+        es3.push_moves(e, a[:batched_steps], v[:batched_steps], u[:batched_steps], 0)
+    for e in range(E):
+        es3.step(batched_steps, engine=e, graph=False, sync=False)
+    es3.sync()
+    mismatch = 0
+    for e in range(E):
+        c2, acc, _ = es3.results(e, 0, batched_steps)
+        if not (np.array_equal(acc, batched_res[e][1]) and
+                np.array_equal(c2.view(np.int64), batched_res[e][0].view(np.int64))):
+            mismatch += 1
+    es3.close()
+    same = {"equal": mismatch == 0, "engines": E, "steps": batched_steps, "engines_differing": mismatch,
+            "check": "every engine's batched steps (warm-up, timed, graph) replayed one engine at a time on fresh "
+                     "engines with the same moves: accept decisions and chi2 bit patterns compared"}
 
     # e2e: public API with host buffers; every step passes all engines' moves
     # from numpy arrays and reads all engines' chi2 and decisions back into
@@ -661,9 +739,13 @@ def run_ours(args):
             import build_ref
             build_ref.build()
             build_ref.import_reference()
-            rate, procs = reference_rate(4, 6, 2, 1, seed=seed, amp=amp)
+            pick = stratified(systems, 16)
+            rate, procs = reference_rate(pick, 200, 3, 1, seed=seed, amp=amp)
+            sample_atoms = float(np.mean([systems[e].box_coords.shape[0] for e in pick]))
             cpu = {"value": rate, "unit": UNIT, "cores": 1, "kind": "reference",
-                   "sample": "fullrmc Cython (ncores=1): 4 engines of this workload x 6 timed steps, 1 core",
+                   "sample": "fullrmc Cython (ncores=1) on 1 core: 16 of the 256 engines, spread evenly over the "
+                             "engines sorted by atom count (mean %.0f atoms; all 256: %.0f), 200 timed steps each"
+                             % (sample_atoms, mean_atoms),
                    "host": _host_cpu()}
         except Exception as exc:
             cpu = {"value": None, "unit": UNIT, "cores": 1, "kind": "reference", "sample": "failed: %s" % exc}
@@ -673,13 +755,9 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
             "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "engines": E, "engines_total": ws * E,
-                       "atoms_total": int(sum(s.box_coords.shape[0] for s in systems)),
-                       "atoms": "log-uniform 1000-20000", "species": "1-4", "rmax": 12.0, "dr": 0.01,
-                       "move": "single-atom translation <= %.1f A" % amp,
-                       "l2": "256 MiB buffer written between timed steps",
-                       "tune": {"tile": tune[0], "threads": tune[1], "ctas_per_sm": tune[2]},
-                       "parallelism": "engines sharded per GPU" if ws > 1 else "single GPU"},
+            "config": workload_config(ws, E, amp, seed),
+            "tune": {"tile": tune[0], "threads": tune[1], "ctas_per_sm": tune[2]},
+            "same_accepts": same,
             "plain": {"steps_per_s": plain_rate, "engines_sampled": len(sample),
                       "batched_over_plain": value / ws / plain_rate},
             "steady_graph": {"ms_per_step": graph_ms, "steps_per_s": E / (graph_ms * 1e-3),
@@ -698,7 +776,12 @@ def run_ours(args):
                                        % (sms, fmax / 1e6, peaks_kind, OPS_PER_PAIR),
                          "note": "achieved counts the reference's pair evaluations (2 (n - 1) per engine and "
                                  "step); engines with a column grid evaluate only the columns of the cells a "
-                                 "moved atom may reach (pairs_evaluated_per_launch)"},
+                                 "moved atom may reach (pairs_evaluated_per_launch)",
+                         "allpairs_kernel": "k_full_tiles",
+                         "allpairs_workload": "100,000 atoms, triclinic 103 A gamma 120, 3 species, r 0-20 A",
+                         "allpairs_ms": allp["ms"],
+                         "allpairs_pairs_per_s": allp["pair_distances_per_s"],
+                         "allpairs_frac": allp["pair_distances_per_s"] / issue_peak},
             "allpairs": dict(allp, roofline_frac=allp["pair_distances_per_s"] / issue_peak,
                              issue_peak_pairs_per_s=issue_peak),
             "serving": serving,
