@@ -65,6 +65,7 @@ SIGNATURES = {
     "frmc_transform_coordinates": [F32P, F32P, i64, F32P],
     "frmc_dev_full_hist_counts": [vp, vp, i64, F32P, cint, i32, f32, f32, f32, i32, vp, vp],
     "frmc_set_full_tune": [cint, cint, cint, cint, cint, f64],
+    "frmc_set_full_aggregate": [cint],
     "frmc_sq_limits": [f32, f32, F32P, F32P],
     "frmc_basis_mode": [F32P, cint],
     "frmc_full_items": [i64, ctypes.POINTER(i64)],

@@ -4,8 +4,8 @@ Every ``csrc/*.cu`` file is compiled in parallel into ``_build/`` and linked
 into ``fullrmc_gb300/_lib/libfrmc_gpu.so``.  The library is rebuilt only when a
 source or header is newer than it.
 
-The library links cuBLAS (shared, with the toolkit's lib64 as its run path)
-for the one plain GEMM of the engines' S(Q) term.
+The library links only the static CUDA runtime: every kernel is the
+library's own.
 
 Flags that matter for parity: ``--fmad=false`` (no contraction of a*b+c; the
 kernels also use explicit round-to-nearest intrinsics), IEEE division and
@@ -81,10 +81,7 @@ def build(verbose: bool = False, jobs: int | None = None, ptxas_info: bool = Fal
         objs = list(pool.map(compile_one, srcs))
     if _stale(LIB, objs):
         tmp = LIB + ".tmp%d" % os.getpid()
-        # cuBLAS (the S(Q) terms' GEMM) is found next to nvcc at run time too
-        cudalib = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(cc))), "lib64")
-        cmd = [cc, ARCH, "-shared", "-o", tmp, *objs, "-L" + cudalib, "-lcublas", "-Xlinker", "-rpath=" + cudalib,
-               "-lcudart_static", "-lrt", "-lpthread", "-ldl"]
+        cmd = [cc, ARCH, "-shared", "-o", tmp, *objs, "-lcudart_static", "-lrt", "-lpthread", "-ldl"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))

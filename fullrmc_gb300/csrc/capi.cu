@@ -261,6 +261,15 @@ int frmc_set_full_tune(int threads, int rows, int queued, int qcap, int ctas_per
     return FRMC_OK;
 }
 
+int frmc_set_full_aggregate(int on)
+{
+    if (on != 0 && on != 1)
+        return set_error(FRMC_E_ARG, "aggregate must be 0 or 1");
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_full_tune.aggregate = on;
+    return FRMC_OK;
+}
+
 int frmc_sq_limits(float minDistance, float maxDistance, float *s_lo, float *s_hi)
 {
     sq_limits(minDistance, maxDistance, s_lo, s_hi);

@@ -38,7 +38,6 @@
 #include <map>
 #include <vector>
 
-#include <cublas_v2.h>
 #include <cuda_fp16.h>
 
 #include "frmc_gpu_engine.h"
@@ -60,6 +59,8 @@ struct EState {
     unsigned tcount;    // entries in the touched-bin list of the current step
     unsigned sq_done;   // reserved (zero)
     int fmt;            // touched-list format of the step: 1 = (flat << 1) | sign, 0 = flat
+    double sf;          // scale factor of the current configuration (dense engines)
+    double sf_prop;     // scale factor of this step's proposal (dense engines with S(Q))
 };
 
 // Work scheduler of one engine set: CTAs claim items with an atomic counter;
@@ -128,7 +129,15 @@ struct EDesc {
     double *R;    // [hs] rfac * invvol: G(b) = R(b) sum_p pair_coef_p n_p(b) - rfac(b)
     double *A;    // [hs] w R^2
     double *Bq;   // [hs] 2 w R (exp - G) of the current configuration
-    double *Sb;   // [hs] S(b) = sum_p pair_coef_p dP_p(b) proposed this step (large hs or S(Q))
+    double *Sb;   // [hs] S(b) = sum_p pair_coef_p dP_p(b) proposed this step (large hs, S(Q) or dense)
+    // Dense engines (scale factor != 1, a fitted scale factor or a window):
+    // every step evaluates window * (s G') over all bins, G' = Gc + R S.
+    int dense, wlen, fit_freq;
+    double sf0, fit_min, fit_max;
+    double *Gc;   // [hs] G of the current configuration (before scale factor and window)
+    double *fnum; // [hs] fit numerator weights times the fit target
+    double *fden; // [hs] fit denominator weights
+    double *win;  // [wlen] window
     // S(Q) term (sq = 1): with x(b) = Rq(b) S(b) the change of the S(Q)
     // shells' G, d(sd_sq) = x^T y - x^T h, y = K x, K = M W M^T,
     // h = 2 M W (S_exp - S).  y is computed exactly in integers from the
@@ -151,14 +160,12 @@ struct EDesc {
     int *evn;           // [kMaxP] their counts n (-1 - n: a delta beyond kSqGemmMaxDelta, sum the
                         // list exactly; INT_MIN: a delta beyond 16 bits, sum the deltas dP)
     // y on the tensor cores: X holds this step's element-pair deltas as fp16
-    // (column q of the engine at X + q xld, bins down the column), the table
-    // in kSqLimbs balanced base-256 digits multiplies all engines' columns in
-    // one GEMM, and Y (column q at Y + q yld, digit l's rows at l hsp) holds
-    // the digit products, exact integers in fp32.
+    // (column q of the engine at X + q xld, bins down the column); the S(Q)
+    // kernel multiplies the table's kSqLimbs balanced base-2048 digits by
+    // every engine's columns (exact integers in fp32).
     __half *X;
-    const float *Y;
-    int xld, yld, hsp;
-    int sq_gemm_max;    // largest |delta| taken through the GEMM (kSqGemmMaxDelta; lower values,
+    int xld, hsp;
+    int sq_gemm_max;    // largest |delta| taken through the product (kSqGemmMaxDelta; lower values,
                         // down to 0 = never and -1 = the dense integer loop, exist for tests)
     // Column grid (nc > 0): the atoms sorted by cell, so that a step sweeps
     // only the cells whose bounding box may come within maxD of a moved atom.
@@ -589,10 +596,82 @@ __device__ double eval_full(const EDesc &D, double *red, double *cb)
             const double w = D.has_dw ? D.dw[b] : 1.0;
             D.Bq[b] = 2.0 * (w * D.R[b]) * e;
             cb[b - c0] = (w * e) * e;
+            if (D.dense)
+                D.Gc[b] = G;
         }
         lanes_add_chunk(red, cb, c0, cn);
     }
     return lanes_total(red);
+}
+
+// Dense engines (scale factor, fitted scale factor, window): the proposed G'
+// = Gc + R S over all bins (with_step = false: the current G), the scale
+// factor s -- fitted, s = clamp(sum fnum G' / sum fden G'^2), when `fit`,
+// else the current one (Core/Constraint.py:1363-1424) -- and
+// sd' = sum w (exp - window * (s G'))^2 with numpy.convolve's 'same' window
+// (PairDistributionConstraints.py:884-893).  Every sum is taken in the fixed
+// lane order.  Thread 0 stores s in *s_sf.
+__device__ __forceinline__ double dense_G(const EDesc &D, int b, bool with_step)
+{
+    return with_step ? fma(D.R[b], __ldcg(D.Sb + b), D.Gc[b]) : D.Gc[b];
+}
+
+__device__ double eval_dense(const EDesc &D, double *red, double *cb, bool with_step, bool fit, double sf,
+                             double *s_sf)
+{
+    if (fit) {
+        double nd[2];
+        for (int pass = 0; pass < 2; ++pass) {
+            lanes_zero(red);
+            for (int c0 = 0; c0 < D.hs; c0 += kChunk) {
+                const int cn = min(kChunk, D.hs - c0);
+                for (int b = c0 + threadIdx.x; b < c0 + cn; b += blockDim.x) {
+                    const double G = dense_G(D, b, with_step);
+                    cb[b - c0] = pass == 0 ? D.fnum[b] * G : D.fden[b] * (G * G);
+                }
+                lanes_add_chunk(red, cb, c0, cn);
+            }
+            nd[pass] = lanes_total(red);
+        }
+        if (nd[1] > 0.0)
+            sf = fmin(fmax(nd[0] / nd[1], D.fit_min), D.fit_max);
+    }
+    const int L = D.wlen, c = (L - 1) / 2;
+    lanes_zero(red);
+    for (int c0 = 0; c0 < D.hs; c0 += kChunk) {
+        const int cn = min(kChunk, D.hs - c0);
+        for (int b = c0 + threadIdx.x; b < c0 + cn; b += blockDim.x) {
+            double u;
+            if (L > 0) {
+                u = 0.0;
+                for (int k = 0; k < L; ++k) {
+                    const int j = b + c - k;
+                    if (j >= 0 && j < D.hs)
+                        u = fma(D.win[k], sf * dense_G(D, j, with_step), u);
+                }
+            } else {
+                u = sf * dense_G(D, b, with_step);
+            }
+            const double e = D.expd[b] - u;
+            const double w = D.has_dw ? D.dw[b] : 1.0;
+            cb[b - c0] = (w * e) * e;
+        }
+        lanes_add_chunk(red, cb, c0, cn);
+    }
+    const double sd = lanes_total(red);
+    if (threadIdx.x == 0)
+        *s_sf = sf;
+    return sd;
+}
+
+// On accept a dense engine's G moves to G' (the bins whose S changed).
+__device__ void dense_commit(const EDesc &D)
+{
+    for (int b = threadIdx.x; b < D.hs; b += blockDim.x) {
+        const double S = __ldcg(D.Sb + b);
+        if (S != 0.0)
+            D.Gc[b] = fma(D.R[b], S, D.Gc[b]);
+    }
 }
 
 // Change of the sum of squared deviations for this step.  With
@@ -604,12 +683,16 @@ __device__ double eval_full(const EDesc &D, double *red, double *cb)
 // in shared memory (chunk) or global memory (Sb) for the commit.  Sums use the
 // fixed lane order, so the result does not depend on the CTA size.
 constexpr int kMaxP = 10;  // element pairs loaded with unrolled loads (ne <= 4)
-// T in kSqLimbs balanced base-256 digits t_l in [-128, 127] (7 digits cover
-// |T| < 2^48).  With |delta| <= kSqGemmMaxDelta and at most 4096 (kSqMaxBins) bins,
-// every digit product sum is an integer of magnitude <= 128 * 32 * 4096 =
-// 2^24, so fp16 inputs with fp32 accumulation give it exactly.
-constexpr int kSqLimbs = 7;
-constexpr int kSqGemmMaxDelta = 32;
+// T in kSqLimbs balanced base-2048 digits t_l in [-1024, 1023] (5 digits
+// cover |T| < 2^54; T stays below 2^48).  fp16 holds every integer up to 2048,
+// so a delta column goes through the tensor-core product when its entries are
+// at most kSqGemmMaxDelta in magnitude and their absolute sum is at most
+// kSqMaxL1: every partial sum of a digit product is then an integer of
+// magnitude <= 1024 * 2^14 = 2^24, which fp32 accumulation holds exactly.
+constexpr int kSqLimbs = 5;
+constexpr int kSqDigitBits = 11;
+constexpr int kSqGemmMaxDelta = 2048;
+constexpr int kSqMaxL1 = 1 << 14;
 
 // SMEM: the element-pair deltas are this CTA's shared-memory copy (one CTA per
 // engine); otherwise they are the engine's global array, filled by several
@@ -649,11 +732,15 @@ __device__ double eval_delta(const EDesc &Dg, int *dP, const double *Ab, const d
     int *__restrict__ gdP = Dg.dP;
     int *__restrict__ evl = Dg.evl;
     __shared__ int s_evn[kMaxP];
+    __shared__ int s_l1[kMaxP];  // sum of |delta| per element pair (S(Q) product bound)
     __shared__ int s_wide;
     __shared__ int s_cnt[kChunk / 32];  // changed bins per 32-bin group, then their list offsets
     __shared__ double tabv[kMaxP * 9];  // pair_coef_q * v, v = -4..4
     if (sq) {
-        for (int q = threadIdx.x; q < kMaxP; q += blockDim.x) s_evn[q] = 0;
+        for (int q = threadIdx.x; q < kMaxP; q += blockDim.x) {
+            s_evn[q] = 0;
+            s_l1[q] = 0;
+        }
         if (threadIdx.x == 0)
             s_wide = 0;
     }
@@ -693,7 +780,7 @@ __device__ double eval_delta(const EDesc &Dg, int *dP, const double *Ab, const d
                             any |= delta_at(q, b) != 0;
                     for (int q = kMaxP; q < np; ++q) any |= delta_at(q, b) != 0;
                 }
-                if ((sq || big) && !any)
+                if ((sq || big || Dg.dense) && !any)
                     Sb[b] = 0.0;
             }
             const unsigned bal = __ballot_sync(0xffffffffu, any);
@@ -754,6 +841,7 @@ __device__ double eval_delta(const EDesc &Dg, int *dP, const double *Ab, const d
                             gdP[q * hs + b] = v;
                         evl[q * hs + atomicAdd(&s_evn[q], 1)] = (b << 16) | (v & 0xffff);
                         Dg.X[q * Dg.xld + b] = __int2half_rn(v);
+                        atomicAdd(&s_l1[q], v < 0 ? -v : v);
                         if (v > Dg.sq_gemm_max || v < -Dg.sq_gemm_max)
                             s_wide = (v > 32767 || v < -32768 || Dg.sq_gemm_max < 0) ? 2 : max(s_wide, 1);
                     }
@@ -771,14 +859,19 @@ __device__ double eval_delta(const EDesc &Dg, int *dP, const double *Ab, const d
             }
             cb[k] = S * fma(a, S, -bq);
             sbs[k] = neg_twice(S);
-            if (big || sq)
+            if (big || sq || Dg.dense)
                 Sb[b] = S;
         }
         lanes_add_chunk(red, cb, 0, n);
     }
     const double total = lanes_total(red);
-    if (sq && (int)threadIdx.x < np)
-        Dg.evn[threadIdx.x] = s_wide == 0 ? s_evn[threadIdx.x] : (s_wide == 1 ? -1 - s_evn[threadIdx.x] : INT_MIN);
+    if (sq && (int)threadIdx.x < np) {
+        // per element pair: n (tensor-core product), -1 - n (exact sum over
+        // the list of deltas) or INT_MIN (exact sum over the dense deltas)
+        const int n = s_evn[threadIdx.x];
+        const bool wide = s_wide == 1 || s_l1[threadIdx.x] > kSqMaxL1;
+        Dg.evn[threadIdx.x] = s_wide == 2 ? INT_MIN : (wide ? -1 - n : n);
+    }
     return total;
 }
 
@@ -905,7 +998,17 @@ __device__ void finish_engine(const EDesc &D, const MovedGroup &g, double *red, 
         }
         __syncthreads();
     }
-    const double dsd = eval_delta<false>(D, D.dP, D.A, D.Bq, red, cb, sbs, sbin, s_nchg, coef, nullptr);
+    double dsd = eval_delta<false>(D, D.dP, D.A, D.Bq, red, cb, sbs, sbin, s_nchg, coef, nullptr);
+    __shared__ double s_sf;
+    double sd_dense = 0.0;
+    if (D.dense) {
+        // the whole model: scale factor (fitted when due) and window
+        const EState &S0 = *D.st;
+        const bool fit = D.fit_freq > 0 && S0.accepted % D.fit_freq == 0;
+        sd_dense = eval_dense(D, red, cb, true, fit, S0.sf, &s_sf);
+        dsd = sd_dense - S0.sd;
+        __syncthreads();
+    }
     if (D.sq) {
         // the S(Q) kernel evaluates its term, decides and commits
         if (threadIdx.x == 0) {
@@ -913,11 +1016,13 @@ __device__ void finish_engine(const EDesc &D, const MovedGroup &g, double *red, 
             S.dsd = dsd;
             S.fmt = 0;
             S.done = 0u;
+            if (D.dense)
+                S.sf_prop = s_sf;
         }
         return;
     }
     const EState &S0 = *D.st;
-    const double sd_new = S0.sd + dsd;
+    const double sd_new = D.dense ? sd_dense : S0.sd + dsd;
     const double chi2_new = sd_new / D.var2;
     if (threadIdx.x == 0) {
         const EMove &m = D.moves[S0.step % D.move_cap];
@@ -960,8 +1065,11 @@ __device__ void finish_engine(const EDesc &D, const MovedGroup &g, double *red, 
             }
         }
     }
-    if (accept)
+    if (accept) {
         commit_moved_group(D, g);
+        if (D.dense)
+            dense_commit(D);
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
         EState &S = *D.st;
@@ -973,6 +1081,8 @@ __device__ void finish_engine(const EDesc &D, const MovedGroup &g, double *red, 
             S.chi2 = chi2_new;
             S.sd = sd_new;
             S.accepted += 1;
+            if (D.dense)
+                S.sf = s_sf;
         }
         S.step += 1;
         S.done = 0u;
@@ -1511,8 +1621,16 @@ __global__ void __launch_bounds__(kMaxEngineThreads, 1) k_engine_step(StepParams
             continue;
         }
         if (!FUSED && p.eval_only) {
-            const double sd = eval_full(D, red, cb);
+            double sd = eval_full(D, red, cb);
+            if (D.dense) {
+                // fullrmc's compute_data fits the scale factor when the
+                // accepted count (0 here) is a multiple of the frequency, for
+                // the standard error only; the kept scale factor is the initial one
+                __shared__ double s_sf0;
+                sd = eval_dense(D, red, cb, false, D.fit_freq > 0, D.sf0, &s_sf0);
+            }
             if (threadIdx.x == 0) {
+                D.st->sf = D.sf0;
                 D.st->sd = sd;
                 D.st->chi2 = sd / D.var2;
                 D.st->done = 0u;
@@ -1581,36 +1699,231 @@ __global__ void k_gather_results(const EDesc *desc, const int *ids, EResult *out
 // ------------------------------------------------------------------ S(Q) term
 // Engines with a StructureFactorConstraint finish every step here.  The
 // histogram kernels have left S(b) in Sb, the element-pair deltas dP_p(b) in
-// the global dP array, the G(r) change in st->dsd and the touched list.  With
-// x(b) = Rq(b) S(b) the change of the S(Q) shells' G(r), the change of the
-// S(Q) term is
+// the global dP array (and as fp16 columns of X), the G(r) change in st->dsd
+// and the touched list.  With x(b) = Rq(b) S(b) the change of the S(Q)
+// shells' G(r), the change of the S(Q) term is
 //   d(sd_sq) = sum_Q w [(e - dS)^2 - e^2] = x^T y - x^T h,
-// e = S_exp - S, dS = M^T x, y = K x, K = M W M^T, h = 2 M W e.
+// e = S_exp - S, dS = M^T x, y = K x, K = M W M^T, h = 2 M W (S_exp - S).
 // y is formed from the integer deltas and the fixed-point table T (K scaled
 // by the shells' 4 pi r / volume and 2^s): z_p(b) = sum_c T[c][b] dP_p(c) is
 // an exact int64 sum, so its value does not depend on the order of the
 // terms, and y(b) = rho0 2^-s sum_p pair_coef_p z_p(b).
-// The O(changed bins x bins) product runs on the tensor cores: T's balanced
-// base-256 digits (fp16) times every engine's fp16 delta columns in one GEMM
-// (sq_gemm), whose fp32 results are exact integers (see kSqLimbs); a step with
-// a delta beyond the GEMM's limit sums its list of deltas exactly instead.
-// k_sq_step takes (engine, block of kSqRows rows) items, combines the digits
-// per element pair (kSqGroups thread groups share the pairs) and forms the
-// rows' share of x (y - h); k_sq_commit adds the shares in block order,
-// decides and commits: counts, Bq -= 2 A S, h -= 2 y, coordinates, and clears
-// dP and the delta columns.
-constexpr int kSqRows = 64;       // rows per item
-constexpr int kSqGroups = 4;      // thread groups (element pairs) per item
-constexpr int kSqThreads = kSqRows * kSqGroups;
+//
+// k_sq_fused does the whole term in one persistent launch over a work list
+// of tile items followed by one commit item per engine:
+// * a tile item is (block of delta columns, block of kSqRows rows): the
+//   block's columns -- whole engines, at most kSqCols columns -- times the
+//   rows' kSqLimbs digit rows of T on the tensor cores (mma.sync, fp16 in,
+//   fp32 accumulate; every product sum is an exact integer, see kSqLimbs),
+//   staged through shared memory by cp.async in double-buffered chunks of
+//   kSqK bins.  The digits are combined into z (modulo 2^64), y = yscale
+//   sum_p pair_coef_p z_p in p order, and the rows' share of x (y - h) is
+//   summed by one warp per engine with a fixed shuffle tree; the tile then
+//   counts itself done in the engine's state.
+// * a commit item waits (bounded) until all the engine's row blocks are done,
+//   adds their shares in block order, decides and commits: counts, Bq -= 2 A S,
+//   h -= 2 y, coordinates, and clears dP and the delta columns.  Its tiles are
+//   claimed before it by CTAs that are running, so the wait always ends.
+// A column whose deltas are too large for exact fp32 products takes the
+// exact integer sum over its list of deltas (or its dense deltas) instead.
+// Every quantity of an engine depends only on that engine's columns, so a
+// chain is the same in any batch and alone.
+constexpr int kSqRows = 32;       // rows per tile
+constexpr int kSqCols = 64;       // delta columns per block (whole engines)
+constexpr int kSqK = 64;          // bins per staged chunk
+constexpr int kSqLd = kSqK + 8;   // shared-memory row stride in halves (conflict-free ldmatrix)
+constexpr int kSqThreads = 256;
 constexpr int kSqMaxBins = 4096;  // histogram bins of an engine with an S(Q) term
-constexpr int kSqBits = 48;       // largest |T| is below 2^48: 2^15 unit deltas fit in an int64 sum
+constexpr int kSqBits = 48;       // largest |T| is below 2^48: 2^14 unit deltas fit in an int64 sum
+constexpr int kSqStageHalves = (kSqLimbs * kSqRows + kSqCols) * kSqLd;
+constexpr int kSqSmemBytes = 2 * kSqStageHalves * 2;
+static_assert(kSqLimbs * kSqRows * (kSqCols + 1) * 4 <= kSqSmemBytes, "epilogue reuses the staging buffers");
+
+// A block of delta columns: engines of one table, adjacent in its X.
+struct SqBlock {
+    const __half *TD;  // [kSqLimbs][hsp][hsp] digit l of T[c][b] at (l hsp + b) hsp + c
+    const __half *X;   // the block's first column (columns are hsp apart)
+    int hsp, hs, ncol, nrb;
+    int e0, neng;      // its engines: engs[e0 .. e0 + neng) = (engine id, first column in the block)
+};
 
 struct SqParams {
     const EDesc *desc;
-    const int2 *items;
+    const SqBlock *blocks;
+    const int2 *engs;
+    const int2 *items;  // (block, row block) tiles, then (-1 - engine id, 0) commits
     int nitems;
     Sched *sched;
+    unsigned *status;
 };
+
+__device__ __forceinline__ void sq_cp16(void *dst, const void *src, bool valid)
+{
+    const unsigned d = smem_addr(dst);
+    const int n = valid ? 16 : 0;  // zero fill
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(n) : "memory");
+}
+
+__device__ __forceinline__ void sq_ldsm_x4(unsigned (&r)[4], const __half *p)
+{
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(smem_addr(p)));
+}
+
+__device__ __forceinline__ void sq_mma(float (&d)[4], const unsigned (&a)[4], unsigned b0, unsigned b1)
+{
+    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, "
+                 "{%8, %9}, {%0, %1, %2, %3};"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// Stage chunk kc of a tile: the digit rows [l][b0 + r][kc kSqK ..] and the
+// block's columns [n][kc kSqK ..] (columns past ncol are zero filled).
+__device__ __forceinline__ void sq_stage(const SqBlock &bk, int b0, int kc, __half *stage)
+{
+    const int c0 = kc * kSqK;
+    constexpr int kChunks = kSqK / 8;  // 16-byte chunks per row
+    constexpr int kArows = kSqLimbs * kSqRows;
+    for (int k = threadIdx.x; k < (kArows + kSqCols) * kChunks; k += kSqThreads) {
+        const int row = k / kChunks, ch = k - row * kChunks;
+        __half *dst = stage + row * kSqLd + ch * 8;
+        if (row < kArows) {
+            const int l = row / kSqRows, r = row - l * kSqRows;
+            const __half *src = bk.TD + ((size_t)l * bk.hsp + b0 + r) * bk.hsp + c0 + ch * 8;
+            sq_cp16(dst, src, true);
+        } else {
+            const int n = row - kArows;
+            const bool valid = n < bk.ncol;
+            const __half *src = bk.X + (size_t)(valid ? n : 0) * bk.hsp + c0 + ch * 8;
+            sq_cp16(dst, src, valid);
+        }
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+// z of column `col` in row r of the tile from the staged fp32 digit sums.
+__device__ __forceinline__ long long sq_combine(const float *accs, int r, int col)
+{
+    unsigned long long acc = 0;
+#pragma unroll
+    for (int l = 0; l < kSqLimbs; ++l)
+        acc += (unsigned long long)(long long)accs[(l * kSqRows + r) * (kSqCols + 1) + col] << (kSqDigitBits * l);
+    return (long long)acc;
+}
+
+__device__ void sq_tile(const SqParams &p, const SqBlock &bk, int rb, __half *smem)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int half = warp & 1;   // rows 16 half .. 16 half + 15 of every digit
+    const int npair = warp >> 1; // columns 16 npair .. 16 npair + 15
+    const int b0 = rb * kSqRows;
+    const int nk = bk.hsp / kSqK;
+    const bool on0 = 16 * npair < bk.ncol, on1 = 16 * npair + 8 < bk.ncol;
+    float acc[kSqLimbs][2][4];
+#pragma unroll
+    for (int l = 0; l < kSqLimbs; ++l)
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+#pragma unroll
+            for (int i = 0; i < 4; ++i) acc[l][j][i] = 0.0f;
+    sq_stage(bk, b0, 0, smem);
+    for (int kc = 0; kc < nk; ++kc) {
+        __half *cur = smem + (kc & 1) * kSqStageHalves;
+        if (kc + 1 < nk) {
+            sq_stage(bk, b0, kc + 1, smem + ((kc + 1) & 1) * kSqStageHalves);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
+        }
+        __syncthreads();
+        if (on0) {
+            const __half *Bs = cur + kSqLimbs * kSqRows * kSqLd;
+#pragma unroll
+            for (int kk = 0; kk < kSqK; kk += 16) {
+                // B fragments of the warp's two 8-column tiles ([n][k] rows)
+                unsigned bf[4];
+                sq_ldsm_x4(bf, Bs + (16 * npair + (lane & 7) + ((lane >> 4) << 3)) * kSqLd + kk +
+                                   ((lane >> 3) & 1) * 8);
+#pragma unroll
+                for (int l = 0; l < kSqLimbs; ++l) {
+                    unsigned af[4];
+                    sq_ldsm_x4(af, cur + (l * kSqRows + 16 * half + (lane & 15)) * kSqLd + kk + (lane >> 4) * 8);
+                    sq_mma(acc[l][0], af, bf[0], bf[1]);
+                    if (on1)
+                        sq_mma(acc[l][1], af, bf[2], bf[3]);
+                }
+            }
+        }
+        __syncthreads();  // the buffer is refilled next round
+    }
+    // fp32 digit sums to shared memory: accs[l][r][col]
+    float *accs = reinterpret_cast<float *>(smem);
+    {
+        const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+        for (int l = 0; l < kSqLimbs; ++l)
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                const int col = 16 * npair + 8 * j + 2 * t;
+                const int r = 16 * half + g;
+                float *o = accs + (l * kSqRows + r) * (kSqCols + 1) + col;
+                o[0] = acc[l][j][0];
+                o[1] = acc[l][j][1];
+                o[8 * (kSqCols + 1)] = acc[l][j][2];
+                o[8 * (kSqCols + 1) + 1] = acc[l][j][3];
+            }
+    }
+    __syncthreads();
+    // one warp per engine, one lane per row
+    for (int k = warp; k < bk.neng; k += kSqThreads / 32) {
+        const int2 ec = p.engs[bk.e0 + k];
+        const EDesc &D = p.desc[ec.x];
+        const int hs = D.hs, np = D.npairs;
+        const int b = b0 + lane;
+        const bool row = b < hs;
+        double y = 0.0;
+        for (int q = 0; q < np; ++q) {
+            const int n = __ldcg(D.evn + q);
+            long long z = 0;
+            if (n >= 0) {
+                z = sq_combine(accs, lane, ec.y + q);
+            } else if (n != INT_MIN) {
+                const int *__restrict__ ev = D.evl + q * hs;
+                if (row)
+                    for (int i = 0; i < -1 - n; ++i) {
+                        const int e = __ldcg(ev + i);
+                        z += (long long)(short)(e & 0xffff) * __ldg(D.T + (size_t)(e >> 16) * hs + b);
+                    }
+            } else {
+                const int *__restrict__ dq = D.dP + q * hs;
+                if (row)
+                    for (int c = 0; c < hs; ++c) {
+                        const int v = __ldcg(dq + c);
+                        if (v)
+                            z += (long long)v * __ldg(D.T + (size_t)c * hs + b);
+                    }
+            }
+            y = fma(D.pc[q] * D.yscale, (double)z, y);
+        }
+        double part = 0.0;
+        if (row) {
+            D.y[b] = y;
+            const double sv = __ldcg(D.Sb + b);
+            if (sv != 0.0)
+                part = (D.Rq[b] * sv) * (y - D.h[b]);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+        if (lane == 0) {
+            D.sqpart[rb] = part;
+            __threadfence();
+            atomicAdd(&D.st->sq_done, 1u);
+        }
+    }
+    __syncthreads();  // the staging buffers are reused by the next item
+}
 
 __device__ void sq_finish(const EDesc &D, int *s_flag, double *s_val, MovedGroup &g)
 {
@@ -1664,6 +1977,8 @@ __device__ void sq_finish(const EDesc &D, int *s_flag, double *s_val, MovedGroup
             D.h[b] = fma(-2.0, __ldcg(D.y + b), D.h[b]);
         }
         commit_moved_group(D, g);
+        if (D.dense)
+            dense_commit(D);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1677,6 +1992,8 @@ __device__ void sq_finish(const EDesc &D, int *s_flag, double *s_val, MovedGroup
             S.sd = s_val[1];
             S.sd_sq = s_val[2];
             S.accepted += 1;
+            if (D.dense)
+                S.sf = S.sf_prop;
         }
         S.step += 1;
         S.tcount = 0u;
@@ -1685,20 +2002,15 @@ __device__ void sq_finish(const EDesc &D, int *s_flag, double *s_val, MovedGroup
     }
 }
 
-// The S(Q) term of one step over (engine, block of kSqRows rows) items: the
-// CTA's four thread groups take the element pairs q = g, g + 4, ... and form
-// z_q(b) for the block's rows -- from the GEMM's digit products, or for a
-// step with a large delta the exact integer sum over the pair's list (or its
-// deltas) -- then y(b) = yscale sum_q pair_coef_q z_q(b) in q order, the
-// block's share of x (y - h) by a fixed tree.  k_sq_commit then decides and
-// commits, one CTA per engine.
-__global__ void __launch_bounds__(kSqThreads) k_sq_step(SqParams p)
+__global__ void __launch_bounds__(kSqThreads) k_sq_fused(SqParams p)
 {
-    __shared__ long long zq[kMaxP][kSqRows];
-    __shared__ int s_n[kMaxP];
-    __shared__ double red[kSqRows];
+    extern __shared__ __align__(16) unsigned char sq_smem_raw[];
+    __half *smem = reinterpret_cast<__half *>(sq_smem_raw);
     __shared__ int s_item;
-    const int r = threadIdx.x % kSqRows, g = threadIdx.x / kSqRows;
+    __shared__ int s_ready;
+    __shared__ double s_val[3];
+    __shared__ int s_flag;
+    __shared__ MovedGroup s_group;
     for (;;) {
         if (threadIdx.x == 0) {
             const unsigned long long k = atomicAdd(&p.sched->claimed, 1ull);
@@ -1709,66 +2021,31 @@ __global__ void __launch_bounds__(kSqThreads) k_sq_step(SqParams p)
         if (it < 0)
             break;
         const int2 item = p.items[it];
-        const EDesc &D = p.desc[item.x];
-        const int hs = D.hs, np = D.npairs;
-        const int b = item.y * kSqRows + r;
-        const bool row = b < hs;
-        if (threadIdx.x < np)
-            s_n[threadIdx.x] = __ldcg(D.evn + threadIdx.x);
-        __syncthreads();
-        for (int q = g; q < np; q += kSqGroups) {
-            const int n = s_n[q];
-            long long z = 0;
-            if (row) {
-                if (n >= 0) {
-                    // sum_l 256^l Y_l(b): the digit products are exact
-                    // integers; the sum is taken modulo 2^64 (|z| < 2^63)
-                    const float *__restrict__ Yq = D.Y + (size_t)q * D.yld + b;
-                    float yl[kSqLimbs];
-#pragma unroll
-                    for (int l = 0; l < kSqLimbs; ++l) yl[l] = __ldcg(Yq + (size_t)l * D.hsp);
-                    unsigned long long acc = 0;
-#pragma unroll
-                    for (int l = 0; l < kSqLimbs; ++l) acc += (unsigned long long)(long long)yl[l] << (8 * l);
-                    z = (long long)acc;
-                } else if (n != INT_MIN) {
-                    const int *__restrict__ ev = D.evl + q * hs;
-                    for (int k = 0; k < -1 - n; ++k) {
-                        const int e = __ldcg(ev + k);
-                        z += (long long)(short)(e & 0xffff) * __ldg(D.T + (size_t)(e >> 16) * hs + b);
-                    }
-                } else {
-                    const int *__restrict__ dq = D.dP + q * hs;
-                    for (int c = 0; c < hs; ++c) {
-                        const int v = __ldcg(dq + c);
-                        if (v)
-                            z += (long long)v * __ldg(D.T + (size_t)c * hs + b);
-                    }
+        if (item.x >= 0) {
+            sq_tile(p, p.blocks[item.x], item.y, smem);
+            continue;
+        }
+        const EDesc &D = p.desc[-1 - item.x];
+        if (threadIdx.x == 0) {
+            // the engine's row blocks were claimed before this item by
+            // running CTAs; a lost one gives up after kSpinLimit polls
+            const volatile unsigned *done = &D.st->sq_done;
+            int ok = 0;
+            for (uint32_t k = 0; k < kSpinLimit; ++k) {
+                if (*done >= (unsigned)D.sqblk) {
+                    ok = 1;
+                    break;
                 }
+                __nanosleep(32);
             }
-            zq[q][r] = z;
+            if (!ok)
+                atomicOr(p.status, DS_BARRIER_TIMEOUT);
+            __threadfence();
+            s_ready = ok;
         }
         __syncthreads();
-        if (g == 0) {
-            double part = 0.0;
-            if (row) {
-                double y = 0.0;
-                for (int q = 0; q < np; ++q) y = fma(D.pc[q] * D.yscale, (double)zq[q][r], y);
-                D.y[b] = y;
-                const double sv = __ldcg(D.Sb + b);
-                if (sv != 0.0)
-                    part = (D.Rq[b] * sv) * (y - D.h[b]);
-            }
-            red[r] = part;
-        }
-        __syncthreads();
-        for (int st = kSqRows / 2; st > 0; st >>= 1) {
-            if ((int)threadIdx.x < st)
-                red[threadIdx.x] += red[threadIdx.x + st];
-            __syncthreads();
-        }
-        if (threadIdx.x == 0)
-            D.sqpart[item.y] = red[0];
+        if (s_ready)
+            sq_finish(D, &s_flag, s_val, s_group);
         __syncthreads();
     }
     if (threadIdx.x == 0) {
@@ -1780,19 +2057,6 @@ __global__ void __launch_bounds__(kSqThreads) k_sq_step(SqParams p)
             __threadfence();
         }
     }
-}
-
-// One CTA per engine (the item of its first row block; the others return):
-// sum the blocks' shares, decide and commit.
-__global__ void __launch_bounds__(kSqThreads) k_sq_commit(SqParams p)
-{
-    __shared__ double s_val[3];
-    __shared__ int s_flag;
-    __shared__ MovedGroup s_group;
-    const int2 item = p.items[blockIdx.x];
-    if (item.y != 0)
-        return;
-    sq_finish(p.desc[item.x], &s_flag, s_val, s_group);
 }
 
 // S(Q) of engine `id`'s current counts (StructureFactorConstraints.py:780-822
@@ -1872,20 +2136,20 @@ __global__ void k_sq_quantize(double *K, const double *R0, int hs, int s)
     }
 }
 
-// The GEMM operand: TL[(l hsp + b) + c (kSqLimbs hsp)] = digit l of T[c][b]
-// (balanced base 256, so T = sum_l 256^l digit_l), zero outside hs x hs.
-__global__ void k_sq_limbs(const long long *T, int hs, int hsp, __half *TL)
+// The product's operand: TD[(l hsp + b) hsp + c] = digit l of T[c][b]
+// (balanced base 2048, so T = sum_l 2048^l digit_l), zero outside hs x hs.
+__global__ void k_sq_digits(const long long *T, int hs, int hsp, __half *TD)
 {
     const long long n = (long long)hsp * hsp;
-    const long long ld = (long long)kSqLimbs * hsp;
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(k / hsp), b = (int)(k - (long long)c * hsp);
+        const int b = (int)(k / hsp), c = (int)(k - (long long)b * hsp);
         long long v = (b < hs && c < hs) ? T[(long long)c * hs + b] : 0;
 #pragma unroll
         for (int l = 0; l < kSqLimbs; ++l) {
-            const long long d = ((v + 128) & 255) - 128;
-            v = (v - d) >> 8;
-            TL[(long long)l * hsp + b + c * ld] = __int2half_rn((int)d);
+            const long long half = 1ll << (kSqDigitBits - 1);
+            const long long d = ((v + half) & ((1ll << kSqDigitBits) - 1)) - half;
+            v = (v - d) >> kSqDigitBits;
+            TD[(long long)l * n + k] = __int2half_rn((int)d);
         }
     }
 }
@@ -1958,12 +2222,11 @@ struct SqTable {
     double *M = nullptr, *w = nullptr, *R0 = nullptr;
     long long *T = nullptr;
     size_t bytes = 0;
-    int hsp = 0;           // hs rounded up to a multiple of 8
-    __half *TL = nullptr;  // [kSqLimbs hsp][hsp] digits of T, column-major GEMM operand
-    // this step's fp16 deltas of every engine on the table (hsp x ncols,
-    // column-major) and their digit products (kSqLimbs hsp x ncols)
+    int hsp = 0;           // hs rounded up to a multiple of kSqK
+    __half *TD = nullptr;  // [kSqLimbs][hsp][hsp] digits of T (k_sq_digits)
+    // this step's fp16 deltas of every engine on the table (ncols columns of
+    // hsp bins)
     __half *X = nullptr;
-    float *Y = nullptr;
     int ncols = 0, cap = 0;
 };
 
@@ -2001,8 +2264,6 @@ struct EngineSet {
     EDesc *fdesc = nullptr;        // descriptors of the fused items, in work-list order
     int fdesc_cap = 0;
     int *fpos = nullptr;           // per fused item: its engine's index in live order (host-buffer steps)
-    cublasHandle_t blas = nullptr; // the S(Q) terms' GEMM (created on first use)
-    void *blas_ws = nullptr;       // its fixed workspace (graph capture allocates nothing)
     int2 *items = nullptr;
     int items_cap = 0;
     int nitems = 0;
@@ -2020,11 +2281,21 @@ struct EngineSet {
     int stage_cap = 0;
     Sched *sched = nullptr;        // [0]: histogram step kernels, [1]: S(Q) kernel
     std::vector<SqTable> tables;
-    std::vector<int2> sq_host;     // (engine, row block) of every live engine with an S(Q) term
+    // S(Q) work lists: the batched list (every block's tiles, then one commit
+    // per engine) at [0, sq_nbatch), then each engine's own list (its tiles
+    // and its commit) at sq_first[id], sq_count[id] items
+    std::vector<int2> sq_host;
+    int sq_nbatch = 0;
     std::vector<int> sq_first, sq_count;
     std::vector<int> sq_xcol;      // per engine id: its first delta column in its table's X
+    std::vector<SqBlock> sq_hblocks;
+    std::vector<int2> sq_hengs;
     int2 *sq_items = nullptr;
     int sq_cap = 0;
+    SqBlock *sq_blocks = nullptr;
+    int sq_blocks_cap = 0;
+    int2 *sq_engs = nullptr;
+    int sq_engs_cap = 0;
     cudaStream_t stream = nullptr;
     std::map<std::pair<int, int>, cudaGraphExec_t> graphs;
     cudaGraphExec_t host_graph[2] = {nullptr, nullptr};  // step_host per slot: copy in, scatter,
@@ -2035,12 +2306,18 @@ struct EngineSet {
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct BlobLayout {
-    size_t box, real, mol, counts, delta, rfac, invvol, expd, dw, pc, pi, pj, dP, pidx, tlist, R, A, Bq, Sb, moves,
+    size_t box, real, mol, counts, delta, rfac, invvol, expd, dw, pc, pi, pj, dP, pidx, tlist, R, A, Bq, Sb, Gc, fnum,
+        fden, win, moves,
         results, st, Rq, rfacq, sqexp, h, y, sqpart, sqv, evl, evn, groups, cbox, cmol, csl, cstart, clo, chi,
         total;
 };
 
 static int spec_group(const frmc_engine_spec &sp) { return sp.group_size > 1 ? sp.group_size : 1; }
+static double spec_scale(const frmc_engine_spec &sp) { return sp.scale_factor == 0.0 ? 1.0 : sp.scale_factor; }
+static bool spec_dense(const frmc_engine_spec &sp)
+{
+    return spec_scale(sp) != 1.0 || sp.fit_frequency > 0 || sp.window_len > 0;
+}
 
 static BlobLayout blob_layout(const frmc_engine_spec &sp)
 {
@@ -2072,6 +2349,11 @@ static BlobLayout blob_layout(const frmc_engine_spec &sp)
     L.A = take(8 * hs);
     L.Bq = take(8 * hs);
     L.Sb = take(8 * hs);
+    const bool dense = spec_dense(sp);
+    L.Gc = take(dense ? 8 * hs : 0);
+    L.fnum = take(dense ? 8 * hs : 0);
+    L.fden = take(dense ? 8 * hs : 0);
+    L.win = take(dense ? 8 * (size_t)sp.window_len : 0);
     L.moves = take(sizeof(EMove) * (size_t)sp.move_cap);
     L.results = take(sizeof(EResult) * (size_t)sp.move_cap);
     L.st = take(sizeof(EState));
@@ -2115,6 +2397,10 @@ static int check_spec(const frmc_engine_spec &sp)
     for (int i = 0; i < sp.n; ++i)
         if (sp.el[i] < 0 || sp.el[i] >= sp.ne)
             return set_error(FRMC_E_ARG, "engine spec: atom %d element out of range", i);
+    if (sp.fit_frequency < 0 || (sp.fit_frequency > 0 && (!sp.fit_num || !(sp.fit_min <= sp.fit_max))) ||
+        sp.window_len < 0 || sp.window_len > 255 || sp.window_len > sp.hs || (sp.window_len > 0 && !sp.window) ||
+        !std::isfinite(sp.scale_factor))
+        return set_error(FRMC_E_ARG, "engine spec: invalid scale factor or window fields");
     if (sp.sq_table >= 0) {
         if (sp.nq < 1 || !sp.sq_rfac || !sp.sq_inv_shell_volume || !sp.sq_experimental ||
             !(sp.sq_variance_squared > 0) || !(sp.sq_rho0 > 0))
@@ -2165,7 +2451,7 @@ static int refresh(EngineSet *s)
         const int dpw = D.dpk ? (D.npairs * D.hs + 1) / 2 : D.npairs * D.hs;  // words of the deltas
         const int dp = (dpw + 3) & ~3, bins = (D.hs + 1) & ~1;
         const int dpi = std::max(s->fused_dp_ints, dp), bi = std::max(s->fused_bins, bins);
-        if (s->fused && fused_dyn_bytes(dpi, bi, kMaxEngineThreads) <= kFusedDynMax &&
+        if (s->fused && !D.dense && fused_dyn_bytes(dpi, bi, kMaxEngineThreads) <= kFusedDynMax &&
             s->slots[id].cost <= kFusedMaxCost) {
             fused_ids.push_back(id);
             s->fused_dp_ints = dpi;
@@ -2174,6 +2460,18 @@ static int refresh(EngineSet *s)
     }
     std::stable_sort(fused_ids.begin(), fused_ids.end(),
                      [s](int a, int b) { return s->slots[a].cost > s->slots[b].cost; });
+    {
+        // When every fused engine gets its own CTA at launch (CTA b takes
+        // item b) and SMs hold more than one CTA, the CTAs past the first wave
+        // share SMs with the first: order that second part cheapest first, so
+        // that the costliest engines share their SM with the cheapest ones.
+        Context *c;
+        FRMC_TRY(get_context(&c));
+        const int wave = c->sms;
+        if (s->ctas_per_sm > 1 && (int)fused_ids.size() > wave &&
+            (long long)fused_ids.size() <= (long long)wave * s->ctas_per_sm)
+            std::reverse(fused_ids.begin() + wave, fused_ids.end());
+    }
     s->fused_item.assign(nslots, -1);
     for (int id : fused_ids) {
         s->fused_item[id] = (int)items.size();
@@ -2187,24 +2485,6 @@ static int refresh(EngineSet *s)
         for (int t = 0; t < D.ntiles; ++t) items.push_back(make_int2(id, t));
     }
     s->nbatch = (int)items.size() - s->nsolo;
-    s->sq_host.clear();
-    s->sq_first.assign(nslots, -1);
-    s->sq_count.assign(nslots, 0);
-    for (int id : s->live) {
-        const EDesc &D = s->slots[id].d;
-        if (!D.sq)
-            continue;
-        s->sq_first[id] = (int)s->sq_host.size();
-        s->sq_count[id] = D.sqblk;
-        for (int k = 0; k < D.sqblk; ++k) s->sq_host.push_back(make_int2(id, k));
-    }
-    if ((int)s->sq_host.size() > s->sq_cap) {
-        if (s->sq_items) cudaFree(s->sq_items);
-        s->sq_items = nullptr;
-        int cap = std::max((int)s->sq_host.size(), 2 * s->sq_cap);
-        FRMC_CUDA(cudaMalloc(&s->sq_items, sizeof(int2) * cap));
-        s->sq_cap = cap;
-    }
     if ((int)fused_ids.size() > s->fdesc_cap) {
         if (s->fdesc) cudaFree(s->fdesc);
         s->fdesc = nullptr;
@@ -2236,10 +2516,9 @@ static int refresh(EngineSet *s)
         FRMC_CUDA(cudaMalloc(&s->dlive, sizeof(int) * cap));
         s->dlive_cap = cap;
     }
-    // S(Q) GEMM columns: each live engine with an S(Q) term owns npairs
-    // adjacent fp16 delta columns of its table's X and the matching digit-
-    // product columns of Y.  X is all zero between steps (the finisher clears
-    // its columns), so columns can be dealt afresh here.
+    // S(Q) delta columns: each live engine with an S(Q) term owns npairs
+    // adjacent fp16 columns of its table's X.  X is all zero between steps
+    // (the finisher clears its columns), so columns can be dealt afresh here.
     s->sq_xcol.assign(nslots, -1);
     for (auto &t : s->tables) t.ncols = 0;
     for (int id : s->live) {
@@ -2251,35 +2530,14 @@ static int refresh(EngineSet *s)
         t.ncols += sl.d.npairs;
     }
     FRMC_CUDA(cudaStreamSynchronize(s->stream));
-    bool any_sq = false;
-    for (const auto &t : s->tables) any_sq |= t.ncols > 0;
-    if (any_sq && !s->blas) {
-        // created here, never inside a stream capture; the workspace is fixed
-        // so that captured GEMMs allocate nothing
-        const cublasStatus_t cs = cublasCreate(&s->blas);
-        if (cs != CUBLAS_STATUS_SUCCESS) {
-            s->blas = nullptr;
-            return set_error(FRMC_E_CUDA, "cublasCreate failed (status %d)", (int)cs);
-        }
-        const size_t ws = 32u << 20;
-        FRMC_CUDA(cudaMalloc(&s->blas_ws, ws));
-        if (cublasSetWorkspace(s->blas, s->blas_ws, ws) != CUBLAS_STATUS_SUCCESS ||
-            cublasSetMathMode(s->blas, (cublasMath_t)(CUBLAS_DEFAULT_MATH |
-                                                       CUBLAS_MATH_DISALLOW_REDUCED_PRECISION_REDUCTION)) !=
-                CUBLAS_STATUS_SUCCESS)
-            return set_error(FRMC_E_CUDA, "cuBLAS workspace / math mode");
-    }
     for (auto &t : s->tables) {
         if (t.ncols <= t.cap)
             continue;
         if (t.X) cudaFree(t.X);
-        if (t.Y) cudaFree(t.Y);
         t.X = nullptr;
-        t.Y = nullptr;
         const int cap = std::max(t.ncols, 2 * t.cap);
         FRMC_CUDA(cudaMalloc(&t.X, sizeof(__half) * (size_t)t.hsp * cap));
         FRMC_CUDA(cudaMemset(t.X, 0, sizeof(__half) * (size_t)t.hsp * cap));
-        FRMC_CUDA(cudaMalloc(&t.Y, sizeof(float) * (size_t)kSqLimbs * t.hsp * cap));
         t.cap = cap;
     }
     for (int id : s->live) {
@@ -2289,10 +2547,91 @@ static int refresh(EngineSet *s)
         const SqTable &t = s->tables[sl.sq_table];
         sl.d.hsp = t.hsp;
         sl.d.xld = t.hsp;
-        sl.d.yld = kSqLimbs * t.hsp;
         sl.d.X = t.X + (size_t)s->sq_xcol[id] * t.hsp;
-        sl.d.Y = t.Y + (size_t)s->sq_xcol[id] * kSqLimbs * t.hsp;
     }
+    // S(Q) work lists.  Blocks of whole engines (at most kSqCols columns, in
+    // live order) per table; the batched list is every block's row-block
+    // tiles, then one commit per engine; each engine also gets a block of its
+    // own and a list of its tiles and commit for steps of that engine alone.
+    s->sq_hblocks.clear();
+    s->sq_hengs.clear();
+    s->sq_host.clear();
+    s->sq_first.assign(nslots, -1);
+    s->sq_count.assign(nslots, 0);
+    for (int ti = 0; ti < (int)s->tables.size(); ++ti) {
+        const SqTable &t = s->tables[ti];
+        const int nrb = (t.hs + kSqRows - 1) / kSqRows;
+        SqBlock cur{};
+        int col0 = 0;
+        bool open = false;
+        for (int id : s->live) {
+            const Slot &sl = s->slots[id];
+            if (!sl.d.sq || sl.sq_table != ti)
+                continue;
+            const int col = s->sq_xcol[id];
+            if (open && col + sl.d.npairs - col0 > kSqCols) {
+                s->sq_hblocks.push_back(cur);
+                open = false;
+            }
+            if (!open) {
+                col0 = col;
+                cur = SqBlock{t.TD, t.X + (size_t)col * t.hsp, t.hsp, t.hs, 0, nrb, (int)s->sq_hengs.size(), 0};
+                open = true;
+            }
+            s->sq_hengs.push_back(make_int2(id, col - col0));
+            cur.neng += 1;
+            cur.ncol = col + sl.d.npairs - col0;
+        }
+        if (open)
+            s->sq_hblocks.push_back(cur);
+    }
+    for (int bi = 0; bi < (int)s->sq_hblocks.size(); ++bi)
+        for (int rb = 0; rb < s->sq_hblocks[bi].nrb; ++rb) s->sq_host.push_back(make_int2(bi, rb));
+    for (int id : s->live)
+        if (s->slots[id].d.sq)
+            s->sq_host.push_back(make_int2(-1 - id, 0));
+    s->sq_nbatch = (int)s->sq_host.size();
+    for (int id : s->live) {
+        const Slot &sl = s->slots[id];
+        if (!sl.d.sq)
+            continue;
+        const SqTable &t = s->tables[sl.sq_table];
+        const int nrb = (t.hs + kSqRows - 1) / kSqRows;
+        const int bi = (int)s->sq_hblocks.size();
+        s->sq_hblocks.push_back(SqBlock{t.TD, sl.d.X, t.hsp, t.hs, sl.d.npairs, nrb, (int)s->sq_hengs.size(), 1});
+        s->sq_hengs.push_back(make_int2(id, 0));
+        s->sq_first[id] = (int)s->sq_host.size();
+        for (int rb = 0; rb < nrb; ++rb) s->sq_host.push_back(make_int2(bi, rb));
+        s->sq_host.push_back(make_int2(-1 - id, 0));
+        s->sq_count[id] = nrb + 1;
+    }
+    if ((int)s->sq_host.size() > s->sq_cap) {
+        if (s->sq_items) cudaFree(s->sq_items);
+        s->sq_items = nullptr;
+        const int cap = std::max((int)s->sq_host.size(), 2 * s->sq_cap);
+        FRMC_CUDA(cudaMalloc(&s->sq_items, sizeof(int2) * cap));
+        s->sq_cap = cap;
+    }
+    if ((int)s->sq_hblocks.size() > s->sq_blocks_cap) {
+        if (s->sq_blocks) cudaFree(s->sq_blocks);
+        s->sq_blocks = nullptr;
+        const int cap = std::max((int)s->sq_hblocks.size(), 2 * s->sq_blocks_cap);
+        FRMC_CUDA(cudaMalloc(&s->sq_blocks, sizeof(SqBlock) * cap));
+        s->sq_blocks_cap = cap;
+    }
+    if ((int)s->sq_hengs.size() > s->sq_engs_cap) {
+        if (s->sq_engs) cudaFree(s->sq_engs);
+        s->sq_engs = nullptr;
+        const int cap = std::max((int)s->sq_hengs.size(), 2 * s->sq_engs_cap);
+        FRMC_CUDA(cudaMalloc(&s->sq_engs, sizeof(int2) * cap));
+        s->sq_engs_cap = cap;
+    }
+    if (!s->sq_hblocks.empty())
+        FRMC_CUDA(cudaMemcpy(s->sq_blocks, s->sq_hblocks.data(), sizeof(SqBlock) * s->sq_hblocks.size(),
+                             cudaMemcpyHostToDevice));
+    if (!s->sq_hengs.empty())
+        FRMC_CUDA(cudaMemcpy(s->sq_engs, s->sq_hengs.data(), sizeof(int2) * s->sq_hengs.size(),
+                             cudaMemcpyHostToDevice));
     std::vector<EDesc> hd(nslots);
     for (int k = 0; k < nslots; ++k) hd[k] = s->slots[k].d;
     FRMC_CUDA(cudaStreamSynchronize(s->stream));
@@ -2357,50 +2696,17 @@ static int launch_items(EngineSet *s, const int2 *items, int count, int eval_onl
     return FRMC_OK;
 }
 
-// S(Q) row blocks [first, first + count) of the set's S(Q) item list.
-// The digit products of every table's delta columns (engine >= 0: that
-// engine's columns only): Y = TL X, fp16 in, fp32 accumulate -- the products
-// are exact integers (see kSqLimbs).
-static int sq_gemm(EngineSet *s, int engine, cudaStream_t st)
-{
-    if (!s->blas)
-        return set_error(FRMC_E_STATE, "S(Q) GEMM before the engine set was refreshed");
-    if (cublasSetStream(s->blas, st) != CUBLAS_STATUS_SUCCESS)
-        return set_error(FRMC_E_CUDA, "cublasSetStream failed");
-    const float one = 1.0f, zero = 0.0f;
-    for (int ti = 0; ti < (int)s->tables.size(); ++ti) {
-        const SqTable &t = s->tables[ti];
-        int col0 = 0, ncol = t.ncols;
-        if (engine >= 0) {
-            if (s->slots[engine].sq_table != ti)
-                continue;
-            col0 = s->sq_xcol[engine];
-            ncol = s->slots[engine].d.npairs;
-        }
-        if (ncol <= 0)
-            continue;
-        const int M = kSqLimbs * t.hsp;
-        const cublasStatus_t bs = cublasGemmEx(
-            s->blas, CUBLAS_OP_N, CUBLAS_OP_N, M, ncol, t.hsp, &one, t.TL, CUDA_R_16F, M,
-            t.X + (size_t)col0 * t.hsp, CUDA_R_16F, t.hsp, &zero, t.Y + (size_t)col0 * M, CUDA_R_32F, M,
-            CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
-        if (bs != CUBLAS_STATUS_SUCCESS)
-            return set_error(FRMC_E_CUDA, "cublasGemmEx failed (%d)", (int)bs);
-    }
-    return FRMC_OK;
-}
-
-static int launch_sq(EngineSet *s, int first, int count, cudaStream_t st, int engine = -1)
+// The S(Q) work list items [first, first + count): tiles, then commits.
+static int launch_sq(EngineSet *s, int first, int count, cudaStream_t st)
 {
     if (count <= 0)
         return FRMC_OK;
-    FRMC_TRY(sq_gemm(s, engine, st));
     Context *c;
     FRMC_TRY(get_context(&c));
-    const int grid = std::min(count, c->sms * 8);
-    SqParams p{s->ddesc, s->sq_items + first, count, s->sched + 1};
-    k_sq_step<<<grid, kSqThreads, 0, st>>>(p);
-    k_sq_commit<<<count, kSqThreads, 0, st>>>(p);
+    const int grid = std::min(count, c->sms * 2);
+    SqParams p{s->ddesc, s->sq_blocks, s->sq_engs, s->sq_items + first, count, s->sched + 1, &s->sched[0].status};
+    FRMC_CUDA(cudaFuncSetAttribute(k_sq_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, kSqSmemBytes));
+    k_sq_fused<<<grid, kSqThreads, kSqSmemBytes, st>>>(p);
     FRMC_CUDA(cudaGetLastError());
     return FRMC_OK;
 }
@@ -2421,7 +2727,7 @@ static int launch_batched(EngineSet *s, cudaStream_t st)
         FRMC_TRY(launch_items(s, s->items + s->nsolo, s->nfused, 0, st, fused_dyn_smem(s), true));
     if (s->nbatch > s->nfused)
         FRMC_TRY(launch_items(s, s->items + s->nsolo + s->nfused, s->nbatch - s->nfused, 0, st));
-    FRMC_TRY(launch_sq(s, 0, (int)s->sq_host.size(), st));
+    FRMC_TRY(launch_sq(s, 0, s->sq_nbatch, st));
     return FRMC_OK;
 }
 
@@ -2742,6 +3048,18 @@ static int add_engine(EngineSet *s, const frmc_engine_spec &sp, int *out_id)
     D.A = (double *)(b + L.A);
     D.Bq = (double *)(b + L.Bq);
     D.Sb = (double *)(b + L.Sb);
+    if (spec_dense(sp)) {
+        D.dense = 1;
+        D.wlen = sp.window_len;
+        D.fit_freq = sp.fit_frequency;
+        D.sf0 = spec_scale(sp);
+        D.fit_min = sp.fit_min;
+        D.fit_max = sp.fit_max;
+        D.Gc = (double *)(b + L.Gc);
+        D.fnum = (double *)(b + L.fnum);
+        D.fden = (double *)(b + L.fden);
+        D.win = (double *)(b + L.win);
+    }
     D.moves = (EMove *)(b + L.moves);
     D.group = spec_group(sp);
     D.groups = D.group > 1 ? (EGroup *)(b + L.groups) : nullptr;
@@ -2832,6 +3150,17 @@ static int add_engine(EngineSet *s, const frmc_engine_spec &sp, int *out_id)
         up(D.clo, cg.clo.data(), 16 * cg.clo.size());
         up(D.chi, cg.chi.data(), 16 * cg.chi.size());
     }
+    std::vector<double> fden;
+    if (D.dense) {
+        fden.assign(sp.hs, 1.0);
+        if (sp.fit_den)
+            for (int bb = 0; bb < sp.hs; ++bb) fden[bb] = sp.fit_den[bb];
+        if (sp.fit_num)
+            up(D.fnum, sp.fit_num, 8 * (size_t)sp.hs);
+        up(D.fden, fden.data(), 8 * fden.size());
+        if (sp.window_len > 0)
+            up(D.win, sp.window, 8 * (size_t)sp.window_len);
+    }
     if (tab) {
         up(D.Rq, Rqt.data(), 8 * Rqt.size());
         up(D.rfacq, sp.sq_rfac, 8 * (size_t)sp.hs);
@@ -2885,13 +3214,10 @@ static void free_set(EngineSet *s)
         if (sl.blob) cudaFree(sl.blob);
     for (auto &t : s->tables) {
         if (t.blob) cudaFree(t.blob);
-        if (t.TL) cudaFree(t.TL);
+        if (t.TD) cudaFree(t.TD);
         if (t.X) cudaFree(t.X);
-        if (t.Y) cudaFree(t.Y);
     }
-    if (s->blas) cublasDestroy(s->blas);
-    if (s->blas_ws) cudaFree(s->blas_ws);
-    void *ptrs[] = {s->ddesc, s->fdesc, s->fpos, s->items, s->dlive, s->sched, s->sq_items};
+    void *ptrs[] = {s->ddesc, s->fdesc, s->fpos, s->items, s->dlive, s->sched, s->sq_items, s->sq_blocks, s->sq_engs};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int k = 0; k < 2; ++k) {
@@ -2922,10 +3248,10 @@ int frmc_engine_footprint(const frmc_engine_spec *spec, int64_t *bytes)
         return set_error(FRMC_E_ARG, "engine_footprint: null argument");
     int64_t b = (int64_t)blob_layout(*spec).total;
     if (spec->sq_table >= 0) {
-        // the engine's columns of its table's fp16 deltas and fp32 digit
-        // products (counted twice: the shared buffers grow by doubling)
-        const int64_t hsp = (spec->hs + 7) & ~7;
-        b += 2 * (int64_t)spec->npairs * hsp * (int64_t)(sizeof(__half) + sizeof(float) * kSqLimbs);
+        // the engine's columns of its table's fp16 deltas (counted twice:
+        // the shared buffer grows by doubling)
+        const int64_t hsp = (spec->hs + kSqK - 1) / kSqK * kSqK;
+        b += 2 * (int64_t)spec->npairs * hsp * (int64_t)sizeof(__half);
     }
     *bytes = b;
     return FRMC_OK;
@@ -3222,7 +3548,7 @@ int frmc_engines_step(void *handle, int32_t engine, int32_t steps, int use_graph
         else
             FRMC_TRY(launch_items(s, s->items + s->item_first[engine], count, 0, sx, 0, false, nullptr, nullptr,
                                   kMaxEngineThreads));
-        return launch_sq(s, s->sq_first[engine], s->sq_count[engine], sx, engine);
+        return launch_sq(s, s->sq_first[engine], s->sq_count[engine], sx);
     };
     if (!use_graph) {
         for (int k = 0; k < steps; ++k) FRMC_TRY(one(st));
@@ -3619,11 +3945,11 @@ int frmc_engines_sq_table(void *handle, int32_t hs, int32_t nq, const double *M,
         ce = cudaGetLastError();
     }
     if (ce == cudaSuccess) {
-        t.hsp = (hs + 7) & ~7;
-        ce = cudaMalloc(&t.TL, sizeof(__half) * (size_t)kSqLimbs * t.hsp * t.hsp);
+        t.hsp = (hs + kSqK - 1) / kSqK * kSqK;
+        ce = cudaMalloc(&t.TD, sizeof(__half) * (size_t)kSqLimbs * t.hsp * t.hsp);
     }
     if (ce == cudaSuccess) {
-        k_sq_limbs<<<c->sms * 4, 256, 0, s->stream>>>(t.T, hs, t.hsp, t.TL);
+        k_sq_digits<<<c->sms * 4, 256, 0, s->stream>>>(t.T, hs, t.hsp, t.TD);
         ce = cudaGetLastError();
         t.bytes += sizeof(__half) * (size_t)kSqLimbs * t.hsp * t.hsp;
     }
@@ -3631,7 +3957,7 @@ int frmc_engines_sq_table(void *handle, int32_t hs, int32_t nq, const double *M,
         ce = cudaStreamSynchronize(s->stream);
     if (ce != cudaSuccess) {
         cudaFree(t.blob);
-        if (t.TL) cudaFree(t.TL);
+        if (t.TD) cudaFree(t.TD);
         return cuda_fail(ce, "S(Q) table");
     }
     s->tables.push_back(t);

@@ -105,6 +105,7 @@ struct FullTune {
     int qcap = 16;      // queue slots per thread
     int ctas_per_sm = 1;
     double min_pairs_tiled = 8.0e6;
+    int aggregate = 0;  // 1: queued pairs binned with warp-aggregated atomics (__match_any_sync)
 };
 
 // All-pairs (i < j) histogram of `n` packed atoms (x, y, z, el bits) into

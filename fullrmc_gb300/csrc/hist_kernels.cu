@@ -78,6 +78,7 @@ struct FullParams {
     long long nitems;
     int qcap;
     int smem_hist;
+    int agg;      // warp-aggregated binning of queued pairs
 };
 
 // Item t of the row-major upper triangle (I <= J) of an nt x nt tile grid.
@@ -162,7 +163,30 @@ __device__ __forceinline__ void flush_queue(const FullParams &p, uint2 *&qp, uin
                                             const int *tm, const RowRegs<R> &rr, unsigned *shist)
 {
     while (__any_sync(0xffffffffu, qp != qb)) {
-        if (qp != qb) {
+        if (p.agg) {
+            // lanes that bin into the same counter add once, with the group's size
+            const unsigned lane = threadIdx.x & 31u;
+            unsigned long long key = ~0ull - lane;  // unique for lanes without a pair
+            unsigned *dst = nullptr;
+            long long flat = 0;
+            if (qp != qb) {
+                qp -= nthr;
+                uint2 e = *qp;
+                int jl = (int)(e.y >> 2);
+                int r = (int)(e.y & 3u);
+                int elj = __float_as_int(tb[jl].w);
+                bool same = pick<R>(rr.mol, r) == tm[jl];
+                int bin = pair_bin(__uint_as_float(e.x), p.minD, p.binw);
+                flat = (pick<R>(rr.rb, r) + elj) * (long long)p.hs + bin;
+                if ((unsigned long long)flat < (unsigned long long)p.total) {
+                    dst = same ? p.intra : (shist ? shist : p.inter);
+                    key = ((unsigned long long)flat << 1) | (same ? 1ull : 0ull);
+                }
+            }
+            const unsigned grp = __match_any_sync(0xffffffffu, key);
+            if (dst && (unsigned)(__ffs(grp) - 1) == lane)
+                atomicAdd(dst + flat, (unsigned)__popc(grp));
+        } else if (qp != qb) {
             qp -= nthr;
             uint2 e = *qp;
             int jl = (int)(e.y >> 2);
@@ -511,6 +535,7 @@ int launch_full_hist_on(int sms, int max_smem_optin, const float4 *atoms, const 
     if (p.item_begin >= p.nitems)
         return FRMC_OK;
     p.qcap = tn.qcap < 2 * R + 2 ? 2 * R + 2 : tn.qcap;
+    p.agg = tn.aggregate ? 1 : 0;
     const size_t base = 16 + (size_t)p.T * 40;
     const size_t hist_bytes = ((size_t)p.total * 4 + 15) & ~(size_t)15;
     const size_t queue_bytes = queued ? (size_t)p.qcap * threads * 8 : 0;

@@ -40,7 +40,9 @@ class _Spec(ctypes.Structure):
                 ("move_cap", ctypes.c_int32), ("sq_table", ctypes.c_int32), ("nq", ctypes.c_int32),
                 ("sq_rfac", F64P), ("sq_inv_shell_volume", F64P), ("sq_experimental", F64P),
                 ("sq_variance_squared", ctypes.c_double), ("sq_rho0", ctypes.c_double),
-                ("group_size", ctypes.c_int32)]
+                ("group_size", ctypes.c_int32), ("scale_factor", ctypes.c_double), ("fit_frequency", ctypes.c_int32),
+                ("fit_min", ctypes.c_double), ("fit_max", ctypes.c_double), ("fit_num", F64P), ("fit_den", F64P),
+                ("window_len", ctypes.c_int32), ("window", F64P)]
 
 
 _vp = ctypes.c_void_p
@@ -94,18 +96,49 @@ def normalized_weighting(counts, scattering):
     return w
 
 
+def window_same(x, window):
+    """numpy.convolve(x, window, 'same') in FP64."""
+    return np.convolve(np.asarray(x, np.float64), np.asarray(window, np.float64), "same")
+
+
 @dataclass
 class PDFModel:
-    """FP64 constants of one PairDistributionConstraint on an r grid."""
+    """FP64 constants of one PairDistributionConstraint (kind "pdf": G(r),
+    PairDistributionConstraints.py:847-895) or PairCorrelationConstraint
+    (kind "gr": g(r), PairCorrelationConstraints.py:126-184) on an r grid.
+
+    scale_factor, adjust_scale_factor = (frequency, minimum, maximum) and
+    window follow the constraints' arguments (Core/Constraint.py:981-1235):
+    the model is window * (s G) for G(r), and window * (1 + s (g - 1)) for
+    g(r); s is refitted (clamped) on the proposal whenever the engine's
+    accepted count is a multiple of a non-zero frequency, and an accepted
+    move keeps its s.  The window is normalized in float32 as fullrmc does.
+
+    On the device both kinds run as G(b) = R(b) S(b) - rfac(b) compared with
+    a shifted experimental curve: for g(r), rfac = 1 (so G is g - 1) and the
+    curve is g_exp - window * 1 (g_exp - 1 without a window), which leaves
+    every deviation unchanged."""
     r: np.ndarray                # experimental r grid (float32, uniform)
-    G_exp: np.ndarray            # experimental G(r)
+    G_exp: np.ndarray            # experimental G(r) (kind "gr": g(r))
     elements_count: np.ndarray   # atoms per element index
     weights: np.ndarray          # (ne, ne) symmetric w_ij
     volume: float
     data_weights: np.ndarray | None = None
     variance_squared: float = 1.0
+    kind: str = "pdf"
+    scale_factor: float = 1.0
+    adjust_scale_factor: tuple = (0, 0.8, 1.2)
+    window: np.ndarray | None = None
 
     def __post_init__(self):
+        if self.kind not in ("pdf", "gr"):
+            raise ValueError("PDFModel.kind must be 'pdf' or 'gr', got %r" % (self.kind,))
+        freq, lo, hi = self.adjust_scale_factor
+        if int(freq) < 0 or not float(lo) <= float(hi):
+            raise ValueError("adjust_scale_factor must be (frequency >= 0, minimum, maximum >= minimum)")
+        self.fit_frequency, self.fit_min, self.fit_max = int(freq), float(lo), float(hi)
+        if not np.isfinite(self.scale_factor) or self.scale_factor == 0:
+            raise ValueError("scale_factor must be a finite non-zero number")
         x = np.asarray(self.r, F32)
         self.r = x
         b = F32(x[1] - x[0])
@@ -120,7 +153,27 @@ class PDFModel:
         n = np.asarray(self.elements_count, np.float64)
         self.n_atoms = int(n.sum())
         self.rho0 = self.n_atoms / float(self.volume)
-        self.rfac = 4.0 * np.pi * x.astype(np.float64) * self.rho0
+        cfac = 4.0 * np.pi * x.astype(np.float64) * self.rho0
+        self.rfac = cfac if self.kind == "pdf" else np.ones(len(x))
+        win = None
+        if self.window is not None:
+            w32 = np.asarray(self.window, F32).ravel()
+            if w32.ndim != 1 or not 0 < len(w32) <= min(255, len(x)):
+                raise ValueError("window must be a 1-D array of at most min(255, bins) values")
+            w32 = w32 / np.sum(w32)   # Constraints/PairDistributionConstraints.py:700 (float32)
+            win = w32.astype(np.float64)
+        self.window_fp64 = win
+        dw = 1.0 if self.data_weights is None else np.asarray(self.data_weights, np.float64)
+        exp = np.asarray(self.G_exp, np.float64)
+        if self.kind == "pdf":
+            self.exp_dev = exp
+            self.fit_num = dw * exp
+            self.fit_den = None
+        else:
+            self.exp_dev = exp - (window_same(np.ones(len(x)), win) if win is not None else 1.0)
+            self.fit_num = dw * cfac * cfac * (exp - 1.0)
+            self.fit_den = cfac * cfac
+        self.dense = self.scale_factor != 1.0 or self.fit_frequency > 0 or win is not None
         ne = len(n)
         pi, pj, pc = [], [], []
         for i in range(ne):
@@ -149,8 +202,22 @@ class PDFModel:
         g /= self.shell_volumes
         return self.rfac * (g - 1.0)
 
-    def chi2_fp64(self, intra, inter):
-        d = np.asarray(self.G_exp, np.float64) - self.G_fp64(intra, inter)
+    def fit_fp64(self, intra, inter):
+        """The fitted scale factor of these counts (the device's formula)."""
+        G = self.G_fp64(intra, inter)
+        den = np.sum((1.0 if self.fit_den is None else self.fit_den) * G * G)
+        if not den > 0:
+            return None
+        return float(min(max(np.sum(self.fit_num * G) / den, self.fit_min), self.fit_max))
+
+    def chi2_fp64(self, intra, inter, scale=None):
+        """The G(r) term of chi2 of these counts at scale factor `scale`
+        (default: the model's scale_factor), FP64, the device's formula."""
+        s = self.scale_factor if scale is None else scale
+        u = s * self.G_fp64(intra, inter)
+        if self.window_fp64 is not None:
+            u = window_same(u, self.window_fp64)
+        d = self.exp_dev - u
         w = 1.0 if self.data_weights is None else np.asarray(self.data_weights, np.float64)
         return float(np.sum(w * d * d) / self.variance_squared)
 
@@ -189,11 +256,19 @@ class SQModel:
     element-pair weights."""
     pdf: PDFModel
     q: np.ndarray                # experimental Q values (float32)
-    S_exp: np.ndarray            # experimental S(Q)
+    S_exp: np.ndarray            # experimental S(Q) (reduced: S(Q) - 1)
     data_weights: np.ndarray | None = None
     variance_squared: float = 1.0
+    reduced: bool = False        # ReducedStructureFactorConstraint (StructureFactorConstraints.py:1255-1262)
+    scale_factor: float = 1.0
+    adjust_scale_factor: tuple = (0, 0.8, 1.2)
+    window: np.ndarray | None = None
 
     def __post_init__(self):
+        if self.scale_factor != 1.0 or int(self.adjust_scale_factor[0]) != 0 or self.window is not None:
+            raise ValueError("the device engines' S(Q) term has no scale factor, fitted scale factor or window "
+                             "(StructureFactorConstraints.py:814-821); use scale_factor=1, "
+                             "adjust_scale_factor=(0, ...) and window=None")
         m = self.pdf
         self.q = np.asarray(self.q, F32)
         self.nq = len(self.q)
@@ -230,7 +305,7 @@ class SQModel:
         return self.rfac * (g - 1.0)
 
     def S_fp64(self, intra, inter):
-        return self.G_fp64(intra, inter) @ self.M + 1.0
+        return self.G_fp64(intra, inter) @ self.M + (0.0 if self.reduced else 1.0)
 
     def sd_fp64(self, intra, inter):
         d = np.asarray(self.S_exp, np.float64) - self.S_fp64(intra, inter)
@@ -344,7 +419,7 @@ def make_spec(system, move_cap, sq_table=-1):
                 pi=np.ascontiguousarray(m.pair_i), pj=np.ascontiguousarray(m.pair_j),
                 pc=np.ascontiguousarray(m.pair_coef), rfac=np.ascontiguousarray(m.rfac),
                 iv=np.ascontiguousarray(1.0 / m.shell_volumes),
-                ex=np.ascontiguousarray(np.asarray(m.G_exp, np.float64)),
+                ex=np.ascontiguousarray(np.asarray(m.exp_dev, np.float64)),
                 dw=None if m.data_weights is None else np.ascontiguousarray(m.data_weights, np.float64))
     sp = _Spec()
     sp.n = arrs["box"].shape[0]
@@ -370,11 +445,23 @@ def make_spec(system, move_cap, sq_table=-1):
     sp.tolerance = float(s.tolerance)
     sp.move_cap = int(move_cap)
     sp.group_size = int(getattr(s, "group_size", 1) or 1)
+    sp.scale_factor = float(m.scale_factor)
+    if m.dense:
+        arrs.update(fnum=np.ascontiguousarray(m.fit_num, np.float64),
+                    fden=None if m.fit_den is None else np.ascontiguousarray(m.fit_den, np.float64),
+                    win=None if m.window_fp64 is None else np.ascontiguousarray(m.window_fp64))
+        sp.fit_frequency = m.fit_frequency
+        sp.fit_min, sp.fit_max = m.fit_min, m.fit_max
+        sp.fit_num = arrs["fnum"].ctypes.data_as(F64P)
+        sp.fit_den = arrs["fden"].ctypes.data_as(F64P) if arrs["fden"] is not None else None
+        if arrs["win"] is not None:
+            sp.window_len = len(arrs["win"])
+            sp.window = arrs["win"].ctypes.data_as(F64P)
     sp.sq_table = -1
     if s.sq is not None:
         q = s.sq
         arrs.update(sq_rfac=np.ascontiguousarray(q.rfac), sq_iv=np.ascontiguousarray(1.0 / q.shell_volumes),
-                    sq_exp=np.ascontiguousarray(np.asarray(q.S_exp, np.float64)))
+                    sq_exp=np.ascontiguousarray(np.asarray(q.S_exp, np.float64) + (1.0 if q.reduced else 0.0)))
         sp.sq_table = int(sq_table)
         sp.nq = q.nq
         sp.sq_rfac = arrs["sq_rfac"].ctypes.data_as(F64P)
@@ -554,8 +641,9 @@ class EngineSet:
         check(load().frmc_engines_set_mode(self.handle, int(bool(fused))))
 
     def set_sq_gemm_limit(self, limit):
-        """Largest element-pair delta the S(Q) product takes through the GEMM
-        (default 32); 0 forces the exact sum over the list of deltas and -1
+        """Largest element-pair delta the S(Q) product takes through the
+        tensor cores (default 2048; a column must also change at most 2^14
+        unit counts); 0 forces the exact sum over the list of deltas and -1
         the dense integer loop (all three give the same integers)."""
         check(load().frmc_engines_set_sq_gemm_limit(self.handle, int(limit)))
 

@@ -1,6 +1,6 @@
 """Small, self-contained runs of the hot kernels, sized for profiling.
 
-    python -m fullrmc_gb300.profile_cases allpairs --n 30000 --reps 3
+    python -m fullrmc_gb300.profile_cases allpairs --n 30000 --reps 3 [--aggregate 1]
     python -m fullrmc_gb300.profile_cases engines --count 64 --steps 5 [--tune 1024,1024,1] [--sq]
     python -m fullrmc_gb300.profile_cases serve --seconds 3 --limit 30
 
@@ -19,7 +19,7 @@ import json
 import numpy as np
 
 
-def allpairs(n, reps):
+def allpairs(n, reps, aggregate=0):
     import torch
     from fullrmc_gb300 import _native as native
     from fullrmc_gb300 import synthetic
@@ -36,6 +36,7 @@ def allpairs(n, reps):
     a4 = torch.empty((n, 4), dtype=torch.float32, device=dev)
     cnt = torch.zeros(2 * total, dtype=torch.int32, device=dev)
     B = np.ascontiguousarray(s.basis)
+    native.call("frmc_set_full_aggregate", int(aggregate))
     with torch.cuda.stream(st):
         native.call("frmc_dev_pack_atoms", c.data_ptr(), el.data_ptr(), n, a4.data_ptr(), st.cuda_stream)
         args = (a4.data_ptr(), mol.data_ptr(), n, B.ctypes.data_as(F32P), 1, ne, m.minDistance, m.maxDistance,
@@ -49,7 +50,9 @@ def allpairs(n, reps):
             ev.append((e0, e1))
     torch.cuda.synchronize()
     ms = [a.elapsed_time(b) for a, b in ev]
-    return {"case": "allpairs", "atoms": n, "ms": ms, "pairs": n * (n - 1) / 2, "in_range": int(cnt.sum().item())}
+    native.call("frmc_set_full_aggregate", 0)
+    return {"case": "allpairs", "atoms": n, "aggregate": int(aggregate), "ms": ms, "pairs": n * (n - 1) / 2,
+            "in_range": int(cnt.sum().item())}
 
 
 def engines(count, steps, tune=None, sq=False):
@@ -91,6 +94,7 @@ def main():
     ap.add_argument("case", choices=["allpairs", "engines", "serve"])
     ap.add_argument("--n", type=int, default=30000)
     ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--aggregate", type=int, default=0, help="all-pairs binning: 1 = warp-aggregated atomics")
     ap.add_argument("--count", type=int, default=64)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--tune", default=None, help="tile,threads,ctas_per_sm of the engine work list")
@@ -100,7 +104,7 @@ def main():
     a = ap.parse_args()
     tune = tuple(int(x) for x in a.tune.split(",")) if a.tune else None
     if a.case == "allpairs":
-        out = allpairs(a.n, a.reps)
+        out = allpairs(a.n, a.reps, a.aggregate)
     elif a.case == "engines":
         out = engines(a.count, a.steps, tune, a.sq)
     else:

@@ -236,6 +236,11 @@ int frmc_dev_full_hist_counts(const void *atoms4, const int32_t *moleculeIndex, 
  * frmc_full_pairs_histograms_coords uses it (below: the row kernel).  Applies
  * to later calls from every thread. */
 int frmc_set_full_tune(int threads, int rows, int queued, int qcap, int ctas_per_sm, double min_pairs_tiled);
+/* Binning of the tiled kernel's queued pairs: 0 (default) plain shared-memory
+ * atomics, 1 warp-aggregated atomics (lanes whose pairs fall in the same
+ * counter are grouped with __match_any_sync and add once).  Counts are the
+ * same either way; the switch exists to measure both. */
+int frmc_set_full_aggregate(int on);
 /* The same all-pairs histogram restricted to work items [item_begin, item_end)
  * of the kernel's (row tile, column tile) triangle, for sharding one system
  * across devices; the per-item partial counts of disjoint ranges sum to the

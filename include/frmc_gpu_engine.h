@@ -71,6 +71,24 @@ typedef struct {
     /* Atoms per move (0 or 1: single-atom moves; up to 16: moves of atom
      * groups such as molecules, pushed with frmc_engines_push_group_moves). */
     int32_t group_size;
+    /* Scale factor and window function of the G(r) term
+     * (PairDistributionConstraints.py:884-893, Core/Constraint.py:1363-1424;
+     * PairCorrelationConstraints.py:155-184 for g(r)).  The model compared
+     * with `experimental` is window * (s G) (numpy.convolve 'same') with
+     * G(b) = R(b) sum_p pair_coef_p n_p(b) - rfac(b).  s is scale_factor, or,
+     * when fit_frequency > 0 and the engine's accepted count is a multiple of
+     * it, clamp(sum fit_num G / sum fit_den G^2, fit_min, fit_max) of the
+     * proposed G (fit_den NULL = 1); an accepted move keeps its s.  A
+     * scale_factor of 0 is taken as 1 (a spec zeroed past group_size).
+     * Engines with s != 1, fit_frequency > 0 or a window evaluate every bin
+     * at every step (they take the tile-split path). */
+    double scale_factor;
+    int32_t fit_frequency;
+    double fit_min, fit_max;
+    const double *fit_num;     /* (hs,) fit numerator weights times the fit target */
+    const double *fit_den;     /* (hs,) fit denominator weights, or NULL        */
+    int32_t window_len;        /* 0: no window; at most 255 and at most hs      */
+    const double *window;      /* (window_len,) the window, already normalized  */
 } frmc_engine_spec;
 
 /* A G(r) -> S(Q) table shared by the set's engines that use the same r shells
@@ -90,8 +108,8 @@ int frmc_engines_sq(void *handle, int32_t e, double *sq);
  * sd_sq / sq_variance_squared. */
 int frmc_engines_terms(void *handle, int32_t e, double *sd, double *sd_sq);
 /* Device bytes one engine of this spec occupies (its state, tables, rings and
- * column grid, and with an S(Q) term its share of the table's GEMM delta and
- * product buffers; the shared S(Q) table itself is not included). */
+ * column grid, and with an S(Q) term its share of the table's fp16 delta
+ * columns; the shared S(Q) table itself is not included). */
 int frmc_engine_footprint(const frmc_engine_spec *spec, int64_t *bytes);
 /* An empty engine set on the current device. */
 int frmc_engines_new(void **handle);
@@ -133,11 +151,14 @@ int frmc_engines_regrid(void *handle, int32_t e);
  * boundaries with w = 1). */
 int frmc_cell_metric(const float *basis, int32_t isPBC, double *w, double *lam, int32_t *mode);
 int frmc_engines_cells(void *handle, int32_t e, int32_t *ncells, int64_t *swept);
-/* The S(Q) term's product y = T x runs as one fp16 GEMM over digits of T when
- * every element-pair delta of the step is at most `limit` in magnitude
- * (default and maximum 32, where the GEMM is exact), else as an exact integer
- * sum over the step's list of deltas; -1 takes the dense integer loop.  All
- * three give the same integers; the lower limits exist to test that. */
+/* The S(Q) term's product y = T x runs on the tensor cores (the library's own
+ * kernel: fp16 base-2048 digits of T times fp16 deltas, fp32 accumulation)
+ * for an element-pair delta column whose entries are at most `limit` in
+ * magnitude (default and maximum 2048) and whose absolute sum is at most
+ * 2^14, where every product sum is an exact integer; other columns take an
+ * exact integer sum over the step's list of deltas; -1 takes the dense
+ * integer loop.  All three give the same integers; the lower limits exist to
+ * test that. */
 int frmc_engines_set_sq_gemm_limit(void *handle, int32_t limit);
 /* All-pairs histograms of the initial coordinates and the initial chi2. */
 int frmc_engines_init(void *handle);

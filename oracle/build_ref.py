@@ -40,6 +40,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF_OUT = os.path.join(HERE, "_ref")
 SRC_DIR = os.path.join(REF_OUT, "src")
 PKG_DIR = os.path.join(REF_OUT, "fullrmc", "Core")
+# Where the reference checkout lies: the FRMC_REFERENCE_ROOT environment
+# variable or `--reference-root` on the command line; the default is this
+# recipe's checkout location.  Without the checkout, stage 2 still compiles
+# the C of an earlier stage 1.
 REFERENCE_ROOT = os.environ.get("FRMC_REFERENCE_ROOT", "/root/reference")
 MODULES = ("pairs_distances", "pairs_histograms", "reciprocal_space",
            "boundary_conditions_collection", "atomic_distances", "atomic_coordination")
@@ -115,5 +119,7 @@ def import_reference():
 
 
 if __name__ == "__main__":
+    if "--reference-root" in sys.argv:
+        REFERENCE_ROOT = sys.argv[sys.argv.index("--reference-root") + 1]
     ok = build()
     print("reference built" if ok else "reference sources unavailable")

@@ -324,6 +324,44 @@ def fit_scale_factor_fp64(experimental, model, dataWeights=None, lo=0.0, hi=np.i
     return float(min(max(sf, lo), hi))
 
 
+def window_same_fp64(x, window):
+    """numpy.convolve(x, window, 'same') in float64:
+    PairDistributionConstraints.py:891-893, PairCorrelationConstraints.py:167-168."""
+    return np.convolve(np.asarray(x, np.float64), np.asarray(window, np.float64), "same")
+
+
+def pdc_model_fp64(intra, inter, elementsCount, weights, volume, shellVolumes, shellCenters, rho0, scale,
+                   window=None):
+    """The PairDistributionConstraint's model: total G(r), times the scale
+    factor, convolved with the window (PairDistributionConstraints.py:847-895;
+    no shape function, no multiframe prior)."""
+    G = scale * total_Gr_fp64(intra, inter, elementsCount, weights, volume, shellVolumes, shellCenters, rho0)
+    return G if window is None else window_same_fp64(G, window)
+
+
+def pcf_model_fp64(intra, inter, elementsCount, weights, volume, shellVolumes, shellCenters, rho0, scale,
+                   window=None):
+    """The PairCorrelationConstraint's model: total g(r); with a scale factor
+    g -> 1 + s G / (4 pi r rho0) with G = 4 pi r rho0 (g - 1); then the window
+    (PairCorrelationConstraints.py:126-169).  Where 4 pi r rho0 is 0 (r = 0)
+    the reference divides 0 by 0; there the restatement keeps 1 + s (g - 1)."""
+    g = total_gr_fp64(intra, inter, elementsCount, weights, volume, shellVolumes)
+    if scale != 1:
+        c = 4.0 * np.pi * np.asarray(shellCenters, np.float64) * float(rho0)
+        G = c * (g - 1.0) * scale
+        safe = np.where(c != 0.0, c, 1.0)
+        g = np.where(c != 0.0, 1.0 + G / safe, 1.0 + scale * (g - 1.0))
+    return g if window is None else window_same_fp64(g, window)
+
+
+def pcf_fit_scale_factor_fp64(experimental, g, shellCenters, rho0, dataWeights=None, lo=0.0, hi=np.inf):
+    """PairCorrelationConstraint's fit: on G(r) = 4 pi r rho0 (g - 1) of both
+    curves (PairCorrelationConstraints.py:171-184)."""
+    c = 4.0 * np.pi * np.asarray(shellCenters, np.float64) * float(rho0)
+    return fit_scale_factor_fp64(c * (np.asarray(experimental, np.float64) - 1.0), c * (np.asarray(g, np.float64) - 1.0),
+                                 dataWeights, lo, hi)
+
+
 def gr_to_sq_fp64(distances, gr, qrange, rho):
     """reciprocal_space.pyx:42-73 in float64."""
     r = np.asarray(distances, np.float64)

@@ -44,6 +44,7 @@ def test_every_declared_symbol_is_exported(lib):
 
 def test_python_signatures_cover_exports(lib):
     from fullrmc_gb300 import _native
+    from fullrmc_gb300 import engine  # noqa: F401  (registers the engine-module entry points)
     for n in declared_symbols():
         if n.startswith("frmc_engine") or n.startswith("frmc_serve") or n.startswith("frmc_batch"):
             continue

@@ -30,13 +30,14 @@ def _digest(*arrays):
     return h.hexdigest()
 
 
-def _set_tune(threads=512, rows=2, queued=-1, qcap=16, ctas=1, min_pairs=8.0e6):
+def _set_tune(threads=512, rows=2, queued=-1, qcap=16, ctas=1, min_pairs=8.0e6, aggregate=0):
     from fullrmc_gb300._native import call
     call("frmc_set_full_tune", threads, rows, queued, qcap, ctas, float(min_pairs))
+    call("frmc_set_full_aggregate", aggregate)
 
 
 @pytest.mark.parametrize("name", ["cfg2_triclinic_100k", "cfg2_triclinic_100k_mol4"])
-@pytest.mark.parametrize("tune", [dict(), dict(threads=256, rows=1, queued=0)])
+@pytest.mark.parametrize("tune", [dict(), dict(threads=256, rows=1, queued=0), dict(aggregate=1)])
 def test_all_pairs_100k_triclinic_equals_reference(name, tune):
     import fullrmc_gb300
     from fullrmc_gb300 import synthetic

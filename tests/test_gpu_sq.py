@@ -187,3 +187,76 @@ def test_table_shape_mismatch_is_refused():
     with pytest.raises((ValueError, NativeError)):
         check(load().frmc_engines_add(es.handle, ctypes.byref(sp), ctypes.byref(i)))
     es.close()
+
+
+def test_sq_many_engines_span_several_column_blocks():
+    """More delta columns than one tile block holds (64): the product is
+    tiled over several blocks of whole engines; every chain is still the
+    same batched, split and alone."""
+    systems = _systems(28, seed=31, nmin=300, nmax=900)
+    assert sum(len(s.model.pair_i) for s in systems) > 64
+    steps = 25
+    mv = _moves(systems, steps, seed=32)
+    base = _run(systems, mv, steps)
+    _same(base, _run(systems, mv, steps, mode="solo", graph=False))
+    _same(base, _run(systems, mv, steps, fused=0))
+    _same(base, _run(systems, mv, steps, gemm_limit=0))
+
+
+def test_sq_large_group_moves_take_the_exact_sum():
+    """16-atom group moves in a dense one-species system with a long r range
+    (0-36 A, 3,601 bins) change more than 2^14 unit counts in one delta
+    column (the per-bin changes partly cancel, so a short range stays far
+    below), beyond the tensor-core product's exact range: those columns take
+    the exact integer sum, and the chain equals the all-list chain (limit 0)
+    bit for bit."""
+    from fullrmc_gb300 import synthetic
+    from fullrmc_gb300.engine import SQModel
+    rng = np.random.default_rng(41)
+    n, G = 40000, 16
+    L = (n / 0.1) ** (1.0 / 3.0)
+    s = synthetic.make_system(rng, n, [1.0], np.diag([L, L, L]), 36.0, molsize=G)
+    q = synthetic.q_grid(0.5, 20.0, 0.05)
+    s.sq = SQModel(pdf=s.model, q=q, S_exp=np.zeros(len(q)))
+    s.sq.S_exp = synthetic.synthetic_S(np.random.default_rng(2), s.sq, s.model.G_exp)
+    s.group_size = G
+    s.groups = np.arange(n, dtype=np.int32).reshape(-1, G)
+    steps = 12
+    from fullrmc_gb300.engine import group_moves
+    mv = group_moves(np.random.default_rng(5), s.groups, steps, 0.4, 20.0)
+    # the first move's unit count changes in the one delta column, on the host
+    import oracle
+    m = s.model
+    kw = dict(basis=s.basis, isPBC=True, numberOfElements=1, minDistance=m.minDistance,
+              maxDistance=m.maxDistance, bin=m.bin, histSize=m.hs)
+    from fullrmc_gb300.engine import group_new_real
+    def delta(box, idx):
+        iM, eM = oracle.multiple_pairs_histograms_coords(idx, box, moleculeIndex=s.mol, elementIndex=s.el,
+                                                         allAtoms=True, **kw)
+        iF, eF = oracle.full_pairs_histograms_coords(box[idx], moleculeIndex=s.mol[idx], elementIndex=s.el[idx],
+                                                     **kw)
+        return (iM - iF) + (eM - eF)
+    l1 = []
+    for k in range(3):
+        idx = mv[0][k]
+        box2 = s.box_coords.copy()
+        box2[idx] = synthetic.transform_f32(s.rbasis, group_new_real(s.real_coords[idx], mv[1][k], mv[2][k]))
+        l1.append(np.abs(delta(box2, idx) - delta(s.box_coords, idx)).sum())
+    assert max(l1) > 2 ** 14, l1
+
+    def run(limit):
+        from fullrmc_gb300.engine import EngineSet
+        es = EngineSet([s], move_cap=64)
+        if limit is not None:
+            es.set_sq_gemm_limit(limit)
+        es.init()
+        es.push_group_moves(0, *mv, 0)
+        es.step(steps, graph=False)
+        out = dict(res=es.results(0, 0, steps), state=es.state(0), terms=es.terms(0), counts=es.counts(0))
+        es.close()
+        return out
+    a, b = run(None), run(0)
+    assert np.array_equal(a["res"][1], b["res"][1])
+    assert np.array_equal(a["res"][0].view(np.int64), b["res"][0].view(np.int64))
+    assert a["state"] == b["state"] and a["terms"] == b["terms"]
+    assert all(np.array_equal(x, y) for x, y in zip(a["counts"], b["counts"]))
