@@ -116,6 +116,33 @@ def load():
         return lib
 
 
+_fast = None
+_fast_tried = False
+
+
+def fastcall():
+    """The compiled fast path of the per-move drop-in calls
+    (``csrc/fastcall.c``, built beside the library), or None when it was not
+    built or ``FRMC_FASTCALL=0``.  It calls the same C entry points as the
+    ctypes wrappers, for the common case of well-formed numpy arguments."""
+    global _fast, _fast_tried
+    if not _fast_tried:
+        _fast_tried = True
+        load()
+        if os.environ.get("FRMC_FASTCALL", "1") != "0":
+            import glob
+            import importlib.machinery
+            import importlib.util
+            paths = sorted(glob.glob(os.path.join(_PKG, "_lib", "_fastcall*.so")))
+            if paths:
+                loader = importlib.machinery.ExtensionFileLoader("fullrmc_gb300._fastcall", paths[0])
+                spec = importlib.util.spec_from_loader(loader.name, loader)
+                mod = importlib.util.module_from_spec(spec)
+                loader.exec_module(mod)
+                _fast = mod
+    return _fast
+
+
 def register(name, argtypes, restype=ctypes.c_int):
     """Declare a further entry point (used by the engine modules)."""
     SIGNATURES[name] = argtypes

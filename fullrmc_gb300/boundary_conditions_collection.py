@@ -14,7 +14,7 @@ from __future__ import annotations
 import numpy as np
 
 from . import _args as A
-from ._native import call, ptr
+from ._native import call, check, fastcall, ptr
 
 NUMPY_FLOAT32 = np.float32
 
@@ -42,6 +42,13 @@ def get_reciprocal_basis(basis):
 
 def transform_coordinates(transMatrix, coords):
     """transCoords[i] = coords[i] . transMatrix (``boundary_conditions_collection.pyx:88-110``)."""
+    fast = fastcall()
+    if fast is not None:
+        r = fast.transform(transMatrix, coords)
+        if r is not None:
+            if type(r) is int:
+                check(r)
+            return r
     M = A.array("transMatrix", transMatrix, np.float32, 2)
     c = A.array("coords", coords, np.float32, 2)
     out = np.empty((c.shape[0], 3), dtype=NUMPY_FLOAT32)

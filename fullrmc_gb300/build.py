@@ -79,14 +79,36 @@ def build(verbose: bool = False, jobs: int | None = None, ptxas_info: bool = Fal
 
     with ThreadPoolExecutor(max_workers=jobs or min(8, len(srcs))) as pool:
         objs = list(pool.map(compile_one, srcs))
-    if _stale(LIB, objs):
+    lib_changed = _stale(LIB, objs)
+    if lib_changed:
         tmp = LIB + ".tmp%d" % os.getpid()
         cmd = [cc, ARCH, "-shared", "-o", tmp, *objs, "-lcudart_static", "-lrt", "-lpthread", "-ldl"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
         os.replace(tmp, LIB)
+    build_fastcall(force=lib_changed)
     return LIB
+
+
+def build_fastcall(force=False):
+    """The CPython fast path of the per-move drop-in calls (csrc/fastcall.c),
+    compiled with the host C compiler against this interpreter's headers and
+    linked to the library beside it."""
+    import sysconfig
+    src = os.path.join(CSRC, "fastcall.c")
+    out = os.path.join(LIBDIR, "_fastcall" + (sysconfig.get_config_var("EXT_SUFFIX") or ".so"))
+    if not force and not _stale(out, [src, LIB, os.path.join(INCLUDE, "frmc_gpu.h")]):
+        return out
+    cc = os.environ.get("CC", "gcc")
+    tmp = out + ".tmp%d" % os.getpid()
+    cmd = [cc, "-shared", "-fPIC", "-O2", "-std=c11", "-I" + sysconfig.get_paths()["include"], "-I" + INCLUDE, src,
+           "-L" + LIBDIR, "-lfrmc_gpu", "-Wl,-rpath,$ORIGIN", "-o", tmp]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("fastcall build failed:\n%s\n%s" % (r.stdout, r.stderr))
+    os.replace(tmp, out)
+    return out
 
 
 if __name__ == "__main__":

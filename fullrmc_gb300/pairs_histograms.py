@@ -11,7 +11,7 @@ from __future__ import annotations
 import numpy as np
 
 from . import _args as A
-from ._native import F32P, I32P, call, ptr
+from ._native import F32P, I32P, call, check, fastcall, ptr
 
 NUMPY_FLOAT32 = np.float32
 NUMPY_INT32 = np.int32
@@ -63,6 +63,14 @@ def multiple_pairs_histograms_coords(indexes, boxCoords, basis, isPBC, moleculeI
                                      allAtoms=True, ncores=1):
     """Histograms of the atoms ``indexes`` against all atoms
     (``Extensions/pairs_histograms.pyx:150-217``).  Returns (hintra, hinter)."""
+    fast = fastcall()
+    if fast is not None:
+        r = fast.multiple(indexes, boxCoords, basis, isPBC, moleculeIndex, elementIndex, numberOfElements,
+                          minDistance, maxDistance, bin, histSize, allAtoms, ncores)
+        if r is not None:
+            if type(r) is int:
+                check(r)
+            return r
     idx = A.array("indexes", indexes, np.int32, 1)
     c = A.array("boxCoords", boxCoords, np.float32, 2)
     B = A.array("basis", basis, np.float32, 2)
@@ -118,6 +126,14 @@ def multiple_pairs_histograms_dists(indexes, distances, moleculeIndex, elementIn
 def full_pairs_histograms_coords(boxCoords, basis, isPBC, moleculeIndex, elementIndex, numberOfElements,
                                  minDistance, maxDistance, bin, histSize, ncores=1):
     """All-pairs (i < j) histograms (``Extensions/pairs_histograms.pyx:289-335``)."""
+    fast = fastcall()
+    if fast is not None:
+        r = fast.full(boxCoords, basis, isPBC, moleculeIndex, elementIndex, numberOfElements, minDistance,
+                      maxDistance, bin, histSize, ncores)
+        if r is not None:
+            if type(r) is int:
+                check(r)
+            return r
     c = A.array("boxCoords", boxCoords, np.float32, 2)
     B = A.array("basis", basis, np.float32, 2)
     isPBC = A.bint(isPBC)

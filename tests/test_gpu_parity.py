@@ -263,3 +263,33 @@ def test_multiple_copy_branch_vs_oracle(gpu):
                        capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "copy branch ok" in r.stdout
+
+
+def test_fast_path_equals_ctypes_path(gpu):
+    """The compiled fast path of the per-move calls gives the ctypes
+    wrappers' results bit for bit (same C entry points)."""
+    from fullrmc_gb300 import _native
+    f = _native.fastcall()
+    if f is None:
+        pytest.skip("fast path not built")
+    a = _system(71, 5000, 3, "xytri", molsize=13, rmax=15.0)
+    try:
+        for idx in (np.array([17], np.int32), np.arange(13 * 40, 13 * 41, dtype=np.int32)):
+            _native._fast = f
+            got_m = gpu.pairs_histograms.multiple_pairs_histograms_coords(indexes=idx, allAtoms=True, **a)
+            sub = dict(a, boxCoords=a["boxCoords"][idx], moleculeIndex=a["moleculeIndex"][idx],
+                       elementIndex=a["elementIndex"][idx])
+            got_f = gpu.pairs_histograms.full_pairs_histograms_coords(**sub)
+            got_t = gpu.boundary_conditions_collection.transform_coordinates(a["basis"], a["boxCoords"][idx])
+            _native._fast = None
+            want_m = gpu.pairs_histograms.multiple_pairs_histograms_coords(indexes=idx, allAtoms=True, **a)
+            want_f = gpu.pairs_histograms.full_pairs_histograms_coords(**sub)
+            want_t = gpu.boundary_conditions_collection.transform_coordinates(a["basis"], a["boxCoords"][idx])
+            for g_, w_ in zip(got_m + got_f, want_m + want_f):
+                assert g_.dtype == w_.dtype and np.array_equal(g_, w_)
+            assert np.array_equal(got_t, want_t)
+        _native._fast = f
+        with pytest.raises(IndexError):
+            gpu.pairs_histograms.multiple_pairs_histograms_coords(indexes=np.array([5000], np.int32), **a)
+    finally:
+        _native._fast = f
