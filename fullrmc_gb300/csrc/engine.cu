@@ -1729,14 +1729,15 @@ __global__ void k_gather_results(const EDesc *desc, const int *ids, EResult *out
 // Every quantity of an engine depends only on that engine's columns, so a
 // chain is the same in any batch and alone.
 constexpr int kSqRows = 32;       // rows per tile
-constexpr int kSqCols = 64;       // delta columns per block (whole engines)
+constexpr int kSqCols = 64;       // delta columns per block at most (whole engines)
 constexpr int kSqK = 64;          // bins per staged chunk
 constexpr int kSqLd = kSqK + 8;   // shared-memory row stride in halves (conflict-free ldmatrix)
+constexpr int kSqStages = 3;      // chunks in flight: the ring hides the L2 latency of the digit rows
 constexpr int kSqThreads = 256;
 constexpr int kSqMaxBins = 4096;  // histogram bins of an engine with an S(Q) term
 constexpr int kSqBits = 48;       // largest |T| is below 2^48: 2^14 unit deltas fit in an int64 sum
 constexpr int kSqStageHalves = (kSqLimbs * kSqRows + kSqCols) * kSqLd;
-constexpr int kSqSmemBytes = 2 * kSqStageHalves * 2;
+constexpr int kSqSmemBytes = kSqStages * kSqStageHalves * 2;
 static_assert(kSqLimbs * kSqRows * (kSqCols + 1) * 4 <= kSqSmemBytes, "epilogue reuses the staging buffers");
 
 // A block of delta columns: engines of one table, adjacent in its X.
@@ -1744,32 +1745,32 @@ struct SqBlock {
     const __half *TD;  // [kSqLimbs][hsp][hsp] digit l of T[c][b] at (l hsp + b) hsp + c
     const __half *X;   // the block's first column (columns are hsp apart)
     int hsp, hs, ncol, nrb;
-    int e0, neng;      // its engines: engs[e0 .. e0 + neng) = (engine id, first column in the block)
+    int e0, neng;      // its engines: engs[e0 .. e0 + neng)
+};
+
+// What a tile needs of one engine of its block, flat (one load; no chain
+// through the descriptor): this step's delta lists and counts, the table,
+// the per-bin arrays of the x (y - h) share, where y and the share go, the
+// engine's completion counter, and its first column in the block.
+struct SqEng {
+    const int *evn, *evl, *dP;
+    const long long *T;
+    const double *pc, *Sb, *Rq, *h;
+    double *y, *sqpart;
+    unsigned *done;
+    double yscale;
+    int hs, np, lc, pad;
 };
 
 struct SqParams {
     const EDesc *desc;
     const SqBlock *blocks;
-    const int2 *engs;
+    const SqEng *engs;
     const int2 *items;  // (block, row block) tiles, then (-1 - engine id, 0) commits
     int nitems;
     Sched *sched;
     unsigned *status;
 };
-
-__device__ __forceinline__ void sq_cp16(void *dst, const void *src, bool valid)
-{
-    const unsigned d = smem_addr(dst);
-    const int n = valid ? 16 : 0;  // zero fill
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(n) : "memory");
-}
-
-__device__ __forceinline__ void sq_ldsm_x4(unsigned (&r)[4], const __half *p)
-{
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                 : "r"(smem_addr(p)));
-}
 
 __device__ __forceinline__ void sq_mma(float (&d)[4], const unsigned (&a)[4], unsigned b0, unsigned b1)
 {
@@ -1779,29 +1780,56 @@ __device__ __forceinline__ void sq_mma(float (&d)[4], const unsigned (&a)[4], un
                  : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-// Stage chunk kc of a tile: the digit rows [l][b0 + r][kc kSqK ..] and the
-// block's columns [n][kc kSqK ..] (columns past ncol are zero filled).
-__device__ __forceinline__ void sq_stage(const SqBlock &bk, int b0, int kc, __half *stage)
+// A tile's copies: each thread always moves the same kSqCopies 16-byte
+// pieces of a chunk (digit rows [l][b0 + r], then the block's columns), so
+// their addresses are formed once per tile and advance by kSqK bins per chunk.
+constexpr int kSqCopies = (kSqLimbs * kSqRows + kSqCols) * (kSqK / 8) / kSqThreads;
+static_assert((kSqLimbs * kSqRows + kSqCols) * (kSqK / 8) % kSqThreads == 0, "whole copies per thread");
+
+struct SqCopies {
+    const __half *src[kSqCopies];  // at chunk 0
+    unsigned dst[kSqCopies];       // shared-memory byte offset within a stage
+    unsigned valid;                // bit j: piece j is read (else zero filled)
+};
+
+__device__ __forceinline__ void sq_copies(const SqBlock &bk, int b0, SqCopies &c)
 {
-    const int c0 = kc * kSqK;
-    constexpr int kChunks = kSqK / 8;  // 16-byte chunks per row
+    constexpr int kChunks = kSqK / 8;  // 16-byte pieces per row
     constexpr int kArows = kSqLimbs * kSqRows;
-    for (int k = threadIdx.x; k < (kArows + kSqCols) * kChunks; k += kSqThreads) {
+    c.valid = 0u;
+#pragma unroll
+    for (int j = 0; j < kSqCopies; ++j) {
+        const int k = threadIdx.x + j * kSqThreads;
         const int row = k / kChunks, ch = k - row * kChunks;
-        __half *dst = stage + row * kSqLd + ch * 8;
+        c.dst[j] = (unsigned)(row * kSqLd + ch * 8) * 2u;
         if (row < kArows) {
             const int l = row / kSqRows, r = row - l * kSqRows;
-            const __half *src = bk.TD + ((size_t)l * bk.hsp + b0 + r) * bk.hsp + c0 + ch * 8;
-            sq_cp16(dst, src, true);
+            c.src[j] = bk.TD + ((size_t)l * bk.hsp + b0 + r) * bk.hsp + ch * 8;
+            c.valid |= 1u << j;
         } else {
             const int n = row - kArows;
-            const bool valid = n < bk.ncol;
-            const __half *src = bk.X + (size_t)(valid ? n : 0) * bk.hsp + c0 + ch * 8;
-            sq_cp16(dst, src, valid);
+            const bool v = n < bk.ncol;
+            c.src[j] = bk.X + (size_t)(v ? n : 0) * bk.hsp + ch * 8;
+            if (v)
+                c.valid |= 1u << j;
         }
     }
-    asm volatile("cp.async.commit_group;" ::: "memory");
 }
+
+// Stage chunk kc of a tile into the stage at shared address `stage`.
+__device__ __forceinline__ void sq_stage(const SqCopies &c, int kc, unsigned stage)
+{
+    const int c0 = kc * kSqK;
+#pragma unroll
+    for (int j = 0; j < kSqCopies; ++j) {
+        const int n = (c.valid >> j) & 1u ? 16 : 0;  // zero fill
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(stage + c.dst[j]), "l"(c.src[j] + c0),
+                     "r"(n)
+                     : "memory");
+    }
+}
+
+__device__ __forceinline__ void sq_commit_group() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 
 // z of column `col` in row r of the tile from the staged fp32 digit sums.
 __device__ __forceinline__ long long sq_combine(const float *accs, int r, int col)
@@ -1817,10 +1845,11 @@ __device__ void sq_tile(const SqParams &p, const SqBlock &bk, int rb, __half *sm
 {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int half = warp & 1;   // rows 16 half .. 16 half + 15 of every digit
-    const int npair = warp >> 1; // columns 16 npair .. 16 npair + 15
+    const int ngrp = warp >> 1;  // columns 16 ngrp .. 16 ngrp + 15 (two 8-column tiles)
     const int b0 = rb * kSqRows;
     const int nk = bk.hsp / kSqK;
-    const bool on0 = 16 * npair < bk.ncol, on1 = 16 * npair + 8 < bk.ncol;
+    const int c0w = 16 * ngrp;
+    const bool on[2] = {c0w < bk.ncol, c0w + 8 < bk.ncol};
     float acc[kSqLimbs][2][4];
 #pragma unroll
     for (int l = 0; l < kSqLimbs; ++l)
@@ -1828,36 +1857,57 @@ __device__ void sq_tile(const SqParams &p, const SqBlock &bk, int rb, __half *sm
         for (int j = 0; j < 2; ++j)
 #pragma unroll
             for (int i = 0; i < 4; ++i) acc[l][j][i] = 0.0f;
-    sq_stage(bk, b0, 0, smem);
+    // a ring of kSqStages chunks: chunk kc lands in stage kc % kSqStages;
+    // one group is committed per chunk (empty past the last), so waiting for
+    // all but kSqStages - 2 groups means chunk kc has landed
+    SqCopies cp;
+    sq_copies(bk, b0, cp);
+    const unsigned sbase = smem_addr(smem);
+    constexpr unsigned kStageBytes = kSqStageHalves * 2u;
+    // the warp's fragment rows: five digit row groups of A, one column group of B
+    const unsigned a_off = (unsigned)((16 * half + (lane & 15)) * kSqLd + (lane >> 4) * 8) * 2u;
+    const unsigned b_off = (unsigned)((kSqLimbs * kSqRows + c0w + (lane & 7) + ((lane >> 4) << 3)) * kSqLd +
+                                      ((lane >> 3) & 1) * 8) * 2u;
+    for (int s = 0; s < kSqStages - 1; ++s) {
+        if (s < nk)
+            sq_stage(cp, s, sbase + s * kStageBytes);
+        sq_commit_group();
+    }
+    int slot = 0;  // kc % kSqStages
     for (int kc = 0; kc < nk; ++kc) {
-        __half *cur = smem + (kc & 1) * kSqStageHalves;
-        if (kc + 1 < nk) {
-            sq_stage(bk, b0, kc + 1, smem + ((kc + 1) & 1) * kSqStageHalves);
-            asm volatile("cp.async.wait_group 1;" ::: "memory");
-        } else {
-            asm volatile("cp.async.wait_group 0;" ::: "memory");
-        }
+        asm volatile("cp.async.wait_group %0;" ::"n"(kSqStages - 2) : "memory");
+        // every thread's copies of chunk kc are visible, and every warp is
+        // done with chunk kc - 1, whose stage is refilled below
         __syncthreads();
-        if (on0) {
-            const __half *Bs = cur + kSqLimbs * kSqRows * kSqLd;
+        const int nxt = kc + kSqStages - 1;
+        if (nxt < nk)
+            sq_stage(cp, nxt, sbase + (slot == 0 ? kSqStages - 1 : slot - 1) * kStageBytes);
+        sq_commit_group();
+        const unsigned cur = sbase + slot * kStageBytes;
+        slot = slot == kSqStages - 1 ? 0 : slot + 1;
+        if (on[0]) {
 #pragma unroll
             for (int kk = 0; kk < kSqK; kk += 16) {
                 // B fragments of the warp's two 8-column tiles ([n][k] rows)
                 unsigned bf[4];
-                sq_ldsm_x4(bf, Bs + (16 * npair + (lane & 7) + ((lane >> 4) << 3)) * kSqLd + kk +
-                                   ((lane >> 3) & 1) * 8);
+                asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];"
+                             : "=r"(bf[0]), "=r"(bf[1]), "=r"(bf[2]), "=r"(bf[3])
+                             : "r"(cur + b_off + kk * 2));
 #pragma unroll
                 for (int l = 0; l < kSqLimbs; ++l) {
                     unsigned af[4];
-                    sq_ldsm_x4(af, cur + (l * kSqRows + 16 * half + (lane & 15)) * kSqLd + kk + (lane >> 4) * 8);
+                    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];"
+                                 : "=r"(af[0]), "=r"(af[1]), "=r"(af[2]), "=r"(af[3])
+                                 : "r"(cur + a_off + (unsigned)(l * kSqRows * kSqLd * 2) + kk * 2));
                     sq_mma(acc[l][0], af, bf[0], bf[1]);
-                    if (on1)
+                    if (on[1])
                         sq_mma(acc[l][1], af, bf[2], bf[3]);
                 }
             }
         }
-        __syncthreads();  // the buffer is refilled next round
     }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    __syncthreads();  // the staging buffers are reused below
     // fp32 digit sums to shared memory: accs[l][r][col]
     float *accs = reinterpret_cast<float *>(smem);
     {
@@ -1866,7 +1916,7 @@ __device__ void sq_tile(const SqParams &p, const SqBlock &bk, int rb, __half *sm
         for (int l = 0; l < kSqLimbs; ++l)
 #pragma unroll
             for (int j = 0; j < 2; ++j) {
-                const int col = 16 * npair + 8 * j + 2 * t;
+                const int col = c0w + 8 * j + 2 * t;
                 const int r = 16 * half + g;
                 float *o = accs + (l * kSqRows + r) * (kSqCols + 1) + col;
                 o[0] = acc[l][j][0];
@@ -1876,60 +1926,76 @@ __device__ void sq_tile(const SqParams &p, const SqBlock &bk, int rb, __half *sm
             }
     }
     __syncthreads();
-    // one warp per engine, one lane per row
+    // one warp per engine, one lane per row; every load an engine needs is
+    // issued before any is used
     for (int k = warp; k < bk.neng; k += kSqThreads / 32) {
-        const int2 ec = p.engs[bk.e0 + k];
-        const EDesc &D = p.desc[ec.x];
-        const int hs = D.hs, np = D.npairs;
+        const SqEng e = p.engs[bk.e0 + k];
         const int b = b0 + lane;
-        const bool row = b < hs;
+        const bool row = b < e.hs;
+        const double sv = row ? __ldcg(e.Sb + b) : 0.0;
+        const double rq = row ? __ldg(e.Rq + b) : 0.0;
+        const double hb = row ? __ldcg(e.h + b) : 0.0;
+        int nq[kMaxP];
+        double cq[kMaxP];
+#pragma unroll
+        for (int q = 0; q < kMaxP; ++q) {
+            nq[q] = q < e.np ? __ldcg(e.evn + q) : 0;
+            cq[q] = q < e.np ? __ldg(e.pc + q) : 0.0;
+        }
         double y = 0.0;
-        for (int q = 0; q < np; ++q) {
-            const int n = __ldcg(D.evn + q);
+#pragma unroll
+        for (int q = 0; q < kMaxP; ++q) {
+            if (q >= e.np)
+                break;
+            const int n = nq[q];
             long long z = 0;
             if (n >= 0) {
-                z = sq_combine(accs, lane, ec.y + q);
+                z = sq_combine(accs, lane, e.lc + q);
             } else if (n != INT_MIN) {
-                const int *__restrict__ ev = D.evl + q * hs;
+                const int *__restrict__ ev = e.evl + q * e.hs;
                 if (row)
                     for (int i = 0; i < -1 - n; ++i) {
-                        const int e = __ldcg(ev + i);
-                        z += (long long)(short)(e & 0xffff) * __ldg(D.T + (size_t)(e >> 16) * hs + b);
+                        const int v = __ldcg(ev + i);
+                        z += (long long)(short)(v & 0xffff) * __ldg(e.T + (size_t)(v >> 16) * e.hs + b);
                     }
             } else {
-                const int *__restrict__ dq = D.dP + q * hs;
+                const int *__restrict__ dq = e.dP + q * e.hs;
                 if (row)
-                    for (int c = 0; c < hs; ++c) {
+                    for (int c = 0; c < e.hs; ++c) {
                         const int v = __ldcg(dq + c);
                         if (v)
-                            z += (long long)v * __ldg(D.T + (size_t)c * hs + b);
+                            z += (long long)v * __ldg(e.T + (size_t)c * e.hs + b);
                     }
             }
-            y = fma(D.pc[q] * D.yscale, (double)z, y);
+            y = fma(cq[q] * e.yscale, (double)z, y);
         }
         double part = 0.0;
         if (row) {
-            D.y[b] = y;
-            const double sv = __ldcg(D.Sb + b);
+            e.y[b] = y;
             if (sv != 0.0)
-                part = (D.Rq[b] * sv) * (y - D.h[b]);
+                part = (rq * sv) * (y - hb);
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-        if (lane == 0) {
-            D.sqpart[rb] = part;
-            __threadfence();
-            atomicAdd(&D.st->sq_done, 1u);
-        }
+        if (lane == 0)
+            e.sqpart[rb] = part;
+    }
+    // release: the barrier orders every warp's y and share stores before the
+    // gpu-scope fences of the threads that count the engines' row blocks done
+    __syncthreads();
+    for (int k = threadIdx.x; k < bk.neng; k += kSqThreads) {
+        __threadfence();
+        atomicAdd(p.engs[bk.e0 + k].done, 1u);
     }
     __syncthreads();  // the staging buffers are reused by the next item
 }
 
+// Decide and commit an engine's step; its moved group `g` was loaded by the
+// caller (before waiting for the row blocks).
 __device__ void sq_finish(const EDesc &D, int *s_flag, double *s_val, MovedGroup &g)
 {
     __shared__ double s_part[kSqMaxBins / kSqRows];
     for (int k = threadIdx.x; k < D.sqblk; k += blockDim.x) s_part[k] = __ldcg(D.sqpart + k);
-    load_moved_group(D, D.st->step, g);
     __syncthreads();
     if (threadIdx.x == 0) {
         double dsq = 0.0;
@@ -1951,9 +2017,17 @@ __device__ void sq_finish(const EDesc &D, int *s_flag, double *s_val, MovedGroup
     if (D.st->fmt) {
         // one CTA's shared-memory deltas: entries (flat << 1) | sign
         if (accept)
-            for (unsigned k = threadIdx.x; k < nt; k += blockDim.x) {
-                const int e = D.tlist[k];
-                atomicAdd(D.counts + (e >> 1), (e & 1) ? 1 : -1);
+            for (unsigned k0 = threadIdx.x; k0 < nt; k0 += 4 * blockDim.x) {
+                int e[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const unsigned k = k0 + u * blockDim.x;
+                    e[u] = k < nt ? __ldcg(D.tlist + k) : -1;
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (e[u] >= 0)
+                        atomicAdd(D.counts + (e[u] >> 1), (e[u] & 1) ? 1 : -1);
             }
     } else {
         // global oriented deltas: atomicExch hands each bin's delta to one entry
@@ -1970,11 +2044,24 @@ __device__ void sq_finish(const EDesc &D, int *s_flag, double *s_val, MovedGroup
     const int nx = D.npairs * D.xld;
     for (int k = threadIdx.x; k < nx; k += blockDim.x) D.X[k] = __float2half_rn(0.0f);
     if (accept) {
-        for (int b = threadIdx.x; b < D.hs; b += blockDim.x) {
-            const double sv = D.Sb[b];
-            if (sv != 0.0)
-                D.Bq[b] = fma(-2.0 * D.A[b], sv, D.Bq[b]);
-            D.h[b] = fma(-2.0, __ldcg(D.y + b), D.h[b]);
+        for (int b0 = threadIdx.x; b0 < D.hs; b0 += 4 * blockDim.x) {
+            double sv[4], yv[4], hv[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int b = b0 + u * blockDim.x;
+                sv[u] = b < D.hs ? __ldcg(D.Sb + b) : 0.0;
+                yv[u] = b < D.hs ? __ldcg(D.y + b) : 0.0;
+                hv[u] = b < D.hs ? D.h[b] : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int b = b0 + u * blockDim.x;
+                if (b < D.hs) {
+                    if (sv[u] != 0.0)
+                        D.Bq[b] = fma(-2.0 * D.A[b], sv[u], D.Bq[b]);
+                    D.h[b] = fma(-2.0, yv[u], hv[u]);
+                }
+            }
         }
         commit_moved_group(D, g);
         if (D.dense)
@@ -2002,7 +2089,7 @@ __device__ void sq_finish(const EDesc &D, int *s_flag, double *s_val, MovedGroup
     }
 }
 
-__global__ void __launch_bounds__(kSqThreads) k_sq_fused(SqParams p)
+__global__ void __launch_bounds__(kSqThreads, 2) k_sq_fused(SqParams p)
 {
     extern __shared__ __align__(16) unsigned char sq_smem_raw[];
     __half *smem = reinterpret_cast<__half *>(sq_smem_raw);
@@ -2026,6 +2113,8 @@ __global__ void __launch_bounds__(kSqThreads) k_sq_fused(SqParams p)
             continue;
         }
         const EDesc &D = p.desc[-1 - item.x];
+        // the moved group does not depend on the tiles: load it first
+        load_moved_group(D, D.st->step, s_group);
         if (threadIdx.x == 0) {
             // the engine's row blocks were claimed before this item by
             // running CTAs; a lost one gives up after kSpinLimit polls
@@ -2036,7 +2125,7 @@ __global__ void __launch_bounds__(kSqThreads) k_sq_fused(SqParams p)
                     ok = 1;
                     break;
                 }
-                __nanosleep(32);
+                __nanosleep(256);
             }
             if (!ok)
                 atomicOr(p.status, DS_BARRIER_TIMEOUT);
@@ -2289,12 +2378,12 @@ struct EngineSet {
     std::vector<int> sq_first, sq_count;
     std::vector<int> sq_xcol;      // per engine id: its first delta column in its table's X
     std::vector<SqBlock> sq_hblocks;
-    std::vector<int2> sq_hengs;
+    std::vector<SqEng> sq_hengs;
     int2 *sq_items = nullptr;
     int sq_cap = 0;
     SqBlock *sq_blocks = nullptr;
     int sq_blocks_cap = 0;
-    int2 *sq_engs = nullptr;
+    SqEng *sq_engs = nullptr;
     int sq_engs_cap = 0;
     cudaStream_t stream = nullptr;
     std::map<std::pair<int, int>, cudaGraphExec_t> graphs;
@@ -2423,6 +2512,29 @@ static void drop_graphs(EngineSet *s)
         s->host_graph[k] = nullptr;
         s->host_graph_E[k] = 0;
     }
+}
+
+// An engine's entry in an S(Q) block: its device arrays and constants.
+static SqEng sq_eng(const EDesc &D, int lc)
+{
+    SqEng e;
+    e.evn = D.evn;
+    e.evl = D.evl;
+    e.dP = D.dP;
+    e.T = D.T;
+    e.pc = D.pc;
+    e.Sb = D.Sb;
+    e.Rq = D.Rq;
+    e.h = D.h;
+    e.y = D.y;
+    e.sqpart = D.sqpart;
+    e.done = &D.st->sq_done;
+    e.yscale = D.yscale;
+    e.hs = D.hs;
+    e.np = D.npairs;
+    e.lc = lc;
+    e.pad = 0;
+    return e;
 }
 
 // Rebuild the work list over live engines and upload descriptors.
@@ -2558,6 +2670,22 @@ static int refresh(EngineSet *s)
     s->sq_host.clear();
     s->sq_first.assign(nslots, -1);
     s->sq_count.assign(nslots, 0);
+    // block width: the batched step's tiles should fill the CTA slots (two
+    // per SM) evenly, since the product's time is set by the busiest SM
+    int width = kSqCols;
+    {
+        long long work = 0, engines = 0;
+        for (const auto &t : s->tables) work += (long long)t.ncols * ((t.hs + kSqRows - 1) / kSqRows);
+        for (int id : s->live) engines += s->slots[id].d.sq ? 1 : 0;
+        Context *c;
+        FRMC_TRY(get_context(&c));
+        // the commits hold a slot each while they wait
+        const long long slots = std::max<long long>(c->sms, 2LL * c->sms - engines);
+        if (work > 0) {
+            const long long w = (work + slots - 1) / slots;
+            width = (int)std::min<long long>(kSqCols, std::max<long long>(kMaxP, (w + 7) / 8 * 8));
+        }
+    }
     for (int ti = 0; ti < (int)s->tables.size(); ++ti) {
         const SqTable &t = s->tables[ti];
         const int nrb = (t.hs + kSqRows - 1) / kSqRows;
@@ -2569,7 +2697,7 @@ static int refresh(EngineSet *s)
             if (!sl.d.sq || sl.sq_table != ti)
                 continue;
             const int col = s->sq_xcol[id];
-            if (open && col + sl.d.npairs - col0 > kSqCols) {
+            if (open && col + sl.d.npairs - col0 > width) {
                 s->sq_hblocks.push_back(cur);
                 open = false;
             }
@@ -2578,7 +2706,7 @@ static int refresh(EngineSet *s)
                 cur = SqBlock{t.TD, t.X + (size_t)col * t.hsp, t.hsp, t.hs, 0, nrb, (int)s->sq_hengs.size(), 0};
                 open = true;
             }
-            s->sq_hengs.push_back(make_int2(id, col - col0));
+            s->sq_hengs.push_back(sq_eng(sl.d, col - col0));
             cur.neng += 1;
             cur.ncol = col + sl.d.npairs - col0;
         }
@@ -2599,7 +2727,7 @@ static int refresh(EngineSet *s)
         const int nrb = (t.hs + kSqRows - 1) / kSqRows;
         const int bi = (int)s->sq_hblocks.size();
         s->sq_hblocks.push_back(SqBlock{t.TD, sl.d.X, t.hsp, t.hs, sl.d.npairs, nrb, (int)s->sq_hengs.size(), 1});
-        s->sq_hengs.push_back(make_int2(id, 0));
+        s->sq_hengs.push_back(sq_eng(sl.d, 0));
         s->sq_first[id] = (int)s->sq_host.size();
         for (int rb = 0; rb < nrb; ++rb) s->sq_host.push_back(make_int2(bi, rb));
         s->sq_host.push_back(make_int2(-1 - id, 0));
@@ -2623,14 +2751,14 @@ static int refresh(EngineSet *s)
         if (s->sq_engs) cudaFree(s->sq_engs);
         s->sq_engs = nullptr;
         const int cap = std::max((int)s->sq_hengs.size(), 2 * s->sq_engs_cap);
-        FRMC_CUDA(cudaMalloc(&s->sq_engs, sizeof(int2) * cap));
+        FRMC_CUDA(cudaMalloc(&s->sq_engs, sizeof(SqEng) * cap));
         s->sq_engs_cap = cap;
     }
     if (!s->sq_hblocks.empty())
         FRMC_CUDA(cudaMemcpy(s->sq_blocks, s->sq_hblocks.data(), sizeof(SqBlock) * s->sq_hblocks.size(),
                              cudaMemcpyHostToDevice));
     if (!s->sq_hengs.empty())
-        FRMC_CUDA(cudaMemcpy(s->sq_engs, s->sq_hengs.data(), sizeof(int2) * s->sq_hengs.size(),
+        FRMC_CUDA(cudaMemcpy(s->sq_engs, s->sq_hengs.data(), sizeof(SqEng) * s->sq_hengs.size(),
                              cudaMemcpyHostToDevice));
     std::vector<EDesc> hd(nslots);
     for (int k = 0; k < nslots; ++k) hd[k] = s->slots[k].d;
@@ -2703,9 +2831,12 @@ static int launch_sq(EngineSet *s, int first, int count, cudaStream_t st)
         return FRMC_OK;
     Context *c;
     FRMC_TRY(get_context(&c));
-    const int grid = std::min(count, c->sms * 2);
     SqParams p{s->ddesc, s->sq_blocks, s->sq_engs, s->sq_items + first, count, s->sched + 1, &s->sched[0].status};
     FRMC_CUDA(cudaFuncSetAttribute(k_sq_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, kSqSmemBytes));
+    // all shared memory: two CTAs fit one SM, so every item of a step starts at once
+    FRMC_CUDA(cudaFuncSetAttribute(k_sq_fused, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                   (int)cudaSharedmemCarveoutMaxShared));
+    const int grid = std::min(count, c->sms * 2);
     k_sq_fused<<<grid, kSqThreads, kSqSmemBytes, st>>>(p);
     FRMC_CUDA(cudaGetLastError());
     return FRMC_OK;
