@@ -38,12 +38,15 @@
 #include <map>
 #include <vector>
 
+#include <cuda.h>
 #include <cuda_fp16.h>
+#include <cudaTypedefs.h>
 
 #include "frmc_gpu_engine.h"
 #include "frmc_math.cuh"
 #include "frmc_ptx.cuh"
 #include "frmc_runtime.h"
+#include "frmc_tc.cuh"
 
 namespace frmc {
 
@@ -57,7 +60,8 @@ struct EState {
     unsigned long long swept;  // columns swept by one-CTA steps (all atoms, or the selected cells')
     unsigned done;      // items of the current step finished
     unsigned tcount;    // entries in the touched-bin list of the current step
-    unsigned sq_done;   // reserved (zero)
+    unsigned sq_done;   // S(Q) tiles of the current step finished (engines with S(Q))
+    unsigned sq_ydone;  // S(Q) row items of the current step finished
     int fmt;            // touched-list format of the step: 1 = (flat << 1) | sign, 0 = flat
     double sf;          // scale factor of the current configuration (dense engines)
     double sf_prop;     // scale factor of this step's proposal (dense engines with S(Q))
@@ -143,7 +147,7 @@ struct EDesc {
     // h = 2 M W (S_exp - S).  y is computed exactly in integers from the
     // element-pair deltas: y(b) = yscale sum_p pair_coef_p z_p(b),
     // z_p(b) = sum_c T[c][b] dP_p(c), T[c][b] = round(K[c][b] R0(c) 2^s).
-    int sq, nq, sqblk;
+    int sq, nq;
     double var2q;
     double yscale;      // rho0 2^-s
     const double *M;    // [hs][nq] G -> S(Q) table (shared)
@@ -154,17 +158,23 @@ struct EDesc {
     double *sqexp;      // [nq] experimental S(Q)
     double *h;          // [hs] 2 M W (S_exp - S) of the current configuration
     double *y;          // [hs] K x of this step
-    double *sqpart;     // [sqblk] this step's partial sums of x (y - h)
+    double *sqpart;     // [hs / kSqRows rounded up] this step's shares of x (y - h), per 128-bin row block
     double *sqv;        // [nq] S(Q) written by the evaluation kernel
     int *evl;           // [npairs][hs] this step's non-zero element-pair deltas, per pair
-    int *evn;           // [kMaxP] their counts n (-1 - n: a delta beyond kSqGemmMaxDelta, sum the
-                        // list exactly; INT_MIN: a delta beyond 16 bits, sum the deltas dP)
+    int *evn;           // [npairs] their counts n (-1 - n: a delta beyond kSqGemmMaxDelta or a column
+                        // sum beyond kSqMaxL1, sum the list exactly; INT_MIN: a delta beyond 16 bits,
+                        // sum the deltas dP), in the table's per-column array
     // y on the tensor cores: X holds this step's element-pair deltas as fp16
     // (column q of the engine at X + q xld, bins down the column); the S(Q)
-    // kernel multiplies the table's kSqLimbs balanced base-2048 digits by
-    // every engine's columns (exact integers in fp32).
+    // kernel multiplies the table's kSqLimbs balanced base-4096 digit planes
+    // by every engine's columns (exact integers in fp32) into Zf, kept as
+    // [plane][row block][table column][kSqRows]: bin b of plane l of column q
+    // at Zf + ((l hsp / kSqRows + b / kSqRows) zcap + q) kSqRows + b % kSqRows;
+    // wide columns go to Zi (column q at Zi + q hsp) by the exact integer path.
     __half *X;
-    int xld, hsp;
+    float *Zf;
+    long long *Zi;
+    int xld, hsp, zcap;
     int sq_gemm_max;    // largest |delta| taken through the product (kSqGemmMaxDelta; lower values,
                         // down to 0 = never and -1 = the dense integer loop, exist for tests)
     // Column grid (nc > 0): the atoms sorted by cell, so that a step sweeps
@@ -683,16 +693,17 @@ __device__ void dense_commit(const EDesc &D)
 // in shared memory (chunk) or global memory (Sb) for the commit.  Sums use the
 // fixed lane order, so the result does not depend on the CTA size.
 constexpr int kMaxP = 10;  // element pairs loaded with unrolled loads (ne <= 4)
-// T in kSqLimbs balanced base-2048 digits t_l in [-1024, 1023] (5 digits
-// cover |T| < 2^54; T stays below 2^48).  fp16 holds every integer up to 2048,
+// T in kSqLimbs balanced base-4096 digits t_l in [-2048, 2047] (4 digits
+// cover |T| < 2^47; T stays below 2^46).  fp16 holds every integer up to 2048,
 // so a delta column goes through the tensor-core product when its entries are
 // at most kSqGemmMaxDelta in magnitude and their absolute sum is at most
-// kSqMaxL1: every partial sum of a digit product is then an integer of
-// magnitude <= 1024 * 2^14 = 2^24, which fp32 accumulation holds exactly.
-constexpr int kSqLimbs = 5;
-constexpr int kSqDigitBits = 11;
+// kSqMaxL1: every partial sum of a digit product, over any subset of the bins,
+// is then an integer of magnitude <= 2048 * 2^13 = 2^24, which fp32
+// accumulation (and fp32 addition of such partial sums) holds exactly.
+constexpr int kSqLimbs = 4;
+constexpr int kSqDigitBits = 12;
 constexpr int kSqGemmMaxDelta = 2048;
-constexpr int kSqMaxL1 = 1 << 14;
+constexpr int kSqMaxL1 = 1 << 13;
 
 // SMEM: the element-pair deltas are this CTA's shared-memory copy (one CTA per
 // engine); otherwise they are the engine's global array, filled by several
@@ -1709,56 +1720,73 @@ __global__ void k_gather_results(const EDesc *desc, const int *ids, EResult *out
 // an exact int64 sum, so its value does not depend on the order of the
 // terms, and y(b) = rho0 2^-s sum_p pair_coef_p z_p(b).
 //
-// k_sq_fused does the whole term in one persistent launch over a work list
-// of tile items followed by one commit item per engine:
-// * a tile item is (block of delta columns, block of kSqRows rows): the
-//   block's columns -- whole engines, at most kSqCols columns -- times the
-//   rows' kSqLimbs digit rows of T on the tensor cores (mma.sync, fp16 in,
-//   fp32 accumulate; every product sum is an exact integer, see kSqLimbs),
-//   staged through shared memory by cp.async in double-buffered chunks of
-//   kSqK bins.  The digits are combined into z (modulo 2^64), y = yscale
-//   sum_p pair_coef_p z_p in p order, and the rows' share of x (y - h) is
-//   summed by one warp per engine with a fixed shuffle tree; the tile then
-//   counts itself done in the engine's state.
-// * a commit item waits (bounded) until all the engine's row blocks are done,
-//   adds their shares in block order, decides and commits: counts, Bq -= 2 A S,
-//   h -= 2 y, coordinates, and clears dP and the delta columns.  Its tiles are
-//   claimed before it by CTAs that are running, so the wait always ends.
-// A column whose deltas are too large for exact fp32 products takes the
-// exact integer sum over its list of deltas (or its dense deltas) instead.
-// Every quantity of an engine depends only on that engine's columns, so a
-// chain is the same in any batch and alone.
-constexpr int kSqRows = 32;       // rows per tile
-constexpr int kSqCols = 64;       // delta columns per block at most (whole engines)
-constexpr int kSqK = 64;          // bins per staged chunk
-constexpr int kSqLd = kSqK + 8;   // shared-memory row stride in halves (conflict-free ldmatrix)
-constexpr int kSqStages = 3;      // chunks in flight: the ring hides the L2 latency of the digit rows
+// k_sq_fused does the whole term in one persistent launch (one CTA per SM)
+// over a work list of tile items, then row items, then one commit item per
+// engine:
+// * a tile item is (block of delta columns, block of kSqRows rows, K split):
+//   the block's columns -- whole engines, at most kSqCols -- times the rows'
+//   kSqLimbs digit planes of T over the split's bins, on the tensor cores:
+//   tcgen05.mma kind::f16 issued by one thread, fp16 operands staged in
+//   shared memory by TMA through a ring of kSqStages stages, one fp32
+//   accumulator per digit plane in TMEM.  Every accumulator is an exact
+//   integer (see kSqLimbs), so the splits' partial sums are added into the
+//   table's fp32 digit products Zf by bulk reductions in L2, in any order
+//   with the same result.  The tile then counts itself done in its engines'
+//   states.
+// * a row item (engine, two row blocks) reads S, Rq and h of its bins, waits
+//   (bounded) until all tiles of the engine's block are done, combines each
+//   bin's digit products into z (int64), forms y and each row block's share
+//   of x (y - h) by a fixed-order sum over its kSqRows bins, and clears the
+//   bins' deltas, delta columns and digit products.  The FP64 work -- a
+//   narrow pipe on this GPU -- is spread over the SMs this way.
+// * a commit item reads what does not depend on the row items (S, h, A, Bq,
+//   the touched list, the state, the moved group), waits (bounded) until its
+//   row items are done, adds the row blocks' shares in block order, decides
+//   and commits: counts, Bq -= 2 A S, h -= 2 y, coordinates.
+// The items an item waits for are claimed before it by CTAs that are
+// running, so every wait ends.
+// A column whose deltas are too large for exact fp32 products is summed
+// exactly in int64 over its list of deltas (or its dense deltas) by the first
+// K split of each row block instead.  Every quantity of an engine depends
+// only on that engine's columns, so a chain is the same in any batch and alone.
+constexpr int kSqRows = 128;      // rows per tile: the MMA's M, one TMEM lane per row
+constexpr int kSqCols = 128;      // delta columns per block at most: kSqLimbs x kSqCols = all 512 TMEM columns
+constexpr int kSqK = 32;          // bins per stage: one 64-byte swizzle row of fp16
+constexpr int kSqStages = 4;      // stages in flight
 constexpr int kSqThreads = 256;
 constexpr int kSqMaxBins = 4096;  // histogram bins of an engine with an S(Q) term
-constexpr int kSqBits = 48;       // largest |T| is below 2^48: 2^14 unit deltas fit in an int64 sum
-constexpr int kSqStageHalves = (kSqLimbs * kSqRows + kSqCols) * kSqLd;
-constexpr int kSqSmemBytes = kSqStages * kSqStageHalves * 2;
-static_assert(kSqLimbs * kSqRows * (kSqCols + 1) * 4 <= kSqSmemBytes, "epilogue reuses the staging buffers");
+constexpr int kSqBits = 46;       // largest |T| is below 2^46 (four balanced base-4096 digits hold 2^47)
+constexpr int kSqPlaneBytes = kSqRows * kSqK * 2;        // one digit plane of a stage: 8 KB
+constexpr int kSqABytes = kSqLimbs * kSqPlaneBytes;      // 32 KB
+constexpr int kSqBBytes = kSqCols * kSqK * 2;            // 8 KB
+constexpr int kSqStageBytes = kSqABytes + kSqBBytes;     // 40 KB
+constexpr int kSqRingBytes = kSqStages * kSqStageBytes;  // 160 KB
+constexpr int kSqSmemBytes = kSqRingBytes + 1024;        // + the 1024-byte alignment of the swizzled tiles
+constexpr int kSqTmemCols = kSqLimbs * kSqCols;          // 512
+constexpr unsigned long long kSqWaitNs = 2000000000ull;  // a bounded wait gives up after 2 s
+static_assert(kSqTmemCols == 512, "one CTA per SM holds all of its TMEM");
+static_assert(2 * kSqCols * kSqRows * 4 <= kSqRingBytes, "the epilogue's two plane buffers fit the ring");
+static_assert(5 * kSqMaxBins * 8 <= kSqRingBytes, "a commit's per-bin arrays fit the ring");
+static_assert(kSqThreads % kSqRows == 0 && kSqRows % 32 == 0, "a row item holds whole row blocks of whole warps");
+static_assert(kSqThreads >= kSqCols && kSqThreads >= kSqRows, "one thread per column and per row");
 
 // A block of delta columns: engines of one table, adjacent in its X.
 struct SqBlock {
-    const __half *TD;  // [kSqLimbs][hsp][hsp] digit l of T[c][b] at (l hsp + b) hsp + c
-    const __half *X;   // the block's first column (columns are hsp apart)
-    int hsp, hs, ncol, nrb;
-    int e0, neng;      // its engines: engs[e0 .. e0 + neng)
+    const CUtensorMap *tm;  // the table's tensor maps: [0] digit planes of T, [1] delta columns X
+    float *Zf;              // the table's fp32 digit products [plane][row block][zcap columns][kSqRows]
+    long long *Zi;          // the table's exact products of wide columns: column c at c hsp
+    const int *cmode;       // the block's product modes (the engines' evn), one per column
+    int col0, ncol, hsp, hs, zcap;
+    int nrb, nsplit, nk;    // row blocks, K splits, K chunks of kSqK bins
+    int e0, neng;           // its engines: engs[e0 .. e0 + neng)
 };
 
-// What a tile needs of one engine of its block, flat (one load; no chain
-// through the descriptor): this step's delta lists and counts, the table,
-// the per-bin arrays of the x (y - h) share, where y and the share go, the
-// engine's completion counter, and its first column in the block.
+// What a tile needs of one engine of its block: its completion counter and,
+// for the exact path of wide columns, its delta lists, deltas and table.
 struct SqEng {
-    const int *evn, *evl, *dP;
+    const int *evl, *dP;
     const long long *T;
-    const double *pc, *Sb, *Rq, *h;
-    double *y, *sqpart;
     unsigned *done;
-    double yscale;
     int hs, np, lc, pad;
 };
 
@@ -1766,302 +1794,408 @@ struct SqParams {
     const EDesc *desc;
     const SqBlock *blocks;
     const SqEng *engs;
-    const int2 *items;  // (block, row block) tiles, then (-1 - engine id, 0) commits
+    // work items (kind, ...): tiles (0, block, row block * nsplit + split),
+    // then row items (1, engine id, first row block << 16 | row blocks, its
+    // block's tiles), then commits (2, engine id, its row items)
+    const int4 *items;
     int nitems;
     Sched *sched;
     unsigned *status;
 };
 
-__device__ __forceinline__ void sq_mma(float (&d)[4], const unsigned (&a)[4], unsigned b0, unsigned b1)
-{
-    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, "
-                 "{%8, %9}, {%0, %1, %2, %3};"
-                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-
-// A tile's copies: each thread always moves the same kSqCopies 16-byte
-// pieces of a chunk (digit rows [l][b0 + r], then the block's columns), so
-// their addresses are formed once per tile and advance by kSqK bins per chunk.
-constexpr int kSqCopies = (kSqLimbs * kSqRows + kSqCols) * (kSqK / 8) / kSqThreads;
-static_assert((kSqLimbs * kSqRows + kSqCols) * (kSqK / 8) % kSqThreads == 0, "whole copies per thread");
-
-struct SqCopies {
-    const __half *src[kSqCopies];  // at chunk 0
-    unsigned dst[kSqCopies];       // shared-memory byte offset within a stage
-    unsigned valid;                // bit j: piece j is read (else zero filled)
+// A CTA's tile pipeline: stage barriers, the accumulator barrier and TMEM.
+// The barriers' phases follow from the CTA's running counts of chunks and
+// tiles, so every wait names the exact phase it needs.
+struct SqPipe {
+    uint64_t full[kSqStages];   // TMA -> MMA: the stage's operands have landed
+    uint64_t empty[kSqStages];  // MMA -> TMA: the MMAs reading the stage have completed
+    uint64_t acc;               // MMA -> epilogue: the tile's accumulators are final
+    uint32_t tmem;              // TMEM base address (lane 0, first column)
+    int fail;                   // a bounded wait gave up: the CTA stops taking items
 };
 
-__device__ __forceinline__ void sq_copies(const SqBlock &bk, int b0, SqCopies &c)
+__device__ __forceinline__ void tmap_acquire(const CUtensorMap *m)
 {
-    constexpr int kChunks = kSqK / 8;  // 16-byte pieces per row
-    constexpr int kArows = kSqLimbs * kSqRows;
-    c.valid = 0u;
-#pragma unroll
-    for (int j = 0; j < kSqCopies; ++j) {
-        const int k = threadIdx.x + j * kSqThreads;
-        const int row = k / kChunks, ch = k - row * kChunks;
-        c.dst[j] = (unsigned)(row * kSqLd + ch * 8) * 2u;
-        if (row < kArows) {
-            const int l = row / kSqRows, r = row - l * kSqRows;
-            c.src[j] = bk.TD + ((size_t)l * bk.hsp + b0 + r) * bk.hsp + ch * 8;
-            c.valid |= 1u << j;
-        } else {
-            const int n = row - kArows;
-            const bool v = n < bk.ncol;
-            c.src[j] = bk.X + (size_t)(v ? n : 0) * bk.hsp + ch * 8;
-            if (v)
-                c.valid |= 1u << j;
-        }
-    }
+    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(m) : "memory");
 }
 
-// Stage chunk kc of a tile into the stage at shared address `stage`.
-__device__ __forceinline__ void sq_stage(const SqCopies &c, int kc, unsigned stage)
+// Wide columns of a tile's block (ks == 0 only): z = sum_c T[c][b] dP(c) in
+// int64 for the tile's rows, over the column's list of deltas (or its dense
+// deltas), into Zi.
+__device__ void sq_tile_exact(const SqParams &p, const SqBlock &bk, int row0)
 {
-    const int c0 = kc * kSqK;
-#pragma unroll
-    for (int j = 0; j < kSqCopies; ++j) {
-        const int n = (c.valid >> j) & 1u ? 16 : 0;  // zero fill
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(stage + c.dst[j]), "l"(c.src[j] + c0),
-                     "r"(n)
-                     : "memory");
-    }
-}
-
-__device__ __forceinline__ void sq_commit_group() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-
-// z of column `col` in row r of the tile from the staged fp32 digit sums.
-__device__ __forceinline__ long long sq_combine(const float *accs, int r, int col)
-{
-    unsigned long long acc = 0;
-#pragma unroll
-    for (int l = 0; l < kSqLimbs; ++l)
-        acc += (unsigned long long)(long long)accs[(l * kSqRows + r) * (kSqCols + 1) + col] << (kSqDigitBits * l);
-    return (long long)acc;
-}
-
-__device__ void sq_tile(const SqParams &p, const SqBlock &bk, int rb, __half *smem)
-{
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int half = warp & 1;   // rows 16 half .. 16 half + 15 of every digit
-    const int ngrp = warp >> 1;  // columns 16 ngrp .. 16 ngrp + 15 (two 8-column tiles)
-    const int b0 = rb * kSqRows;
-    const int nk = bk.hsp / kSqK;
-    const int c0w = 16 * ngrp;
-    const bool on[2] = {c0w < bk.ncol, c0w + 8 < bk.ncol};
-    float acc[kSqLimbs][2][4];
-#pragma unroll
-    for (int l = 0; l < kSqLimbs; ++l)
-#pragma unroll
-        for (int j = 0; j < 2; ++j)
-#pragma unroll
-            for (int i = 0; i < 4; ++i) acc[l][j][i] = 0.0f;
-    // a ring of kSqStages chunks: chunk kc lands in stage kc % kSqStages;
-    // one group is committed per chunk (empty past the last), so waiting for
-    // all but kSqStages - 2 groups means chunk kc has landed
-    SqCopies cp;
-    sq_copies(bk, b0, cp);
-    const unsigned sbase = smem_addr(smem);
-    constexpr unsigned kStageBytes = kSqStageHalves * 2u;
-    // the warp's fragment rows: five digit row groups of A, one column group of B
-    const unsigned a_off = (unsigned)((16 * half + (lane & 15)) * kSqLd + (lane >> 4) * 8) * 2u;
-    const unsigned b_off = (unsigned)((kSqLimbs * kSqRows + c0w + (lane & 7) + ((lane >> 4) << 3)) * kSqLd +
-                                      ((lane >> 3) & 1) * 8) * 2u;
-    for (int s = 0; s < kSqStages - 1; ++s) {
-        if (s < nk)
-            sq_stage(cp, s, sbase + s * kStageBytes);
-        sq_commit_group();
-    }
-    int slot = 0;  // kc % kSqStages
-    for (int kc = 0; kc < nk; ++kc) {
-        asm volatile("cp.async.wait_group %0;" ::"n"(kSqStages - 2) : "memory");
-        // every thread's copies of chunk kc are visible, and every warp is
-        // done with chunk kc - 1, whose stage is refilled below
-        __syncthreads();
-        const int nxt = kc + kSqStages - 1;
-        if (nxt < nk)
-            sq_stage(cp, nxt, sbase + (slot == 0 ? kSqStages - 1 : slot - 1) * kStageBytes);
-        sq_commit_group();
-        const unsigned cur = sbase + slot * kStageBytes;
-        slot = slot == kSqStages - 1 ? 0 : slot + 1;
-        if (on[0]) {
-#pragma unroll
-            for (int kk = 0; kk < kSqK; kk += 16) {
-                // B fragments of the warp's two 8-column tiles ([n][k] rows)
-                unsigned bf[4];
-                asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];"
-                             : "=r"(bf[0]), "=r"(bf[1]), "=r"(bf[2]), "=r"(bf[3])
-                             : "r"(cur + b_off + kk * 2));
-#pragma unroll
-                for (int l = 0; l < kSqLimbs; ++l) {
-                    unsigned af[4];
-                    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];"
-                                 : "=r"(af[0]), "=r"(af[1]), "=r"(af[2]), "=r"(af[3])
-                                 : "r"(cur + a_off + (unsigned)(l * kSqRows * kSqLd * 2) + kk * 2));
-                    sq_mma(acc[l][0], af, bf[0], bf[1]);
-                    if (on[1])
-                        sq_mma(acc[l][1], af, bf[2], bf[3]);
-                }
-            }
-        }
-    }
-    asm volatile("cp.async.wait_group 0;" ::: "memory");
-    __syncthreads();  // the staging buffers are reused below
-    // fp32 digit sums to shared memory: accs[l][r][col]
-    float *accs = reinterpret_cast<float *>(smem);
-    {
-        const int g = lane >> 2, t = lane & 3;
-#pragma unroll
-        for (int l = 0; l < kSqLimbs; ++l)
-#pragma unroll
-            for (int j = 0; j < 2; ++j) {
-                const int col = c0w + 8 * j + 2 * t;
-                const int r = 16 * half + g;
-                float *o = accs + (l * kSqRows + r) * (kSqCols + 1) + col;
-                o[0] = acc[l][j][0];
-                o[1] = acc[l][j][1];
-                o[8 * (kSqCols + 1)] = acc[l][j][2];
-                o[8 * (kSqCols + 1) + 1] = acc[l][j][3];
-            }
-    }
-    __syncthreads();
-    // one warp per engine, one lane per row; every load an engine needs is
-    // issued before any is used
-    for (int k = warp; k < bk.neng; k += kSqThreads / 32) {
+    for (int k = 0; k < bk.neng; ++k) {
         const SqEng e = p.engs[bk.e0 + k];
-        const int b = b0 + lane;
-        const bool row = b < e.hs;
-        const double sv = row ? __ldcg(e.Sb + b) : 0.0;
-        const double rq = row ? __ldg(e.Rq + b) : 0.0;
-        const double hb = row ? __ldcg(e.h + b) : 0.0;
-        int nq[kMaxP];
-        double cq[kMaxP];
-#pragma unroll
-        for (int q = 0; q < kMaxP; ++q) {
-            nq[q] = q < e.np ? __ldcg(e.evn + q) : 0;
-            cq[q] = q < e.np ? __ldg(e.pc + q) : 0.0;
-        }
-        double y = 0.0;
-#pragma unroll
-        for (int q = 0; q < kMaxP; ++q) {
-            if (q >= e.np)
-                break;
-            const int n = nq[q];
+        for (int q = 0; q < e.np; ++q) {
+            const int n = __ldcg(bk.cmode + e.lc + q);
+            if (n >= 0)
+                continue;
+            const int b = row0 + (int)threadIdx.x;
+            if ((int)threadIdx.x >= kSqRows || b >= e.hs)
+                continue;
             long long z = 0;
-            if (n >= 0) {
-                z = sq_combine(accs, lane, e.lc + q);
-            } else if (n != INT_MIN) {
+            if (n != INT_MIN) {
                 const int *__restrict__ ev = e.evl + q * e.hs;
-                if (row)
-                    for (int i = 0; i < -1 - n; ++i) {
-                        const int v = __ldcg(ev + i);
-                        z += (long long)(short)(v & 0xffff) * __ldg(e.T + (size_t)(v >> 16) * e.hs + b);
-                    }
+                for (int i = 0; i < -1 - n; ++i) {
+                    const int v = __ldcg(ev + i);
+                    z += (long long)(short)(v & 0xffff) * __ldg(e.T + (size_t)(v >> 16) * e.hs + b);
+                }
             } else {
                 const int *__restrict__ dq = e.dP + q * e.hs;
-                if (row)
-                    for (int c = 0; c < e.hs; ++c) {
-                        const int v = __ldcg(dq + c);
-                        if (v)
-                            z += (long long)v * __ldg(e.T + (size_t)c * e.hs + b);
-                    }
+                for (int c = 0; c < e.hs; ++c) {
+                    const int v = __ldcg(dq + c);
+                    if (v)
+                        z += (long long)v * __ldg(e.T + (size_t)c * e.hs + b);
+                }
             }
-            y = fma(cq[q] * e.yscale, (double)z, y);
+            bk.Zi[(size_t)(bk.col0 + e.lc + q) * bk.hsp + b] = z;
         }
-        double part = 0.0;
-        if (row) {
-            e.y[b] = y;
-            if (sv != 0.0)
-                part = (rq * sv) * (y - hb);
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-        if (lane == 0)
-            e.sqpart[rb] = part;
     }
-    // release: the barrier orders every warp's y and share stores before the
-    // gpu-scope fences of the threads that count the engines' row blocks done
-    __syncthreads();
+}
+
+// One tile item: rows [rb kSqRows, +kSqRows) of the block's digit products
+// over K split ks.  `chunks` and `tiles` are the CTA's running counts.
+__device__ void sq_tile(const SqParams &p, const SqBlock &bk, int rb, int ks, unsigned char *ring, SqPipe &pp,
+                        uint32_t &chunks, uint32_t &tiles)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int kb = ks * bk.nk / bk.nsplit, n = (ks + 1) * bk.nk / bk.nsplit - kb;
+    const int row0 = rb * kSqRows;
+    const uint32_t npad = (uint32_t)((bk.ncol + 15) & ~15);
+    // the block's product modes (read now, used after the product)
+    const int mode = (int)threadIdx.x < bk.ncol ? __ldcg(bk.cmode + threadIdx.x) : 0;
+    if (n > 0) {
+        if (warp == 0) {
+            if (lane == 0) {
+                // producer and MMA issuer: chunk i of the tile is the CTA's
+                // chunk g0 + i, in stage (g0 + i) % kSqStages
+                const CUtensorMap *tmA = bk.tm, *tmB = bk.tm + 1;
+                tmap_acquire(tmA);
+                tmap_acquire(tmB);
+                const uint32_t idesc = idesc_f16_m128(npad);
+                const uint32_t g0 = chunks;
+                int issued = 0;
+                auto load = [&](int i) {
+                    const uint32_t s = (g0 + i) % kSqStages;
+                    unsigned char *st = ring + s * kSqStageBytes;
+                    mbar_arrive_expect_tx(&pp.full[s], kSqStageBytes);
+                    const int x = (kb + i) * kSqK;
+                    tma_load_3d(st, tmA, x, row0, 0, &pp.full[s]);
+                    tma_load_2d(st + kSqABytes, tmB, x, bk.col0, &pp.full[s]);
+                    issued = i + 1;
+                };
+                auto wait_empty = [&](int i) {
+                    const uint32_t g = g0 + i;
+                    return mbar_wait_ns(&pp.empty[g % kSqStages], (g / kSqStages) & 1u, kSqWaitNs, p.status);
+                };
+                for (int i = 0; i < min(n, kSqStages); ++i) load(i);
+                int done = 0;
+                for (int i = 0; i < n; ++i) {
+                    const uint32_t g = g0 + i, s = g % kSqStages;
+                    if (!mbar_wait_ns(&pp.full[s], (g / kSqStages) & 1u, kSqWaitNs, p.status)) {
+                        pp.fail = 1;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t a0 = smem_addr(ring + s * kSqStageBytes), b0 = a0 + kSqABytes;
+#pragma unroll
+                    for (int kk = 0; kk < kSqK / 16; ++kk)
+#pragma unroll
+                        for (int l = 0; l < kSqLimbs; ++l)
+                            tc_mma_f16(pp.tmem + (uint32_t)(l * kSqCols),
+                                       sdesc_k_sw64(a0 + (uint32_t)(l * kSqPlaneBytes + kk * 32)),
+                                       sdesc_k_sw64(b0 + (uint32_t)(kk * 32)), idesc, (uint32_t)(i | kk));
+                    tc_commit(&pp.empty[s]);
+                    done = i + 1;
+                    // refill the previous chunk's stage once its MMAs are done
+                    if (i >= 1 && i - 1 + kSqStages < n) {
+                        if (!wait_empty(i - 1)) {
+                            pp.fail = 1;
+                            break;
+                        }
+                        load(i - 1 + kSqStages);
+                    }
+                }
+                tc_commit(&pp.acc);
+                // the stages whose MMAs were not waited for above (every
+                // chunk's completion is consumed once, in order)
+                if (!pp.fail)
+                    for (int i = max(0, n - kSqStages); i < n; ++i)
+                        if (!wait_empty(i)) {
+                            pp.fail = 1;
+                            break;
+                        }
+                if (pp.fail) {
+                    // let the copies in flight land before the CTA stops
+                    for (int i = done; i < issued; ++i) {
+                        const uint32_t g = g0 + i;
+                        mbar_wait_ns(&pp.full[g % kSqStages], (g / kSqStages) & 1u, kSqWaitNs, nullptr);
+                    }
+                }
+            }
+            __syncwarp();
+        }
+        chunks += (uint32_t)n;
+        if (!mbar_wait_ns(&pp.acc, tiles & 1u, kSqWaitNs, p.status))
+            pp.fail = 1;
+        tiles += 1;
+        tc_fence_after();
+        __syncthreads();
+        if (pp.fail)
+            return;
+        // epilogue, one digit plane at a time: warps w and w + 4 share TMEM
+        // lanes 32 (w % 4) .. + 31 (the tile's rows) and split the columns;
+        // the accumulators go TMEM -> registers -> a plane buffer in the ring
+        // (column-major, kSqRows per column, the block's columns adjacent as
+        // in Zf) -> one bulk fp32 reduction into Zf in L2 (exact integers:
+        // any order of the splits' additions gives the same sums)
+        const int quarter = warp & 3, part = warp >> 2;
+        const uint32_t half = npad >> 1;  // a multiple of 8
+        const size_t zrb = (size_t)bk.zcap * kSqRows;
+        const size_t zplane = (size_t)(bk.hsp / kSqRows) * zrb;
+        float *planes = reinterpret_cast<float *>(ring);
+        for (int l = 0; l < kSqLimbs; ++l) {
+            float *buf = planes + (l & 1) * (kSqCols * kSqRows);
+            if (l >= 2) {
+                if (threadIdx.x == 0)
+                    bulk_wait_read<1>();  // plane l - 2's reduction has read this buffer
+                __syncthreads();
+            }
+            for (uint32_t c = part * half; c < (part + 1) * half; c += 8) {
+                uint32_t r[8];
+                tmem_ld8(pp.tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(l * kSqCols) + c, r);
+                tmem_ld_wait();
+#pragma unroll
+                for (int j = 0; j < 8; ++j) buf[(c + j) * kSqRows + 32 * quarter + lane] = __uint_as_float(r[j]);
+            }
+            fence_proxy_async_smem();
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                // the block's columns are adjacent: one reduction per plane
+                bulk_reduce_add_f32(bk.Zf + (size_t)l * zplane + (size_t)rb * zrb + (size_t)bk.col0 * kSqRows, buf,
+                                    (uint32_t)bk.ncol * kSqRows * 4u);
+                bulk_commit_group();
+            }
+        }
+        tc_fence_before();  // the TMEM reads come before the next tile's MMAs
+        if (threadIdx.x == 0) {
+            bulk_wait<0>();
+            fence_proxy_async_global();
+        }
+    }
+    const int wide = __syncthreads_or(mode < 0);
+    if (wide && ks == 0) {
+        sq_tile_exact(p, bk, row0);
+        __syncthreads();
+    }
+    // release: the barriers above order every Zf / Zi write before the
+    // gpu-scope fences of the threads that count the engines' tiles done
     for (int k = threadIdx.x; k < bk.neng; k += kSqThreads) {
         __threadfence();
         atomicAdd(p.engs[bk.e0 + k].done, 1u);
     }
-    __syncthreads();  // the staging buffers are reused by the next item
+    __syncthreads();  // the ring is reused by the next item
 }
 
-// Decide and commit an engine's step; its moved group `g` was loaded by the
-// caller (before waiting for the row blocks).
-__device__ void sq_finish(const EDesc &D, int *s_flag, double *s_val, MovedGroup &g)
+// Bounded wait (thread 0) until *counter >= target; false after kSqWaitNs.
+__device__ bool sq_wait_count(const unsigned *counter, unsigned target, unsigned *status)
 {
-    __shared__ double s_part[kSqMaxBins / kSqRows];
-    for (int k = threadIdx.x; k < D.sqblk; k += blockDim.x) s_part[k] = __ldcg(D.sqpart + k);
+    const volatile unsigned *c = counter;
+    if (*c >= target)
+        return true;
+    const unsigned long long t0 = global_ns();
+    while (*c < target) {
+        if (global_ns() - t0 > kSqWaitNs) {
+            atomicOr(status, DS_BARRIER_TIMEOUT);
+            return false;
+        }
+        __nanosleep(128);
+    }
+    return true;
+}
+
+// A row item: bins [rb0 kSqRows, (rb0 + rbn) kSqRows) of one engine (rbn <=
+// kSqThreads / kSqRows), one bin per thread, once the `ntiles` tiles of its
+// block are done.  y(b) = sum_p coef_p z_p(b) in p order; row block rb's share
+// of x (y - h) is summed over its bins by a fixed tree (each warp's shuffle
+// tree, then its four warps in order), so it does not depend on how row
+// blocks are grouped into items.
+__device__ void sq_row_item(const SqParams &p, const EDesc &D, int rb0, int rbn, int ntiles)
+{
+    __shared__ int s_mode[kMaxP];
+    __shared__ double s_coef[kMaxP];
+    __shared__ double s_wp[kSqThreads / 32];
+    __shared__ int s_ok;
+    const int hs = D.hs, np = D.npairs, hsp = D.hsp;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int rbl = (int)threadIdx.x / kSqRows, b = (rb0 + rbl) * kSqRows + (int)threadIdx.x % kSqRows;
+    const bool row = rbl < rbn && b < hs;
+    const size_t zrb = (size_t)D.zcap * kSqRows, zplane = (size_t)(hsp / kSqRows) * zrb;
+    // what does not depend on the tiles
+    const double sv = row ? __ldcg(D.Sb + b) : 0.0;
+    const double rq = row ? __ldg(D.Rq + b) : 0.0;
+    const double hb = row ? __ldcg(D.h + b) : 0.0;
+    if ((int)threadIdx.x < np) {
+        s_mode[threadIdx.x] = __ldcg(D.evn + threadIdx.x);
+        s_coef[threadIdx.x] = __ldg(D.pc + threadIdx.x) * D.yscale;
+    }
+    if (threadIdx.x == 0)
+        s_ok = sq_wait_count(&D.st->sq_done, (unsigned)ntiles, p.status) ? 1 : 0;
+    __syncthreads();
+    if (!s_ok)
+        return;
+    __threadfence();
+    // every load of the bin is issued before any is used
+    float *zb = D.Zf + (size_t)(b / kSqRows) * zrb + (b % kSqRows);
+    float f[kMaxP][kSqLimbs];
+    long long zi[kMaxP];
+#pragma unroll
+    for (int q = 0; q < kMaxP; ++q) {
+        const bool on = row && q < np, tc = on && s_mode[q] >= 0;
+#pragma unroll
+        for (int l = 0; l < kSqLimbs; ++l) f[q][l] = tc ? __ldcg(zb + l * zplane + q * kSqRows) : 0.0f;
+        zi[q] = (on && !tc) ? __ldcg(D.Zi + (size_t)q * hsp + b) : 0ll;
+    }
+    double y = 0.0;
+#pragma unroll
+    for (int q = 0; q < kMaxP; ++q) {
+        if (q >= np)
+            break;
+        long long z = zi[q];
+        if (s_mode[q] >= 0) {
+            // fp32 -> int32 is exact (|digit product| <= 2^24); planes combine in int64
+            unsigned long long u = 0;
+#pragma unroll
+            for (int l = 0; l < kSqLimbs; ++l)
+                u += (unsigned long long)(long long)__float2int_rn(f[q][l]) << (kSqDigitBits * l);
+            z = (long long)u;
+        }
+        y = fma(s_coef[q], (double)z, y);
+    }
+    double part = 0.0;
+    if (row) {
+        D.y[b] = y;
+        if (sv != 0.0)
+            part = (rq * sv) * (y - hb);
+        // the bin's deltas, delta columns and digit products are spent
+        for (int q = 0; q < np; ++q) {
+            D.dP[q * hs + b] = 0;
+            D.X[q * D.xld + b] = __float2half_rn(0.0f);
+#pragma unroll
+            for (int l = 0; l < kSqLimbs; ++l) zb[l * zplane + q * kSqRows] = 0.0f;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if (lane == 0)
+        s_wp[warp] = part;
+    __syncthreads();
+    constexpr int kW = kSqRows / 32;  // warps per row block
+    if ((int)threadIdx.x < rbn) {
+        const double *w = s_wp + threadIdx.x * kW;
+        double t = w[0];
+#pragma unroll
+        for (int k = 1; k < kW; ++k) t += w[k];
+        D.sqpart[rb0 + threadIdx.x] = t;
+    }
+    // release: the barrier orders every y, share and clearing store before
+    // the gpu-scope fence of the thread that counts the item done
     __syncthreads();
     if (threadIdx.x == 0) {
-        double dsq = 0.0;
-        for (int k = 0; k < D.sqblk; ++k) dsq += s_part[k];
+        __threadfence();
+        atomicAdd(&D.st->sq_ydone, 1u);
+    }
+}
+
+// Decide and commit an engine's step once its `nrow` row items are done.
+// What does not depend on them -- the descriptor's fields, S, h, A, Bq, the
+// touched list, the state and the moved group -- is read before the wait.
+// Shared memory (the ring): S, h, y, then A and Bq where they fit.
+__device__ void sq_commit(const SqParams &p, const EDesc &D, int nrow, unsigned char *ring, MovedGroup &g)
+{
+    constexpr int kTl = 8;  // touched-list entries per thread read before the wait
+    __shared__ double s_val[4];
+    __shared__ double s_part[kSqMaxBins / kSqRows];
+    __shared__ int s_ready, s_flag;
+    const int hs = D.hs, hsp = D.hsp;
+    const int nrb = (hs + kSqRows - 1) / kSqRows;
+    const double var2 = D.var2, var2q = D.var2q, tol = D.tol;
+    double *sS = reinterpret_cast<double *>(ring);
+    double *sH = sS + hsp, *sY = sH + hsp, *sA = sY + hsp, *sB = sA + hsp;
+    // 1. everything that does not depend on the row items
+    load_moved_group(D, D.st->step, g);
+    for (int b = threadIdx.x; b < hs; b += kSqThreads) {
+        sS[b] = __ldcg(D.Sb + b);
+        sH[b] = __ldcg(D.h + b);
+        sA[b] = __ldcg(D.A + b);
+        sB[b] = __ldcg(D.Bq + b);
+    }
+    const unsigned nt = __ldcg(&D.st->tcount);
+    const int fmt = __ldcg(&D.st->fmt);
+    int tl[kTl];
+#pragma unroll
+    for (int i = 0; i < kTl; ++i) {
+        const unsigned k = threadIdx.x + i * kSqThreads;
+        tl[i] = (fmt && k < nt) ? __ldcg(D.tlist + k) : -1;
+    }
+    if (threadIdx.x == 32) {
         const EState &S0 = *D.st;
-        const double sd_new = S0.sd + S0.dsd;
-        const double sq_new = S0.sd_sq + dsq;
-        const double chi2_new = sd_new / D.var2 + sq_new / D.var2q;
-        const EMove &m = D.moves[S0.step % D.move_cap];
-        const bool reject = (chi2_new > S0.chi2) && (m.u > D.tol);
-        *s_flag = reject ? 0 : 1;
-        s_val[0] = chi2_new;
-        s_val[1] = sd_new;
-        s_val[2] = sq_new;
+        s_val[0] = S0.sd + S0.dsd;
+        s_val[1] = S0.sd_sq;
+    }
+    // 2. the row items
+    if (threadIdx.x == 0)
+        s_ready = sq_wait_count(&D.st->sq_ydone, (unsigned)nrow, p.status) ? 1 : 0;
+    __syncthreads();
+    if (!s_ready)
+        return;
+    __threadfence();
+    for (int k = threadIdx.x; k < nrb; k += kSqThreads) s_part[k] = __ldcg(D.sqpart + k);
+    for (int b = threadIdx.x; b < hs; b += kSqThreads) sY[b] = __ldcg(D.y + b);
+    __syncthreads();
+    // 3. the row blocks' shares in block order, the decision
+    if (threadIdx.x == 0) {
+        double dsq = 0.0;
+        for (int k = 0; k < nrb; ++k) dsq += s_part[k];
+        const double sd_new = s_val[0];
+        const double sq_new = s_val[1] + dsq;
+        const double chi2_new = sd_new / var2 + sq_new / var2q;
+        const bool reject = (chi2_new > g.chi2) && (g.u > tol);
+        s_flag = reject ? 0 : 1;
+        s_val[2] = chi2_new;
+        s_val[3] = sq_new;
     }
     __syncthreads();
-    const bool accept = *s_flag != 0;
-    const unsigned nt = D.st->tcount;
-    if (D.st->fmt) {
+    const bool accept = s_flag != 0;
+    // 4. counts
+    if (fmt) {
         // one CTA's shared-memory deltas: entries (flat << 1) | sign
-        if (accept)
-            for (unsigned k0 = threadIdx.x; k0 < nt; k0 += 4 * blockDim.x) {
-                int e[4];
+        if (accept) {
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const unsigned k = k0 + u * blockDim.x;
-                    e[u] = k < nt ? __ldcg(D.tlist + k) : -1;
-                }
-#pragma unroll
-                for (int u = 0; u < 4; ++u)
-                    if (e[u] >= 0)
-                        atomicAdd(D.counts + (e[u] >> 1), (e[u] & 1) ? 1 : -1);
+            for (int i = 0; i < kTl; ++i)
+                if (tl[i] >= 0)
+                    atomicAdd(D.counts + (tl[i] >> 1), (tl[i] & 1) ? 1 : -1);
+            for (unsigned k = threadIdx.x + kTl * kSqThreads; k < nt; k += kSqThreads) {
+                const int e = __ldcg(D.tlist + k);
+                atomicAdd(D.counts + (e >> 1), (e & 1) ? 1 : -1);
             }
+        }
     } else {
         // global oriented deltas: atomicExch hands each bin's delta to one entry
-        for (unsigned k = threadIdx.x; k < nt; k += blockDim.x) {
+        for (unsigned k = threadIdx.x; k < nt; k += kSqThreads) {
             const int f = D.tlist[k];
             const int d = atomicExch(D.delta + f, 0);
             if (accept && d)
                 D.counts[f] += d;
         }
     }
-    const int nph = D.npairs * D.hs;
-    for (int k = threadIdx.x; k < nph; k += blockDim.x) D.dP[k] = 0;
-    // the engine's fp16 delta columns are adjacent: clear them for the next step
-    const int nx = D.npairs * D.xld;
-    for (int k = threadIdx.x; k < nx; k += blockDim.x) D.X[k] = __float2half_rn(0.0f);
+    // 5. the accepted step: Bq -= 2 A S, h -= 2 y, coordinates
     if (accept) {
-        for (int b0 = threadIdx.x; b0 < D.hs; b0 += 4 * blockDim.x) {
-            double sv[4], yv[4], hv[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int b = b0 + u * blockDim.x;
-                sv[u] = b < D.hs ? __ldcg(D.Sb + b) : 0.0;
-                yv[u] = b < D.hs ? __ldcg(D.y + b) : 0.0;
-                hv[u] = b < D.hs ? D.h[b] : 0.0;
-            }
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int b = b0 + u * blockDim.x;
-                if (b < D.hs) {
-                    if (sv[u] != 0.0)
-                        D.Bq[b] = fma(-2.0 * D.A[b], sv[u], D.Bq[b]);
-                    D.h[b] = fma(-2.0, yv[u], hv[u]);
-                }
-            }
+        for (int b = threadIdx.x; b < hs; b += kSqThreads) {
+            const double sv = sS[b];
+            if (sv != 0.0)
+                D.Bq[b] = fma(-2.0 * sA[b], sv, sB[b]);
+            D.h[b] = fma(-2.0, sY[b], sH[b]);
         }
         commit_moved_group(D, g);
         if (D.dense)
@@ -2070,14 +2204,14 @@ __device__ void sq_finish(const EDesc &D, int *s_flag, double *s_val, MovedGroup
     __syncthreads();
     if (threadIdx.x == 0) {
         EState &S = *D.st;
-        EResult &r = D.results[S.step % D.move_cap];
-        r.chi2_new = s_val[0];
+        EResult &r = D.results[g.step % D.move_cap];
+        r.chi2_new = s_val[2];
         r.accepted = accept ? 1 : 0;
         r.atom = g.atom[0];
         if (accept) {
-            S.chi2 = s_val[0];
-            S.sd = s_val[1];
-            S.sd_sq = s_val[2];
+            S.chi2 = s_val[2];
+            S.sd = s_val[0];
+            S.sd_sq = s_val[3];
             S.accepted += 1;
             if (D.dense)
                 S.sf = S.sf_prop;
@@ -2085,57 +2219,62 @@ __device__ void sq_finish(const EDesc &D, int *s_flag, double *s_val, MovedGroup
         S.step += 1;
         S.tcount = 0u;
         S.sq_done = 0u;
+        S.sq_ydone = 0u;
         S.dsd = 0.0;
     }
 }
 
-__global__ void __launch_bounds__(kSqThreads, 2) k_sq_fused(SqParams p)
+__global__ void __launch_bounds__(kSqThreads, 1) k_sq_fused(SqParams p)
 {
     extern __shared__ __align__(16) unsigned char sq_smem_raw[];
-    __half *smem = reinterpret_cast<__half *>(sq_smem_raw);
+    // the swizzled operand tiles start on 1024-byte boundaries
+    unsigned char *ring = sq_smem_raw + ((1024u - (smem_addr(sq_smem_raw) & 1023u)) & 1023u);
+    __shared__ SqPipe pp;
     __shared__ int s_item;
-    __shared__ int s_ready;
-    __shared__ double s_val[3];
-    __shared__ int s_flag;
     __shared__ MovedGroup s_group;
+    const int warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kSqStages; ++s) {
+            mbar_init(&pp.full[s], 1);
+            mbar_init(&pp.empty[s], 1);
+        }
+        mbar_init(&pp.acc, 1);
+        pp.fail = 0;
+        mbar_fence_init();
+    }
+    if (warp == 0) {
+        tmem_alloc(&pp.tmem, kSqTmemCols);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    uint32_t chunks = 0, tiles = 0;
     for (;;) {
         if (threadIdx.x == 0) {
             const unsigned long long k = atomicAdd(&p.sched->claimed, 1ull);
-            s_item = k < (unsigned long long)p.nitems ? (int)k : -1;
+            s_item = (k < (unsigned long long)p.nitems && !pp.fail) ? (int)k : -1;
         }
         __syncthreads();
         const int it = s_item;
         if (it < 0)
             break;
-        const int2 item = p.items[it];
-        if (item.x >= 0) {
-            sq_tile(p, p.blocks[item.x], item.y, smem);
-            continue;
-        }
-        const EDesc &D = p.desc[-1 - item.x];
-        // the moved group does not depend on the tiles: load it first
-        load_moved_group(D, D.st->step, s_group);
-        if (threadIdx.x == 0) {
-            // the engine's row blocks were claimed before this item by
-            // running CTAs; a lost one gives up after kSpinLimit polls
-            const volatile unsigned *done = &D.st->sq_done;
-            int ok = 0;
-            for (uint32_t k = 0; k < kSpinLimit; ++k) {
-                if (*done >= (unsigned)D.sqblk) {
-                    ok = 1;
-                    break;
-                }
-                __nanosleep(256);
-            }
-            if (!ok)
-                atomicOr(p.status, DS_BARRIER_TIMEOUT);
-            __threadfence();
-            s_ready = ok;
+        const int4 item = p.items[it];
+        if (item.x == 0) {
+            const SqBlock &bk = p.blocks[item.y];
+            sq_tile(p, bk, item.z / bk.nsplit, item.z % bk.nsplit, ring, pp, chunks, tiles);
+        } else if (item.x == 1) {
+            sq_row_item(p, p.desc[item.y], item.z >> 16, item.z & 0xffff, item.w);
+        } else {
+            sq_commit(p, p.desc[item.y], item.z, ring, s_group);
         }
         __syncthreads();
-        if (s_ready)
-            sq_finish(D, &s_flag, s_val, s_group);
-        __syncthreads();
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(pp.tmem, kSqTmemCols);
     }
     if (threadIdx.x == 0) {
         __threadfence();
@@ -2226,7 +2365,7 @@ __global__ void k_sq_quantize(double *K, const double *R0, int hs, int s)
 }
 
 // The product's operand: TD[(l hsp + b) hsp + c] = digit l of T[c][b]
-// (balanced base 2048, so T = sum_l 2048^l digit_l), zero outside hs x hs.
+// (balanced base 4096, so T = sum_l 4096^l digit_l), zero outside hs x hs.
 __global__ void k_sq_digits(const long long *T, int hs, int hsp, __half *TD)
 {
     const long long n = (long long)hsp * hsp;
@@ -2311,12 +2450,18 @@ struct SqTable {
     double *M = nullptr, *w = nullptr, *R0 = nullptr;
     long long *T = nullptr;
     size_t bytes = 0;
-    int hsp = 0;           // hs rounded up to a multiple of kSqK
-    __half *TD = nullptr;  // [kSqLimbs][hsp][hsp] digits of T (k_sq_digits)
+    int hsp = 0;           // hs rounded up to a multiple of kSqRows
+    __half *TD = nullptr;  // [kSqLimbs][hsp][hsp] digit planes of T (k_sq_digits)
     // this step's fp16 deltas of every engine on the table (ncols columns of
-    // hsp bins)
+    // hsp bins), their fp32 digit products (kSqLimbs planes of hsp per
+    // column), the exact products of wide columns, the columns' product
+    // modes; room for cap columns
     __half *X = nullptr;
+    float *Zf = nullptr;
+    long long *Zi = nullptr;
+    int *cmode = nullptr;
     int ncols = 0, cap = 0;
+    CUtensorMap *maps = nullptr;  // device: [0] digit planes (bin, row, plane), [1] X (bin, column)
 };
 
 // dynamic shared memory of a one-CTA step at the largest CTA (the static
@@ -2348,6 +2493,7 @@ struct EngineSet {
     std::vector<int> item_count;
     std::vector<int> fused_item;  // per engine id: its one-CTA item in the batched list (or -1)
     int tile = 1024, threads = 256, ctas_per_sm = 2;  // the usual autotuner choice on GB300
+    int sq_split_max = 0;  // K splits of an S(Q) row block at most (0: as many as fill the SMs)
     EDesc *ddesc = nullptr;
     int ddesc_cap = 0;
     EDesc *fdesc = nullptr;        // descriptors of the fused items, in work-list order
@@ -2373,13 +2519,13 @@ struct EngineSet {
     // S(Q) work lists: the batched list (every block's tiles, then one commit
     // per engine) at [0, sq_nbatch), then each engine's own list (its tiles
     // and its commit) at sq_first[id], sq_count[id] items
-    std::vector<int2> sq_host;
+    std::vector<int4> sq_host;
     int sq_nbatch = 0;
     std::vector<int> sq_first, sq_count;
     std::vector<int> sq_xcol;      // per engine id: its first delta column in its table's X
     std::vector<SqBlock> sq_hblocks;
     std::vector<SqEng> sq_hengs;
-    int2 *sq_items = nullptr;
+    int4 *sq_items = nullptr;
     int sq_cap = 0;
     SqBlock *sq_blocks = nullptr;
     int sq_blocks_cap = 0;
@@ -2397,7 +2543,7 @@ static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 struct BlobLayout {
     size_t box, real, mol, counts, delta, rfac, invvol, expd, dw, pc, pi, pj, dP, pidx, tlist, R, A, Bq, Sb, Gc, fnum,
         fden, win, moves,
-        results, st, Rq, rfacq, sqexp, h, y, sqpart, sqv, evl, evn, groups, cbox, cmol, csl, cstart, clo, chi,
+        results, st, Rq, rfacq, sqexp, h, y, sqpart, sqv, evl, groups, cbox, cmol, csl, cstart, clo, chi,
         total;
 };
 
@@ -2453,10 +2599,9 @@ static BlobLayout blob_layout(const frmc_engine_spec &sp)
     L.sqexp = take(8 * nq);
     L.h = take(8 * hq);
     L.y = take(8 * hq);
-    L.sqpart = take(sq ? 8 * (size_t)((sp.hs + kSqRows - 1) / kSqRows) : 0);
+    L.sqpart = take(sq ? 8 * (size_t)((sp.hs + 127) / 128) : 0);
     L.sqv = take(8 * nq);
     L.evl = take(sq ? 4 * (size_t)sp.npairs * hs : 0);
-    L.evn = take(sq ? 4 * 16 : 0);
     L.groups = take(G > 1 ? sizeof(EGroup) * (size_t)sp.move_cap : 0);
     L.cbox = take(16 * n);
     L.cmol = take(4 * n);
@@ -2514,22 +2659,60 @@ static void drop_graphs(EngineSet *s)
     }
 }
 
+// A table's TMA operand descriptors: [0] the digit planes as a 3-D tensor
+// (bin c, row b, plane l) read in boxes of kSqK x kSqRows x kSqLimbs, [1] the
+// delta columns (bin, column) read in boxes of kSqK x kSqCols.  Both use the
+// 64-byte swizzle that the MMAs' shared-memory descriptors name; reads past
+// the last column fill zeros.
+static int sq_encode_maps(SqTable &t)
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        FRMC_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+        if (!fn || q != cudaDriverEntryPointSuccess)
+            return set_error(FRMC_E_CUDA, "S(Q) table: the driver offers no cuTensorMapEncodeTiled");
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    CUtensorMap m[2];
+    std::memset(m, 0, sizeof m);
+    const cuuint64_t hsp = (cuuint64_t)t.hsp;
+    const cuuint32_t unit[3] = {1, 1, 1};
+    {
+        const cuuint64_t dims[3] = {hsp, hsp, (cuuint64_t)kSqLimbs};
+        const cuuint64_t strides[2] = {hsp * 2, hsp * hsp * 2};
+        const cuuint32_t box[3] = {(cuuint32_t)kSqK, (cuuint32_t)kSqRows, (cuuint32_t)kSqLimbs};
+        const CUresult r = encode(&m[0], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, t.TD, dims, strides, box, unit,
+                                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS)
+            return set_error(FRMC_E_CUDA, "S(Q) table: digit-plane tensor map (driver error %d)", (int)r);
+    }
+    if (t.X) {
+        const cuuint64_t dims[2] = {hsp, (cuuint64_t)t.cap};
+        const cuuint64_t strides[1] = {hsp * 2};
+        const cuuint32_t box[2] = {(cuuint32_t)kSqK, (cuuint32_t)kSqCols};
+        const CUresult r = encode(&m[1], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, t.X, dims, strides, box, unit,
+                                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS)
+            return set_error(FRMC_E_CUDA, "S(Q) table: delta-column tensor map (driver error %d)", (int)r);
+    }
+    if (!t.maps)
+        FRMC_CUDA(cudaMalloc(&t.maps, sizeof m));
+    FRMC_CUDA(cudaMemcpy(t.maps, m, sizeof m, cudaMemcpyHostToDevice));
+    return FRMC_OK;
+}
+
 // An engine's entry in an S(Q) block: its device arrays and constants.
 static SqEng sq_eng(const EDesc &D, int lc)
 {
     SqEng e;
-    e.evn = D.evn;
     e.evl = D.evl;
     e.dP = D.dP;
     e.T = D.T;
-    e.pc = D.pc;
-    e.Sb = D.Sb;
-    e.Rq = D.Rq;
-    e.h = D.h;
-    e.y = D.y;
-    e.sqpart = D.sqpart;
     e.done = &D.st->sq_done;
-    e.yscale = D.yscale;
     e.hs = D.hs;
     e.np = D.npairs;
     e.lc = lc;
@@ -2646,98 +2829,153 @@ static int refresh(EngineSet *s)
         if (t.ncols <= t.cap)
             continue;
         if (t.X) cudaFree(t.X);
+        if (t.Zf) cudaFree(t.Zf);
+        if (t.Zi) cudaFree(t.Zi);
+        if (t.cmode) cudaFree(t.cmode);
         t.X = nullptr;
-        const int cap = std::max(t.ncols, 2 * t.cap);
-        FRMC_CUDA(cudaMalloc(&t.X, sizeof(__half) * (size_t)t.hsp * cap));
-        FRMC_CUDA(cudaMemset(t.X, 0, sizeof(__half) * (size_t)t.hsp * cap));
+        t.Zf = nullptr;
+        t.Zi = nullptr;
+        t.cmode = nullptr;
+        // at least one block's width, so that a column box never passes the end
+        const int cap = std::max(std::max(t.ncols, 2 * t.cap), kSqCols);
+        const size_t hsp = (size_t)t.hsp;
+        FRMC_CUDA(cudaMalloc(&t.X, sizeof(__half) * hsp * cap));
+        FRMC_CUDA(cudaMemset(t.X, 0, sizeof(__half) * hsp * cap));
+        FRMC_CUDA(cudaMalloc(&t.Zf, sizeof(float) * kSqLimbs * hsp * cap));
+        FRMC_CUDA(cudaMemset(t.Zf, 0, sizeof(float) * kSqLimbs * hsp * cap));
+        FRMC_CUDA(cudaMalloc(&t.Zi, sizeof(long long) * hsp * cap));
+        FRMC_CUDA(cudaMalloc(&t.cmode, sizeof(int) * cap));
+        FRMC_CUDA(cudaMemset(t.cmode, 0, sizeof(int) * cap));
         t.cap = cap;
+        FRMC_TRY(sq_encode_maps(t));
     }
     for (int id : s->live) {
         Slot &sl = s->slots[id];
         if (!sl.d.sq)
             continue;
         const SqTable &t = s->tables[sl.sq_table];
+        const size_t col = (size_t)s->sq_xcol[id];
         sl.d.hsp = t.hsp;
         sl.d.xld = t.hsp;
-        sl.d.X = t.X + (size_t)s->sq_xcol[id] * t.hsp;
+        sl.d.X = t.X + col * t.hsp;
+        sl.d.Zf = t.Zf + col * kSqRows;
+        sl.d.zcap = t.cap;
+        sl.d.Zi = t.Zi + col * t.hsp;
+        sl.d.evn = t.cmode + col;
     }
     // S(Q) work lists.  Blocks of whole engines (at most kSqCols columns, in
-    // live order) per table; the batched list is every block's row-block
-    // tiles, then one commit per engine; each engine also gets a block of its
-    // own and a list of its tiles and commit for steps of that engine alone.
+    // live order) per table; the batched list is every block's tiles (row
+    // blocks x K splits), then one commit per engine; each engine also gets a
+    // block of its own and a list of its tiles and commit for steps of that
+    // engine alone.  The K splits let a list's tiles about fill the SMs (one
+    // CTA each): more splits shorten each tile's product but add partial
+    // sums for L2 to reduce.
     s->sq_hblocks.clear();
     s->sq_hengs.clear();
     s->sq_host.clear();
     s->sq_first.assign(nslots, -1);
     s->sq_count.assign(nslots, 0);
-    // block width: the batched step's tiles should fill the CTA slots (two
-    // per SM) evenly, since the product's time is set by the busiest SM
-    int width = kSqCols;
-    {
-        long long work = 0, engines = 0;
-        for (const auto &t : s->tables) work += (long long)t.ncols * ((t.hs + kSqRows - 1) / kSqRows);
-        for (int id : s->live) engines += s->slots[id].d.sq ? 1 : 0;
-        Context *c;
-        FRMC_TRY(get_context(&c));
-        // the commits hold a slot each while they wait
-        const long long slots = std::max<long long>(c->sms, 2LL * c->sms - engines);
-        if (work > 0) {
-            const long long w = (work + slots - 1) / slots;
-            width = (int)std::min<long long>(kSqCols, std::max<long long>(kMaxP, (w + 7) / 8 * 8));
-        }
-    }
+    Context *ctx;
+    FRMC_TRY(get_context(&ctx));
+    auto splits = [&](long long rowblocks, int nk) {
+        long long k = std::max<long long>(1, ctx->sms / std::max<long long>(1, rowblocks));
+        if (s->sq_split_max > 0)
+            k = std::min<long long>(k, s->sq_split_max);
+        return (int)std::min<long long>(k, nk);
+    };
+    auto new_block = [&](const SqTable &t, int col0) {
+        SqBlock b{};
+        b.tm = t.maps;
+        b.Zf = t.Zf;
+        b.zcap = t.cap;
+        b.Zi = t.Zi;
+        b.cmode = t.cmode + col0;
+        b.col0 = col0;
+        b.hsp = t.hsp;
+        b.hs = t.hs;
+        b.nrb = (t.hs + kSqRows - 1) / kSqRows;
+        b.nk = (t.hs + kSqK - 1) / kSqK;
+        b.nsplit = 1;
+        b.e0 = (int)s->sq_hengs.size();
+        return b;
+    };
+    std::vector<int> block_of(nslots, -1);
     for (int ti = 0; ti < (int)s->tables.size(); ++ti) {
         const SqTable &t = s->tables[ti];
-        const int nrb = (t.hs + kSqRows - 1) / kSqRows;
         SqBlock cur{};
-        int col0 = 0;
         bool open = false;
         for (int id : s->live) {
             const Slot &sl = s->slots[id];
             if (!sl.d.sq || sl.sq_table != ti)
                 continue;
             const int col = s->sq_xcol[id];
-            if (open && col + sl.d.npairs - col0 > width) {
+            if (open && col + sl.d.npairs - cur.col0 > kSqCols) {
                 s->sq_hblocks.push_back(cur);
                 open = false;
             }
             if (!open) {
-                col0 = col;
-                cur = SqBlock{t.TD, t.X + (size_t)col * t.hsp, t.hsp, t.hs, 0, nrb, (int)s->sq_hengs.size(), 0};
+                cur = new_block(t, col);
                 open = true;
             }
-            s->sq_hengs.push_back(sq_eng(sl.d, col - col0));
+            block_of[id] = (int)s->sq_hblocks.size();
+            s->sq_hengs.push_back(sq_eng(sl.d, col - cur.col0));
             cur.neng += 1;
-            cur.ncol = col + sl.d.npairs - col0;
+            cur.ncol = col + sl.d.npairs - cur.col0;
         }
         if (open)
             s->sq_hblocks.push_back(cur);
     }
-    for (int bi = 0; bi < (int)s->sq_hblocks.size(); ++bi)
-        for (int rb = 0; rb < s->sq_hblocks[bi].nrb; ++rb) s->sq_host.push_back(make_int2(bi, rb));
+    {
+        long long rowblocks = 0;
+        for (const auto &bk : s->sq_hblocks) rowblocks += bk.nrb;
+        for (auto &bk : s->sq_hblocks) bk.nsplit = splits(rowblocks, bk.nk);
+    }
+    // row items: kSqThreads / kSqRows row blocks each
+    constexpr int kRowsPerItem = kSqThreads / kSqRows;
+    auto push_rows = [&](int id, int nrb, int ntiles) {
+        int n = 0;
+        for (int rb = 0; rb < nrb; rb += kRowsPerItem, ++n)
+            s->sq_host.push_back(make_int4(1, id, (rb << 16) | std::min(kRowsPerItem, nrb - rb), ntiles));
+        return n;
+    };
+    for (int bi = 0; bi < (int)s->sq_hblocks.size(); ++bi) {
+        const SqBlock &bk = s->sq_hblocks[bi];
+        for (int k = 0; k < bk.nrb * bk.nsplit; ++k) s->sq_host.push_back(make_int4(0, bi, k, 0));
+    }
+    std::vector<int> nrow(nslots, 0);
+    for (int id : s->live)
+        if (s->slots[id].d.sq) {
+            const SqBlock &bk = s->sq_hblocks[block_of[id]];
+            nrow[id] = push_rows(id, bk.nrb, bk.nrb * bk.nsplit);
+        }
     for (int id : s->live)
         if (s->slots[id].d.sq)
-            s->sq_host.push_back(make_int2(-1 - id, 0));
+            s->sq_host.push_back(make_int4(2, id, nrow[id], 0));
     s->sq_nbatch = (int)s->sq_host.size();
     for (int id : s->live) {
         const Slot &sl = s->slots[id];
         if (!sl.d.sq)
             continue;
         const SqTable &t = s->tables[sl.sq_table];
-        const int nrb = (t.hs + kSqRows - 1) / kSqRows;
         const int bi = (int)s->sq_hblocks.size();
-        s->sq_hblocks.push_back(SqBlock{t.TD, sl.d.X, t.hsp, t.hs, sl.d.npairs, nrb, (int)s->sq_hengs.size(), 1});
+        SqBlock bk = new_block(t, s->sq_xcol[id]);
+        bk.neng = 1;
+        bk.ncol = sl.d.npairs;
+        bk.nsplit = splits(bk.nrb, bk.nk);
+        s->sq_hblocks.push_back(bk);
         s->sq_hengs.push_back(sq_eng(sl.d, 0));
         s->sq_first[id] = (int)s->sq_host.size();
-        for (int rb = 0; rb < nrb; ++rb) s->sq_host.push_back(make_int2(bi, rb));
-        s->sq_host.push_back(make_int2(-1 - id, 0));
-        s->sq_count[id] = nrb + 1;
+        const int ntiles = bk.nrb * bk.nsplit;
+        for (int k = 0; k < ntiles; ++k) s->sq_host.push_back(make_int4(0, bi, k, 0));
+        const int nr = push_rows(id, bk.nrb, ntiles);
+        s->sq_host.push_back(make_int4(2, id, nr, 0));
+        s->sq_count[id] = ntiles + nr + 1;
     }
     if ((int)s->sq_host.size() > s->sq_cap) {
         if (s->sq_items) cudaFree(s->sq_items);
         s->sq_items = nullptr;
         const int cap = std::max((int)s->sq_host.size(), 2 * s->sq_cap);
-        FRMC_CUDA(cudaMalloc(&s->sq_items, sizeof(int2) * cap));
+        FRMC_CUDA(cudaMalloc(&s->sq_items, sizeof(int4) * cap));
         s->sq_cap = cap;
     }
     if ((int)s->sq_hblocks.size() > s->sq_blocks_cap) {
@@ -2781,7 +3019,7 @@ static int refresh(EngineSet *s)
     if (!s->live.empty())
         FRMC_CUDA(cudaMemcpy(s->dlive, s->live.data(), sizeof(int) * s->live.size(), cudaMemcpyHostToDevice));
     if (!s->sq_host.empty())
-        FRMC_CUDA(cudaMemcpy(s->sq_items, s->sq_host.data(), sizeof(int2) * s->sq_host.size(),
+        FRMC_CUDA(cudaMemcpy(s->sq_items, s->sq_host.data(), sizeof(int4) * s->sq_host.size(),
                              cudaMemcpyHostToDevice));
     s->nitems = (int)items.size();
     drop_graphs(s);
@@ -2833,10 +3071,8 @@ static int launch_sq(EngineSet *s, int first, int count, cudaStream_t st)
     FRMC_TRY(get_context(&c));
     SqParams p{s->ddesc, s->sq_blocks, s->sq_engs, s->sq_items + first, count, s->sched + 1, &s->sched[0].status};
     FRMC_CUDA(cudaFuncSetAttribute(k_sq_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, kSqSmemBytes));
-    // all shared memory: two CTAs fit one SM, so every item of a step starts at once
-    FRMC_CUDA(cudaFuncSetAttribute(k_sq_fused, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                   (int)cudaSharedmemCarveoutMaxShared));
-    const int grid = std::min(count, c->sms * 2);
+    // one CTA per SM: it holds the SM's shared-memory ring and all of its TMEM
+    const int grid = std::min(count, c->sms);
     k_sq_fused<<<grid, kSqThreads, kSqSmemBytes, st>>>(p);
     FRMC_CUDA(cudaGetLastError());
     return FRMC_OK;
@@ -3215,7 +3451,6 @@ static int add_engine(EngineSet *s, const frmc_engine_spec &sp, int *out_id)
     if (tab) {
         D.sq = 1;
         D.nq = sp.nq;
-        D.sqblk = (sp.hs + kSqRows - 1) / kSqRows;
         D.var2q = sp.sq_variance_squared;
         D.M = tab->M;
         D.T = tab->T;
@@ -3230,7 +3465,6 @@ static int add_engine(EngineSet *s, const frmc_engine_spec &sp, int *out_id)
         D.sqpart = (double *)(b + L.sqpart);
         D.sqv = (double *)(b + L.sqv);
         D.evl = (int *)(b + L.evl);
-        D.evn = (int *)(b + L.evn);
         Rqt.resize(sp.hs);
         for (int bb = 0; bb < sp.hs; ++bb) Rqt[bb] = sp.sq_rfac[bb] * sp.sq_inv_shell_volume[bb];
     }
@@ -3347,6 +3581,10 @@ static void free_set(EngineSet *s)
         if (t.blob) cudaFree(t.blob);
         if (t.TD) cudaFree(t.TD);
         if (t.X) cudaFree(t.X);
+        if (t.Zf) cudaFree(t.Zf);
+        if (t.Zi) cudaFree(t.Zi);
+        if (t.cmode) cudaFree(t.cmode);
+        if (t.maps) cudaFree(t.maps);
     }
     void *ptrs[] = {s->ddesc, s->fdesc, s->fpos, s->items, s->dlive, s->sched, s->sq_items, s->sq_blocks, s->sq_engs};
     for (void *p : ptrs)
@@ -3379,10 +3617,12 @@ int frmc_engine_footprint(const frmc_engine_spec *spec, int64_t *bytes)
         return set_error(FRMC_E_ARG, "engine_footprint: null argument");
     int64_t b = (int64_t)blob_layout(*spec).total;
     if (spec->sq_table >= 0) {
-        // the engine's columns of its table's fp16 deltas (counted twice:
-        // the shared buffer grows by doubling)
-        const int64_t hsp = (spec->hs + kSqK - 1) / kSqK * kSqK;
-        b += 2 * (int64_t)spec->npairs * hsp * (int64_t)sizeof(__half);
+        // the engine's columns of its table's fp16 deltas, fp32 digit
+        // products and exact products (counted twice: the shared buffers grow
+        // by doubling)
+        const int64_t hsp = (spec->hs + kSqRows - 1) / kSqRows * kSqRows;
+        b += 2 * (int64_t)spec->npairs *
+             (hsp * (int64_t)(sizeof(__half) + kSqLimbs * sizeof(float) + sizeof(long long)) + 4);
     }
     *bytes = b;
     return FRMC_OK;
@@ -3500,6 +3740,16 @@ int frmc_engines_set_sq_gemm_limit(void *handle, int32_t limit)
     if (!s || limit < -1 || limit > kSqGemmMaxDelta)
         return set_error(FRMC_E_ARG, "engines_set_sq_gemm_limit: limit must be in [-1, %d]", kSqGemmMaxDelta);
     for (auto &sl : s->slots) sl.d.sq_gemm_max = limit;
+    s->dirty = true;
+    return FRMC_OK;
+}
+
+int frmc_engines_set_sq_splits(void *handle, int32_t max_splits)
+{
+    EngineSet *s = as_set(handle);
+    if (!s || max_splits < 0)
+        return set_error(FRMC_E_ARG, "engines_set_sq_splits: need max_splits >= 0");
+    s->sq_split_max = max_splits;
     s->dirty = true;
     return FRMC_OK;
 }
@@ -4076,7 +4326,7 @@ int frmc_engines_sq_table(void *handle, int32_t hs, int32_t nq, const double *M,
         ce = cudaGetLastError();
     }
     if (ce == cudaSuccess) {
-        t.hsp = (hs + kSqK - 1) / kSqK * kSqK;
+        t.hsp = (hs + kSqRows - 1) / kSqRows * kSqRows;
         ce = cudaMalloc(&t.TD, sizeof(__half) * (size_t)kSqLimbs * t.hsp * t.hsp);
     }
     if (ce == cudaSuccess) {
@@ -4090,6 +4340,12 @@ int frmc_engines_sq_table(void *handle, int32_t hs, int32_t nq, const double *M,
         cudaFree(t.blob);
         if (t.TD) cudaFree(t.TD);
         return cuda_fail(ce, "S(Q) table");
+    }
+    if (const int rc = sq_encode_maps(t)) {
+        cudaFree(t.blob);
+        cudaFree(t.TD);
+        if (t.maps) cudaFree(t.maps);
+        return rc;
     }
     s->tables.push_back(t);
     *table = (int32_t)s->tables.size() - 1;

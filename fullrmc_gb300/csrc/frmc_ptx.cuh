@@ -74,6 +74,15 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32
     return false;
 }
 
+// 16 bytes global -> shared through L2 (both 16-byte aligned); completed by
+// cp_async_wait_all() of the issuing thread.
+__device__ __forceinline__ void cp_async16(void *dst_smem, const void *src_gmem)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst_smem)), "l"(src_gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // 1-D bulk copy global -> shared (both 16-byte aligned, bytes % 16 == 0).
 // Hint: bring the line holding p into L2 (no register result, never faults
 // on a valid address).

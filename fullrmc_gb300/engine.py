@@ -67,6 +67,7 @@ register("frmc_engines_cells", [_vp, _i32, ctypes.POINTER(_i32), ctypes.POINTER(
 register("frmc_engines_regrid", [_vp, _i32])
 register("frmc_cell_metric", [F32P, _i32, F64P, F64P, ctypes.POINTER(_i32)])
 register("frmc_engines_set_sq_gemm_limit", [_vp, ctypes.c_int32])
+register("frmc_engines_set_sq_splits", [_vp, ctypes.c_int32])
 register("frmc_engines_init", [_vp])
 register("frmc_engines_push_moves", [_vp, _i32, I32P, F32P, F32P, _i32, _i64, ctypes.c_int])
 register("frmc_engines_step", [_vp, _i32, _i32, ctypes.c_int, _vp])
@@ -642,10 +643,16 @@ class EngineSet:
 
     def set_sq_gemm_limit(self, limit):
         """Largest element-pair delta the S(Q) product takes through the
-        tensor cores (default 2048; a column must also change at most 2^14
+        tensor cores (default 2048; a column must also change at most 2^13
         unit counts); 0 forces the exact sum over the list of deltas and -1
         the dense integer loop (all three give the same integers)."""
         check(load().frmc_engines_set_sq_gemm_limit(self.handle, int(limit)))
+
+    def set_sq_splits(self, max_splits):
+        """At most `max_splits` K splits per 128-row block of the S(Q)
+        product (0, the default: enough to fill the SMs).  The products are
+        exact integers, so this changes a step's time, not its result."""
+        check(load().frmc_engines_set_sq_splits(self.handle, int(max_splits)))
 
     TUNE_CANDIDATES = ((1024, 256, 2), (1024, 512, 1), (2048, 512, 1), (1024, 384, 1), (512, 128, 4),
                        (1024, 256, 4), (2048, 256, 2))

@@ -152,14 +152,18 @@ int frmc_engines_regrid(void *handle, int32_t e);
 int frmc_cell_metric(const float *basis, int32_t isPBC, double *w, double *lam, int32_t *mode);
 int frmc_engines_cells(void *handle, int32_t e, int32_t *ncells, int64_t *swept);
 /* The S(Q) term's product y = T x runs on the tensor cores (the library's own
- * kernel: fp16 base-2048 digits of T times fp16 deltas, fp32 accumulation)
- * for an element-pair delta column whose entries are at most `limit` in
- * magnitude (default and maximum 2048) and whose absolute sum is at most
- * 2^14, where every product sum is an exact integer; other columns take an
- * exact integer sum over the step's list of deltas; -1 takes the dense
- * integer loop.  All three give the same integers; the lower limits exist to
- * test that. */
+ * tcgen05 kernel: fp16 base-4096 digit planes of T times fp16 deltas, fp32
+ * accumulators in tensor memory) for an element-pair delta column whose
+ * entries are at most `limit` in magnitude (default and maximum 2048) and
+ * whose absolute sum is at most 2^13, where every product sum is an exact
+ * integer; other columns take an exact integer sum over the step's list of
+ * deltas; -1 takes the dense integer loop.  All three give the same
+ * integers; the lower limits exist to test that. */
 int frmc_engines_set_sq_gemm_limit(void *handle, int32_t limit);
+/* At most `max_splits` K splits per 128-row block of the S(Q) product (0, the
+ * default: as many as let one step's tiles fill the SMs).  The products are
+ * exact integers, so the split changes the time of a step, not its result. */
+int frmc_engines_set_sq_splits(void *handle, int32_t max_splits);
 /* All-pairs histograms of the initial coordinates and the initial chi2. */
 int frmc_engines_init(void *handle);
 /* Moves for steps [first_step, first_step + count) of engine e: atoms (count,),
