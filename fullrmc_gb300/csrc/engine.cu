@@ -1961,13 +1961,20 @@ __device__ void sq_tile(const SqParams &p, const SqBlock &bk, int rb, int ks, un
                     bulk_wait_read<1>();  // plane l - 2's reduction has read this buffer
                 __syncthreads();
             }
-            for (uint32_t c = part * half; c < (part + 1) * half; c += 8) {
-                uint32_t r[8];
-                tmem_ld8(pp.tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(l * kSqCols) + c, r);
-                tmem_ld_wait();
+            // up to kSqCols / 2 columns per thread: every load before one wait
+            uint32_t r[kSqCols / 16][8];
+            const uint32_t c0 = part * half, taddr = pp.tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(l * kSqCols) + c0;
 #pragma unroll
-                for (int j = 0; j < 8; ++j) buf[(c + j) * kSqRows + 32 * quarter + lane] = __uint_as_float(r[j]);
-            }
+            for (int k = 0; k < kSqCols / 16; ++k)
+                if ((uint32_t)(8 * k) < half)
+                    tmem_ld8(taddr + 8 * k, r[k]);
+            tmem_ld_wait();
+#pragma unroll
+            for (int k = 0; k < kSqCols / 16; ++k)
+                if ((uint32_t)(8 * k) < half)
+#pragma unroll
+                    for (int j = 0; j < 8; ++j)
+                        buf[(c0 + 8 * k + j) * kSqRows + 32 * quarter + lane] = __uint_as_float(r[k][j]);
             fence_proxy_async_smem();
             __syncthreads();
             if (threadIdx.x == 0) {
@@ -2142,6 +2149,7 @@ __device__ void sq_commit(const SqParams &p, const EDesc &D, int nrow, unsigned 
         const EState &S0 = *D.st;
         s_val[0] = S0.sd + S0.dsd;
         s_val[1] = S0.sd_sq;
+        s_val[2] = s_val[0] / var2;  // the G(r) term of the new chi2
     }
     // 2. the row items
     if (threadIdx.x == 0)
@@ -2151,15 +2159,13 @@ __device__ void sq_commit(const SqParams &p, const EDesc &D, int nrow, unsigned 
         return;
     __threadfence();
     for (int k = threadIdx.x; k < nrb; k += kSqThreads) s_part[k] = __ldcg(D.sqpart + k);
-    for (int b = threadIdx.x; b < hs; b += kSqThreads) sY[b] = __ldcg(D.y + b);
     __syncthreads();
     // 3. the row blocks' shares in block order, the decision
     if (threadIdx.x == 0) {
         double dsq = 0.0;
         for (int k = 0; k < nrb; ++k) dsq += s_part[k];
-        const double sd_new = s_val[0];
         const double sq_new = s_val[1] + dsq;
-        const double chi2_new = sd_new / var2 + sq_new / var2q;
+        const double chi2_new = s_val[2] + sq_new / var2q;
         const bool reject = (chi2_new > g.chi2) && (g.u > tol);
         s_flag = reject ? 0 : 1;
         s_val[2] = chi2_new;
@@ -2191,6 +2197,7 @@ __device__ void sq_commit(const SqParams &p, const EDesc &D, int nrow, unsigned 
     }
     // 5. the accepted step: Bq -= 2 A S, h -= 2 y, coordinates
     if (accept) {
+        for (int b = threadIdx.x; b < hs; b += kSqThreads) sY[b] = __ldcg(D.y + b);
         for (int b = threadIdx.x; b < hs; b += kSqThreads) {
             const double sv = sS[b];
             if (sv != 0.0)
