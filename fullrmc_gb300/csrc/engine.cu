@@ -1502,9 +1502,18 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, 
         const unsigned nt = *s_tcount;
         const int *__restrict__ tl = D.tlist;
         int *__restrict__ cnt = D.counts;
-        for (unsigned k = threadIdx.x; k < nt; k += blockDim.x) {
-            const int e = tl[k];
-            atomicAdd(cnt + (e >> 1), (e & 1) ? 1 : -1);
+        // four entries' loads in flight before their atomics
+        for (unsigned k0 = threadIdx.x; k0 < nt; k0 += 4 * blockDim.x) {
+            int e[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const unsigned k = k0 + u * blockDim.x;
+                e[u] = k < nt ? __ldcg(tl + k) : -1;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (e[u] >= 0)
+                    atomicAdd(cnt + (e[u] >> 1), (e[u] & 1) ? 1 : -1);
         }
         double *__restrict__ Bq = D.Bq;
         if (D.hs > kChunk) {
@@ -1602,13 +1611,18 @@ __global__ void __launch_bounds__(kMaxEngineThreads, 1) k_engine_step(StepParams
         }
         __syncthreads();
     }
+    // a fused launch with an item per CTA needs no scheduler: CTA b takes
+    // item b and leaves
+    const bool one_each = FUSED && p.nitems <= (int)gridDim.x;
     for (;;) {
         if (threadIdx.x == 0) {
             // fused launches: item blockIdx.x first (the list is largest
             // first), then items gridDim.x, gridDim.x + 1, ... by claim
             unsigned long long k;
             if (FUSED)
-                k = fused_items == 0 ? blockIdx.x : gridDim.x + atomicAdd(&p.sched->claimed, 1ull);
+                k = fused_items == 0 ? blockIdx.x
+                                     : (one_each ? (unsigned long long)p.nitems
+                                                 : gridDim.x + atomicAdd(&p.sched->claimed, 1ull));
             else
                 k = atomicAdd(&p.sched->claimed, 1ull);
             s_item = k < (unsigned long long)p.nitems ? (int)k : -1;
@@ -1676,7 +1690,7 @@ __global__ void __launch_bounds__(kMaxEngineThreads, 1) k_engine_step(StepParams
         __syncthreads();
     }
     // The last CTA to leave resets the scheduler for the next launch.
-    if (threadIdx.x == 0) {
+    if (!one_each && threadIdx.x == 0) {
         __threadfence();
         const unsigned f = atomicAdd(&p.sched->finished, 1u);
         if (f == gridDim.x - 1) {
