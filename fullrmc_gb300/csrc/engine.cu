@@ -158,6 +158,7 @@ struct EDesc {
     double *sqexp;      // [nq] experimental S(Q)
     double *h;          // [hs] 2 M W (S_exp - S) of the current configuration
     double *y;          // [hs] K x of this step
+    double *gsq;        // [hs] G on the S(Q) shells of the current counts (set-up and reports)
     double *sqpart;     // [hs / kSqRows rounded up] this step's shares of x (y - h), per 128-bin row block
     double *sqv;        // [nq] S(Q) written by the evaluation kernel
     int *evl;           // [npairs][hs] this step's non-zero element-pair deltas, per pair
@@ -2309,30 +2310,67 @@ __global__ void __launch_bounds__(kSqThreads, 1) k_sq_fused(SqParams p)
 }
 
 // S(Q) of engine `id`'s current counts (StructureFactorConstraints.py:780-822
-// with scale factor 1 and no window): G_S(b) = Rq(b) sum_p pair_coef_p n_p(b)
-// - rfacq(b) in shared memory, S(q) = sum_b G_S(b) M[b][q] + 1 into sqv.
-// With commit, also sd_sq = sum_q w (S_exp - S)^2, h(b) = 2 sum_q M[b][q] w
-// (S_exp - S) and the chain's chi2 (set-up).  One CTA, fixed summation orders.
-__global__ void __launch_bounds__(512) k_sq_eval(const EDesc *desc, int id, int commit)
+// with scale factor 1 and no window), in four short launches so that the
+// FP64 work -- GB300's narrow pipe -- spreads over the SMs:
+// - k_sq_gs: G_S(b) = Rq(b) sum_p pair_coef_p n_p(b) - rfacq(b) into gsq;
+// - k_sq_sv: S(q) = sum_b G_S(b) M[b][q] + 1 into sqv, one thread per q, b in
+//   increasing order;
+// with commit (set-up), also
+// - k_sq_hv: h(b) = 2 sum_q M[b][q] w (S_exp - S), one warp per b (lanes over
+//   q, a fixed shuffle tree);
+// - k_sq_sd: sd_sq = sum_q w (S_exp - S)^2 (fixed-order lanes) and the
+//   chain's chi2.
+// Each value is formed by the same operations in the same order wherever
+// its thread runs.
+__global__ void __launch_bounds__(512) k_sq_gs(const EDesc *desc, int id)
 {
-    extern __shared__ double gs[];  // [hs]
+    const EDesc &D = desc[id];
+    for (int b = threadIdx.x; b < D.hs; b += blockDim.x) {
+        double S = 0.0;
+        for (int q = 0; q < D.npairs; ++q) S = fma(D.pc[q], (double)pair_count(D, q, b), S);
+        D.gsq[b] = fma(D.Rq[b], S, -D.rfacq[b]);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_sq_sv(const EDesc *desc, int id)
+{
+    const EDesc &D = desc[id];
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= D.nq)
+        return;
+    const int hs = D.hs, nq = D.nq;
+    const double *__restrict__ gs = D.gsq;
+    const double *__restrict__ M = D.M;
+    double a = 0.0;
+    for (int b = 0; b < hs; ++b) a = fma(__ldg(gs + b), __ldg(M + (size_t)b * nq + q), a);
+    D.sqv[q] = a + 1.0;
+}
+
+__global__ void __launch_bounds__(256) k_sq_hv(const EDesc *desc, int id)
+{
+    const EDesc &D = desc[id];
+    const int lane = threadIdx.x & 31;
+    const int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (b >= D.hs)
+        return;
+    const int nq = D.nq;
+    const double *row = D.M + (size_t)b * nq;
+    double a = 0.0;
+    for (int q = lane; q < nq; q += 32) {
+        const double w = D.wq ? D.wq[q] : 1.0;
+        a = fma(row[q], w * (D.sqexp[q] - D.sqv[q]), a);
+    }
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if (lane == 0)
+        D.h[b] = 2.0 * a;
+}
+
+__global__ void __launch_bounds__(512) k_sq_sd(const EDesc *desc, int id)
+{
     __shared__ double red[kRedLanes];
     __shared__ double cb[kChunk];
     const EDesc &D = desc[id];
-    const int hs = D.hs, nq = D.nq;
-    for (int b = threadIdx.x; b < hs; b += blockDim.x) {
-        double S = 0.0;
-        for (int q = 0; q < D.npairs; ++q) S = fma(D.pc[q], (double)pair_count(D, q, b), S);
-        gs[b] = fma(D.Rq[b], S, -D.rfacq[b]);
-    }
-    __syncthreads();
-    for (int q = threadIdx.x; q < nq; q += blockDim.x) {
-        double a = 0.0;
-        for (int b = 0; b < hs; ++b) a = fma(gs[b], D.M[(size_t)b * nq + q], a);
-        D.sqv[q] = a + 1.0;
-    }
-    if (!commit)
-        return;
+    const int nq = D.nq;
     lanes_zero(red);
     for (int c0 = 0; c0 < nq; c0 += kChunk) {
         const int cn = min(kChunk, nq - c0);
@@ -2344,18 +2382,6 @@ __global__ void __launch_bounds__(512) k_sq_eval(const EDesc *desc, int id, int 
         lanes_add_chunk(red, cb, c0, cn);
     }
     const double sdq = lanes_total(red);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    for (int b = warp; b < hs; b += nwarps) {
-        const double *row = D.M + (size_t)b * nq;
-        double a = 0.0;
-        for (int q = lane; q < nq; q += 32) {
-            const double w = D.wq ? D.wq[q] : 1.0;
-            a = fma(row[q], w * (D.sqexp[q] - D.sqv[q]), a);
-        }
-        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-        if (lane == 0)
-            D.h[b] = 2.0 * a;
-    }
     if (threadIdx.x == 0) {
         EState &S = *D.st;
         S.sd_sq = sdq;
@@ -2564,7 +2590,7 @@ static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 struct BlobLayout {
     size_t box, real, mol, counts, delta, rfac, invvol, expd, dw, pc, pi, pj, dP, pidx, tlist, R, A, Bq, Sb, Gc, fnum,
         fden, win, moves,
-        results, st, Rq, rfacq, sqexp, h, y, sqpart, sqv, evl, groups, cbox, cmol, csl, cstart, clo, chi,
+        results, st, Rq, rfacq, sqexp, h, y, gsq, sqpart, sqv, evl, groups, cbox, cmol, csl, cstart, clo, chi,
         total;
 };
 
@@ -2620,6 +2646,7 @@ static BlobLayout blob_layout(const frmc_engine_spec &sp)
     L.sqexp = take(8 * nq);
     L.h = take(8 * hq);
     L.y = take(8 * hq);
+    L.gsq = take(8 * hq);
     L.sqpart = take(sq ? 8 * (size_t)((sp.hs + 127) / 128) : 0);
     L.sqv = take(8 * nq);
     L.evl = take(sq ? 4 * (size_t)sp.npairs * hs : 0);
@@ -3121,9 +3148,13 @@ static int launch_batched(EngineSet *s, cudaStream_t st)
 
 static int launch_sq_eval(EngineSet *s, int id, int commit, cudaStream_t st)
 {
-    const int bytes = 8 * s->slots[id].d.hs;
-    FRMC_CUDA(cudaFuncSetAttribute(k_sq_eval, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-    k_sq_eval<<<1, 512, bytes, st>>>(s->ddesc, id, commit);
+    const EDesc &D = s->slots[id].d;
+    k_sq_gs<<<1, 512, 0, st>>>(s->ddesc, id);
+    k_sq_sv<<<(D.nq + 127) / 128, 128, 0, st>>>(s->ddesc, id);
+    if (commit) {
+        k_sq_hv<<<(D.hs + 7) / 8, 256, 0, st>>>(s->ddesc, id);
+        k_sq_sd<<<1, 512, 0, st>>>(s->ddesc, id);
+    }
     FRMC_CUDA(cudaGetLastError());
     return FRMC_OK;
 }
@@ -3483,6 +3514,7 @@ static int add_engine(EngineSet *s, const frmc_engine_spec &sp, int *out_id)
         D.sqexp = (double *)(b + L.sqexp);
         D.h = (double *)(b + L.h);
         D.y = (double *)(b + L.y);
+        D.gsq = (double *)(b + L.gsq);
         D.sqpart = (double *)(b + L.sqpart);
         D.sqv = (double *)(b + L.sqv);
         D.evl = (int *)(b + L.evl);

@@ -52,12 +52,15 @@ def _oracle_chi2(oracle_mod, s, intra, inter):
     return s.model.chi2_fp64(intra, inter) + sd_sq / s.sq.variance_squared
 
 
-def _run(systems, moves, steps, mode="batched", fused=1, graph=True, chunk=None, tune=None, gemm_limit=None):
+def _run(systems, moves, steps, mode="batched", fused=1, graph=True, chunk=None, tune=None, gemm_limit=None,
+         splits=None):
     from fullrmc_gb300.engine import EngineSet
     es = EngineSet(systems, move_cap=max(64, steps), tune=tune)
     es.set_mode(fused)
     if gemm_limit is not None:
         es.set_sq_gemm_limit(gemm_limit)
+    if splits is not None:
+        es.set_sq_splits(splits)
     es.init()
     for e, (a, v, u) in enumerate(moves):
         es.push_moves(e, a[:steps], v[:steps], u[:steps], 0)
@@ -145,10 +148,10 @@ def test_sq_chains_identical_solo_batched_fused_split():
 
 
 def test_sq_gemm_digits_give_the_integer_sums_exactly():
-    """The tensor-core product (fp16 digits of T times fp16 deltas, fp32
-    accumulation) yields the same integers as the exact sum over the list of
-    deltas (limit 0) and the dense integer loop (limit -1): the chains agree
-    bit for bit, fused and tile-split."""
+    """The tensor-core product (fp16 digit planes of T times fp16 deltas,
+    fp32 accumulators in tensor memory) yields the same integers as the exact
+    sum over the list of deltas (limit 0) and the dense integer loop (limit
+    -1): the chains agree bit for bit, fused and tile-split."""
     systems = _systems(3, seed=17, nmin=800, nmax=2600)
     steps = 40
     mv = _moves(systems, steps, seed=6, amp=0.5)
@@ -190,11 +193,11 @@ def test_table_shape_mismatch_is_refused():
 
 
 def test_sq_many_engines_span_several_column_blocks():
-    """More delta columns than one tile block holds (64): the product is
+    """More delta columns than one tile block holds (128): the product is
     tiled over several blocks of whole engines; every chain is still the
     same batched, split and alone."""
-    systems = _systems(28, seed=31, nmin=300, nmax=900)
-    assert sum(len(s.model.pair_i) for s in systems) > 64
+    systems = _systems(56, seed=31, nmin=300, nmax=900)
+    assert sum(len(s.model.pair_i) for s in systems) > 128
     steps = 25
     mv = _moves(systems, steps, seed=32)
     base = _run(systems, mv, steps)
@@ -207,9 +210,9 @@ def test_sq_large_group_moves_take_the_exact_sum():
     """16-atom group moves in a dense one-species system with a long r range
     (0-36 A, 3,601 bins) change more than 2^14 unit counts in one delta
     column (the per-bin changes partly cancel, so a short range stays far
-    below), beyond the tensor-core product's exact range: those columns take
-    the exact integer sum, and the chain equals the all-list chain (limit 0)
-    bit for bit."""
+    below), beyond the tensor-core product's exact range (2^13): those
+    columns take the exact integer sum, and the chain equals the all-list
+    chain (limit 0) bit for bit."""
     from fullrmc_gb300 import synthetic
     from fullrmc_gb300.engine import SQModel
     rng = np.random.default_rng(41)
@@ -260,3 +263,17 @@ def test_sq_large_group_moves_take_the_exact_sum():
     assert np.array_equal(a["res"][0].view(np.int64), b["res"][0].view(np.int64))
     assert a["state"] == b["state"] and a["terms"] == b["terms"]
     assert all(np.array_equal(x, y) for x, y in zip(a["counts"], b["counts"]))
+
+
+def test_sq_k_splits_do_not_change_the_chain():
+    """The tensor-core product splits each 128-row block's bins over K
+    splits whose fp32 partial sums are added in L2 in any order; every
+    partial sum is an exact integer, so one split, a few and as many as fill
+    the SMs give bit-identical chains, batched and alone."""
+    systems = _systems(12, seed=23, nmin=900, nmax=3000)
+    steps = 30
+    mv = _moves(systems, steps, seed=24)
+    base = _run(systems, mv, steps)
+    _same(base, _run(systems, mv, steps, splits=1))
+    _same(base, _run(systems, mv, steps, splits=3, graph=False))
+    _same(base, _run(systems, mv, steps, splits=2, mode="solo", chunk=9))
