@@ -277,3 +277,40 @@ def test_sq_k_splits_do_not_change_the_chain():
     _same(base, _run(systems, mv, steps, splits=1))
     _same(base, _run(systems, mv, steps, splits=3, graph=False))
     _same(base, _run(systems, mv, steps, splits=2, mode="solo", chunk=9))
+
+
+def test_sq_odd_small_and_largest_histograms_in_one_batch(oracle_mod):
+    """Three S(Q) tables in one batched step: 338 bins (neither K chunks of 32
+    nor row blocks of 128 divide it), 1,001 bins and 4,091 bins (32 row
+    blocks of 128, next to the 4,096-bin limit); each engine's chain replays
+    on the oracle to 1e-10 and equals the same engine stepped alone."""
+    from fullrmc_gb300 import synthetic
+    from fullrmc_gb300.hostloop import HostPDFChain
+    specs = [(900, 3.37, (0.5, 25.0, 0.02)), (1200, 10.0, (0.5, 20.0, 0.02)), (2500, 40.9, (0.5, 10.0, 0.05))]
+    systems = []
+    for k, (n, rmax, qg) in enumerate(specs):
+        rng = np.random.default_rng([61, k])
+        B = synthetic.random_box(rng, n, 0.09)
+        systems.append(synthetic.make_system(np.random.default_rng([62, k]), n, [0.6, 0.4], B, rmax,
+                                             q=synthetic.q_grid(*qg)))
+    assert [s.model.hs for s in systems] == [338, 1001, 4091]
+    steps = 40
+    mv = _moves(systems, steps, seed=63, amp=0.4)
+    res = _run(systems, mv, steps)
+    _same(res, _run(systems, mv, steps, mode="solo", graph=False))
+    for e, s in enumerate(systems):
+        chain = HostPDFChain(s, oracle_mod, oracle_mod)
+        chain.compute_data()
+        chi2 = _oracle_chi2(oracle_mod, s, *chain.data)
+        a, v, u = mv[e]
+        for k in range(steps):
+            acc = bool(res[e]["acc"][k])
+            chain.step(a[k], v[k][None, :], u[k], force=acc)
+            c_new = _oracle_chi2(oracle_mod, s, chain.last[0], chain.last[1])
+            assert abs(c_new - res[e]["chi2"][k]) <= TOL * abs(c_new), (e, k)
+            assert acc == (not (res[e]["chi2"][k] > chi2 and u[k] > 0.0)), (e, k)
+            if acc:
+                chi2 = res[e]["chi2"][k]
+        assert np.array_equal(res[e]["counts"][0].astype(np.float32), chain.data[0])
+        assert np.array_equal(res[e]["counts"][1].astype(np.float32), chain.data[1])
+        assert int(res[e]["acc"].sum()) > 0
