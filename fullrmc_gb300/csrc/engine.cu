@@ -65,6 +65,20 @@ struct EState {
     int fmt;            // touched-list format of the step: 1 = (flat << 1) | sign, 0 = flat
     double sf;          // scale factor of the current configuration (dense engines)
     double sf_prop;     // scale factor of this step's proposal (dense engines with S(Q))
+    // The next step's single-atom move as a fused step stages it while it
+    // runs: the ring entry and the moved atom's data at the end of the step.
+    // The next step uses it, instead of two dependent loads through the
+    // ring, while nx_step is its step and nx_gen the ring's generation `gen`
+    // (every write of the move ring raises gen once its data have landed).
+    unsigned gen;
+    unsigned nx_gen;
+    long long nx_step;
+    int nx_atom;
+    float nx_v[3];
+    float nx_u;
+    int nx_mol;
+    int2 nx_csl;
+    float4 nx_box, nx_real;
 };
 
 // Work scheduler of one engine set: CTAs claim items with an atomic counter;
@@ -276,6 +290,48 @@ __device__ __forceinline__ float3 to_box(const Basis &RB, float x, float y, floa
 __device__ void load_moved_group(const EDesc &D, long long step, MovedGroup &g, const EMove *staged = nullptr)
 {
     const int G = D.group;
+    if (G == 1) {
+        if (threadIdx.x == 0) {
+            // the move and the moved atom as the previous step staged them
+            // (read with the state: one load hop), else through the ring
+            const EState &S = *D.st;
+            const long long nxs = S.nx_step;
+            const unsigned nxg = S.nx_gen, gen = S.gen;
+            int a = S.nx_atom, mol = S.nx_mol;
+            float v0 = S.nx_v[0], v1 = S.nx_v[1], v2 = S.nx_v[2], u = S.nx_u;
+            float4 ob = S.nx_box, orl = S.nx_real;
+            int2 sl = S.nx_csl;
+            g.accepted = S.accepted;
+            g.sd = S.sd;
+            g.chi2 = S.chi2;
+            if (staged || nxs != step || nxg != gen) {
+                const EMove &m = staged ? *staged : D.moves[step % D.move_cap];
+                a = m.atom;
+                v0 = m.v[0]; v1 = m.v[1]; v2 = m.v[2]; u = m.u;
+                ob = D.box[a];
+                orl = D.real[a];
+                mol = D.mol[a];
+                if (D.nc > 0)
+                    sl = D.csl[a];
+            }
+            const float rx = __fadd_rn(orl.x, v0), ry = __fadd_rn(orl.y, v1), rz = __fadd_rn(orl.z, v2);
+            const float3 nw = D.bm == BM_IBC ? make_float3(rx, ry, rz) : to_box(D.RB, rx, ry, rz);
+            g.u = u;
+            g.step = step;
+            g.n = 1;
+            g.atom[0] = a;
+            g.el[0] = __float_as_int(ob.w);
+            g.mol[0] = mol;
+            g.o[0][0] = ob.x; g.o[0][1] = ob.y; g.o[0][2] = ob.z;
+            g.nw[0][0] = nw.x; g.nw[0][1] = nw.y; g.nw[0][2] = nw.z;
+            g.nr[0][0] = rx; g.nr[0][1] = ry; g.nr[0][2] = rz;
+            if (D.nc > 0) {
+                g.slot[0] = sl.x;
+                g.cell[0] = sl.y;
+            }
+        }
+        return;
+    }
     const EMove &m = staged ? *staged : D.moves[step % D.move_cap];
     if (threadIdx.x == 0) {
         g.u = m.u;
@@ -283,28 +339,6 @@ __device__ void load_moved_group(const EDesc &D, long long step, MovedGroup &g, 
         g.accepted = D.st->accepted;
         g.sd = D.st->sd;
         g.chi2 = D.st->chi2;
-    }
-    if (G == 1) {
-        if (threadIdx.x == 0) {
-            const int a = m.atom;
-            const float4 ob = D.box[a];
-            const float4 orl = D.real[a];
-            const float rx = __fadd_rn(orl.x, m.v[0]), ry = __fadd_rn(orl.y, m.v[1]), rz = __fadd_rn(orl.z, m.v[2]);
-            const float3 nw = D.bm == BM_IBC ? make_float3(rx, ry, rz) : to_box(D.RB, rx, ry, rz);
-            g.n = 1;
-            g.atom[0] = a;
-            g.el[0] = __float_as_int(ob.w);
-            g.mol[0] = D.mol[a];
-            g.o[0][0] = ob.x; g.o[0][1] = ob.y; g.o[0][2] = ob.z;
-            g.nw[0][0] = nw.x; g.nw[0][1] = nw.y; g.nw[0][2] = nw.z;
-            g.nr[0][0] = rx; g.nr[0][1] = ry; g.nr[0][2] = rz;
-            if (D.nc > 0) {
-                const int2 sl = D.csl[a];
-                g.slot[0] = sl.x;
-                g.cell[0] = sl.y;
-            }
-        }
-        return;
     }
     const EGroup &gm = D.groups[step % D.move_cap];
     const int t = threadIdx.x;
@@ -1432,6 +1466,32 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, 
         cs1 = D.cstart[threadIdx.x + 1];
     }
     load_moved_group(D, D.st->step, g, hm);
+    // the next step's move: its ring entry now, the moved atom's data after
+    // the sweep, into the state at the commit (single-atom engines whose step
+    // ends here and whose moves come from the ring); the ring's generation is
+    // read before the entry
+    __shared__ __align__(16) struct {
+        float4 box, real;
+        long long step;
+        unsigned gen;
+        int atom, mol;
+        float v[3], u;
+        int2 csl;
+    } s_next;
+    const bool stage_next = !hm && D.group == 1 && !D.sq;
+    if (stage_next && threadIdx.x == 64) {
+        const unsigned gen = ld_acquire_u32(&D.st->gen);
+        const long long s1 = __ldcg(&D.st->step) + 1;
+        const EMove *m = D.moves + s1 % D.move_cap;
+        cp_async4(&s_next.atom, &m->atom);
+        cp_async4(&s_next.v[0], &m->v[0]);
+        cp_async4(&s_next.v[1], &m->v[1]);
+        cp_async4(&s_next.v[2], &m->v[2]);
+        cp_async4(&s_next.u, &m->u);
+        cp_async_commit();
+        s_next.step = s1;
+        s_next.gen = gen;
+    }
     const int np = D.npairs;
     const int nph = np * D.hs;
     if (D.dpk) {
@@ -1478,6 +1538,20 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, 
         }
     }
     __syncthreads();
+    if (stage_next && threadIdx.x == 64) {
+        cp_async_wait_all();
+        const int a = s_next.atom;
+        if (a >= 0 && a < D.n) {
+            cp_async16(&s_next.box, D.box + a);
+            cp_async16(&s_next.real, D.real + a);
+            cp_async4(&s_next.mol, D.mol + a);
+            if (D.nc > 0)
+                cp_async8(&s_next.csl, D.csl + a);
+            cp_async_commit();
+        } else {
+            s_next.step = -1;  // an entry never pushed: nothing to stage
+        }
+    }
     mbar_wait(bar, parity, status);
     const double dsd = eval_delta<true>(D, sdP, sA, sBq, red, cb, sbs, sbin, s_nchg, coef, q.nz);
     if (D.sq) {
@@ -1548,6 +1622,27 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, 
             S.accepted = g.accepted + 1;
         }
         S.step = g.step + 1;
+    }
+    if (stage_next && threadIdx.x == 64 && s_next.step >= 0) {
+        cp_async_wait_all();
+        EState &S = *D.st;
+        float4 nb = s_next.box, nr = s_next.real;
+        if (accept && s_next.atom == g.atom[0]) {
+            // this step moved the same atom: its coordinates as just committed
+            nb = make_float4(g.nw[0][0], g.nw[0][1], g.nw[0][2], __int_as_float(g.el[0]));
+            nr = make_float4(g.nr[0][0], g.nr[0][1], g.nr[0][2], 0.0f);
+        }
+        S.nx_atom = s_next.atom;
+        S.nx_v[0] = s_next.v[0];
+        S.nx_v[1] = s_next.v[1];
+        S.nx_v[2] = s_next.v[2];
+        S.nx_u = s_next.u;
+        S.nx_mol = s_next.mol;
+        S.nx_csl = s_next.csl;
+        S.nx_box = nb;
+        S.nx_real = nr;
+        S.nx_gen = s_next.gen;
+        S.nx_step = s_next.step;
     }
 }
 
@@ -1710,8 +1805,15 @@ __global__ void k_scatter_moves(const EDesc *desc, const int *ids, const EMove *
     if (k < count) {
         const EDesc &D = desc[ids[k]];
         D.moves[D.st->step % D.move_cap] = staged[k];
+        // a move staged for this step from the ring is stale now
+        __threadfence();
+        atomicAdd(&D.st->gen, 1u);
     }
 }
+
+// A write of engine `st`'s move ring has landed (stream order): staged moves
+// read before it are stale.
+__global__ void k_bump_gen(EState *st) { atomicAdd(&st->gen, 1u); }
 
 __global__ void k_gather_results(const EDesc *desc, const int *ids, EResult *out, int count)
 {
@@ -3175,6 +3277,7 @@ static int init_engine(EngineSet *s, int id)
     FRMC_CUDA(cudaMemsetAsync(D.counts, 0, sizeof(int) * 2 * D.total, s->stream));
     FRMC_CUDA(cudaMemsetAsync(D.delta, 0, sizeof(int) * 2 * D.total, s->stream));
     FRMC_CUDA(cudaMemsetAsync(D.st, 0, sizeof(EState), s->stream));
+    FRMC_CUDA(cudaMemsetAsync(&D.st->nx_step, 0xff, sizeof(long long), s->stream));  // no staged move
     unsigned *cnt = (unsigned *)D.counts;
     FullTune tn;
     if (D.n >= 2) {
@@ -3900,6 +4003,8 @@ int frmc_engines_push_moves(void *handle, int32_t e, const int32_t *atoms, const
         done += chunk;
         pos = 0;
     }
+    k_bump_gen<<<1, 1, 0, s->stream>>>(D.st);  // after the copies: staged moves are stale
+    FRMC_CUDA(cudaGetLastError());
     FRMC_CUDA(cudaStreamSynchronize(s->stream));
     return FRMC_OK;
 }
@@ -3956,6 +4061,8 @@ int frmc_engines_push_group_moves(void *handle, int32_t e, const int32_t *atoms,
         done += chunk;
         pos = 0;
     }
+    k_bump_gen<<<1, 1, 0, s->stream>>>(D.st);  // after the copies: staged moves are stale
+    FRMC_CUDA(cudaGetLastError());
     FRMC_CUDA(cudaStreamSynchronize(s->stream));
     return FRMC_OK;
 }
@@ -4322,6 +4429,10 @@ int frmc_engines_regrid(void *handle, int32_t e)
     D.clam2 = cg.clam2;
     D.cthr2 = cg.cthr2;
     sl.cost = (cg.nc > 0 ? 4 * (long long)std::ceil(cg.sweep) : (long long)D.n) * D.group;
+    // a staged next move holds the moved atom's old cell-order slot and cell
+    k_bump_gen<<<1, 1, 0, s->stream>>>(D.st);
+    FRMC_CUDA(cudaGetLastError());
+    FRMC_CUDA(cudaStreamSynchronize(s->stream));
     s->dirty = true;  // descriptors and the work list are rebuilt before the next step
     return FRMC_OK;
 }

@@ -83,6 +83,26 @@ __device__ __forceinline__ void cp_async16(void *dst_smem, const void *src_gmem)
 
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
+// 4 or 8 bytes global -> shared (naturally aligned), through L1.
+__device__ __forceinline__ void cp_async4(void *dst_smem, const void *src_gmem)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(dst_smem)), "l"(src_gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_async8(void *dst_smem, const void *src_gmem)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_addr(dst_smem)), "l"(src_gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
 // 1-D bulk copy global -> shared (both 16-byte aligned, bytes % 16 == 0).
 // Hint: bring the line holding p into L2 (no register result, never faults
 // on a valid address).
