@@ -279,3 +279,39 @@ def test_real_data_chain_replays_on_oracle(oracle_mod):
     assert np.array_equal(res["counts"][1].astype(np.float32), chain.data[1])
     assert np.array_equal(res["coords"][0], chain.box)
     assert 0 < int(res["acc"].sum()) < steps
+
+
+def test_moves_pushed_after_a_step_replace_the_staged_ones():
+    """A single-atom step stages the next step's move (and its atom's data)
+    while it runs; pushing new moves for those steps afterwards must win.  A
+    chain whose moves for steps K.. are replaced after K steps equals a chain
+    that had the replacements from the start, batched and alone; so does one
+    whose grids are rebuilt between the two halves."""
+    from fullrmc_gb300.engine import EngineSet
+    systems = _systems(count=4, seed=21)
+    K = 30
+    first = _moves(systems, 2 * K, seed=22)
+    second = _moves(systems, 2 * K, seed=23)
+    merged = [(np.concatenate([a1[:K], a2[K:]]), np.concatenate([v1[:K], v2[K:]]), np.concatenate([u1[:K], u2[K:]]))
+              for (a1, v1, u1), (a2, v2, u2) in zip(first, second)]
+    want = _run(systems, merged, 2 * K, "batched", graph=False)
+    for engine, regrid in ((-1, False), (1, False), (-1, True)):
+        es = EngineSet(systems, move_cap=2 * K)
+        es.init()
+        for e, (a, v, u) in enumerate(first):
+            es.push_moves(e, a, v, u, 0)
+        for e in ([-1] if engine == -1 else range(len(systems))):
+            es.step(K, engine=e, graph=False)
+        for e, (a, v, u) in enumerate(second):
+            es.push_moves(e, a[K:], v[K:], u[K:], K)
+        if regrid:
+            for e in range(len(systems)):
+                es.regrid(e)
+        for e in ([-1] if engine == -1 else range(len(systems))):
+            es.step(K, engine=e, graph=False)
+        for e in range(len(systems)):
+            c2, acc, _ = es.results(e, 0, 2 * K)
+            assert np.array_equal(acc, want[e]["acc"]), (engine, regrid, e)
+            assert np.array_equal(c2.view(np.int64), want[e]["chi2"].view(np.int64)), (engine, regrid, e)
+            assert all(np.array_equal(x, y) for x, y in zip(es.counts(e), want[e]["counts"]))
+        es.close()
