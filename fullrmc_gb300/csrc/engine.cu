@@ -1260,7 +1260,7 @@ __device__ __forceinline__ float cell_gap(float a, float b, int pbc)
 // ints of scratch); returns the number of columns to sweep.  Column v of the sweep is atom
 // Bse[c] + v of the cell order, c the last cell with P[c] <= v.
 __device__ int cell_select(const EDesc &D, const MovedGroup &g, float4 lo, float4 hi, int st0, int st1, int *P,
-                           int *Bse, int *wsum)
+                           int *Bse, int *wsum, float4 lo1, float4 hi1, int st01, int st11)
 {
     float plo[3], phi[3];
 #pragma unroll
@@ -1279,7 +1279,13 @@ __device__ int cell_select(const EDesc &D, const MovedGroup &g, float4 lo, float
     int carry = 0;
     for (int c0 = 0; c0 < nc; c0 += blockDim.x) {
         const int c = c0 + (int)threadIdx.x;
-        if (c0 > 0 && c < nc) {
+        if (c0 == (int)blockDim.x) {
+            // the second round's cell, read by the caller ahead of the barrier
+            lo = lo1;
+            hi = hi1;
+            st0 = st01;
+            st1 = st11;
+        } else if (c0 > 0 && c < nc) {
             lo = D.clo[c];
             hi = D.chi[c];
             st0 = D.cstart[c];
@@ -1465,6 +1471,16 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, 
         cs0 = D.cstart[threadIdx.x];
         cs1 = D.cstart[threadIdx.x + 1];
     }
+    // and its cell of the second round (grids of up to 2 blockDim cells)
+    float4 clo1 = make_float4(0.f, 0.f, 0.f, 0.f), chi1 = clo1;
+    int cs01 = 0, cs11 = 0;
+    if ((int)(threadIdx.x + blockDim.x) < nc) {
+        const int c = threadIdx.x + blockDim.x;
+        clo1 = D.clo[c];
+        chi1 = D.chi[c];
+        cs01 = D.cstart[c];
+        cs11 = D.cstart[c + 1];
+    }
     load_moved_group(D, D.st->step, g, hm);
     // the next step's move: its ring entry now, the moved atom's data after
     // the sweep, into the state at the commit (single-atom engines whose step
@@ -1503,7 +1519,7 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, 
     for (int k = threadIdx.x; k < D.hs; k += blockDim.x) q.nz[k] = 0;
     for (int qq = threadIdx.x; qq < np; qq += blockDim.x) coef[qq] = D.pc[qq];
     __syncthreads();
-    const int ncol = nc > 0 ? cell_select(D, g, clo, chi, cs0, cs1, cP, cB, cB + kMaxCells) : D.n;
+    const int ncol = nc > 0 ? cell_select(D, g, clo, chi, cs0, cs1, cP, cB, cB + kMaxCells, clo1, chi1, cs01, cs11) : D.n;
     if (threadIdx.x == 0)
         atomicAdd(&D.st->swept, (unsigned long long)ncol);
 #define FRMC_COLUMNS(G_, C_)                                                                           \
