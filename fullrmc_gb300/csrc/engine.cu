@@ -30,7 +30,9 @@
 // Nothing spins, so the kernel cannot hang; a chain's arithmetic depends only
 // on its own data and every reduction has a fixed order, so a chain gives
 // bit-identical results alone or batched with any other chains, under any
-// tile or CTA configuration.
+// tile or CTA configuration.  Engines with a StructureFactorConstraint term
+// finish their step in a second persistent kernel (k_sq_fused, below), whose
+// items wait only for items listed before them, with bounded waits.
 #include <algorithm>
 #include <climits>
 #include <cmath>
@@ -2765,7 +2767,7 @@ static BlobLayout blob_layout(const frmc_engine_spec &sp)
     L.h = take(8 * hq);
     L.y = take(8 * hq);
     L.gsq = take(8 * hq);
-    L.sqpart = take(sq ? 8 * (size_t)((sp.hs + 127) / 128) : 0);
+    L.sqpart = take(sq ? 8 * (size_t)((sp.hs + kSqRows - 1) / kSqRows) : 0);
     L.sqv = take(8 * nq);
     L.evl = take(sq ? 4 * (size_t)sp.npairs * hs : 0);
     L.groups = take(G > 1 ? sizeof(EGroup) * (size_t)sp.move_cap : 0);
