@@ -400,7 +400,9 @@ __device__ void load_moved_group(const EDesc &D, long long step, MovedGroup &g, 
 // Commit of an accepted move: the moved atoms' coordinates, their copies in
 // cell order and their cells' bounds (one thread, as atoms of a group may
 // share a cell).
-__device__ void commit_moved_group(const EDesc &D, const MovedGroup &g)
+// cb: the bounds of atom 0's cell as cell selection read them (single-atom
+// steps with a grid), or null to read them here.
+__device__ void commit_moved_group(const EDesc &D, const MovedGroup &g, const float4 *cb = nullptr)
 {
     for (int t = threadIdx.x; t < g.n; t += blockDim.x) {
         const int a = g.atom[t];
@@ -413,7 +415,7 @@ __device__ void commit_moved_group(const EDesc &D, const MovedGroup &g)
     if (D.nc > 0 && threadIdx.x == 0) {
         for (int t = 0; t < g.n; ++t) {
             const int c = g.cell[t];
-            float4 lo = D.clo[c], hi = D.chi[c];
+            float4 lo = (cb && t == 0) ? cb[0] : D.clo[c], hi = (cb && t == 0) ? cb[1] : D.chi[c];
             lo.x = fminf(lo.x, g.nw[t][0]);
             lo.y = fminf(lo.y, g.nw[t][1]);
             lo.z = fminf(lo.z, g.nw[t][2]);
@@ -1262,7 +1264,7 @@ __device__ __forceinline__ float cell_gap(float a, float b, int pbc)
 // ints of scratch); returns the number of columns to sweep.  Column v of the sweep is atom
 // Bse[c] + v of the cell order, c the last cell with P[c] <= v.
 __device__ int cell_select(const EDesc &D, const MovedGroup &g, float4 lo, float4 hi, int st0, int st1, int *P,
-                           int *Bse, int *wsum, float4 lo1, float4 hi1, int st01, int st11)
+                           int *Bse, int *wsum, float4 lo1, float4 hi1, int st01, int st11, float4 *cb0)
 {
     float plo[3], phi[3];
 #pragma unroll
@@ -1292,6 +1294,11 @@ __device__ int cell_select(const EDesc &D, const MovedGroup &g, float4 lo, float
             hi = D.chi[c];
             st0 = D.cstart[c];
             st1 = D.cstart[c + 1];
+        }
+        if (c < nc && c == g.cell[0]) {
+            // the moved atom's cell: its bounds for the commit
+            cb0[0] = lo;
+            cb0[1] = hi;
         }
         int take = 0;
         if (c < nc && st1 > st0) {
@@ -1521,7 +1528,8 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, 
     for (int k = threadIdx.x; k < D.hs; k += blockDim.x) q.nz[k] = 0;
     for (int qq = threadIdx.x; qq < np; qq += blockDim.x) coef[qq] = D.pc[qq];
     __syncthreads();
-    const int ncol = nc > 0 ? cell_select(D, g, clo, chi, cs0, cs1, cP, cB, cB + kMaxCells, clo1, chi1, cs01, cs11) : D.n;
+    __shared__ float4 s_cb[2];  // the moved atom's cell bounds (grids), for the commit
+    const int ncol = nc > 0 ? cell_select(D, g, clo, chi, cs0, cs1, cP, cB, cB + kMaxCells, clo1, chi1, cs01, cs11, s_cb) : D.n;
     if (threadIdx.x == 0)
         atomicAdd(&D.st->swept, (unsigned long long)ncol);
 #define FRMC_COLUMNS(G_, C_)                                                                           \
@@ -1623,7 +1631,7 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, 
                 Bq[b] = fma(sA[b], sbs[k], sBq[b]);
             }
         }
-        commit_moved_group(D, g);
+        commit_moved_group(D, g, (nc > 0 && g.n == 1) ? s_cb : nullptr);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
