@@ -57,6 +57,8 @@ SIGNATURES = {
     "frmc_multiple_pairs_histograms_coords": [I32P, i64, F32P, i64, F32P, cint, I32P, I32P, i32, f32, f32, f32, i32,
                                               cint, F32P, F32P],
     "frmc_full_pairs_histograms_coords": [F32P, i64, F32P, cint, I32P, I32P, i32, f32, f32, f32, i32, F32P, F32P],
+    "frmc_group_move_delta_histograms": [I32P, i64, F32P, i64, F32P, F32P, cint, I32P, I32P, i32, f32, f32, f32, i32,
+                                         I32P, I32P],
     "frmc_multiple_pairs_histograms_dists": [I32P, i64, F32P, i64, I32P, I32P, i32, f32, f32, f32, i32, cint, F32P,
                                              F32P],
     "frmc_gr_to_sq": [F32P, F32P, i64, F32P, i64, f64, F64P],

@@ -4,9 +4,9 @@
 // context's stream, run the kernels, copy the results back and synchronise;
 // they keep no host data between calls (fullrmc mutates its coordinate array
 // between calls, PairDistributionConstraints.py:1092-1122).
+#include <algorithm>
 #include <climits>
 #include <cmath>
-#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -557,6 +557,55 @@ int frmc_multiple_pairs_histograms_coords(const int32_t *indexes, int64_t K, con
                          c->buf[BUF_ROWS].as<int>(), (int)K, allAtoms, basis_mode(B, isPBC), make_basis(B),
                          minDistance, maxDistance, bin, ne, hs, cnt, cnt + total, c->stream));
     return counts_out(c, total, nullptr, nullptr, hintra, hinter);
+}
+
+int frmc_group_move_delta_histograms(const int32_t *indexes, int64_t K, const float *boxCoords, int64_t n,
+                                     const float *newBoxCoords, const float *basis, int isPBC,
+                                     const int32_t *moleculeIndex, const int32_t *elementIndex, int32_t ne,
+                                     float minDistance, float maxDistance, float bin, int32_t hs, int32_t *dintra,
+                                     int32_t *dinter)
+{
+    int64_t total;
+    TRY(check_n(n, "boxCoords"));
+    TRY(check_hist(ne, hs, &total));
+    if (K < 0 || K > 1024)
+        return set_error(FRMC_E_ARG, "group_move_delta_histograms: %lld moved atoms (at most 1024)", (long long)K);
+    TRY(check_indexes(indexes, K, n));
+    if (total == 0)
+        return FRMC_OK;
+    memset(dintra, 0, total * 4);
+    memset(dinter, 0, total * 4);
+    if (K == 0 || n == 0)
+        return FRMC_OK;
+    const float *B = isPBC ? basis : kIdentity;
+    // the group in group order, then its atoms sorted with their positions
+    std::vector<int32_t> rows(3 * (size_t)K);
+    std::vector<std::pair<int32_t, int32_t>> order((size_t)K);
+    for (int64_t k = 0; k < K; ++k) {
+        rows[k] = indexes[k];
+        order[k] = std::make_pair(indexes[k], (int32_t)k);
+    }
+    std::sort(order.begin(), order.end());
+    for (int64_t k = 0; k < K; ++k) {
+        rows[K + k] = order[k].first;
+        rows[2 * K + k] = order[k].second;
+    }
+    LOCKED_CTX(c);
+    TRY(upload_atoms(c, boxCoords, moleculeIndex, elementIndex, n));
+    TRY(c->buf[BUF_ROWS].ensure(K * 12 + 16));
+    TRY(h2d(c->buf[BUF_ROWS].p, rows.data(), K * 12, c->stream));
+    TRY(c->buf[BUF_AUX0].ensure(K * 12 + 16));
+    TRY(h2d(c->buf[BUF_AUX0].p, newBoxCoords, K * 12, c->stream));
+    TRY(c->buf[BUF_AUX1].ensure(total * 8 + 16));
+    int *d = c->buf[BUF_AUX1].as<int>();
+    FRMC_CUDA(cudaMemsetAsync(d, 0, total * 8, c->stream));
+    const int *rw = c->buf[BUF_ROWS].as<int>();
+    TRY(launch_group_delta(c->buf[BUF_COORDS].as<float>(), c->buf[BUF_AUX0].as<float>(), c->buf[BUF_EL].as<int>(),
+                           c->buf[BUF_MOL].as<int>(), (int)n, rw, rw + K, (int)K, basis_mode(B, isPBC), make_basis(B),
+                           minDistance, maxDistance, bin, ne, hs, d, d + total, c->stream));
+    TRY(d2h(dintra, d, total * 4, c->stream));
+    TRY(d2h(dinter, d + total, total * 4, c->stream));
+    return finish(c);
 }
 
 int frmc_multiple_pairs_histograms_dists(const int32_t *indexes, int64_t K, const float *distances, int64_t n,

@@ -135,6 +135,13 @@ int launch_rows_hist(const float *coords, const int *el, const int *mol, int n, 
                      int allAtoms, int bm, const Basis &B, float minD, float maxD, float binw, int ne, int hs,
                      unsigned *intra, unsigned *inter, cudaStream_t st);
 
+// A group move's change of fullrmc's before/after-move data (M - F after
+// minus M - F before) into signed counts; rows in group order, sorted = the
+// rows in increasing order followed by their group positions (2K ints).
+int launch_group_delta(const float *coords, const float *newc, const int *el, const int *mol, int n, const int *rows,
+                       const int *sorted, int K, int bm, const Basis &B, float minD, float maxD, float binw, int ne,
+                       int hs, int *intra, int *inter, cudaStream_t st);
+
 // Histogram of given distances: dists is (n, K) row-major, column k holds the
 // distances of atom rows[k].
 int launch_dists_hist(const float *dists, int n, int K, const int *rows, const int *el, const int *mol,

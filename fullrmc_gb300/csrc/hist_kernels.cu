@@ -24,6 +24,7 @@
 //
 // Counts are uint32 and converted to the reference's float32 values by
 // k_counts_to_f32, which reproduces sequential float32 additions of 1.0.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 
@@ -374,6 +375,169 @@ __global__ void __launch_bounds__(256) k_rows_vs_all(RowsParams p)
         if ((s >= p.s_lo) & (s < p.s_hi))
             bin_count(s, p.minD, p.binw, srb[k], elj, p.hs, p.total, smol[k] == molj, p.intra, p.inter, nullptr);
     }
+}
+
+// --------------------------------------------------- a group move's delta
+// The change of fullrmc's before/after-move data for a moved group
+// (PairDistributionConstraints.py:1044-1129): after - before of M - F, with M
+// the group's rows against all atoms (allAtoms, multiple_pairs_histograms_
+// coords on the group) and F the group's own pairs (full_pairs_histograms_
+// coords on the group's coordinates), before with every atom at `coords`,
+// after with the group's atoms at `newc`.  Every pair takes the reference's
+// float32 order (pair_s, pair_bin); counts are signed.
+struct GroupDeltaParams {
+    const float *coords;  // (n, 3) box coordinates before the move
+    const float *newc;    // (K, 3) the group's box coordinates after, in group order
+    const int *el;
+    const int *mol;
+    const int *rows;      // (K) the group's atoms, group order
+    const int *sorted;    // (2K) the group's atoms in increasing order, then their group positions
+    int n, K, nchunk;
+    Basis B;
+    float s_lo, s_hi, minD, binw;
+    int ne, hs;
+    long long total;
+    int *intra, *inter;
+};
+
+__device__ __forceinline__ void delta_count(const GroupDeltaParams &p, float s, long long rowbase, int elj,
+                                            bool same_mol, int v)
+{
+    if (!((s >= p.s_lo) & (s < p.s_hi)))
+        return;
+    const long long flat = (rowbase + elj) * (long long)p.hs + pair_bin(s, p.minD, p.binw);
+    if ((unsigned long long)flat < (unsigned long long)p.total)
+        atomicAdd((same_mol ? p.intra : p.inter) + flat, v);
+}
+
+constexpr int kGroupDeltaMax = 1024;  // atoms of a group in one call at most
+
+template <int BM>
+__global__ void __launch_bounds__(256) k_group_delta(GroupDeltaParams p)
+{
+    __shared__ int sidx[kGroupDeltaMax], spos[kGroupDeltaMax];
+    __shared__ float ox[kRowChunk], oy[kRowChunk], oz[kRowChunk], nx[kRowChunk], ny[kRowChunk], nz[kRowChunk];
+    __shared__ int sa[kRowChunk], smol[kRowChunk];
+    __shared__ long long srb[kRowChunk];
+    if ((int)blockIdx.y == p.nchunk) {
+        // F: the group's own pairs (positions q < r), at [el(q)][el(r)]:
+        // + before, - after
+        const long long npair = (long long)p.K * (p.K - 1) / 2;
+        for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < npair;
+             t += (long long)gridDim.x * blockDim.x) {
+            int r = 1;
+            long long q = t;
+            while (q >= r) {
+                q -= r;
+                ++r;
+            }
+            const int a = p.rows[q], b = p.rows[r];
+            const long long rb = (long long)p.el[a] * p.ne;
+            const bool same = p.mol[a] == p.mol[b];
+            const float s0 = pair_s<BM>(p.coords[3 * (long long)a], p.coords[3 * (long long)a + 1],
+                                        p.coords[3 * (long long)a + 2], p.coords[3 * (long long)b],
+                                        p.coords[3 * (long long)b + 1], p.coords[3 * (long long)b + 2], p.B);
+            const float s1 = pair_s<BM>(p.newc[3 * q], p.newc[3 * q + 1], p.newc[3 * q + 2], p.newc[3 * (long long)r],
+                                        p.newc[3 * (long long)r + 1], p.newc[3 * (long long)r + 2], p.B);
+            delta_count(p, s0, rb, p.el[b], same, 1);
+            delta_count(p, s1, rb, p.el[b], same, -1);
+        }
+        return;
+    }
+    // M: the group's rows of this chunk against every column j != row atom,
+    // - before, + after (column j after the move: its new position when it is
+    // in the group)
+    for (int k = threadIdx.x; k < p.K; k += blockDim.x) {
+        sidx[k] = p.sorted[k];
+        spos[k] = p.sorted[p.K + k];
+    }
+    const int k0 = blockIdx.y * kRowChunk;
+    const int kc = min(kRowChunk, p.K - k0);
+    for (int k = threadIdx.x; k < kc; k += blockDim.x) {
+        const int a = p.rows[k0 + k];
+        sa[k] = a;
+        ox[k] = p.coords[3 * (long long)a];
+        oy[k] = p.coords[3 * (long long)a + 1];
+        oz[k] = p.coords[3 * (long long)a + 2];
+        nx[k] = p.newc[3 * (long long)(k0 + k)];
+        ny[k] = p.newc[3 * (long long)(k0 + k) + 1];
+        nz[k] = p.newc[3 * (long long)(k0 + k) + 2];
+        smol[k] = p.mol[a];
+        srb[k] = (long long)p.el[a] * p.ne;
+    }
+    __syncthreads();
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= p.n)
+        return;
+    const float cx = p.coords[3 * (long long)j], cy = p.coords[3 * (long long)j + 1],
+                cz = p.coords[3 * (long long)j + 2];
+    float ax = cx, ay = cy, az = cz;
+    {
+        int lo = 0, hi = p.K;  // first sorted entry >= j
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (sidx[mid] < j)
+                lo = mid + 1;
+            else
+                hi = mid;
+        }
+        if (lo < p.K && sidx[lo] == j) {
+            const int m = spos[lo];
+            ax = p.newc[3 * (long long)m];
+            ay = p.newc[3 * (long long)m + 1];
+            az = p.newc[3 * (long long)m + 2];
+        }
+    }
+    const int elj = p.el[j], molj = p.mol[j];
+    for (int k = 0; k < kc; ++k) {
+        if (j == sa[k])
+            continue;
+        const bool same = smol[k] == molj;
+        delta_count(p, pair_s<BM>(ox[k], oy[k], oz[k], cx, cy, cz, p.B), srb[k], elj, same, -1);
+        delta_count(p, pair_s<BM>(nx[k], ny[k], nz[k], ax, ay, az, p.B), srb[k], elj, same, 1);
+    }
+}
+
+int launch_group_delta(const float *coords, const float *newc, const int *el, const int *mol, int n, const int *rows,
+                       const int *sorted, int K, int bm, const Basis &B, float minD, float maxD, float binw, int ne,
+                       int hs, int *intra, int *inter, cudaStream_t st)
+{
+    if (K <= 0 || n <= 0)
+        return FRMC_OK;
+    if (K > kGroupDeltaMax)
+        return set_error(FRMC_E_ARG, "a group move of %d atoms (at most %d)", K, kGroupDeltaMax);
+    GroupDeltaParams p;
+    p.coords = coords;
+    p.newc = newc;
+    p.el = el;
+    p.mol = mol;
+    p.rows = rows;
+    p.sorted = sorted;
+    p.n = n;
+    p.K = K;
+    p.nchunk = (K + kRowChunk - 1) / kRowChunk;
+    p.B = B;
+    sq_limits(minD, maxD, &p.s_lo, &p.s_hi);
+    p.minD = minD;
+    p.binw = binw;
+    p.ne = ne;
+    p.hs = hs;
+    p.total = (long long)ne * ne * hs;
+    p.intra = intra;
+    p.inter = inter;
+    // blocks (column tile, row chunk) for M, and one more row of blocks for F
+    const long long npair = (long long)K * (K - 1) / 2;
+    const long long gx = std::max<long long>((n + 255) / 256, std::min<long long>((npair + 255) / 256, 4096));
+    dim3 grid((unsigned)gx, (unsigned)(p.nchunk + 1));
+    switch (bm) {
+    case BM_IBC: k_group_delta<BM_IBC><<<grid, 256, 0, st>>>(p); break;
+    case BM_DIAG: k_group_delta<BM_DIAG><<<grid, 256, 0, st>>>(p); break;
+    case BM_XYTRI: k_group_delta<BM_XYTRI><<<grid, 256, 0, st>>>(p); break;
+    case BM_LOWER: k_group_delta<BM_LOWER><<<grid, 256, 0, st>>>(p); break;
+    default: k_group_delta<BM_GENERAL><<<grid, 256, 0, st>>>(p); break;
+    }
+    FRMC_CUDA(cudaGetLastError());
+    return FRMC_OK;
 }
 
 // ------------------------------------------------------------ given distances

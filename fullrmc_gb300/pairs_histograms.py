@@ -95,6 +95,42 @@ def multiple_pairs_histograms_coords(indexes, boxCoords, basis, isPBC, moleculeI
     return hintra, hinter
 
 
+def group_move_delta_histograms(indexes, boxCoords, newBoxCoords, basis, isPBC, moleculeIndex, elementIndex,
+                                numberOfElements, minDistance, maxDistance, bin, histSize):
+    """The change of a PairDistributionConstraint's data for moving the atoms
+    ``indexes`` from their rows of ``boxCoords`` to ``newBoxCoords`` (one row
+    per index, same order), in one device launch: (M - F) after minus (M - F)
+    before, M = multiple_pairs_histograms_coords(indexes, ..., allAtoms=True)
+    and F = full_pairs_histograms_coords on the group alone, which is what
+    ``compute_before_move`` and ``compute_after_move`` subtract and add
+    (``Constraints/PairDistributionConstraints.py:1044-1129``).  Returns
+    (dintra, dinter), int32 (ne, ne, hs), equal to the differences of the four
+    reference histograms.  An extension of this module (at most 1024 moved
+    atoms); fullrmc's constraints keep calling the reference functions."""
+    idx = A.array("indexes", indexes, np.int32, 1)
+    c = A.array("boxCoords", boxCoords, np.float32, 2)
+    nc = A.array("newBoxCoords", newBoxCoords, np.float32, 2)
+    B = A.array("basis", basis, np.float32, 2)
+    isPBC = A.bint(isPBC)
+    mol = A.array("moleculeIndex", moleculeIndex, np.int32, 1)
+    el = A.array("elementIndex", elementIndex, np.int32, 1)
+    ne, hs = _hist_shape(numberOfElements, histSize)
+    minDistance, maxDistance, bin = (A.float32("minDistance", minDistance), A.float32("maxDistance", maxDistance),
+                                     A.float32("bin", bin))
+    n = c.shape[0]
+    A.need_len("moleculeIndex", mol, n)
+    A.need_len("elementIndex", el, n)
+    if nc.shape != (idx.shape[0], 3):
+        raise ValueError("newBoxCoords must be (%d, 3), one row per index" % idx.shape[0])
+    dintra = np.zeros((ne, ne, hs), dtype=np.int32)
+    dinter = np.zeros((ne, ne, hs), dtype=np.int32)
+    if idx.shape[0] == 0 or n == 0 or dintra.size == 0:
+        return dintra, dinter
+    call("frmc_group_move_delta_histograms", ptr(idx, I32P), idx.shape[0], ptr(c), n, ptr(nc), ptr(B), int(isPBC),
+         ptr(mol, I32P), ptr(el, I32P), ne, minDistance, maxDistance, bin, hs, ptr(dintra, I32P), ptr(dinter, I32P))
+    return dintra, dinter
+
+
 def multiple_pairs_histograms_dists(indexes, distances, moleculeIndex, elementIndex, numberOfElements,
                                     minDistance, maxDistance, bin, histSize, allAtoms=True, ncores=1):
     """Histograms from a (n, k) distance matrix whose column i belongs to atom

@@ -142,6 +142,22 @@ int frmc_shape_function(const float *boxCoords, int64_t n, const float *basis, i
                         const double *rValues, int32_t nr, double *Gr, double *Sq, double *Gshape);
 /* pairs_histograms.pyx:225-281 multiple_pairs_histograms_dists: distances is
  * (n, K) row-major, column k belongs to atom indexes[k]. */
+/* The change of fullrmc's before/after-move data for one group move, in one
+ * launch: (M - F) after minus (M - F) before, where M is
+ * multiple_pairs_histograms_coords(indexes, ..., allAtoms=True) and F is
+ * full_pairs_histograms_coords on the group's own coordinates
+ * (PairDistributionConstraints.py:1044-1129, compute_before_move and
+ * compute_after_move).  boxCoords (n, 3) are all atoms before the move,
+ * newBoxCoords (K, 3) the group's atoms after it, in the order of indexes
+ * (at most 1024).  dintra / dinter (ne, ne, hs) int32 receive signed counts;
+ * every pair takes the reference's float32 order, so the counts equal the
+ * differences of the four reference histograms exactly.  An extension of the
+ * module, not a reference export. */
+int frmc_group_move_delta_histograms(const int32_t *indexes, int64_t K, const float *boxCoords, int64_t n,
+                                     const float *newBoxCoords, const float *basis, int isPBC,
+                                     const int32_t *moleculeIndex, const int32_t *elementIndex, int32_t ne,
+                                     float minDistance, float maxDistance, float bin, int32_t hs, int32_t *dintra,
+                                     int32_t *dinter);
 int frmc_multiple_pairs_histograms_dists(const int32_t *indexes, int64_t K, const float *distances, int64_t n,
                                          const int32_t *moleculeIndex, const int32_t *elementIndex, int32_t ne,
                                          float minDistance, float maxDistance, float bin, int32_t hs, int allAtoms,
