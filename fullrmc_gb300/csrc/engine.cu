@@ -1711,6 +1711,11 @@ __global__ void __launch_bounds__(kMaxEngineThreads, 1) k_engine_step(StepParams
     __shared__ unsigned s_tcount;
     __shared__ int s_last, s_flag, s_item;
     __shared__ __align__(8) uint64_t s_bar;
+    // fused items read their descriptor from this copy: the sweep streams the
+    // engine's columns through L1, which would otherwise evict the descriptor
+    // and turn every later field read into an L2 round trip
+    __shared__ __align__(16) EDesc s_desc;
+    static_assert(sizeof(EDesc) % 8 == 0, "the descriptor is copied in 8-byte words");
     extern __shared__ __align__(16) int sdP[];
     (void)sdP;
     uint32_t fused_items = 0;
@@ -1751,6 +1756,13 @@ __global__ void __launch_bounds__(kMaxEngineThreads, 1) k_engine_step(StepParams
         }
         __syncthreads();
         const int it = s_item;
+        if (FUSED && it >= 0) {
+            // the previous item's last reads of s_desc came before the
+            // barrier that ended it
+            const long long *src = reinterpret_cast<const long long *>(p.fdesc + it);
+            long long *dst = reinterpret_cast<long long *>(&s_desc);
+            for (int k = threadIdx.x; k < (int)(sizeof(EDesc) / 8); k += blockDim.x) dst[k] = src[k];
+        }
         __syncthreads();
         if (it < 0)
             break;
@@ -1760,7 +1772,7 @@ __global__ void __launch_bounds__(kMaxEngineThreads, 1) k_engine_step(StepParams
             warm_item(p, (long long)it + gridDim.x);
         if (FUSED) {
             const int hp = p.hmoves ? p.fpos[it] : 0;
-            engine_fused(D, sdP, sA, sBq, &s_bar, fused_items & 1u, &p.sched->status, red, cb, sbs, sbin, &s_nchg,
+            engine_fused(s_desc, sdP, sA, sBq, &s_bar, fused_items & 1u, &p.sched->status, red, cb, sbs, sbin, &s_nchg,
                          coef, &s_flag, &s_tcount, s_group, cq, p.hmoves ? p.hmoves + hp : nullptr,
                          p.hres ? p.hres + hp : nullptr);
             ++fused_items;
