@@ -1155,6 +1155,9 @@ __device__ void finish_engine(const EDesc &D, const MovedGroup &g, double *red, 
 // per thread, entry k of thread t at [k * blockDim + t] (conflict-free).
 constexpr int kColQueue = 8;
 constexpr int kMaxEngineThreads = 512;  // CTA size limit of the step kernels (128 registers per thread)
+// Touched-list entries per thread of the one-CTA step read ahead of the
+// decision (a single-atom move touches at most 2 n + 8 oriented bins).
+constexpr int kTouchAhead = 8;
 // The one-CTA step keeps the column grid's prefix and bases, the warps'
 // packed queue lists and the element-pair index table in the evaluation
 // scratch cb until the evaluation: ints at [0, kCellInts), the lists, then
@@ -1590,6 +1593,16 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, 
         }
         return;
     }
+    // the touched list's first kTouchAhead entries per thread are read (an L2
+    // round trip) while thread 0 decides
+    const unsigned nt = *s_tcount;
+    const int *__restrict__ tl = D.tlist;
+    int ta[kTouchAhead];
+#pragma unroll
+    for (int u = 0; u < kTouchAhead; ++u) {
+        const unsigned k = threadIdx.x + u * blockDim.x;
+        ta[u] = k < nt ? __ldcg(tl + k) : -1;
+    }
     // the state and the move's uniform number were read at set-up
     const double sd_new = g.sd + dsd;
     const double chi2_new = sd_new / D.var2;
@@ -1600,11 +1613,13 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, 
     __syncthreads();
     const bool accept = *s_flag != 0;
     if (accept) {
-        const unsigned nt = *s_tcount;
-        const int *__restrict__ tl = D.tlist;
         int *__restrict__ cnt = D.counts;
-        // four entries' loads in flight before their atomics
-        for (unsigned k0 = threadIdx.x; k0 < nt; k0 += 4 * blockDim.x) {
+#pragma unroll
+        for (int u = 0; u < kTouchAhead; ++u)
+            if (ta[u] >= 0)
+                atomicAdd(cnt + (ta[u] >> 1), (ta[u] & 1) ? 1 : -1);
+        // the rest (group moves), four entries' loads in flight before their atomics
+        for (unsigned k0 = threadIdx.x + kTouchAhead * blockDim.x; k0 < nt; k0 += 4 * blockDim.x) {
             int e[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
