@@ -1072,9 +1072,10 @@ __device__ void finish_engine(const EDesc &D, const MovedGroup &g, double *red, 
         return;
     }
     const EState &S0 = *D.st;
-    const double sd_new = D.dense ? sd_dense : S0.sd + dsd;
-    const double chi2_new = sd_new / D.var2;
+    double sd_new = 0.0, chi2_new = 0.0;  // thread 0's
     if (threadIdx.x == 0) {
+        sd_new = D.dense ? sd_dense : S0.sd + dsd;
+        chi2_new = sd_new / D.var2;
         const EMove &m = D.moves[S0.step % D.move_cap];
         const bool reject = (chi2_new > S0.chi2) && (m.u > D.tol);
         *s_flag = reject ? 0 : 1;
@@ -1603,10 +1604,12 @@ __device__ void engine_fused(const EDesc &D, int *sdP, double *sA, double *sBq, 
         const unsigned k = threadIdx.x + u * blockDim.x;
         ta[u] = k < nt ? __ldcg(tl + k) : -1;
     }
-    // the state and the move's uniform number were read at set-up
-    const double sd_new = g.sd + dsd;
-    const double chi2_new = sd_new / D.var2;
+    // the state and the move's uniform number were read at set-up; thread 0
+    // alone forms the new chi2 (FP64 division) and decides
+    double sd_new = 0.0, chi2_new = 0.0;
     if (threadIdx.x == 0) {
+        sd_new = g.sd + dsd;
+        chi2_new = sd_new / D.var2;
         const bool reject = (chi2_new > g.chi2) && (g.u > D.tol);
         *s_flag = reject ? 0 : 1;
     }
