@@ -281,10 +281,10 @@ int frmc_dev_multiple_hist_counts(const int32_t *indexes, int64_t K, const float
  * loading the library holds until exit: 2*ne*ne*hs above 1048576 returns
  * FRMC_E_ARG, and so does n above INT_MAX / 4 (the limit of
  * frmc_dev_full_hist_counts).  The first call on a device is its set-up: it
- * resolves that array's device address, so make it before any stream capture
- * begins.  All calls share the array, so calls that overlap on the GPU (other
- * streams, other threads) race.  Every call copies its status word back and
- * synchronises `stream` before returning. */
+ * resolves that array's device address.  All calls share the array, so calls
+ * that overlap on the GPU (other streams, other threads) race.  Every call
+ * copies its status word back and synchronises `stream` before returning, so
+ * the call is synchronous and cannot be recorded into a CUDA graph. */
 int frmc_dev_full_pairs_histograms_noalloc(const void *atoms4, const int32_t *moleculeIndex, int64_t n,
                                            const float *basis_host, int isPBC, int32_t ne, float minDistance,
                                            float maxDistance, float bin, int32_t hs, float *hintra, float *hinter,
