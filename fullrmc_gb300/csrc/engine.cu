@@ -878,6 +878,7 @@ __device__ double eval_delta(const EDesc &Dg, int *dP, const double *Ab, const d
             const double a = A[b];
             const double bq = Bq[b];
             double S = 0.0;
+            bool wide_v = false;  // a delta beyond the table's -4..4 (one CTA's shared deltas)
 #pragma unroll
             for (int q = 0; q < kMaxP; ++q) {
                 if (q >= np)
@@ -895,7 +896,29 @@ __device__ double eval_delta(const EDesc &Dg, int *dP, const double *Ab, const d
                         if (v > Dg.sq_gemm_max || v < -Dg.sq_gemm_max)
                             s_wide = (v > 32767 || v < -32768 || Dg.sq_gemm_max < 0) ? 2 : max(s_wide, 1);
                     }
-                    S += (unsigned)(v + 4) <= 8u ? tabv[q * 9 + v + 4] : coef[q] * (double)v;
+                    if (SMEM) {
+                        // the table only: the product below would otherwise be
+                        // formed for every delta and discarded
+                        if ((unsigned)(v + 4) <= 8u)
+                            S += tabv[q * 9 + v + 4];
+                        else
+                            wide_v = true;
+                    } else {
+                        S += (unsigned)(v + 4) <= 8u ? tabv[q * 9 + v + 4] : coef[q] * (double)v;
+                    }
+                }
+            }
+            if (SMEM && __any_sync(__activemask(), wide_v) && wide_v) {
+                // a rare delta beyond -4..4: the sum again, in the same order
+                // (the shared deltas are still in place)
+                S = 0.0;
+#pragma unroll
+                for (int q = 0; q < kMaxP; ++q) {
+                    if (q >= np)
+                        break;
+                    const int v = delta_at(q, b);
+                    if (v)
+                        S += (unsigned)(v + 4) <= 8u ? tabv[q * 9 + v + 4] : coef[q] * (double)v;
                 }
             }
             for (int q = kMaxP; q < np; ++q) {

@@ -315,3 +315,46 @@ def test_moves_pushed_after_a_step_replace_the_staged_ones():
             assert np.array_equal(c2.view(np.int64), want[e]["chi2"].view(np.int64)), (engine, regrid, e)
             assert all(np.array_equal(x, y) for x, y in zip(es.counts(e), want[e]["counts"]))
         es.close()
+
+
+def test_lattice_deltas_beyond_four_agree_and_replay(oracle_mod):
+    """A simple cubic lattice of one element: an atom moved off its site
+    leaves six neighbours at one distance, twelve at the next, so its
+    element-pair deltas reach -6 and -12 in one bin, beyond the evaluation's
+    -4..4 table.  One-CTA and tile-split steps give bit-identical chains, and
+    the chain replays on the oracle."""
+    from fullrmc_gb300 import synthetic
+    from fullrmc_gb300.engine import EngineSet
+    from fullrmc_gb300.hostloop import HostPDFChain
+    m, a = 12, 2.2
+    L = m * a
+    s = synthetic.make_system(np.random.default_rng(17), m ** 3, [1.0], np.diag([L, L, L]), 10.0)
+    g = np.stack(np.meshgrid(np.arange(m), np.arange(m), np.arange(m), indexing="ij"), -1).reshape(-1, 3)
+    s.real_coords = (g * a + 0.1).astype(np.float32)
+    s.box_coords = synthetic.transform_f32(s.rbasis, s.real_coords)
+    systems = [s]
+    steps = 60
+    mv = _moves(systems, steps, seed=8, amp=0.3)
+    out = []
+    for fused in (1, 0):
+        es = EngineSet(systems, move_cap=64)
+        es.set_mode(fused)
+        es.init()
+        a_, v_, u_ = mv[0]
+        es.push_moves(0, a_, v_, u_, 0)
+        es.step(steps, graph=False)
+        out.append([dict(zip(("chi2", "acc", "atoms"), es.results(0, 0, steps)), state=es.state(0),
+                         counts=es.counts(0), coords=es.coords(0))])
+        es.close()
+    _same(out[0], out[1])
+    res = out[0][0]
+    chain = HostPDFChain(s, oracle_mod, oracle_mod)
+    chain.compute_data()
+    a_, v_, u_ = mv[0]
+    for k in range(steps):
+        acc = bool(res["acc"][k])
+        chain.step(a_[k], v_[k][None, :], u_[k], force=acc)
+        c_new = s.model.chi2_fp64(chain.last[0], chain.last[1])
+        assert abs(c_new - res["chi2"][k]) <= 1e-10 * abs(c_new), k
+    assert np.array_equal(res["counts"][0].astype(np.float32), chain.data[0])
+    assert np.array_equal(res["counts"][1].astype(np.float32), chain.data[1])
