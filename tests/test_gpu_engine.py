@@ -358,3 +358,42 @@ def test_lattice_deltas_beyond_four_agree_and_replay(oracle_mod):
         assert abs(c_new - res["chi2"][k]) <= 1e-10 * abs(c_new), k
     assert np.array_equal(res["counts"][0].astype(np.float32), chain.data[0])
     assert np.array_equal(res["counts"][1].astype(np.float32), chain.data[1])
+
+
+def test_bins_past_the_histogram_land_in_the_next_row(oracle_mod):
+    """maxDistance 40 bins beyond minDistance + hs * bin: a pair in one of
+    those bins is counted in bins 0.. of the next oriented row, as the
+    reference's unchecked index does (and dropped past the last row).  The
+    element-pair deltas follow the same rows; one-CTA and tile-split steps
+    agree bit for bit and the chain replays on the oracle."""
+    from fullrmc_gb300.engine import EngineSet
+    from fullrmc_gb300.hostloop import HostPDFChain
+    systems = _systems(count=2, seed=29, nmin=900, nmax=1600)
+    for s in systems:
+        m = s.model
+        m.maxDistance = np.float32(m.minDistance + np.float32(m.hs + 40) * m.bin)
+    steps = 60
+    mv = _moves(systems, steps, seed=10, amp=0.4)
+    out = []
+    for fused in (1, 0):
+        es = EngineSet(systems, move_cap=64)
+        es.set_mode(fused)
+        es.init()
+        for e, (a_, v_, u_) in enumerate(mv):
+            es.push_moves(e, a_, v_, u_, 0)
+        es.step(steps, graph=False)
+        out.append([dict(zip(("chi2", "acc", "atoms"), es.results(e, 0, steps)), state=es.state(e),
+                         counts=es.counts(e), coords=es.coords(e)) for e in range(len(systems))])
+        es.close()
+    _same(out[0], out[1])
+    for e, s in enumerate(systems):
+        res = out[0][e]
+        chain = HostPDFChain(s, oracle_mod, oracle_mod)
+        chain.compute_data()
+        a_, v_, u_ = mv[e]
+        for k in range(steps):
+            chain.step(a_[k], v_[k][None, :], u_[k], force=bool(res["acc"][k]))
+            c_new = s.model.chi2_fp64(chain.last[0], chain.last[1])
+            assert abs(c_new - res["chi2"][k]) <= 1e-10 * abs(c_new), k
+        assert np.array_equal(res["counts"][0].astype(np.float32), chain.data[0])
+        assert np.array_equal(res["counts"][1].astype(np.float32), chain.data[1])
