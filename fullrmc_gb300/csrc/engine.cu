@@ -557,8 +557,8 @@ __device__ void item_delta(const EDesc &Dg, int tile, const MovedGroup &g, int t
 
 // FP64 reductions with a fixed order that does not depend on the CTA size:
 // bin b's contribution c(b) is computed by any thread into shared memory,
-// then lane L (0..255) sums the contributions of bins b = L (mod 256) in
-// increasing order and a fixed binary tree combines the 256 lanes.
+// then lane L (0 .. kRedLanes - 1) sums the contributions of bins b = L (mod
+// kRedLanes) in increasing order and a fixed binary tree combines the lanes.
 constexpr int kChunk = 2048;    // bins per shared-memory chunk
 
 __device__ void lanes_zero(double *red)
@@ -754,7 +754,7 @@ constexpr int kSqMaxL1 = 1 << 13;
 // chunk, in increasing bin order (sbin[k]); the FP64 work then runs on the
 // list only, so each warp-level FP64 instruction -- the FP64 pipe is narrow
 // on this GPU -- serves up to 32 changed bins.  Lane L of the fixed-order
-// reduction sums the list entries k = L (mod 256) in increasing k.  For
+// reduction sums the list entries k = L (mod kRedLanes) in increasing k.  For
 // hs <= kChunk the list, its -2 S values (sbs[k]) and its length (*s_nchg)
 // stay in shared memory for the commit; larger histograms, and engines with
 // an S(Q) term, also keep S in the global Sb (zero for unchanged bins).
