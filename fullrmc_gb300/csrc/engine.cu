@@ -2250,11 +2250,14 @@ __device__ void sq_row_item(const SqParams &p, const EDesc &D, int rb0, int rbn,
     __threadfence();
     // every load of the bin is issued before any is used
     float *zb = D.Zf + (size_t)(b / kSqRows) * zrb + (b % kSqRows);
+    // an element pair without a non-zero delta this step (mode 0) has z = 0 in
+    // every bin and nothing to clear: it is skipped (adding its +-0 product
+    // would leave y unchanged, y being +0 or non-zero)
     float f[kMaxP][kSqLimbs];
     long long zi[kMaxP];
 #pragma unroll
     for (int q = 0; q < kMaxP; ++q) {
-        const bool on = row && q < np, tc = on && s_mode[q] >= 0;
+        const bool on = row && q < np && s_mode[q] != 0, tc = on && s_mode[q] >= 0;
 #pragma unroll
         for (int l = 0; l < kSqLimbs; ++l) f[q][l] = tc ? __ldcg(zb + l * zplane + q * kSqRows) : 0.0f;
         zi[q] = (on && !tc) ? __ldcg(D.Zi + (size_t)q * hsp + b) : 0ll;
@@ -2264,6 +2267,8 @@ __device__ void sq_row_item(const SqParams &p, const EDesc &D, int rb0, int rbn,
     for (int q = 0; q < kMaxP; ++q) {
         if (q >= np)
             break;
+        if (s_mode[q] == 0)
+            continue;
         long long z = zi[q];
         if (s_mode[q] >= 0) {
             // fp32 -> int32 is exact (|digit product| <= 2^24); planes combine in int64
@@ -2282,6 +2287,8 @@ __device__ void sq_row_item(const SqParams &p, const EDesc &D, int rb0, int rbn,
             part = (rq * sv) * (y - hb);
         // the bin's deltas, delta columns and digit products are spent
         for (int q = 0; q < np; ++q) {
+            if (s_mode[q] == 0)
+                continue;
             D.dP[q * hs + b] = 0;
             D.X[q * D.xld + b] = __float2half_rn(0.0f);
 #pragma unroll
