@@ -270,6 +270,9 @@ struct StepParams {
     const EMove *hmoves;
     EResult *hres;
     const int *fpos;
+    // one-CTA launches with one item per CTA: per item, the SM that ran it
+    // (bits 48..63) and its CTA's time on the item in ns, or null
+    unsigned long long *place;
 };
 
 constexpr int kRedLanes = 64;
@@ -1812,12 +1815,20 @@ __global__ void __launch_bounds__(kMaxEngineThreads, 1) k_engine_step(StepParams
         if (FUSED && fused_items == 0 && threadIdx.x == 32)
             warm_item(p, (long long)it + gridDim.x);
         if (FUSED) {
+            __shared__ unsigned long long s_titem;  // the item's start (placement record)
+            if (p.place && threadIdx.x == 0)
+                s_titem = global_ns();
             const int hp = p.hmoves ? p.fpos[it] : 0;
             engine_fused(s_desc, sdP, sA, sBq, &s_bar, fused_items & 1u, &p.sched->status, red, cb, sbs, sbin, &s_nchg,
                          coef, &s_flag, &s_tcount, s_group, cq, p.hmoves ? p.hmoves + hp : nullptr,
                          p.hres ? p.hres + hp : nullptr);
             ++fused_items;
             __syncthreads();
+            if (p.place && threadIdx.x == 0) {
+                unsigned sm;
+                asm volatile("mov.u32 %0, %%smid;" : "=r"(sm));
+                p.place[it] = ((unsigned long long)sm << 48) | ((global_ns() - s_titem) & 0xffffffffffffull);
+            }
             continue;
         }
         if (!FUSED && p.eval_only) {
@@ -2771,6 +2782,16 @@ struct EngineSet {
     cudaGraphExec_t host_graph[2] = {nullptr, nullptr};  // step_host per slot: copy in, scatter,
     int host_graph_E[2] = {0, 0};                        // step, gather, copy out
     bool dirty = true;
+    // Measured placement (frmc_engines_place): the one-CTA batched launch
+    // assigns CTA b to an SM the same way every time for a given grid and
+    // CTA shape, so recorded steps show which CTAs hold an SM alone and which
+    // share one; the work list then gives the lone CTAs the engines that
+    // took longest and pairs the rest longest with shortest.
+    unsigned long long *place_dev = nullptr;
+    int place_cap = 0;
+    bool place_rec = false;             // record in the next one-CTA launches
+    std::vector<int> place_order;       // engine id per fused item, or empty
+    long long place_key = -1;           // the launch shape the order was measured for
 };
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -2957,6 +2978,14 @@ static SqEng sq_eng(const EDesc &D, int lc)
 }
 
 // Rebuild the work list over live engines and upload descriptors.
+// The launch shape a measured placement belongs to: the one-CTA items, the
+// CTA size, CTAs per SM and the dynamic shared memory of the launch.
+static long long place_key(const EngineSet *s, int nfused)
+{
+    return (((long long)nfused * 1031 + s->threads) * 17 + s->ctas_per_sm) * 4194301 +
+           fused_dyn_bytes(s->fused_dp_ints, s->fused_bins, s->threads);
+}
+
 static int refresh(EngineSet *s)
 {
     if (!s->dirty)
@@ -3002,6 +3031,16 @@ static int refresh(EngineSet *s)
         if (s->ctas_per_sm > 1 && (int)fused_ids.size() > wave &&
             (long long)fused_ids.size() <= (long long)wave * s->ctas_per_sm)
             std::reverse(fused_ids.begin() + wave, fused_ids.end());
+    }
+    // a measured placement of the same engines and launch shape replaces it
+    if (!s->place_order.empty()) {
+        std::vector<int> a = fused_ids, b = s->place_order;
+        std::sort(a.begin(), a.end());
+        std::sort(b.begin(), b.end());
+        if (a == b && s->place_key == place_key(s, (int)fused_ids.size()))
+            fused_ids = s->place_order;
+        else
+            s->place_order.clear();
     }
     s->fused_item.assign(nslots, -1);
     for (int id : fused_ids) {
@@ -3279,7 +3318,9 @@ static int launch_items(EngineSet *s, const int2 *items, int count, int eval_onl
     const long long first = items - (s->items + s->nsolo);
     const EDesc *fd = fused ? s->fdesc + first : nullptr;
     StepParams p{s->ddesc, fd, items, count, s->tile, eval_only, fused ? s->fused_dp_ints : 0,
-                 fused ? s->fused_bins : 0, s->sched, nullptr, nullptr, nullptr};
+                 fused ? s->fused_bins : 0, s->sched, nullptr, nullptr, nullptr, nullptr};
+    if (fused && s->place_rec && count <= grid && first == 0 && count <= s->place_cap)
+        p.place = s->place_dev;
     if (fused && hmoves) {
         p.hmoves = hmoves;
         p.hres = hres;
@@ -3828,7 +3869,8 @@ static void free_set(EngineSet *s)
         if (t.cmode) cudaFree(t.cmode);
         if (t.maps) cudaFree(t.maps);
     }
-    void *ptrs[] = {s->ddesc, s->fdesc, s->fpos, s->items, s->dlive, s->sched, s->sq_items, s->sq_blocks, s->sq_engs};
+    void *ptrs[] = {s->ddesc, s->fdesc,    s->fpos,      s->items,    s->dlive,
+                    s->sched, s->sq_items, s->sq_blocks, s->sq_engs,  s->place_dev};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int k = 0; k < 2; ++k) {
@@ -4366,6 +4408,93 @@ int frmc_engines_step_host_collect(void *handle, int32_t slot, double *chi2_new,
     if (!s)
         return set_error(FRMC_E_ARG, "null handle");
     return step_host_collect(s, slot, chi2_new, accepted);
+}
+
+int frmc_engines_place(void *handle, int32_t steps)
+{
+    EngineSet *s = as_set(handle);
+    if (!s || steps < 1)
+        return set_error(FRMC_E_ARG, "engines_place: steps must be at least 1");
+    if (s->stage_busy[0] || s->stage_busy[1])
+        return set_error(FRMC_E_STATE, "engines_place: a host-buffer step is in flight");
+    FRMC_TRY(refresh(s));
+    Context *c;
+    FRMC_TRY(get_context(&c));
+    const int n = s->nfused;
+    if (n < 2 || n > c->sms * s->ctas_per_sm)
+        return FRMC_OK;  // no one-CTA launch with one item per CTA: nothing to place
+    if (s->place_cap < n) {
+        if (s->place_dev)
+            cudaFree(s->place_dev);
+        s->place_dev = nullptr;
+        s->place_cap = 0;
+        FRMC_CUDA(cudaMalloc(&s->place_dev, sizeof(unsigned long long) * n));
+        s->place_cap = n;
+    }
+    // engine id per fused item (fused_item holds the item's index in the
+    // whole list, whose first nsolo items are the one-engine tiles)
+    std::vector<int> ids(n, -1);
+    for (int id : s->live) {
+        const int k = s->fused_item[id] - s->nsolo;
+        if (s->fused_item[id] >= 0 && k >= 0 && k < n)
+            ids[k] = id;
+    }
+    for (int k = 0; k < n; ++k)
+        if (ids[k] < 0)
+            return set_error(FRMC_E_STATE, "engines_place: the work list is inconsistent");
+    std::vector<unsigned long long> rec(n);
+    std::vector<double> took(s->slots.size(), 0.0);
+    std::vector<int> sm0(n, -1);
+    bool repeat = true;
+    s->place_rec = true;
+    int rc = FRMC_OK;
+    for (int k = 0; k < steps && !rc; ++k) {
+        rc = launch_batched(s, s->stream);
+        if (!rc) {
+            cudaError_t ce = cudaMemcpyAsync(rec.data(), s->place_dev, sizeof(unsigned long long) * n,
+                                             cudaMemcpyDeviceToHost, s->stream);
+            if (ce == cudaSuccess)
+                ce = cudaStreamSynchronize(s->stream);
+            if (ce != cudaSuccess)
+                rc = cuda_fail(ce, "engines_place");
+        }
+        for (int b = 0; b < n && !rc; ++b) {
+            const int sm = (int)(rec[b] >> 48);
+            took[ids[b]] += (double)(rec[b] & 0xffffffffffffull);
+            if (k == 0)
+                sm0[b] = sm;
+            else if (sm0[b] != sm)
+                repeat = false;
+        }
+    }
+    s->place_rec = false;
+    if (rc)
+        return rc;
+    if (!repeat) {
+        // the SMs did not repeat from step to step: keep the cost order
+        s->place_order.clear();
+        return FRMC_OK;
+    }
+    // CTAs by SM; engines longest first
+    std::map<int, std::vector<int>> by_sm;
+    for (int b = 0; b < n; ++b) by_sm[sm0[b]].push_back(b);
+    std::vector<int> eng = ids;
+    std::stable_sort(eng.begin(), eng.end(), [&took](int a, int b) { return took[a] > took[b]; });
+    std::vector<int> order(n, -1);
+    int lo = 0, hi = n - 1;
+    for (auto &g : by_sm)
+        if (g.second.size() == 1)
+            order[g.second[0]] = eng[lo++];
+    for (auto &g : by_sm)
+        if (g.second.size() > 1) {
+            order[g.second[0]] = eng[lo++];
+            for (size_t j = 1; j < g.second.size(); ++j) order[g.second[j]] = eng[hi--];
+        }
+    s->place_order = order;
+    s->place_key = place_key(s, n);
+    s->dirty = true;
+    drop_graphs(s);
+    return refresh(s);  // the new work list now, not at the next step
 }
 
 int frmc_engines_sync(void *handle)

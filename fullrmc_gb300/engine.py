@@ -71,6 +71,7 @@ register("frmc_engines_set_sq_splits", [_vp, ctypes.c_int32])
 register("frmc_engines_init", [_vp])
 register("frmc_engines_push_moves", [_vp, _i32, I32P, F32P, F32P, _i32, _i64, ctypes.c_int])
 register("frmc_engines_step", [_vp, _i32, _i32, ctypes.c_int, _vp])
+register("frmc_engines_place", [_vp, _i32])
 register("frmc_engines_push_group_moves", [_vp, _i32, I32P, I32P, F32P, F32P, _i32, _i64])
 register("frmc_engines_sync", [_vp])
 register("frmc_engines_state", [_vp, _i32, F64P, ctypes.POINTER(_i64), ctypes.POINTER(_i64)])
@@ -677,6 +678,14 @@ class EngineSet:
                 best = (dt, tn)
         self.set_tune(*best[1])
         return best[1]
+
+    def place(self, steps=3):
+        """Measured placement of the batched launch: `steps` batched steps
+        (they advance every chain) record which engines' CTAs share an SM
+        and how long each engine took; the work list then gives the CTAs
+        that hold an SM alone the longest engines and pairs the rest longest
+        with shortest.  Results do not depend on the placement."""
+        check(load().frmc_engines_place(self.handle, int(steps)))
 
     def get_tune(self):
         v = [ctypes.c_int() for _ in range(4)]

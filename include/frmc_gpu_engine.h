@@ -185,6 +185,17 @@ int frmc_engines_push_group_moves(void *handle, int32_t e, const int32_t *atoms,
  * captures the launches in a CUDA graph (cached per engine/steps).  Returns
  * without synchronising; stream NULL = the set's own stream. */
 int frmc_engines_step(void *handle, int32_t engine, int32_t steps, int use_graph, void *stream);
+/* Measured placement of the batched one-CTA launch (no counterpart in
+ * fullrmc).  Runs `steps` batched steps (they advance every chain like
+ * frmc_engines_step, on the set's own stream, synchronously) recording for
+ * each engine its CTA's SM and time.  Where one item per CTA is launched and
+ * the CTAs landed on the same SMs in every recorded step, the work list is
+ * reordered for this set of engines and launch shape: the CTAs that hold an
+ * SM alone get the engines that took longest, and on shared SMs the longest
+ * remaining engine goes with the shortest.  Results do not depend on the
+ * order; adding or removing engines or changing the tuning falls back to the
+ * cost order.  Returns FRMC_E_STATE while a host-buffer step is in flight. */
+int frmc_engines_place(void *handle, int32_t steps);
 /* One batched step of every live engine from host buffers: atoms (E,), vecs
  * (E, 3), u (E,) in live-id order are uploaded in one copy, the step runs,
  * and each engine's new chi2 and decision come back in one copy (chi2_new,

@@ -397,3 +397,28 @@ def test_bins_past_the_histogram_land_in_the_next_row(oracle_mod):
             assert abs(c_new - res["chi2"][k]) <= 1e-10 * abs(c_new), k
         assert np.array_equal(res["counts"][0].astype(np.float32), chain.data[0])
         assert np.array_equal(res["counts"][1].astype(np.float32), chain.data[1])
+
+
+def test_measured_placement_keeps_chains():
+    """frmc_engines_place reorders the batched work list from recorded SMs
+    and times; the chains equal those of a set stepped in the cost order."""
+    from fullrmc_gb300.engine import EngineSet
+    systems = _systems(count=6, seed=31, nmin=700, nmax=3000)
+    steps = 40
+    mv = _moves(systems, steps, seed=12)
+    out = []
+    for place in (False, True):
+        es = EngineSet(systems, move_cap=64)
+        es.init()
+        for e, (a_, v_, u_) in enumerate(mv):
+            es.push_moves(e, a_, v_, u_, 0)
+        if place:
+            es.place(3)
+            es.step(steps - 3, graph=False)
+        else:
+            es.step(steps, graph=False)
+        es.sync()
+        out.append([dict(zip(("chi2", "acc", "atoms"), es.results(e, 0, steps)), state=es.state(e),
+                         counts=es.counts(e), coords=es.coords(e)) for e in range(len(systems))])
+        es.close()
+    _same(out[0], out[1])
