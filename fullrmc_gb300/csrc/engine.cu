@@ -1203,7 +1203,7 @@ __host__ __device__ constexpr int fused_cb_cap(int fused_bins, int threads)
 }
 
 struct ColQueue {
-    float *s0, *s1;   // squared distances before / after the move
+    float2 *s;        // squared distances before (x) / after (y) the move
     unsigned *info;   // el(j) | same molecule << 8 | accepted before << 9 | after << 10 | group atom << 11
     int *nz;          // per bin: element pairs whose delta is non-zero
     unsigned short *list;  // per warp: 32 * kColQueue queue indexes, the warp's entries packed
@@ -1232,7 +1232,8 @@ __device__ __forceinline__ void flush_columns(const ColView &D, const MovedGroup
     __syncwarp();
     for (int e = (int)lane; e < total; e += 32) {
         const int k = lst[e];
-        const float s0 = q.s0[k], s1 = q.s1[k];
+        const float2 sk = q.s[k];
+        const float s0 = sk.x, s1 = sk.y;
         const unsigned info = q.info[k];
         const int elj = (int)(info & 0xffu);
         const int gi = (int)(info >> 11);
@@ -1408,37 +1409,46 @@ __device__ void fused_columns(const EDesc &Dg, int *sdP, int *nz, unsigned *s_tc
     const int step = kItemUnroll * blockDim.x;
     const int G = GROUP ? g.n : 1;
     const int self0 = CELL ? g.slot[0] : g.atom[0];
+    const int mola0 = g.mol[0];
     int qn = 0;
+    // a batch: coordinates, molecules (a single atom compares them once, into
+    // the bits of `same`, after the next batch's loads are issued) and the
+    // bits of `vmask` (column u exists and is not a moved atom): bit masks
+    // leave registers to the batch in flight and the flushes
     float4 c[kItemUnroll];
     int mj[kItemUnroll];
-    int jc[kItemUnroll];  // the columns' indexes (cell order with a grid)
+    unsigned vmask = 0u, same = 0u;
 #pragma unroll
     for (int u = 0; u < kItemUnroll; ++u) {
         const int v = u * blockDim.x + threadIdx.x;
         const int j = v < ncol ? (CELL ? cell_column(cP, cB, nc, v) : v) : -1;
-        jc[u] = j;
+        bool ok = j >= 0 && j != self0;
+        if (GROUP)
+            for (int t = 1; t < G; ++t) ok &= j != (CELL ? g.slot[t] : g.atom[t]);
+        vmask |= (ok ? 1u : 0u) << u;
         c[u] = j >= 0 ? D.box[j] : make_float4(0.f, 0.f, 0.f, 0.f);
         mj[u] = j >= 0 ? D.mol[j] : 0;
     }
     for (int jb = 0; jb < ncol; jb += step) {
         float4 cn[kItemUnroll];
-        int mn[kItemUnroll], jn[kItemUnroll];
+        int mn[kItemUnroll];
+        unsigned vmaskn = 0u;
 #pragma unroll
         for (int u = 0; u < kItemUnroll; ++u) {
             const int v = jb + step + u * blockDim.x + threadIdx.x;
             const int j = v < ncol ? (CELL ? cell_column(cP, cB, nc, v) : v) : -1;
-            jn[u] = j;
-            cn[u] = j >= 0 ? D.box[j] : make_float4(0.f, 0.f, 0.f, 0.f);
-            mn[u] = j >= 0 ? D.mol[j] : 0;
-        }
-        bool valid[kItemUnroll];
-#pragma unroll
-        for (int u = 0; u < kItemUnroll; ++u) {
-            const int j = jc[u];
             bool ok = j >= 0 && j != self0;
             if (GROUP)
                 for (int t = 1; t < G; ++t) ok &= j != (CELL ? g.slot[t] : g.atom[t]);
-            valid[u] = ok;
+            vmaskn |= (ok ? 1u : 0u) << u;
+            cn[u] = j >= 0 ? D.box[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+            mn[u] = j >= 0 ? D.mol[j] : 0;
+        }
+        if (!GROUP) {
+            // (after the next batch's loads are issued)
+            same = 0u;
+#pragma unroll
+            for (int u = 0; u < kItemUnroll; ++u) same |= (mj[u] == mola0 ? 1u : 0u) << u;
         }
         for (int gi = 0; gi < G; ++gi) {
             if (__any_sync(0xffffffffu, qn > kColQueue - kItemUnroll))
@@ -1448,23 +1458,24 @@ __device__ void fused_columns(const EDesc &Dg, int *sdP, int *nz, unsigned *s_tc
             const int mola = g.mol[gi];
 #pragma unroll
             for (int u = 0; u < kItemUnroll; ++u) {
+                const bool valid = (vmask >> u) & 1u;
                 const float s0 = pair_s<BM>(o.x, o.y, o.z, c[u].x, c[u].y, c[u].z, D.B);
                 const float s1 = pair_s<BM>(nw.x, nw.y, nw.z, c[u].x, c[u].y, c[u].z, D.B);
-                const bool a0 = valid[u] & (s0 >= D.s_lo) & (s0 < D.s_hi);
-                const bool a1 = valid[u] & (s1 >= D.s_lo) & (s1 < D.s_hi);
+                const bool a0 = valid & (s0 >= D.s_lo) & (s0 < D.s_hi);
+                const bool a1 = valid & (s1 >= D.s_lo) & (s1 < D.s_hi);
+                const unsigned sm = GROUP ? (mj[u] == mola ? 1u : 0u) : ((same >> u) & 1u);
                 const int k = qn * (int)blockDim.x + (int)threadIdx.x;
-                q.s0[k] = s0;
-                q.s1[k] = s1;
-                q.info[k] = ((unsigned)__float_as_int(c[u].w) & 0xffu) | ((mj[u] == mola ? 1u : 0u) << 8) |
-                            ((a0 ? 1u : 0u) << 9) | ((a1 ? 1u : 0u) << 10) | ((unsigned)gi << 11);
+                q.s[k] = make_float2(s0, s1);
+                q.info[k] = ((unsigned)__float_as_int(c[u].w) & 0xffu) | (sm << 8) | ((a0 ? 1u : 0u) << 9) |
+                            ((a1 ? 1u : 0u) << 10) | ((unsigned)gi << 11);
                 qn += (a0 | a1) ? 1 : 0;
             }
         }
+        vmask = vmaskn;
 #pragma unroll
         for (int u = 0; u < kItemUnroll; ++u) {
             c[u] = cn[u];
             mj[u] = mn[u];
-            jc[u] = jn[u];
         }
     }
     flush_columns(D, g, sdP, nz, s_tcount, q, qn);
@@ -1769,9 +1780,8 @@ __global__ void __launch_bounds__(kMaxEngineThreads, 1) k_engine_step(StepParams
         // dynamic layout: element-pair deltas, then A and Bq (16-byte aligned)
         sA = reinterpret_cast<double *>(sdP + p.fused_dp_ints);
         sBq = sA + p.fused_bins;
-        cq.s0 = reinterpret_cast<float *>(sBq + p.fused_bins);
-        cq.s1 = cq.s0 + kColQueue * blockDim.x;
-        cq.info = reinterpret_cast<unsigned *>(cq.s1 + kColQueue * blockDim.x);
+        cq.s = reinterpret_cast<float2 *>(sBq + p.fused_bins);  // 8-byte aligned
+        cq.info = reinterpret_cast<unsigned *>(cq.s + kColQueue * blockDim.x);
         cq.nz = reinterpret_cast<int *>(cq.info + kColQueue * blockDim.x);
         cb = reinterpret_cast<double *>(cq.nz + p.fused_bins);  // fused_bins is even: 8-byte aligned
         sbs = cb + fused_cb_cap(p.fused_bins, blockDim.x);
