@@ -599,9 +599,9 @@ def run_ours(args):
     st = torch.cuda.Stream()
     sp = st.cuda_stream
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-    # the first warm-up steps measure the placement of the batched launch
+    # the warm-up steps (up to 8) measure the placement of the batched launch
     # (batched steps like the others; the library reorders its work list)
-    P = min(3, W)
+    P = min(8, W)
     if P > 0:
         es.place(P)
     with torch.cuda.stream(st):
