@@ -422,3 +422,29 @@ def test_measured_placement_keeps_chains():
                          counts=es.counts(e), coords=es.coords(e)) for e in range(len(systems))])
         es.close()
     _same(out[0], out[1])
+
+
+def test_host_steps_after_a_placement_match_ring_steps():
+    """After frmc_engines_place reorders the work list, host-buffer steps
+    (whose moves and results follow the live-engine order) still give every
+    engine its own chain."""
+    from fullrmc_gb300.engine import EngineSet
+    systems = _systems(count=7, seed=37, nmin=700, nmax=2500)
+    steps = 30
+    mv = _moves(systems, steps, seed=14)
+    ring = _run(systems, mv, steps, "batched")
+    es = EngineSet(systems, move_cap=8)
+    es.init()
+    for e, (a_, v_, u_) in enumerate(mv):
+        es.push_moves(e, a_[:3], v_[:3], u_[:3], 0)
+    es.place(3)
+    A = np.stack([m[0] for m in mv])
+    V = np.stack([m[1] for m in mv])
+    U = np.stack([m[2] for m in mv])
+    for k in range(3, steps):
+        c2, acc = es.step_host(A[:, k], V[:, k, :], U[:, k])
+        for e in range(len(systems)):
+            assert c2[e] == ring[e]["chi2"][k] and acc[e] == ring[e]["acc"][k], (k, e)
+    for e in range(len(systems)):
+        assert es.state(e) == ring[e]["state"]
+    es.close()
