@@ -2988,6 +2988,28 @@ static SqEng sq_eng(const EDesc &D, int lc)
 }
 
 // Rebuild the work list over live engines and upload descriptors.
+// Placement of n one-CTA items over the CTAs of a launch: CTA b ran on SM
+// sm[b] and its item took t[b].  pos[b] = the item that CTA b gets: the CTAs
+// that hold an SM alone take the longest items, and on a shared SM the first
+// CTA takes the longest remaining item and the others the shortest ones.
+static void place_positions(int n, const int *sm, const double *t, int *pos)
+{
+    std::map<int, std::vector<int>> by_sm;
+    for (int b = 0; b < n; ++b) by_sm[sm[b]].push_back(b);
+    std::vector<int> items(n);
+    for (int b = 0; b < n; ++b) items[b] = b;
+    std::stable_sort(items.begin(), items.end(), [t](int a, int b) { return t[a] > t[b]; });
+    int lo = 0, hi = n - 1;
+    for (auto &g : by_sm)
+        if (g.second.size() == 1)
+            pos[g.second[0]] = items[lo++];
+    for (auto &g : by_sm)
+        if (g.second.size() > 1) {
+            pos[g.second[0]] = items[lo++];
+            for (size_t j = 1; j < g.second.size(); ++j) pos[g.second[j]] = items[hi--];
+        }
+}
+
 // The launch shape a measured placement belongs to: the one-CTA items, the
 // CTA size, CTAs per SM and the dynamic shared memory of the launch.
 static long long place_key(const EngineSet *s, int nfused)
@@ -4420,6 +4442,16 @@ int frmc_engines_step_host_collect(void *handle, int32_t slot, double *chi2_new,
     return step_host_collect(s, slot, chi2_new, accepted);
 }
 
+int frmc_engines_place_positions(int32_t n, const int32_t *sm, const double *t, int32_t *pos)
+{
+    if (n < 0 || (n > 0 && (!sm || !t || !pos)))
+        return set_error(FRMC_E_ARG, "place_positions: invalid arguments");
+    std::vector<int> smi(sm, sm + n), p(n);
+    place_positions(n, smi.data(), t, p.data());
+    for (int b = 0; b < n; ++b) pos[b] = p[b];
+    return FRMC_OK;
+}
+
 int frmc_engines_place(void *handle, int32_t steps)
 {
     EngineSet *s = as_set(handle);
@@ -4485,21 +4517,12 @@ int frmc_engines_place(void *handle, int32_t steps)
         s->place_order.clear();
         return FRMC_OK;
     }
-    // CTAs by SM; engines longest first
-    std::map<int, std::vector<int>> by_sm;
-    for (int b = 0; b < n; ++b) by_sm[sm0[b]].push_back(b);
-    std::vector<int> eng = ids;
-    std::stable_sort(eng.begin(), eng.end(), [&took](int a, int b) { return took[a] > took[b]; });
+    std::vector<double> t(n);
+    for (int b = 0; b < n; ++b) t[b] = took[ids[b]];
+    std::vector<int> pos(n);
+    place_positions(n, sm0.data(), t.data(), pos.data());
     std::vector<int> order(n, -1);
-    int lo = 0, hi = n - 1;
-    for (auto &g : by_sm)
-        if (g.second.size() == 1)
-            order[g.second[0]] = eng[lo++];
-    for (auto &g : by_sm)
-        if (g.second.size() > 1) {
-            order[g.second[0]] = eng[lo++];
-            for (size_t j = 1; j < g.second.size(); ++j) order[g.second[j]] = eng[hi--];
-        }
+    for (int b = 0; b < n; ++b) order[b] = ids[pos[b]];
     s->place_order = order;
     s->place_key = place_key(s, n);
     s->dirty = true;

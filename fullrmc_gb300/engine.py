@@ -72,6 +72,7 @@ register("frmc_engines_init", [_vp])
 register("frmc_engines_push_moves", [_vp, _i32, I32P, F32P, F32P, _i32, _i64, ctypes.c_int])
 register("frmc_engines_step", [_vp, _i32, _i32, ctypes.c_int, _vp])
 register("frmc_engines_place", [_vp, _i32])
+register("frmc_engines_place_positions", [_i32, I32P, F64P, I32P])
 register("frmc_engines_push_group_moves", [_vp, _i32, I32P, I32P, F32P, F32P, _i32, _i64])
 register("frmc_engines_sync", [_vp])
 register("frmc_engines_state", [_vp, _i32, F64P, ctypes.POINTER(_i64), ctypes.POINTER(_i64)])
@@ -678,6 +679,19 @@ class EngineSet:
                 best = (dt, tn)
         self.set_tune(*best[1])
         return best[1]
+
+    @staticmethod
+    def place_positions(sm, took):
+        """The ordering `place` applies (host only): CTA b ran on SM sm[b] and
+        its item took took[b]; returns the item each CTA gets."""
+        sm = np.ascontiguousarray(sm, np.int32)
+        took = np.ascontiguousarray(took, np.float64)
+        if sm.shape != took.shape or sm.ndim != 1:
+            raise ValueError("place_positions: sm and took must be 1-D arrays of one length")
+        pos = np.empty(sm.size, np.int32)
+        check(load().frmc_engines_place_positions(int(sm.size), sm.ctypes.data_as(I32P),
+                                                  took.ctypes.data_as(F64P), pos.ctypes.data_as(I32P)))
+        return pos
 
     def place(self, steps=3):
         """Measured placement of the batched launch: `steps` batched steps

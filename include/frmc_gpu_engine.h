@@ -196,6 +196,12 @@ int frmc_engines_step(void *handle, int32_t engine, int32_t steps, int use_graph
  * order; adding or removing engines or changing the tuning falls back to the
  * cost order.  Returns FRMC_E_STATE while a host-buffer step is in flight. */
 int frmc_engines_place(void *handle, int32_t steps);
+/* The ordering frmc_engines_place applies, on the host (no GPU): CTA b of a
+ * launch of n one-CTA items ran on SM sm[b] and its item took t[b]; pos[b]
+ * receives the item CTA b gets.  CTAs alone on their SM take the longest
+ * items; on a shared SM the first CTA takes the longest remaining item and
+ * the others the shortest. */
+int frmc_engines_place_positions(int32_t n, const int32_t *sm, const double *t, int32_t *pos);
 /* One batched step of every live engine from host buffers: atoms (E,), vecs
  * (E, 3), u (E,) in live-id order are uploaded in one copy, the step runs,
  * and each engine's new chi2 and decision come back in one copy (chi2_new,

@@ -95,3 +95,26 @@ def test_basis_modes(lib):
     assert mode([[103, 0, 0], [-51.5, 89.2, 0], [0, 0, 103]]) == 2
     assert mode([[10, 0, 0], [2, 9, 0], [1, 2, 8]]) == 3
     assert mode([[10, 1, 0], [2, 9, 0], [1, 2, 8]]) == 4
+
+
+def test_place_positions_orders_lone_and_shared_sms(lib):
+    """The measured placement's ordering (host only): CTAs alone on an SM
+    take the longest items; on a shared SM the first CTA takes the longest
+    remaining item and the others the shortest."""
+    from fullrmc_gb300.engine import EngineSet
+    sm = [0, 1, 1, 2, 2, 3]            # CTAs 0 and 5 hold SMs 0 and 3 alone
+    took = [1.0, 5.0, 3.0, 6.0, 2.0, 4.0]
+    # items by time: 3, 1, 5, 2, 4, 0; lone CTAs 0, 5 get 3, 1; SM 1: 5 and
+    # the shortest, 0; SM 2: 2 and 4
+    assert EngineSet.place_positions(sm, took).tolist() == [3, 5, 0, 2, 4, 1]
+    rng = np.random.default_rng(4)
+    for n in (1, 7, 256):
+        sm = rng.integers(0, max(1, n // 2), n)
+        took = rng.random(n)
+        pos = EngineSet.place_positions(sm, took)
+        assert sorted(pos.tolist()) == list(range(n))  # every item once
+        lone = [b for b in range(n) if (sm == sm[b]).sum() == 1]
+        if lone:
+            longest = set(np.argsort(-took, kind="stable")[:len(lone)].tolist())
+            assert {int(pos[b]) for b in lone} == longest
+    assert EngineSet.place_positions([], []).tolist() == []
