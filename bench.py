@@ -693,6 +693,12 @@ def run_ours(args):
     # submits step k + 1 before it collects step k's results.
     es2 = EngineSet(systems, move_cap=4, tune=tune)
     es2.init()
+    # the placement of the batched launch, measured on three ring steps
+    pm = [translation_moves(np.random.default_rng([seed, 6000 + e]), s.box_coords.shape[0], 3, amp)
+          for e, s in enumerate(systems)]
+    for e, (a, v, u) in enumerate(pm):
+        es2.push_moves(e, a, v, u, 0)
+    es2.place(3)
     hm = [translation_moves(np.random.default_rng([seed, 5000 + e]), s.box_coords.shape[0], W + K, amp)
           for e, s in enumerate(systems)]
     A = np.ascontiguousarray(np.stack([m[0] for m in hm]).T)        # (steps, engines)
