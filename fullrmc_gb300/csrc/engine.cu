@@ -4459,6 +4459,8 @@ int frmc_engines_place(void *handle, int32_t steps)
         return set_error(FRMC_E_ARG, "engines_place: steps must be at least 1");
     if (s->stage_busy[0] || s->stage_busy[1])
         return set_error(FRMC_E_STATE, "engines_place: a host-buffer step is in flight");
+    // steps launched on other streams finish first (a set-up call)
+    FRMC_CUDA(cudaDeviceSynchronize());
     FRMC_TRY(refresh(s));
     Context *c;
     FRMC_TRY(get_context(&c));

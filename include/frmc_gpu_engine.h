@@ -194,7 +194,8 @@ int frmc_engines_step(void *handle, int32_t engine, int32_t steps, int use_graph
  * SM alone get the engines that took longest, and on shared SMs the longest
  * remaining engine goes with the shortest.  Results do not depend on the
  * order; adding or removing engines or changing the tuning falls back to the
- * cost order.  Returns FRMC_E_STATE while a host-buffer step is in flight. */
+ * cost order.  Waits for all work on the device first.  Returns
+ * FRMC_E_STATE while a host-buffer step is in flight. */
 int frmc_engines_place(void *handle, int32_t steps);
 /* The ordering frmc_engines_place applies, on the host (no GPU): CTA b of a
  * launch of n one-CTA items ran on SM sm[b] and its item took t[b]; pos[b]
